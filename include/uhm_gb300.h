@@ -1,0 +1,138 @@
+/*
+ * uhm_gb300 C ABI.
+ *
+ * Part 1 mirrors the reference's Fortran/C interface one to one
+ * (UHM/include/uhm/wrapper/fort.hxx:47-190, implemented in
+ * UHM/src/wrapper/fort.cxx:47-321): same names (trailing underscore, the
+ * UHM_C2F convention of UHM/include/uhm/util.hxx:39), arguments passed by
+ * pointer, mesh / element / node handles as `long` casts of C++ pointers,
+ * `void` returns.  Where the reference aborts on bad input, these record an
+ * error that uhm_gpu_get_status / uhm_gpu_get_last_error report.
+ *
+ * Part 2 (uhm_gpu_*) adds what the device path needs and the reference has
+ * no call for: tree construction through the Element API (the reference
+ * builds trees with METIS, which this path does not use), status codes,
+ * precision / refinement control, bulk transfers and timings.
+ *
+ * Constants (UHM/include/uhm/wrapper/fort.f90:33-53):
+ *   UHM_REAL = 101, UHM_COMPLEX = 103 (unsupported), UHM_LHS = 1, UHM_RHS = 2,
+ *   UHM_PHYSICS_SINGLE = 1, UHM_PHYSICS_MULTI = 2.
+ */
+#ifndef UHM_GB300_H
+#define UHM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Part 1: reference interface (fort.hxx) ---------------------------- */
+/* fort.hxx:51-52 */ void uhm_initialize_fla_(void);
+/* fort.hxx:52    */ void uhm_finalize_fla_(void);
+/* fort.hxx:54-55 */ void uhm_set_num_threads_(int* n_threads);
+/* fort.hxx:55    */ void uhm_get_num_threads_(int* n_threads);
+/* fort.hxx:57-58 */ void uhm_set_hier_block_size_(int* size);
+/* fort.hxx:58    */ void uhm_get_hier_block_size_(int* size);
+/* fort.hxx:67-68 */ void uhm_reset_flop_(void);
+/* fort.hxx:68    */ void uhm_get_flop_(double* flop);
+/* fort.hxx:69    */ void uhm_get_buffer_used_(double* buffer);
+/* fort.hxx:70    */ void uhm_get_max_buffer_used_(double* buffer);
+/* fort.hxx:71    */ void uhm_is_multithreading_enable_(int* flag);
+/* fort.hxx:72    */ void uhm_is_hier_matrix_enable_(int* flag);
+/* fort.hxx:73    */ void uhm_timer_(double* t);
+
+/* fort.hxx:77-78 */ void uhm_mesh_create_(long* mesh);
+/* fort.hxx:78    */ void uhm_mesh_delete_(long* mesh);
+/* fort.hxx:79-80 */ void uhm_add_element_(long* mesh, long* elt);
+/* fort.hxx:81-86 */ void uhm_add_node_(long* mesh, int* id, int* phy, int* n_dof, int* p, long* nod);
+/* fort.hxx:87-88 */ void uhm_element_add_node_(long* elt, long* nod);
+/* fort.hxx:89-97 */ void uhm_copy_in_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
+                                       int* node_disp, int* nods, int* side, double* buffer);
+/* fort.hxx:98-106*/ void uhm_copy_out_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
+                                        int* node_disp, int* nods, int* side, double* buffer);
+/* fort.hxx:107   */ void uhm_mesh_disp_(long* mesh);
+/* fort.hxx:108-109*/ void uhm_get_n_dof_(long* mesh, int* n_dof);
+/* fort.hxx:110-111*/ void uhm_get_n_nonzero_(long* mesh, int* n_nonzero);
+/* fort.hxx:112-119*/ void uhm_estimate_cost_(long* mesh, int* method, int* datatype, int* n_rhs,
+                                             double* flop_decompose, double* flop_solve,
+                                             unsigned* n_nonzero_factor, double* buffer);
+/* fort.hxx:120-121*/ void uhm_mesh_import_(long* mesh, char* filename);
+/* fort.hxx:122   */ void uhm_build_tree_(long* mesh);
+/* fort.hxx:123-125*/ void uhm_create_matrix_without_buffer_(long* mesh, int* datatype, int* n_rhs);
+/* fort.hxx:126   */ void uhm_create_leaf_matrix_buffer_(long* mesh);
+/* fort.hxx:127-128*/ void uhm_create_element_matrix_buffer_(long* mesh, int* is_schur);
+/* fort.hxx:129   */ void uhm_set_rhs_(long* mesh);
+/* fort.hxx:133   */ void uhm_lock_(long* mesh);
+/* fort.hxx:134   */ void uhm_unlock_(long* mesh);
+
+/* fort.hxx:137-142 decomposition */
+void uhm_chol_with_free_(long* mesh);
+void uhm_lu_nopiv_with_free_(long* mesh);
+void uhm_lu_piv_with_free_(long* mesh);
+/* fort.hxx:145-150 solution */
+void uhm_solve_chol_(long* mesh);
+void uhm_solve_lu_nopiv_(long* mesh);
+void uhm_solve_lu_piv_(long* mesh);
+/* fort.hxx:153-158 checking (computes the residual on the element matrices) */
+void uhm_check_chol_(long* mesh);
+void uhm_check_lu_nopiv_(long* mesh);
+void uhm_check_lu_piv_(long* mesh);
+/* fort.hxx:161-162 residual: ||b - A x||_1 on the unassembled operator */
+void uhm_get_residual_(long* mesh, double* res);
+
+/* ---- Part 2: device-path additions (no counterpart in fort.hxx) ------- */
+/* Mesh_::add_element(int gen) (UHM/include/uhm/mesh/mesh.hxx:160) */
+int uhm_gpu_add_element_with_generation(long* mesh, int* gen, long* elt);
+/* Element_::set_parent / add_child (UHM/include/uhm/mesh/element.hxx:104,139) */
+int uhm_gpu_element_set_parent(long* elt, long* parent);
+int uhm_gpu_element_add_child(long* elt, long* child);
+
+/* 0 = ok; 4 = device allocation failed; 5..9 = API misuse; 11 = front not
+ * positive definite; 12 = zero pivot; 13 = NaN; 20 = refinement missed its
+ * tolerance (solution redone in FP64); 30 = unsupported call. */
+int uhm_gpu_get_status(long* mesh);
+int uhm_gpu_get_last_error(long* mesh, char* buf, int len);
+
+/* mode 0: plain FP64 fronts.  mode 1: mixed precision, fronts in
+ * default_prec (0 FP64, 1 FP32, 2 BF16-split tensor-core Schur update) with
+ * FP64 iterative refinement on the element matrices until the backward error
+ * is <= tol or max_iter corrections have been applied. */
+int uhm_gpu_set_mode(long* mesh, int mode, int default_prec, double tol, int max_iter);
+/* per-front precision, indexed by element id (-1 = default) */
+int uhm_gpu_set_front_precision(long* mesh, int n, const int* prec_by_element_id);
+
+/* Bulk element transfer for all leaves in element-id order: nods_all holds
+ * each leaf's node ids back to back (element's node count each, single
+ * physics); buffer holds each leaf's m x m matrix (LHS) or m x n_rhs block
+ * (RHS), column-major, back to back.  Same semantics as one uhm_copy_in_ per
+ * leaf, with one host-to-device copy. */
+int uhm_gpu_copy_in_leaves(long* mesh, int side, const int* nods_all, const double* buffer,
+                           long n_values);
+/* solution for all leaves, same layout as the RHS of uhm_gpu_copy_in_leaves */
+int uhm_gpu_copy_out_leaves(long* mesh, double* buffer, long n_values);
+/* solution of listed nodes (single physics ids), each node's dofs in order */
+int uhm_gpu_get_node_solution(long* mesh, int n_nodes, const int* node_ids, double* out,
+                              long n_values);
+
+/* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), A the assembled sum of
+ * element matrices, evaluated in FP64 on the device */
+int uhm_gpu_backward_error(long* mesh, double* berr);
+/* out[0..7] = upload ms, factor ms, solve ms, refine ms, total ms,
+ * refinement iterations, backward error, kernel launches */
+int uhm_gpu_get_timing(long* mesh, double* out);
+
+/* front table after lock + create_matrix_without_buffer: per front (leaf to
+ * root order) the element id, generation, fs, ss */
+int uhm_gpu_get_n_fronts(long* mesh, int* n);
+int uhm_gpu_get_fronts(long* mesh, int n, int* elt_id, int* generation, int* fs, int* ss);
+/* node ids of one front, factor nodes then schur nodes, in front order */
+int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_factor,
+                            int* n_schur);
+
+/* pinned host memory for the bulk transfers */
+void* uhm_gpu_host_alloc(long bytes);
+void uhm_gpu_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

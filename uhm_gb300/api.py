@@ -1,0 +1,372 @@
+"""Python mirror of UHM's Mesh API over the C ABI of include/uhm_gb300.h.
+
+Method names and argument meaning follow ``uhm::Mesh_`` / the Fortran
+interface (UHM/include/uhm/mesh/mesh.hxx:82-293,
+UHM/include/uhm/wrapper/fort.hxx:47-190).  Every call goes through
+``libuhm_gb300.so``; there is no Python or CPU fallback for the numerics: if
+the library cannot be loaded, importing this module fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libuhm_gb300.so")
+
+UHM_REAL, UHM_COMPLEX = 101, 103
+UHM_LHS, UHM_RHS = 1, 2
+UHM_PHYSICS_SINGLE, UHM_PHYSICS_MULTI = 1, 2
+UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV = 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"uhm_gb300 native library missing: {LIB_PATH} "
+                               "(build it with `python -m uhm_gb300.build`)")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+_P = C.POINTER
+_l, _i, _d = C.c_long, C.c_int, C.c_double
+
+
+def _declare(L):
+    def sig(name, args, res=None):
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    sig("uhm_mesh_create_", [_P(_l)])
+    sig("uhm_mesh_delete_", [_P(_l)])
+    sig("uhm_add_element_", [_P(_l), _P(_l)])
+    sig("uhm_add_node_", [_P(_l), _P(_i), _P(_i), _P(_i), _P(_i), _P(_l)])
+    sig("uhm_element_add_node_", [_P(_l), _P(_l)])
+    sig("uhm_copy_in_", [_P(_l), _P(_l), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_d)])
+    sig("uhm_copy_out_", [_P(_l), _P(_l), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_i), _P(_d)])
+    sig("uhm_get_n_dof_", [_P(_l), _P(_i)])
+    sig("uhm_get_n_nonzero_", [_P(_l), _P(_i)])
+    sig("uhm_estimate_cost_", [_P(_l), _P(_i), _P(_i), _P(_i), _P(_d), _P(_d), _P(C.c_uint), _P(_d)])
+    sig("uhm_mesh_import_", [_P(_l), C.c_char_p])
+    sig("uhm_build_tree_", [_P(_l)])
+    sig("uhm_create_matrix_without_buffer_", [_P(_l), _P(_i), _P(_i)])
+    sig("uhm_create_leaf_matrix_buffer_", [_P(_l)])
+    sig("uhm_create_element_matrix_buffer_", [_P(_l), _P(_i)])
+    sig("uhm_set_rhs_", [_P(_l)])
+    sig("uhm_lock_", [_P(_l)])
+    sig("uhm_unlock_", [_P(_l)])
+    for n in ("chol_with_free", "lu_nopiv_with_free", "lu_piv_with_free", "solve_chol",
+              "solve_lu_nopiv", "solve_lu_piv", "check_chol", "check_lu_nopiv", "check_lu_piv"):
+        sig(f"uhm_{n}_", [_P(_l)])
+    sig("uhm_get_residual_", [_P(_l), _P(_d)])
+    sig("uhm_get_flop_", [_P(_d)])
+    sig("uhm_reset_flop_", [])
+    sig("uhm_set_num_threads_", [_P(_i)])
+    sig("uhm_gpu_add_element_with_generation", [_P(_l), _P(_i), _P(_l)], _i)
+    sig("uhm_gpu_element_set_parent", [_P(_l), _P(_l)], _i)
+    sig("uhm_gpu_element_add_child", [_P(_l), _P(_l)], _i)
+    sig("uhm_gpu_get_status", [_P(_l)], _i)
+    sig("uhm_gpu_get_last_error", [_P(_l), C.c_char_p, _i], _i)
+    sig("uhm_gpu_set_mode", [_P(_l), _i, _i, _d, _i], _i)
+    sig("uhm_gpu_set_front_precision", [_P(_l), _i, _P(_i)], _i)
+    sig("uhm_gpu_copy_in_leaves", [_P(_l), _i, _P(_i), _P(_d), _l], _i)
+    sig("uhm_gpu_copy_out_leaves", [_P(_l), _P(_d), _l], _i)
+    sig("uhm_gpu_get_node_solution", [_P(_l), _i, _P(_i), _P(_d), _l], _i)
+    sig("uhm_gpu_backward_error", [_P(_l), _P(_d)], _i)
+    sig("uhm_gpu_get_timing", [_P(_l), _P(_d)], _i)
+    sig("uhm_gpu_get_n_fronts", [_P(_l), _P(_i)], _i)
+    sig("uhm_gpu_get_fronts", [_P(_l), _i, _P(_i), _P(_i), _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_get_front_nodes", [_P(_l), _i, _i, _P(_i), _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_host_alloc", [_l], C.c_void_p)
+    sig("uhm_gpu_host_free", [C.c_void_p])
+
+
+class UHMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def _ip(v):
+    return C.byref(_i(int(v)))
+
+
+def _arr(a, dtype, ctype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a, a.ctypes.data_as(_P(ctype))
+
+
+class Mesh:
+    """Handle to a ``uhm::Mesh_`` living in the native library."""
+
+    def __init__(self):
+        self.L = lib()
+        self.h = _l(0)
+        self.L.uhm_mesh_create_(C.byref(self.h))
+        self._elements = {}
+        self.n_rhs = 1
+
+    def __del__(self):
+        try:
+            if self.h.value:
+                self.L.uhm_mesh_delete_(C.byref(self.h))
+        except Exception:
+            pass
+
+    # -- errors --------------------------------------------------------
+    def status(self) -> int:
+        return int(self.L.uhm_gpu_get_status(C.byref(self.h)))
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self.L.uhm_gpu_get_last_error(C.byref(self.h), buf, 1024)
+        return buf.value.decode()
+
+    def _check(self, code=None):
+        st = self.status() if code is None else code
+        if st:
+            raise UHMError(st, self.last_error())
+
+    # -- topology --------------------------------------------------------
+    def add_node(self, id, n_dof, p=None, phy=0):
+        nod = _l(0)
+        self.L.uhm_add_node_(C.byref(self.h), _ip(id), _ip(phy), _ip(n_dof),
+                             _ip(n_dof if p is None else p), C.byref(nod))
+        return nod.value
+
+    def add_element(self, gen=None):
+        e = _l(0)
+        if gen is None:
+            self.L.uhm_add_element_(C.byref(self.h), C.byref(e))
+        else:
+            self.L.uhm_gpu_add_element_with_generation(C.byref(self.h), _ip(gen), C.byref(e))
+        return e.value
+
+    def element_add_node(self, elt, nod):
+        self.L.uhm_element_add_node_(C.byref(_l(elt)), C.byref(_l(nod)))
+
+    def set_parent(self, elt, parent):
+        self.L.uhm_gpu_element_set_parent(C.byref(_l(elt)), C.byref(_l(parent)))
+
+    def add_child(self, elt, child):
+        self.L.uhm_gpu_element_add_child(C.byref(_l(elt)), C.byref(_l(child)))
+
+    def lock(self):
+        self.L.uhm_lock_(C.byref(self.h))
+        self._check()
+
+    def unlock(self):
+        self.L.uhm_unlock_(C.byref(self.h))
+
+    def import_file(self, path: str):
+        self.L.uhm_mesh_import_(C.byref(self.h), path.encode())
+        self._check()
+
+    # -- matrices ----------------------------------------------------------
+    def create_matrix_without_buffer(self, datatype=UHM_REAL, n_rhs=1):
+        self.n_rhs = n_rhs
+        self.L.uhm_create_matrix_without_buffer_(C.byref(self.h), _ip(datatype), _ip(n_rhs))
+        self._check()
+
+    def create_matrix_buffer(self):
+        self.L.uhm_create_element_matrix_buffer_(C.byref(self.h), _ip(0))
+
+    def copy_in(self, elt, nods, side, buf, datatype=UHM_REAL):
+        buf = np.asfortranarray(buf, dtype=np.float64)
+        m = buf.shape[0]
+        n = buf.shape[1] if buf.ndim == 2 else 1
+        nods_a, nods_p = _arr(nods, np.int32, _i)
+        self.L.uhm_copy_in_(C.byref(self.h), C.byref(_l(elt)), _ip(datatype), _ip(m), _ip(n),
+                            _ip(UHM_PHYSICS_SINGLE), nods_p, _ip(side),
+                            buf.ctypes.data_as(_P(_d)))
+        self._check()
+
+    def copy_out(self, elt, nods, m, n=1, datatype=UHM_REAL):
+        out = np.zeros((m, n), order="F")
+        nods_a, nods_p = _arr(nods, np.int32, _i)
+        self.L.uhm_copy_out_(C.byref(self.h), C.byref(_l(elt)), _ip(datatype), _ip(m), _ip(n),
+                             _ip(UHM_PHYSICS_SINGLE), nods_p, _ip(UHM_RHS),
+                             out.ctypes.data_as(_P(_d)))
+        self._check()
+        return out
+
+    def set_rhs(self):
+        self.L.uhm_set_rhs_(C.byref(self.h))
+
+    # -- factor / solve ------------------------------------------------------
+    def _call(self, name):
+        getattr(self.L, f"uhm_{name}_")(C.byref(self.h))
+        self._check()
+
+    def chol_with_free(self):
+        self._call("chol_with_free")
+
+    def lu_piv_with_free(self):
+        self._call("lu_piv_with_free")
+
+    def lu_nopiv_with_free(self):
+        self._call("lu_nopiv_with_free")
+
+    def solve_chol(self):
+        self._call("solve_chol")
+
+    def solve_lu_piv(self):
+        self._call("solve_lu_piv")
+
+    def solve_lu_nopiv(self):
+        self._call("solve_lu_nopiv")
+
+    def factor(self, method):
+        {UHM_CHOL: self.chol_with_free, UHM_LU_PIV: self.lu_piv_with_free,
+         UHM_LU_NOPIV: self.lu_nopiv_with_free}[method]()
+
+    def solve(self, method):
+        {UHM_CHOL: self.solve_chol, UHM_LU_PIV: self.solve_lu_piv,
+         UHM_LU_NOPIV: self.solve_lu_nopiv}[method]()
+
+    def get_residual(self) -> float:
+        r = _d(0)
+        self.L.uhm_get_residual_(C.byref(self.h), C.byref(r))
+        self._check()
+        return r.value
+
+    def backward_error(self) -> float:
+        r = _d(0)
+        self._check(self.L.uhm_gpu_backward_error(C.byref(self.h), C.byref(r)))
+        return r.value
+
+    def set_mode(self, mode=0, default_prec=PREC_FP32, tol=1e-12, max_iter=10):
+        self._check(self.L.uhm_gpu_set_mode(C.byref(self.h), mode, default_prec, tol, max_iter))
+
+    def set_front_precision(self, prec_by_element_id):
+        a, p = _arr(prec_by_element_id, np.int32, _i)
+        self._check(self.L.uhm_gpu_set_front_precision(C.byref(self.h), len(a), p))
+
+    def timing(self) -> dict:
+        out = (_d * 8)()
+        self.L.uhm_gpu_get_timing(C.byref(self.h), out)
+        keys = ["upload_ms", "factor_ms", "solve_ms", "refine_ms", "total_ms", "ir_iters",
+                "berr", "kernel_launches"]
+        return dict(zip(keys, list(out)))
+
+    def get_n_dof(self) -> int:
+        n = _i(0)
+        self.L.uhm_get_n_dof_(C.byref(self.h), C.byref(n))
+        return n.value
+
+    def estimate_cost(self, method, n_rhs=1):
+        fd, fs, buf = _d(0), _d(0), _d(0)
+        nnz = C.c_uint(0)
+        self.L.uhm_estimate_cost_(C.byref(self.h), _ip(method), _ip(UHM_REAL), _ip(n_rhs),
+                                  C.byref(fd), C.byref(fs), C.byref(nnz), C.byref(buf))
+        return fd.value, fs.value
+
+    # -- structure ------------------------------------------------------------
+    def fronts(self):
+        n = _i(0)
+        self.L.uhm_gpu_get_n_fronts(C.byref(self.h), C.byref(n))
+        self._check()
+        n = n.value
+        eid, gen, fs, ss = (np.zeros(n, np.int32) for _ in range(4))
+        self.L.uhm_gpu_get_fronts(C.byref(self.h), n, eid.ctypes.data_as(_P(_i)),
+                                  gen.ctypes.data_as(_P(_i)), fs.ctypes.data_as(_P(_i)),
+                                  ss.ctypes.data_as(_P(_i)))
+        return eid, gen, fs, ss
+
+    def front_nodes(self, elt_id, cap=1 << 20):
+        ids = np.zeros(cap, np.int32)
+        nf, ns = _i(0), _i(0)
+        self._check(self.L.uhm_gpu_get_front_nodes(C.byref(self.h), elt_id, cap,
+                                                   ids.ctypes.data_as(_P(_i)), C.byref(nf), C.byref(ns)))
+        return ids[:nf.value], ids[nf.value:nf.value + ns.value]
+
+    def node_solution(self, node_ids, ndof, n_rhs=1):
+        ids, p = _arr(node_ids, np.int32, _i)
+        rows = int(np.asarray(ndof)[ids].sum())
+        out = np.zeros((rows, n_rhs), order="F")
+        self._check(self.L.uhm_gpu_get_node_solution(C.byref(self.h), len(ids), p,
+                                                     out.ctypes.data_as(_P(_d)), rows * n_rhs))
+        return out
+
+    # -- bulk ------------------------------------------------------------------
+    def copy_in_leaves(self, side, buf, nods_all=None):
+        buf = np.ascontiguousarray(buf, dtype=np.float64)
+        np_ = None
+        if nods_all is not None:
+            nods_all, np_ = _arr(nods_all, np.int32, _i)
+        self._check(self.L.uhm_gpu_copy_in_leaves(C.byref(self.h), side, np_,
+                                                  buf.ctypes.data_as(_P(_d)), buf.size))
+
+    def copy_out_leaves(self, n_values, out=None):
+        if out is None:
+            out = np.zeros(n_values)
+        self._check(self.L.uhm_gpu_copy_out_leaves(C.byref(self.h), out.ctypes.data_as(_P(_d)),
+                                                   n_values))
+        return out
+
+
+def pinned_empty(n: int, dtype=np.float64):
+    """numpy array backed by page-locked host memory (freed with the array)."""
+    L = lib()
+    nbytes = int(n) * np.dtype(dtype).itemsize
+    ptr = L.uhm_gpu_host_alloc(max(nbytes, 16))
+    if not ptr:
+        raise MemoryError("uhm_gpu_host_alloc failed")
+    buf = (C.c_char * nbytes).from_address(ptr)
+    arr = np.frombuffer(buf, dtype=dtype, count=n)
+
+    class _Owner:
+        def __del__(self_inner):
+            L.uhm_gpu_host_free(C.c_void_p(ptr))
+    arr_owner = _Owner()
+    arr = arr.view()
+    arr.flags.writeable = True
+    _keep[id(arr)] = arr_owner
+    return arr
+
+
+_keep = {}
+
+
+def load_spec(spec, n_rhs=None, bulk=True, pinned=False):
+    """Feed a uhm_gb300.hpfem.MeshSpec through the Mesh API: nodes, leaf
+    elements (add_element + element_add_node), the tree through
+    add_element(gen) / set_parent / add_child, lock,
+    create_matrix_without_buffer, copy_in of every element matrix and rhs."""
+    n_rhs = spec.n_rhs if n_rhs is None else n_rhs
+    m = Mesh()
+    nods = {}
+    for nid, nd, p in zip(spec.node_id.tolist(), spec.node_ndof.tolist(), spec.node_p.tolist()):
+        nods[nid] = m.add_node(nid, nd, p)
+    elts = []
+    gen = spec.generation.tolist()
+    for e in range(spec.n_elements):
+        elts.append(m.add_element(gen[e]))
+    for e in range(spec.n_leaves):
+        for nid in spec.element_nodes(e).tolist():
+            m.element_add_node(elts[e], nods[nid])
+    for e in range(spec.n_elements):
+        for c in spec.children(e).tolist():
+            m.set_parent(elts[c], elts[e])
+            m.add_child(elts[e], elts[c])
+    m.lock()
+    m.create_matrix_without_buffer(UHM_REAL, n_rhs)
+    m._elts = elts
+    if bulk:
+        nods_all = spec.elem_node.astype(np.int32)
+        m.copy_in_leaves(UHM_LHS, spec.mats, nods_all)
+        m.copy_in_leaves(UHM_RHS, spec.rhs)
+    else:
+        for e in range(spec.n_leaves):
+            nl = spec.element_nodes(e)
+            m.copy_in(elts[e], nl, UHM_LHS, spec.element_matrix(e))
+            m.copy_in(elts[e], nl, UHM_RHS, spec.element_rhs(e))
+    return m

@@ -1,0 +1,294 @@
+// C ABI of include/uhm_gb300.h: the reference's Fortran interface
+// (UHM/src/wrapper/fort.cxx:47-321) plus the uhm_gpu_* additions.
+#include "../../include/uhm_gb300.h"
+
+#include <omp.h>
+#include <sys/time.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+#include "mesh.hpp"
+
+using uhm::Element;
+using uhm::Mesh;
+using uhm::Node;
+
+namespace {
+int g_hier_block = 256;          // UHM/src/matrix/uhm/matrix.cxx:39-42 default
+double g_flop = 0.0;
+double g_buffer = 0.0, g_buffer_max = 0.0;
+thread_local std::string g_err;  // errors raised before a mesh exists
+
+Mesh M(long* h) { return reinterpret_cast<Mesh>(*h); }
+
+void set_err(Mesh m, const std::string& msg, int code) {
+  g_err = msg;
+  if (m) {
+    m->eng().status = code ? code : (m->eng().status ? m->eng().status : 30);
+    m->eng().last_error = msg;
+  }
+  std::fprintf(stderr, "uhm_gb300: %s\n", msg.c_str());
+}
+
+template <class F>
+int guard(Mesh m, F&& f) {
+  try {
+    f();
+    return m && m->engine ? m->engine->status : 0;
+  } catch (const std::exception& e) {
+    set_err(m, e.what(), m && m->engine && m->engine->status ? m->engine->status : 30);
+    return m && m->engine ? m->engine->status : 30;
+  }
+}
+
+void account_flops(Mesh m, int method, bool factor) {
+  double dec = 0, sol = 0, buf = 0;
+  unsigned nnz = 0;
+  m->estimate_cost(method, m->datatype, m->n_rhs, dec, sol, nnz, buf);
+  g_flop += factor ? dec : sol;
+  if (factor) {
+    g_buffer = buf;
+    g_buffer_max = std::max(g_buffer_max, buf);
+  }
+}
+}  // namespace
+
+extern "C" {
+
+void uhm_initialize_fla_(void) {}
+void uhm_finalize_fla_(void) {}
+void uhm_set_num_threads_(int* n) { if (n && *n > 0) omp_set_num_threads(*n); }
+void uhm_get_num_threads_(int* n) { *n = omp_get_max_threads(); }
+void uhm_set_hier_block_size_(int* s) { if (s && *s > 0) g_hier_block = *s; }
+void uhm_get_hier_block_size_(int* s) { *s = g_hier_block; }
+void uhm_reset_flop_(void) { g_flop = 0.0; }
+void uhm_get_flop_(double* f) { *f = g_flop; }
+void uhm_get_buffer_used_(double* b) { *b = g_buffer; }
+void uhm_get_max_buffer_used_(double* b) { *b = g_buffer_max; }
+void uhm_is_multithreading_enable_(int* f) { *f = 1; }
+void uhm_is_hier_matrix_enable_(int* f) { *f = 1; }
+void uhm_timer_(double* t) {
+  timeval tv;
+  gettimeofday(&tv, nullptr);
+  *t = tv.tv_sec + tv.tv_usec * 1e-6;
+}
+
+void uhm_mesh_create_(long* mesh) { *mesh = reinterpret_cast<long>(new uhm::Mesh_()); }
+void uhm_mesh_delete_(long* mesh) {
+  delete M(mesh);
+  *mesh = 0;
+}
+void uhm_add_element_(long* mesh, long* elt) {
+  guard(M(mesh), [&] { *elt = reinterpret_cast<long>(M(mesh)->add_element()); });
+}
+void uhm_add_node_(long* mesh, int* id, int* phy, int* n_dof, int* p, long* nod) {
+  guard(M(mesh), [&] { *nod = reinterpret_cast<long>(M(mesh)->add_node(std::make_pair(*id, *phy), *n_dof, *p)); });
+}
+void uhm_element_add_node_(long* elt, long* nod) {
+  reinterpret_cast<Element>(*elt)->add_node(reinterpret_cast<Node>(*nod));
+}
+void uhm_copy_in_(long* mesh, long* elt, int* dt, int* mm, int* nn, int* node_disp, int* nods,
+                  int* side, double* buffer) {
+  guard(M(mesh), [&] {
+    M(mesh)->copy_in(reinterpret_cast<Element>(*elt), *dt, *mm, *nn, *node_disp, nods, *side, buffer);
+  });
+}
+void uhm_copy_out_(long* mesh, long* elt, int* dt, int* mm, int* nn, int* node_disp, int* nods,
+                   int* side, double* buffer) {
+  guard(M(mesh), [&] {
+    M(mesh)->copy_out(reinterpret_cast<Element>(*elt), *dt, *mm, *nn, *node_disp, nods, *side, buffer);
+  });
+}
+void uhm_mesh_disp_(long* mesh) {
+  Mesh m = M(mesh);
+  std::printf("-Mesh-\n  n_nodes [ %d ], n_elements [ %d ], locked [ %d ]\n", m->get_n_nodes(),
+              m->get_n_elements(), m->is_locked());
+}
+void uhm_get_n_dof_(long* mesh, int* n) { *n = (int)M(mesh)->get_n_dof(); }
+void uhm_get_n_nonzero_(long* mesh, int* n) { *n = (int)M(mesh)->get_n_nonzero(); }
+void uhm_estimate_cost_(long* mesh, int* method, int* dt, int* n_rhs, double* fd, double* fs,
+                        unsigned* nnz, double* buf) {
+  M(mesh)->estimate_cost(*method, *dt, *n_rhs, *fd, *fs, *nnz, *buf);
+}
+void uhm_mesh_import_(long* mesh, char* filename) {
+  guard(M(mesh), [&] {
+    if (!M(mesh)->import_file(filename)) throw std::runtime_error("import_file failed");
+  });
+}
+void uhm_build_tree_(long* mesh) {
+  set_err(M(mesh), "build_tree: METIS-based tree construction is not part of this library; "
+                   "build the tree with uhm_gpu_add_element_with_generation / uhm_gpu_element_set_parent", 30);
+}
+void uhm_create_matrix_without_buffer_(long* mesh, int* dt, int* n_rhs) {
+  guard(M(mesh), [&] { M(mesh)->create_matrix_without_buffer(*dt, *n_rhs); });
+}
+void uhm_create_leaf_matrix_buffer_(long* mesh) { M(mesh)->create_leaf_matrix_buffer(); }
+void uhm_create_element_matrix_buffer_(long* mesh, int* is_schur) {
+  M(mesh)->create_element_matrix_buffer(*is_schur);
+}
+void uhm_set_rhs_(long* mesh) { M(mesh)->set_rhs(); }
+void uhm_lock_(long* mesh) { guard(M(mesh), [&] { M(mesh)->lock(); }); }
+void uhm_unlock_(long* mesh) { guard(M(mesh), [&] { M(mesh)->unlock(); }); }
+
+void uhm_chol_with_free_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->chol_with_free(); account_flops(M(mesh), uhm::UHM_CHOL, true); });
+}
+void uhm_lu_nopiv_with_free_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->lu_nopiv_with_free(); account_flops(M(mesh), uhm::UHM_LU_NOPIV, true); });
+}
+void uhm_lu_piv_with_free_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->lu_piv_with_free(); account_flops(M(mesh), uhm::UHM_LU_PIV, true); });
+}
+void uhm_solve_chol_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->solve_chol(); account_flops(M(mesh), uhm::UHM_CHOL, false); });
+}
+void uhm_solve_lu_nopiv_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->solve_lu_nopiv(); account_flops(M(mesh), uhm::UHM_LU_NOPIV, false); });
+}
+void uhm_solve_lu_piv_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->solve_lu_piv(); account_flops(M(mesh), uhm::UHM_LU_PIV, false); });
+}
+void uhm_check_chol_(long* mesh) { M(mesh)->check_chol(); }
+void uhm_check_lu_nopiv_(long* mesh) { M(mesh)->check_lu_nopiv(); }
+void uhm_check_lu_piv_(long* mesh) { M(mesh)->check_lu_piv(); }
+void uhm_get_residual_(long* mesh, double* res) {
+  guard(M(mesh), [&] { *res = M(mesh)->get_residual(); });
+}
+
+// ---- Part 2 ---------------------------------------------------------------
+int uhm_gpu_add_element_with_generation(long* mesh, int* gen, long* elt) {
+  return guard(M(mesh), [&] { *elt = reinterpret_cast<long>(M(mesh)->add_element(*gen)); });
+}
+int uhm_gpu_element_set_parent(long* elt, long* parent) {
+  try {
+    reinterpret_cast<Element>(*elt)->set_parent(reinterpret_cast<Element>(*parent));
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 7;
+  }
+}
+int uhm_gpu_element_add_child(long* elt, long* child) {
+  reinterpret_cast<Element>(*elt)->add_child(reinterpret_cast<Element>(*child));
+  return 0;
+}
+int uhm_gpu_get_status(long* mesh) {
+  Mesh m = M(mesh);
+  return m && m->engine ? m->engine->status : 0;
+}
+int uhm_gpu_get_last_error(long* mesh, char* buf, int len) {
+  Mesh m = M(mesh);
+  std::string s = m && m->engine && !m->engine->last_error.empty() ? m->engine->last_error : g_err;
+  if (len > 0) {
+    std::strncpy(buf, s.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)s.size();
+}
+int uhm_gpu_set_mode(long* mesh, int mode, int default_prec, double tol, int max_iter) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    if (e.mode != mode || e.default_prec != default_prec) e.invalidate_plan();
+    e.mode = mode;
+    e.default_prec = default_prec;
+    e.ir_tol = tol;
+    e.ir_max = max_iter;
+  });
+}
+int uhm_gpu_set_front_precision(long* mesh, int n, const int* prec) {
+  return guard(M(mesh), [&] {
+    uhm::Mesh_* m = M(mesh);
+    uhm::Engine& e = m->eng();
+    e.ensure_plan();
+    e.front_prec_override.assign(e.fronts.size(), -1);
+    for (auto& f : e.fronts) {
+      int id = f.e->get_id();
+      if (id < n) e.front_prec_override[f.slot] = prec[id];
+    }
+    e.invalidate_plan();
+  });
+}
+int uhm_gpu_copy_in_leaves(long* mesh, int side, const int* nods_all, const double* buffer,
+                           long n_values) {
+  return guard(M(mesh), [&] {
+    uhm::Mesh_* m = M(mesh);
+    uhm::Engine& e = m->eng();
+    e.ensure_plan();
+    if (nods_all) e.set_leaf_nodes(nods_all);
+    e.copy_in_leaves(side, buffer, n_values);
+  });
+}
+int uhm_gpu_copy_out_leaves(long* mesh, double* buffer, long n_values) {
+  return guard(M(mesh), [&] { M(mesh)->eng().copy_out_leaves(buffer, n_values); });
+}
+int uhm_gpu_get_node_solution(long* mesh, int n_nodes, const int* ids, double* out, long n_values) {
+  return guard(M(mesh), [&] { M(mesh)->eng().node_solution(n_nodes, ids, out, n_values); });
+}
+int uhm_gpu_backward_error(long* mesh, double* berr) {
+  return guard(M(mesh), [&] { *berr = M(mesh)->eng().backward_error(); });
+}
+int uhm_gpu_get_timing(long* mesh, double* out) {
+  return guard(M(mesh), [&] {
+    const uhm::Timing& t = M(mesh)->eng().timing;
+    out[0] = t.upload_ms;
+    out[1] = t.factor_ms;
+    out[2] = t.solve_ms;
+    out[3] = t.refine_ms;
+    out[4] = t.total_ms;
+    out[5] = t.ir_iters;
+    out[6] = t.berr;
+    out[7] = (double)t.kernel_launches;
+  });
+}
+int uhm_gpu_get_n_fronts(long* mesh, int* n) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    e.ensure_plan();
+    *n = (int)e.fronts.size();
+  });
+}
+int uhm_gpu_get_fronts(long* mesh, int n, int* eid, int* gen, int* fs, int* ss) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    e.ensure_plan();
+    for (int i = 0; i < n && i < (int)e.fronts.size(); ++i) {
+      eid[i] = e.fronts[i].e->get_id();
+      gen[i] = e.fronts[i].e->get_generation();
+      fs[i] = e.fronts[i].fs;
+      ss[i] = e.fronts[i].ss;
+    }
+  });
+}
+int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* nf, int* ns) {
+  return guard(M(mesh), [&] {
+    Element e = M(mesh)->find_element(elt_id);
+    if (!e) throw std::invalid_argument("no such element");
+    int k = 0;
+    for (auto& pr : e->factor)
+      if (k < cap) ids[k++] = pr.first->get_id().first;
+    for (auto& pr : e->schur)
+      if (k < cap) ids[k++] = pr.first->get_id().first;
+    *nf = (int)e->factor.size();
+    *ns = (int)e->schur.size();
+  });
+}
+void* uhm_gpu_host_alloc(long bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+void uhm_gpu_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,890 @@
+// Host side of the device engine: plan (front table, extend-add maps, launch
+// program), HBM arenas, element staging, factor / solve / residual drivers.
+#include "engine.hpp"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <unordered_map>
+
+namespace uhm {
+using namespace uhm_gpu;
+
+static constexpr int SMALL_MAX_F64 = 160;   // whole front in shared memory (200 KB)
+static constexpr int SMALL_MAX_F32 = 224;
+static constexpr int NB = 64;               // panel width of the blocked kernels
+static constexpr int ASM_TJ = 16;           // assembly column tile (k_factor.cu)
+static constexpr int TRSM_RB = 64;
+static constexpr int GEMV_RB = 256;
+static constexpr int LUROW_CB = 64;
+static constexpr int TILE = 64;             // trailing-update tile (k_tile_update)
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t e_ = (x);                                                              \
+    if (e_ != cudaSuccess)                                                             \
+      throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+Engine::Engine(Mesh_* m) : mesh(m) {}
+
+Engine::~Engine() {
+  try {
+    free_device();
+  } catch (...) {
+  }
+  release_staging();
+  if (stream) cudaStreamDestroy(stream);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+}
+
+void Engine::fail(const std::string& msg, int code) {
+  status = code;
+  last_error = msg;
+  throw std::runtime_error(msg);
+}
+
+void* Engine::dmalloc(size_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail("device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e), 4);
+  }
+  allocations.push_back(p);
+  return p;
+}
+
+void Engine::free_device() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (void* p : allocations) cudaFree(p);
+  allocations.clear();
+  dev_ok = false;
+  ctx = DevCtx{};
+  d_items = nullptr;
+  d_b = d_x = d_r = d_d = d_erhs = d_y = d_red = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// plan: fronts in leaf -> root order, grouped by generation
+// ---------------------------------------------------------------------------
+void Engine::ensure_plan() {
+  if (plan_ok) return;
+  if (!mesh->is_locked()) fail("mesh is not locked", 5);
+  fronts.clear();
+  levels.clear();
+  int slot = 0;
+  for (auto& kv : mesh->by_generation) {
+    levels.emplace_back();
+    for (Element e : kv.second) {
+      if (!e->is_matrix_created()) fail("create_matrix_without_buffer has not been called", 5);
+      HostFront hf;
+      hf.e = e;
+      hf.slot = slot;
+      e->slot = slot;
+      hf.level = (int)levels.size() - 1;
+      std::pair<int, int> d = e->get_n_dof();
+      hf.fs = d.first;
+      hf.ss = d.second;
+      hf.n = hf.fs + hf.ss;
+      hf.g0 = e->factor.empty() ? 0 : e->factor[0].first->get_offset();
+      int o = hf.g0;
+      for (auto& pr : e->factor) {
+        if (pr.first->get_offset() != o) fail("factor dofs of a front are not contiguous", 6);
+        o += pr.first->get_n_dof();
+      }
+      fronts.push_back(hf);
+      levels.back().push_back(slot);
+      ++slot;
+    }
+  }
+  n_global = 0;
+  for (auto& f : fronts) {
+    f.parent = f.e->parent ? f.e->parent->slot : -1;
+    f.children.clear();
+    for (Element c : f.e->children) f.children.push_back(c->slot);
+    n_global += f.fs;
+  }
+  // element staging: one slot per leaf (matrix m*m and rhs m*n_rhs)
+  esrc.clear();
+  esrc_of_slot.assign(fronts.size(), -1);
+  emat_total = erhs_total = 0;
+  const int nr = mesh->n_rhs;
+  for (Element e : mesh->leaves) {
+    ElemSource es;
+    es.e = e;
+    es.slot = e->slot;
+    int m = 0;
+    for (auto& kv : e->nodes) m += kv.first->get_n_dof();
+    es.m = m;
+    es.mat_off = emat_total;
+    es.rhs_off = erhs_total;
+    emat_total += (int64_t)m * m;
+    erhs_total += (int64_t)m * nr;
+    esrc_of_slot[e->slot] = (int)esrc.size();
+    esrc.push_back(std::move(es));
+  }
+  size_t need = (size_t)(emat_total + erhs_total) * sizeof(double);
+  if (need > h_pinned_bytes || !h_pinned) {
+    release_staging();
+    // page-locked staging; plain host memory when no device is present
+    // (symbolic analysis and structure queries need no GPU)
+    if (cudaMallocHost((void**)&h_pinned, std::max<size_t>(need, 64)) != cudaSuccess) {
+      cudaGetLastError();
+      h_pinned = (double*)std::malloc(std::max<size_t>(need, 64));
+      h_pinned_is_malloc = true;
+      if (!h_pinned) fail("host allocation failed", 4);
+    }
+    h_pinned_bytes = need;
+  }
+  emat_dirty = erhs_dirty = true;
+  anorm_inf = -1.0;
+  plan_ok = true;
+  dev_ok = false;
+  factored = false;
+  h_x_valid = false;
+}
+
+void Engine::release_staging() {
+  if (!h_pinned) return;
+  if (h_pinned_is_malloc) std::free(h_pinned);
+  else cudaFreeHost(h_pinned);
+  h_pinned = nullptr;
+  h_pinned_is_malloc = false;
+  h_pinned_bytes = 0;
+}
+
+static std::unordered_map<Node, int> front_positions(Element e) {
+  std::unordered_map<Node, int> pos;
+  int fs = 0;
+  for (auto& pr : e->factor) { pos[pr.first] = pr.second; fs += pr.first->get_n_dof(); }
+  for (auto& pr : e->schur) pos[pr.first] = fs + pr.second;
+  return pos;
+}
+
+// ---------------------------------------------------------------------------
+// copy_in / copy_out  (Mesh_::copy_in / copy_out, UHM/src/mesh/interf.cxx:108-204)
+// ---------------------------------------------------------------------------
+void Engine::element_map(Element e, int nod_disp, const int* nods,
+                         std::vector<std::pair<int, int>>& order, std::vector<int>& pos,
+                         std::vector<int32_t>& gd) {
+  order.clear();
+  pos.clear();
+  gd.clear();
+  auto fpos = front_positions(e);
+  for (int i = 0; i < e->get_n_nodes(); ++i) {
+    std::pair<int, int> id = nod_disp == UHM_PHYSICS_MULTI ? std::make_pair(nods[2 * i], nods[2 * i + 1])
+                                                           : std::make_pair(nods[i], 0);
+    Node nd = mesh->find_node(id);
+    if (!nd) fail("copy_in: cannot find node in the mesh", 7);
+    order.push_back(id);
+    if (!nd->get_n_dof()) continue;
+    auto it = fpos.find(nd);
+    if (it == fpos.end()) fail("copy_in: node does not belong to the element", 7);
+    for (int k = 0; k < nd->get_n_dof(); ++k) {
+      pos.push_back(it->second + k);
+      gd.push_back(nd->get_offset() + k);
+    }
+  }
+}
+
+void Engine::set_leaf_nodes(const int* nods_all) {
+  ensure_plan();
+  int64_t k = 0;
+  for (auto& es : esrc) {
+    std::vector<std::pair<int, int>> order;
+    std::vector<int> pos;
+    std::vector<int32_t> gd;
+    element_map(es.e, UHM_PHYSICS_SINGLE, nods_all + k, order, pos, gd);
+    k += es.e->get_n_nodes();
+    if ((int)pos.size() != es.m) fail("set_leaf_nodes: element size mismatch", 7);
+    if (!es.node_order.empty() && es.node_order != order)
+      fail("set_leaf_nodes: node order differs from an earlier copy_in", 7);
+    if (es.node_order.empty()) dev_ok = false;
+    es.node_order = order;
+    es.pos = pos;
+    es.gdof = gd;
+  }
+}
+
+void Engine::fetch_x() {
+  if (h_x_valid) return;
+  h_x.resize((size_t)n_global * mesh->n_rhs);
+  CK(cudaMemcpyAsync(h_x.data(), d_x, sizeof(double) * h_x.size(), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  h_x_valid = true;
+}
+
+void Engine::node_solution(int n_nodes, const int* ids, double* out, int64_t n_values) {
+  ensure_plan();
+  if (!factored) fail("node_solution: nothing solved", 9);
+  fetch_x();
+  const int nr = mesh->n_rhs;
+  int64_t rows = 0;
+  for (int i = 0; i < n_nodes; ++i) {
+    Node nd = mesh->find_node(ids[i]);
+    if (!nd) fail("node_solution: unknown node", 7);
+    rows += nd->get_n_dof();
+  }
+  if (rows * nr != n_values) fail("node_solution: size mismatch", 7);
+  int64_t r = 0;
+  for (int i = 0; i < n_nodes; ++i) {
+    Node nd = mesh->find_node(ids[i]);
+    for (int k = 0; k < nd->get_n_dof(); ++k, ++r)
+      for (int q = 0; q < nr; ++q) out[r + q * rows] = h_x[(size_t)(nd->get_offset() + k) + (size_t)q * n_global];
+  }
+}
+
+void Engine::copy_in(Element e, int m, int n, int nod_disp, const int* nods, int side,
+                     const double* buf) {
+  ensure_plan();
+  if (m <= 0 || n <= 0) fail("copy_in: dimension is null", 7);
+  std::vector<std::pair<int, int>> order;
+  std::vector<int> pos;
+  std::vector<int32_t> gd;
+  element_map(e, nod_disp, nods, order, pos, gd);
+  if ((int)pos.size() != m) fail("copy_in: m does not match the element's dofs", 7);
+  int ei = esrc_of_slot[e->slot];
+  if (ei < 0) fail("copy_in: only leaf elements carry element matrices in this engine", 7);
+  ElemSource& es = esrc[ei];
+  if (es.m != m) fail("copy_in: size mismatch", 7);
+  bool first = es.node_order.empty();
+  std::vector<int> perm;   // user row -> stored row
+  if (first) {
+    es.node_order = order;
+    es.pos = pos;
+    es.gdof = gd;
+  } else if (order != es.node_order) {
+    std::unordered_map<int, int> row_of;
+    for (int r = 0; r < m; ++r) row_of[es.pos[r]] = r;
+    perm.resize(m);
+    for (int r = 0; r < m; ++r) perm[r] = row_of[pos[r]];
+  }
+  auto rowmap = [&](int r) { return perm.empty() ? r : perm[r]; };
+  if (side == UHM_LHS) {
+    double* dst = h_pinned + es.mat_off;
+    if (!es.has_lhs) std::memset(dst, 0, sizeof(double) * (size_t)m * m);
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) dst[rowmap(i) + (int64_t)rowmap(j) * m] += buf[i + (int64_t)j * m];
+    es.has_lhs = true;
+    emat_dirty = true;
+    anorm_inf = -1.0;
+    dev_ok = dev_ok && !first;   // maps change when an element appears
+    factored = false;
+  } else {
+    if (n != mesh->n_rhs) fail("copy_in: n_rhs mismatch", 7);
+    double* dst = h_pinned + emat_total + es.rhs_off;
+    if (!es.has_rhs) std::memset(dst, 0, sizeof(double) * (size_t)m * n);
+    for (int q = 0; q < n; ++q)
+      for (int i = 0; i < m; ++i) dst[rowmap(i) + (int64_t)q * m] += buf[i + (int64_t)q * m];
+    es.has_rhs = true;
+    erhs_dirty = true;
+    if (first) dev_ok = false;
+  }
+}
+
+void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
+  ensure_plan();
+  for (auto& es : esrc)
+    if (es.node_order.empty()) fail("copy_in_leaves: element maps unknown (call uhm_gpu_set_leaf_nodes first)", 7);
+  if (side == UHM_LHS) {
+    if (n_values != emat_total) fail("copy_in_leaves: size mismatch", 7);
+    if (!dev_ok) {
+      std::memcpy(h_pinned, buf, sizeof(double) * (size_t)emat_total);
+      for (auto& es : esrc) es.has_lhs = true;
+      emat_dirty = true;
+    } else {
+      CK(cudaMemcpyAsync(ctx.emat, buf, sizeof(double) * (size_t)emat_total, cudaMemcpyHostToDevice, stream));
+      emat_dirty = false;
+    }
+    factored = false;
+    anorm_inf = -1.0;
+  } else {
+    if (n_values != erhs_total) fail("copy_in_leaves: size mismatch", 7);
+    if (!dev_ok) {
+      std::memcpy(h_pinned + emat_total, buf, sizeof(double) * (size_t)erhs_total);
+      for (auto& es : esrc) es.has_rhs = true;
+      erhs_dirty = true;
+    } else {
+      CK(cudaMemcpyAsync(d_erhs, buf, sizeof(double) * (size_t)erhs_total, cudaMemcpyHostToDevice, stream));
+      erhs_dirty = false;
+    }
+  }
+}
+
+void Engine::copy_out(Element e, int m, int n, int nod_disp, const int* nods, int side, double* buf) {
+  ensure_plan();
+  if (side != UHM_RHS) fail("copy_out: only the solution (UHM_RHS) is supported", 7);
+  if (!factored) fail("copy_out: nothing solved", 9);
+  fetch_x();
+  int r = 0;
+  for (int i = 0; i < e->get_n_nodes(); ++i) {
+    std::pair<int, int> id = nod_disp == UHM_PHYSICS_MULTI ? std::make_pair(nods[2 * i], nods[2 * i + 1])
+                                                           : std::make_pair(nods[i], 0);
+    Node nd = mesh->find_node(id);
+    if (!nd) fail("copy_out: cannot find node in the mesh", 7);
+    for (int k = 0; k < nd->get_n_dof(); ++k, ++r) {
+      if (r >= m) fail("copy_out: m too small", 7);
+      for (int q = 0; q < n && q < mesh->n_rhs; ++q)
+        buf[r + (int64_t)q * m] = h_x[(size_t)(nd->get_offset() + k) + (size_t)q * n_global];
+    }
+  }
+}
+
+void Engine::copy_out_leaves(double* buf, int64_t n_values) {
+  ensure_plan();
+  if (n_values != erhs_total) fail("copy_out_leaves: size mismatch", 7);
+  const int nr = mesh->n_rhs;
+  if (!factored) fail("copy_out_leaves: nothing solved", 9);
+  fetch_x();
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)esrc.size(); ++k) {
+    const ElemSource& es = esrc[k];
+    double* dst = buf + es.rhs_off;
+    for (int q = 0; q < nr; ++q)
+      for (int r = 0; r < es.m; ++r) dst[r + (int64_t)q * es.m] = h_x[(size_t)es.gdof[r] + (size_t)q * n_global];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// sources, maps and launch programs
+// ---------------------------------------------------------------------------
+int64_t Engine::add_items(const std::vector<Item>& it) {
+  int64_t off = (int64_t)h_items.size();
+  h_items.insert(h_items.end(), it.begin(), it.end());
+  return off;
+}
+
+void Engine::build_plan(int method) {
+  (void)method;
+  const int nr = mesh->n_rhs;
+  // precision per front
+  for (auto& f : fronts) {
+    int p = PREC_FP64;
+    if (mode == 1) {
+      p = default_prec;
+      if ((int)front_prec_override.size() > f.slot && front_prec_override[f.slot] >= 0)
+        p = front_prec_override[f.slot];
+    }
+    f.prec = p;
+  }
+  arena64_n = arena32_n = vec_n = piv_n = 0;
+  h_fronts.assign(fronts.size(), FrontDev{});
+  h_srcs.clear();
+  h_inv.clear();
+  h_colptr.clear();
+  h_colsrc.clear();
+  h_sgi.clear();
+  std::vector<std::unordered_map<Node, int>> fpos(fronts.size());
+  for (auto& f : fronts) fpos[f.slot] = front_positions(f.e);
+  // arena and slab offsets
+  for (auto& f : fronts) {
+    const int n = f.n;
+    const int dt = f.prec == PREC_FP64 ? F64 : F32;
+    int64_t& an = dt == F64 ? arena64_n : arena32_n;
+    f.off = an;
+    an += ((int64_t)n * n + 63) / 64 * 64;
+    f.voff = vec_n;
+    vec_n += (int64_t)n * nr;
+    f.piv_off = piv_n;
+    piv_n += f.fs;
+  }
+  // assembly sources in summation order: the element matrix (copy_in), then
+  // the children in child order (op_merge, UHM/src/operation/element.cxx:150-162)
+  for (auto& f : fronts) {
+    const int n = f.n;
+    f.src0 = (int)h_srcs.size();
+    std::vector<std::vector<int32_t>> invs;
+    const int ei = esrc_of_slot[f.slot];
+    if (ei >= 0 && esrc[ei].has_lhs) {
+      const ElemSource& es = esrc[ei];
+      SrcDev sd{};
+      sd.off = es.mat_off;
+      sd.ld = es.m;
+      sd.dtype = F64;
+      sd.is_child = 0;
+      sd.slot = ei;
+      h_srcs.push_back(sd);
+      std::vector<int32_t> inv(n, -1);
+      for (int r = 0; r < es.m; ++r) inv[es.pos[r]] = r;
+      invs.push_back(std::move(inv));
+    }
+    for (int cs : f.children) {
+      const HostFront& c = fronts[cs];
+      SrcDev sd{};
+      sd.off = c.off + c.fs + (int64_t)c.fs * c.n;
+      sd.ld = c.n;
+      sd.dtype = c.prec == PREC_FP64 ? F64 : F32;
+      sd.is_child = 1;
+      sd.slot = cs;
+      h_srcs.push_back(sd);
+      std::vector<int32_t> inv(n, -1);
+      int r = 0;
+      for (auto& pr : c.e->schur) {
+        auto it = fpos[f.slot].find(pr.first);
+        if (it == fpos[f.slot].end()) fail("child schur node missing in parent", 6);
+        for (int k = 0; k < pr.first->get_n_dof(); ++k, ++r) inv[it->second + k] = r;
+      }
+      invs.push_back(std::move(inv));
+    }
+    f.nsrc = (int)invs.size();
+    f.inv_off = (int64_t)h_inv.size();
+    for (auto& v : invs) h_inv.insert(h_inv.end(), v.begin(), v.end());
+    f.colptr_off = (int64_t)h_colptr.size();
+    for (int J = 0; J < n; ++J) {
+      h_colptr.push_back((int64_t)h_colsrc.size());
+      for (int s2 = 0; s2 < (int)invs.size(); ++s2)
+        if (invs[s2][J] >= 0) h_colsrc.push_back(make_int2(s2, invs[s2][J]));
+    }
+    h_colptr.push_back((int64_t)h_colsrc.size());
+    f.sgi_off = (int64_t)h_sgi.size();
+    for (auto& pr : f.e->schur)
+      for (int k = 0; k < pr.first->get_n_dof(); ++k) h_sgi.push_back(pr.first->get_offset() + k);
+  }
+  for (auto& f : fronts) {
+    FrontDev& d = h_fronts[f.slot];
+    d.off = f.off;
+    d.voff = f.voff;
+    d.inv_off = f.inv_off;
+    d.colptr_off = f.colptr_off;
+    d.sgi_off = f.sgi_off;
+    d.piv_off = f.piv_off;
+    d.n = f.n;
+    d.fs = f.fs;
+    d.ss = f.ss;
+    d.dtype = f.prec == PREC_FP64 ? F64 : F32;
+    d.g0 = f.g0;
+    d.src0 = f.src0;
+    d.nsrc = f.nsrc;
+    d.status_slot = f.slot;
+  }
+  // element residual tables (elements with a matrix, in leaf order)
+  h_emat_off.clear();
+  h_elem_m.clear();
+  h_emap_off.clear();
+  h_emap.clear();
+  h_y_off.clear();
+  y_total = 0;
+  for (auto& es : esrc) {
+    h_emat_off.push_back(es.mat_off);
+    h_elem_m.push_back(es.m);
+    h_emap_off.push_back((int64_t)h_emap.size());
+    if ((int)es.gdof.size() == es.m) h_emap.insert(h_emap.end(), es.gdof.begin(), es.gdof.end());
+    else h_emap.insert(h_emap.end(), es.m, 0);
+    h_y_off.push_back(es.rhs_off);
+  }
+  y_total = erhs_total;
+}
+
+void Engine::build_programs(int method) {
+  const bool chol = method == UHM_CHOL;
+  const int nr = mesh->n_rhs;
+  h_items.clear();
+  fac_ops.clear();
+  fwd_ops.clear();
+  bwd_ops.clear();
+  auto push = [&](std::vector<Op>& ops, int kind, int dtype, int nb, int param, const std::vector<Item>& it) {
+    if (it.empty()) return;
+    Op op{kind, dtype, nb, param, add_items(it), (int)it.size()};
+    ops.push_back(op);
+  };
+  const int small_max[2] = {SMALL_MAX_F64, SMALL_MAX_F32};
+  for (auto& lv : levels) {
+    for (int dt = 0; dt < 2; ++dt) {
+      std::vector<int> fl;
+      for (int s : lv)
+        if (h_fronts[s].dtype == dt) fl.push_back(s);
+      if (fl.empty()) continue;
+      std::vector<Item> asm_items, small_items;
+      std::vector<int> large;
+      int max_small = 1;
+      for (int s : fl) {
+        const int n = fronts[s].n;
+        for (int J0 = 0; J0 < n; J0 += ASM_TJ) asm_items.push_back(Item{s, J0, 0, 0});
+        if (n <= small_max[dt]) {
+          small_items.push_back(Item{s, 0, 0, 0});
+          max_small = std::max(max_small, n);
+        } else {
+          large.push_back(s);
+        }
+      }
+      push(fac_ops, OP_ASSEMBLE, dt, 0, chol ? 1 : 0, asm_items);
+      push(fac_ops, OP_SMALL_FACTOR, dt, 0, max_small, small_items);
+      int maxfs = 0;
+      for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
+      for (int k0 = 0; k0 < maxfs; k0 += NB) {
+        std::vector<Item> p_items, t_items, u_items;
+        for (int s : large) {
+          const HostFront& f = fronts[s];
+          if (f.fs <= k0) continue;
+          const int kb = std::min(NB, f.fs - k0);
+          const int base = k0 + kb;
+          p_items.push_back(Item{s, k0, 0, 0});
+          if (chol) {
+            for (int r0 = base; r0 < f.n; r0 += TRSM_RB) t_items.push_back(Item{s, k0, r0, 0});
+            const int T = (f.n - base + TILE - 1) / TILE;
+            for (int ti = 0; ti < T; ++ti)
+              for (int tj = 0; tj <= ti; ++tj) u_items.push_back(Item{s, k0, ti, tj});
+          } else {
+            for (int c0 = base; c0 < f.n; c0 += LUROW_CB) t_items.push_back(Item{s, k0, c0, 0});
+            const int T = (f.n - base + TILE - 1) / TILE;
+            for (int ti = 0; ti < T; ++ti)
+              for (int tj = 0; tj < T; ++tj) u_items.push_back(Item{s, k0, ti, tj});
+          }
+        }
+        if (chol) {
+          push(fac_ops, OP_POTRF, dt, NB, 0, p_items);
+          push(fac_ops, OP_TRSM, dt, NB, 0, t_items);
+          push(fac_ops, OP_SYRK, dt, NB, 0, u_items);
+        } else {
+          push(fac_ops, OP_GETRF, dt, NB, method == UHM_LU_PIV ? 1 : 0, p_items);
+          push(fac_ops, OP_LUROW, dt, NB, 0, t_items);
+          push(fac_ops, OP_GEMM, dt, NB, 0, u_items);
+        }
+      }
+    }
+  }
+  // solve programs
+  const int gm = chol ? M_CHOL : (method == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV);
+  auto solve_small = [&](const HostFront& f, int dt) {
+    return f.n <= small_max[dt] && (int64_t)f.n * nr <= 8192;
+  };
+  for (auto& lv : levels) {
+    std::vector<Item> g_items;
+    for (int s : lv) g_items.push_back(Item{s, 0, 0, 0});
+    push(fwd_ops, OP_FWD_GATHER, 0, 0, gm, g_items);
+    for (int dt = 0; dt < 2; ++dt) {
+      std::vector<Item> sm;
+      std::vector<int> large;
+      for (int s : lv) {
+        if (h_fronts[s].dtype != dt) continue;
+        if (solve_small(fronts[s], dt)) sm.push_back(Item{s, 0, 0, 0});
+        else large.push_back(s);
+      }
+      push(fwd_ops, OP_FWD_SMALL, dt, 0, gm, sm);
+      int maxfs = 0;
+      for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
+      for (int k0 = 0; k0 < maxfs; k0 += NB) {
+        std::vector<Item> tv, gv;
+        for (int s : large) {
+          const HostFront& f = fronts[s];
+          if (f.fs <= k0) continue;
+          const int kb = std::min(NB, f.fs - k0);
+          tv.push_back(Item{s, k0, 0, 0});
+          for (int r0 = k0 + kb; r0 < f.n; r0 += GEMV_RB) gv.push_back(Item{s, k0, r0, 0});
+        }
+        push(fwd_ops, OP_TRSV_F, dt, NB, gm, tv);
+        push(fwd_ops, OP_GEMV_F, dt, NB, gm, gv);
+      }
+    }
+  }
+  for (int li = (int)levels.size() - 1; li >= 0; --li) {
+    auto& lv = levels[li];
+    std::vector<Item> p_items;
+    for (int s : lv) p_items.push_back(Item{s, 0, 0, 0});
+    push(bwd_ops, OP_BWD_PREP, 0, 0, gm, p_items);
+    for (int dt = 0; dt < 2; ++dt) {
+      std::vector<Item> sm, st;
+      std::vector<int> large;
+      for (int s : lv) {
+        if (h_fronts[s].dtype != dt) continue;
+        if (solve_small(fronts[s], dt)) sm.push_back(Item{s, 0, 0, 0});
+        else { large.push_back(s); st.push_back(Item{s, 0, 0, 0}); }
+      }
+      push(bwd_ops, OP_BWD_SMALL, dt, 0, gm, sm);
+      int maxfs = 0;
+      for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
+      int last = maxfs == 0 ? -1 : ((maxfs - 1) / NB) * NB;
+      for (int k0 = last; k0 >= 0; k0 -= NB) {
+        std::vector<Item> tv;
+        for (int s : large)
+          if (fronts[s].fs > k0) tv.push_back(Item{s, k0, 0, 0});
+        push(bwd_ops, OP_GEMV_B, dt, NB, gm, tv);
+        push(bwd_ops, OP_TRSV_B, dt, NB, gm, tv);
+      }
+      push(bwd_ops, OP_BWD_STORE, dt, 0, gm, st);
+    }
+  }
+  for (auto& f : fronts)
+    if (!solve_small(f, h_fronts[f.slot].dtype) && nr > 16)
+      fail("more than 16 right-hand sides on a large front is not supported", 8);
+}
+
+void Engine::alloc_device(int method) {
+  free_device();
+  if (!stream) {
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+  }
+  const int nr = mesh->n_rhs;
+  ctx.fronts = (FrontDev*)dmalloc(sizeof(FrontDev) * h_fronts.size());
+  ctx.srcs = (SrcDev*)dmalloc(sizeof(SrcDev) * std::max<size_t>(1, h_srcs.size()));
+  ctx.inv = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_inv.size()));
+  ctx.colptr = (int64_t*)dmalloc(sizeof(int64_t) * h_colptr.size());
+  ctx.colsrc = (int2*)dmalloc(sizeof(int2) * std::max<size_t>(1, h_colsrc.size()));
+  ctx.sgi = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_sgi.size()));
+  ctx.piv = (int32_t*)dmalloc(sizeof(int32_t) * std::max<int64_t>(1, piv_n));
+  ctx.a64 = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, arena64_n));
+  ctx.a32 = (float*)dmalloc(sizeof(float) * std::max<int64_t>(1, arena32_n));
+  ctx.emat = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, emat_total));
+  ctx.vec = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, vec_n));
+  ctx.status = (int*)dmalloc(sizeof(int) * fronts.size());
+  ctx.n_rhs = nr;
+  ctx.symmetric = method == UHM_CHOL ? 1 : 0;
+  d_items = (Item*)dmalloc(sizeof(Item) * std::max<size_t>(1, h_items.size()));
+  const size_t gv = sizeof(double) * (size_t)std::max<int64_t>(1, n_global) * nr;
+  d_b = (double*)dmalloc(gv);
+  d_x = (double*)dmalloc(gv);
+  d_r = (double*)dmalloc(gv);
+  d_d = (double*)dmalloc(gv);
+  d_erhs = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, erhs_total));
+  d_y = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, y_total));
+  d_red = (double*)dmalloc(sizeof(double) * 2048);
+  d_emat_off = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, h_emat_off.size()));
+  d_elem_m = (int*)dmalloc(sizeof(int) * std::max<size_t>(1, h_elem_m.size()));
+  d_emap_off = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, h_emap_off.size()));
+  d_emap = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_emap.size()));
+  d_y_off = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, h_y_off.size()));
+  // dof -> (element, row) CSR for the deterministic residual gather
+  std::vector<int64_t> cnt(n_global + 1, 0);
+  for (size_t k = 0; k < esrc.size(); ++k)
+    if ((int)esrc[k].gdof.size() == esrc[k].m)
+      for (int32_t g : esrc[k].gdof) cnt[g + 1]++;
+  for (int64_t i = 0; i < n_global; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> idx(cnt[n_global]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (size_t k = 0; k < esrc.size(); ++k)
+    if ((int)esrc[k].gdof.size() == esrc[k].m)
+      for (int r = 0; r < esrc[k].m; ++r) {
+        const int64_t v = (h_y_off[k] + r) | ((int64_t)esrc[k].m << 40);
+        idx[fill[esrc[k].gdof[r]]++] = v;
+      }
+  d_dof_ptr = (int64_t*)dmalloc(sizeof(int64_t) * cnt.size());
+  d_dof_idx = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, idx.size()));
+  auto up = [&](void* d, const void* h, size_t bytes) {
+    if (bytes) CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, stream));
+  };
+  up(ctx.fronts, h_fronts.data(), sizeof(FrontDev) * h_fronts.size());
+  up(ctx.srcs, h_srcs.data(), sizeof(SrcDev) * h_srcs.size());
+  up(ctx.inv, h_inv.data(), sizeof(int32_t) * h_inv.size());
+  up(ctx.colptr, h_colptr.data(), sizeof(int64_t) * h_colptr.size());
+  up(ctx.colsrc, h_colsrc.data(), sizeof(int2) * h_colsrc.size());
+  up(ctx.sgi, h_sgi.data(), sizeof(int32_t) * h_sgi.size());
+  up(d_items, h_items.data(), sizeof(Item) * h_items.size());
+  up(d_emat_off, h_emat_off.data(), sizeof(int64_t) * h_emat_off.size());
+  up(d_elem_m, h_elem_m.data(), sizeof(int) * h_elem_m.size());
+  up(d_emap_off, h_emap_off.data(), sizeof(int64_t) * h_emap_off.size());
+  up(d_emap, h_emap.data(), sizeof(int32_t) * h_emap.size());
+  up(d_y_off, h_y_off.data(), sizeof(int64_t) * h_y_off.size());
+  up(d_dof_ptr, cnt.data(), sizeof(int64_t) * cnt.size());
+  up(d_dof_idx, idx.data(), sizeof(int64_t) * idx.size());
+  CK(cudaStreamSynchronize(stream));
+  dev_ok = true;
+  method_built = method;
+  emat_dirty = erhs_dirty = true;
+}
+
+void Engine::upload_elements() {
+  if (emat_dirty) {
+    CK(cudaMemcpyAsync(ctx.emat, h_pinned, sizeof(double) * (size_t)emat_total, cudaMemcpyHostToDevice, stream));
+    emat_dirty = false;
+  }
+}
+
+void Engine::assemble_rhs() {
+  if (erhs_dirty) {
+    CK(cudaMemcpyAsync(d_erhs, h_pinned + emat_total, sizeof(double) * (size_t)erhs_total,
+                       cudaMemcpyHostToDevice, stream));
+    erhs_dirty = false;
+  }
+  launch_dof_gather(d_dof_ptr, d_dof_idx, d_erhs, nullptr, n_global, d_b, n_global, mesh->n_rhs, 0, stream);
+}
+
+void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
+  for (const Op& op : ops) {
+    const Item* it = d_items + op.item_off;
+    switch (op.kind) {
+      case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, stream); break;
+      case OP_SMALL_FACTOR:
+        launch_small_factor(ctx, it, op.n_items, op.dtype,
+                            ctx.symmetric ? M_CHOL : (method_built == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV),
+                            op.param, stream);
+        break;
+      case OP_POTRF: launch_potrf_diag(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_GETRF: launch_getrf_panel(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
+      case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
+      case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
+      case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, stream); break;
+      case OP_TRSV_F: launch_trsv_block(ctx, it, op.n_items, op.dtype, op.param, op.nb, 0, stream); break;
+      case OP_GEMV_F: launch_gemv_panel(ctx, it, op.n_items, op.dtype, op.param, op.nb, 0, stream); break;
+      case OP_BWD_PREP: launch_bwd_prepare(ctx, it, op.n_items, 0, op.param, g_out, n_global, stream); break;
+      case OP_BWD_SMALL: launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, stream); break;
+      case OP_GEMV_B: launch_gemv_panel(ctx, it, op.n_items, op.dtype, op.param, op.nb, 1, stream); break;
+      case OP_TRSV_B: launch_trsv_block(ctx, it, op.n_items, op.dtype, op.param, op.nb, 1, stream); break;
+      case OP_BWD_STORE: launch_bwd_store(ctx, it, op.n_items, g_out, n_global, stream); break;
+    }
+    timing.kernel_launches++;
+  }
+  CK(cudaGetLastError());
+}
+
+void Engine::check_status(const char* where) {
+  std::vector<int> st(fronts.size());
+  CK(cudaMemcpy(st.data(), ctx.status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < st.size(); ++i)
+    if (st[i]) {
+      const char* what = st[i] == ST_NOT_SPD ? "front is not positive definite"
+                         : st[i] == ST_ZERO_PIVOT ? "zero pivot" : "NaN in front";
+      status = 10 + st[i];
+      last_error = std::string(where) + ": " + what + " (element " + std::to_string(fronts[i].e->get_id()) + ")";
+      return;
+    }
+}
+
+void Engine::factor(int method) {
+  ensure_plan();
+  for (auto& es : esrc)
+    if (!es.has_lhs) fail("factor: an element matrix has not been copied in", 7);
+  if (!dev_ok || method_built != method) {
+    build_plan(method);
+    build_programs(method);
+    alloc_device(method);
+  }
+  status = 0;
+  last_error.clear();
+  timing = Timing{};
+  CK(cudaEventRecord(ev0, stream));
+  upload_elements();
+  CK(cudaMemsetAsync(ctx.status, 0, sizeof(int) * fronts.size(), stream));
+  CK(cudaEventRecord(ev1, stream));
+  CK(cudaEventSynchronize(ev1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  timing.upload_ms = ms;
+  CK(cudaEventRecord(ev0, stream));
+  run_ops(fac_ops, nullptr, nullptr);
+  CK(cudaEventRecord(ev1, stream));
+  CK(cudaEventSynchronize(ev1));
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  timing.factor_ms = ms;
+  check_status("factor");
+  factored = true;
+  factored_method = method;
+  h_x_valid = false;
+}
+
+void Engine::solve_into(int method, double* rhs, double* out, int phase) {
+  (void)method;
+  if (phase & 1) run_ops(fwd_ops, rhs, out);
+  if (phase & 2) run_ops(bwd_ops, rhs, out);
+}
+
+void Engine::solve(int method, int phase) {
+  if (!factored) fail("solve: the mesh has not been factorised", 9);
+  if (method != factored_method) fail("solve: method differs from the factorisation", 9);
+  float ms = 0;
+  CK(cudaEventRecord(ev0, stream));
+  if (phase & 1) assemble_rhs();
+  solve_into(method, d_b, d_x, phase);
+  CK(cudaEventRecord(ev1, stream));
+  CK(cudaEventSynchronize(ev1));
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  timing.solve_ms = ms;
+  h_x_valid = false;
+}
+
+void Engine::compute_residual(const double* x, double* r) {
+  launch_elem_gemv(ctx.emat, d_emat_off, d_elem_m, d_emap_off, d_emap, x, n_global, d_y, d_y_off,
+                   (int)esrc.size(), mesh->n_rhs, stream);
+  launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, d_b, n_global, r, n_global, mesh->n_rhs, 1, stream);
+}
+
+double Engine::residual_norm1() {
+  if (!factored) fail("residual: nothing solved", 9);
+  compute_residual(d_x, d_r);
+  std::vector<double> r((size_t)n_global * mesh->n_rhs);
+  CK(cudaMemcpyAsync(r.data(), d_r, sizeof(double) * r.size(), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  double best = 0;
+  for (int q = 0; q < mesh->n_rhs; ++q) {
+    double s = 0;
+    for (int64_t i = 0; i < n_global; ++i) s += std::fabs(r[i + q * n_global]);
+    best = std::max(best, s);
+  }
+  return best;
+}
+
+// ||A||_inf of the assembled operator sum_e P_e^T A_e P_e (host, once per factorisation)
+double Engine::operator_norm_inf() {
+  if (anorm_inf >= 0) return anorm_inf;
+  std::vector<double> host_mats;
+  const double* mats = h_pinned;
+  if (!emat_dirty && dev_ok) {
+    host_mats.resize(emat_total);
+    CK(cudaMemcpy(host_mats.data(), ctx.emat, sizeof(double) * emat_total, cudaMemcpyDeviceToHost));
+    mats = host_mats.data();
+  }
+  // dof -> list of (element, row)
+  std::vector<int64_t> cnt(n_global + 1, 0);
+  for (auto& es : esrc)
+    for (int32_t g : es.gdof) cnt[g + 1]++;
+  for (int64_t i = 0; i < n_global; ++i) cnt[i + 1] += cnt[i];
+  std::vector<std::pair<int, int>> lst(cnt[n_global]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int k = 0; k < (int)esrc.size(); ++k)
+    for (int r = 0; r < esrc[k].m; ++r) lst[fill[esrc[k].gdof[r]]++] = {k, r};
+  double best = 0.0;
+#pragma omp parallel reduction(max : best)
+  {
+    std::vector<double> row(n_global, 0.0);
+    std::vector<char> seen(n_global, 0);
+    std::vector<int32_t> touched;
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n_global; ++i) {
+      touched.clear();
+      for (int64_t k = cnt[i]; k < cnt[i + 1]; ++k) {
+        const ElemSource& es = esrc[lst[k].first];
+        const int l = lst[k].second;
+        const double* A = mats + es.mat_off;
+        for (int j = 0; j < es.m; ++j) {
+          const int32_t c = es.gdof[j];
+          if (!seen[c]) { seen[c] = 1; touched.push_back(c); }
+          row[c] += A[l + (int64_t)j * es.m];
+        }
+      }
+      double s = 0.0;
+      for (int32_t c : touched) { s += std::fabs(row[c]); row[c] = 0.0; seen[c] = 0; }
+      best = std::max(best, s);
+    }
+  }
+  anorm_inf = best;
+  return best;
+}
+
+double Engine::backward_error() {
+  if (!factored) fail("backward_error: nothing solved", 9);
+  compute_residual(d_x, d_r);
+  const int64_t nv = n_global * mesh->n_rhs;
+  launch_absmax(d_r, nv, d_red, stream);
+  launch_absmax(d_x, nv, d_red + 512, stream);
+  launch_absmax(d_b, nv, d_red + 1024, stream);
+  double h[3];
+  CK(cudaMemcpyAsync(&h[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  CK(cudaMemcpyAsync(&h[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  CK(cudaMemcpyAsync(&h[2], d_red + 1024, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  const double an = operator_norm_inf();
+  return h[0] / (an * h[1] + h[2]);
+}
+
+}  // namespace uhm

@@ -1,0 +1,185 @@
+// Device engine behind Mesh_: one HBM arena for all fronts, precomputed
+// extend-add maps, and a level-by-level program of batched kernel launches.
+//
+// Replaces, for the hot path, the reference's per-front OpenMP task tree
+// (Scheduler_::execute_tree, UHM/src/operation/scheduler.cxx:210-258) and
+// the per-front Matrix_FLA_ buffers (UHM/src/matrix/uhm/fla/matrix.cxx:75-164):
+// all fronts of one generation are processed by the same launches.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+#include "mesh.hpp"
+
+namespace uhm {
+
+// precision of a front's factorisation
+enum FrontPrec : int { PREC_FP64 = 0, PREC_FP32 = 1, PREC_BF16X3 = 2 };
+
+struct HostFront {
+  Element e = nullptr;
+  int slot = 0, level = 0;
+  int n = 0, fs = 0, ss = 0, g0 = 0;
+  int parent = -1;
+  std::vector<int> children;       // slots, in child order
+  int prec = PREC_FP64;
+  int64_t off = 0, voff = 0, inv_off = 0, colptr_off = 0, sgi_off = 0, piv_off = 0;
+  int src0 = 0, nsrc = 0;
+};
+
+struct ElemSource {                // a copy_in'd element matrix / rhs
+  Element e = nullptr;
+  int slot = -1;                   // front it scatters into
+  int m = 0;
+  std::vector<int> pos;            // user row -> front position
+  std::vector<int32_t> gdof;       // user row -> global dof (elimination order)
+  std::vector<std::pair<int, int>> node_order;  // node ids in user order (for reuse check)
+  int64_t mat_off = -1;            // element arena offset (doubles)
+  int64_t rhs_off = -1;            // element rhs staging offset (doubles)
+  bool has_lhs = false, has_rhs = false;
+};
+
+struct Op {
+  int kind;
+  int dtype;
+  int nb;
+  int param;
+  int64_t item_off;
+  int n_items;
+};
+
+enum OpKind : int {
+  OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
+  OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
+  OP_TRSV_B, OP_BWD_STORE
+};
+
+struct Timing {
+  double upload_ms = 0, factor_ms = 0, solve_ms = 0, refine_ms = 0, total_ms = 0;
+  int ir_iters = 0;
+  double berr = -1, berr_first = -1;
+  int64_t kernel_launches = 0;
+};
+
+class Engine {
+ public:
+  explicit Engine(Mesh_* m);
+  ~Engine();
+
+  // --- set-up -----------------------------------------------------------
+  void invalidate_plan() { plan_ok = false; }
+  void copy_in(Element e, int m, int n, int nod_disp, const int* nods, int side,
+               const double* buf);
+  void copy_out(Element e, int m, int n, int nod_disp, const int* nods, int side, double* buf);
+  // bulk: element matrices of all leaves, in leaf order (Mesh_::leaves), each
+  // m_e x m_e column-major in the element's own node order, back to back
+  void copy_in_leaves(int side, const double* buf, int64_t n_values);
+  void copy_out_leaves(double* buf, int64_t n_values);
+  // element maps of all leaves from their node lists (leaf order, single physics)
+  void set_leaf_nodes(const int* nods_all);
+  void node_solution(int n_nodes, const int* ids, double* out, int64_t n_values);
+
+  // --- numerics -----------------------------------------------------------
+  void factor(int method);
+  void solve(int method, int phase);          // 1 forward, 2 backward, 3 both
+  double residual_norm1();                    // sum |b - A x| (unassembled A)
+  double backward_error();                    // ||b-Ax||/(||A|| ||x|| + ||b||), inf-norms
+
+  // --- configuration ------------------------------------------------------
+  int mode = 0;            // 0 plain FP64, 1 mixed (per-front precision + IR)
+  int default_prec = PREC_FP32;
+  double ir_tol = 1e-12;
+  int ir_max = 10;
+  std::vector<int> front_prec_override;       // by slot, -1 = default
+  int status = 0;
+  std::string last_error;
+  Timing timing;
+
+  // --- introspection ------------------------------------------------------
+  std::vector<HostFront> fronts;              // by slot (leaf -> root order)
+  std::vector<std::vector<int>> levels;       // slots per generation, leaf -> root
+  int64_t n_global = 0;
+  void ensure_plan();
+  int method_built = 0;
+
+ private:
+  Mesh_* mesh;
+  bool plan_ok = false;
+  bool dev_ok = false;
+  bool factored = false;
+  int factored_method = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // element sources
+  std::vector<ElemSource> esrc;
+  std::vector<int> esrc_of_slot;              // slot -> index in esrc (or -1)
+  std::vector<double> h_emat;                 // staged element matrices (host)
+  std::vector<double> h_erhs;                 // staged element rhs
+  int64_t emat_total = 0, erhs_total = 0;
+  bool emat_dirty = true, erhs_dirty = true;
+  double* h_pinned = nullptr;
+  bool h_pinned_is_malloc = false;
+  size_t h_pinned_bytes = 0;
+
+  // host-side device images
+  std::vector<uhm_gpu::FrontDev> h_fronts;
+  std::vector<uhm_gpu::SrcDev> h_srcs;
+  std::vector<int32_t> h_inv, h_sgi;
+  std::vector<int64_t> h_colptr;
+  std::vector<int2> h_colsrc;
+  std::vector<uhm_gpu::Item> h_items;
+  std::vector<Op> fac_ops, fwd_ops, bwd_ops;
+  int64_t arena64_n = 0, arena32_n = 0, vec_n = 0, piv_n = 0;
+
+  // device memory
+  uhm_gpu::DevCtx ctx{};
+  uhm_gpu::Item* d_items = nullptr;
+  double* d_b = nullptr;        // assembled rhs (elimination order)
+  double* d_x = nullptr;        // solution
+  double* d_r = nullptr;        // residual / correction rhs
+  double* d_d = nullptr;        // correction
+  double* d_erhs = nullptr;     // element rhs (FP64)
+  double* d_y = nullptr;        // per-element A_e x_e
+  double* d_red = nullptr;      // reduction scratch
+  int64_t* d_emat_off = nullptr;
+  int* d_elem_m = nullptr;
+  int64_t* d_emap_off = nullptr;
+  int32_t* d_emap = nullptr;
+  int64_t* d_y_off = nullptr;
+  int64_t* d_dof_ptr = nullptr;
+  int64_t* d_dof_idx = nullptr;
+  std::vector<int64_t> h_emat_off, h_emap_off, h_y_off;
+  std::vector<int> h_elem_m;
+  std::vector<int32_t> h_emap;
+  int64_t y_total = 0;
+  std::vector<void*> allocations;
+  double anorm_inf = -1.0;
+  std::vector<double> h_x;      // cached solution on host
+  bool h_x_valid = false;
+
+  void build_plan(int method);
+  void build_programs(int method);
+  void alloc_device(int method);
+  void free_device();
+  void upload_elements();
+  void assemble_rhs();
+  void run_ops(const std::vector<Op>& ops, double* g_in, double* g_out);
+  void solve_into(int method, double* rhs, double* out, int phase);
+  void compute_residual(const double* x, double* r);
+  double operator_norm_inf();
+  void check_status(const char* where);
+  void* dmalloc(size_t bytes);
+  int64_t add_items(const std::vector<uhm_gpu::Item>& it);
+  void fail(const std::string& msg, int code);
+  void element_map(Element e, int nod_disp, const int* nods, std::vector<std::pair<int, int>>& order,
+                   std::vector<int>& pos, std::vector<int32_t>& gd);
+  void fetch_x();
+  void release_staging();
+};
+
+}  // namespace uhm

@@ -1,0 +1,116 @@
+// Device data layout shared by the host engine and the CUDA kernels.
+//
+// One front = one column-major n x n panel (n = fs + ss, ld = n) holding
+//   [ ATL ATR ]      ATL fs x fs  (factor block)
+//   [ ABL ABR ]      ABR ss x ss  (Schur complement after the partial factor)
+// which restates Matrix_FLA_'s four buffers (UHM/include/uhm/matrix/uhm/fla.hxx:59-63)
+// as one contiguous panel in HBM.  Fronts live in one arena per storage type
+// (FP64 or FP32).  Right-hand sides travel in a global vector in elimination
+// order (dofs eliminated at front f are the contiguous range g0..g0+fs), plus
+// a per-front vector slab of n x n_rhs for the tree sweeps.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace uhm_gpu {
+
+enum DType : int { F64 = 0, F32 = 1 };
+enum Method : int { M_CHOL = 1, M_LU_NOPIV = 2, M_LU_PIV = 3 };
+
+struct FrontDev {
+  int64_t off;        // element offset of the panel in its arena
+  int64_t voff;       // element offset of the n x n_rhs vector slab (FP64)
+  int64_t inv_off;    // offset of this front's inverse maps (nsrc x n int32)
+  int64_t colptr_off; // offset of this front's n+1 column-source pointers
+  int64_t sgi_off;    // offset of the ss global dof indices of the schur rows
+  int64_t piv_off;    // offset of the fs pivot entries (LU)
+  int n, fs, ss;
+  int dtype;          // storage/compute type of the panel
+  int g0;             // first global dof eliminated here
+  int src0, nsrc;     // assembly sources [src0, src0 + nsrc)
+  int status_slot;
+};
+
+// An assembly source: an element matrix (full, FP64) or a child front's ABR.
+struct SrcDev {
+  int64_t off;        // offset of entry (0,0) of the source block in its arena
+  int ld;
+  int dtype;          // F64 / F32 (element matrices are F64)
+  int is_child;       // 1: child ABR (lower triangle valid when symmetric)
+  int slot;           // child front slot (or element index)
+};
+
+// Work item for per-front launches: front slot + tile / step data.
+struct Item {
+  int front;
+  int a, b, c;        // kernel-specific (tile row, tile col, step start ...)
+};
+
+// Status words written by kernels (breakdown detection): per front.
+enum Status : int { ST_OK = 0, ST_NOT_SPD = 1, ST_ZERO_PIVOT = 2, ST_NAN = 3 };
+
+struct DevCtx {
+  FrontDev* fronts;
+  SrcDev* srcs;
+  int32_t* inv;       // inverse maps
+  int64_t* colptr;    // per front: n+1 offsets into colsrc
+  int2* colsrc;       // (source local index, source column)
+  int32_t* sgi;       // schur-row global dofs
+  int32_t* piv;       // pivots (LU), relative to the front's first row
+  double* a64;        // FP64 panel arena
+  float* a32;         // FP32 panel arena
+  double* emat;       // element matrices (FP64, retained for the residual)
+  double* vec;        // per-front vector slabs
+  int* status;        // per-front status
+  int n_rhs;
+  int symmetric;      // Cholesky: lower triangles only
+};
+
+// ---- kernel launchers (implemented in the .cu files) ----------------------
+void launch_assemble(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
+                     cudaStream_t s);
+void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                         int max_n, cudaStream_t s);
+void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                       cudaStream_t s);
+void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                       cudaStream_t s);
+void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                        cudaStream_t s);
+// LU (partial pivoting restricted to the factor rows, or none)
+void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                        int pivot, cudaStream_t s);
+void launch_lu_row_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                          int pivot, cudaStream_t s);
+void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
+                        cudaStream_t s);
+
+// tree solves over the global vector g (N x n_rhs, column-major, ld N)
+void launch_fwd_gather(const DevCtx& c, const Item* items, int n_items, const double* g,
+                       int64_t ldg, int method, cudaStream_t s);
+void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                      cudaStream_t s);
+void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                      double* g, int64_t ldg, cudaStream_t s);
+void launch_trsv_block(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                       int nb, int upper, cudaStream_t s);
+void launch_gemv_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                       int nb, int upper, cudaStream_t s);
+void launch_bwd_prepare(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                        const double* g, int64_t ldg, cudaStream_t s);
+void launch_bwd_store(const DevCtx& c, const Item* items, int n_items, double* g, int64_t ldg,
+                      cudaStream_t s);
+
+// element-wise residual r = b - sum_e P_e^T A_e P_e x, deterministic gather
+void launch_elem_gemv(const double* emat, const int64_t* emat_off, const int* elem_m,
+                      const int64_t* emap_off, const int32_t* emap, const double* x, int64_t ldx,
+                      double* y, const int64_t* y_off, int n_elem, int n_rhs, cudaStream_t s);
+void launch_dof_gather(const int64_t* ptr, const int64_t* idx, const double* y, const double* b,
+                       int64_t ldb, double* r, int64_t N, int n_rhs, int sub_from_b,
+                       cudaStream_t s);
+void launch_absmax(const double* v, int64_t n, double* out, cudaStream_t s);
+void launch_axpy(double* y, const double* x, int64_t n, double alpha, cudaStream_t s);
+void launch_convert_panels(const DevCtx& c, const Item* items, int n_items, int to_f32,
+                           cudaStream_t s);
+
+}  // namespace uhm_gpu

@@ -1,0 +1,444 @@
+// Host restatement of UHM's mesh layer and symbolic analysis.
+//   Node_      UHM/src/mesh/node.cxx
+//   Element_   UHM/src/mesh/element.cxx
+//   Mesh_      UHM/src/mesh/mesh.cxx, matrix.cxx, interf.cxx, chol.cxx, lu_piv.cxx
+// The numerical methods delegate to the device engine (engine.hpp).
+#include "mesh.hpp"
+
+#include <algorithm>
+#include <cassert>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+
+#include "engine.hpp"
+
+namespace uhm {
+
+bool NodeIdLess::operator()(const Node_* a, const Node_* b) const { return a->id < b->id; }
+bool ElementIdLess::operator()(const Element_* a, const Element_* b) const { return a->id < b->id; }
+
+// ---------------------------------------------------------------------------
+// Node_
+// ---------------------------------------------------------------------------
+void Node_::clean_connectivity() {
+  for (auto it = owner.begin(); it != owner.end();) {
+    if (!(*it)->is_leaf()) it = owner.erase(it);
+    else ++it;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Element_
+// ---------------------------------------------------------------------------
+std::pair<int, int> Element_::get_n_dof() const {
+  std::pair<int, int> r(0, 0);
+  for (auto& kv : nodes) {
+    if (kv.second == UHM_SEPARATED_FACTOR) r.first += kv.first->get_n_dof();
+    else if (kv.second == UHM_SEPARATED_SCHUR) r.second += kv.first->get_n_dof();
+  }
+  return r;
+}
+
+int Element_::get_height() const {
+  int h = 0;
+  const Element_* e = this;
+  while (e->parent) { e = e->parent; ++h; }
+  return h;
+}
+
+void Element_::set_parent(Element p) {
+  if (!p) throw std::invalid_argument("set_parent: null element");
+  parent = p;
+}
+
+void Element_::add_node(Node n, int separated) {
+  auto r = nodes.insert(std::make_pair(n, separated));
+  r.first->second = separated;
+  if (r.second) n->add_owner(this);
+}
+
+void Element_::update_generation() {
+  if (is_leaf()) return;
+  int gen = 0;
+  for (Element c : children) gen = std::min(gen, c->get_generation());
+  generation = gen - 1;
+}
+
+// element.cxx:272-286: a node is eliminated here iff it has one owner and default kind
+void Element_::separate_nodes() {
+  for (auto& kv : nodes) {
+    if (!kv.first->get_n_owner()) throw std::logic_error("node without owner");
+    kv.second = (kv.first->get_n_owner() == 1 && kv.first->get_kind() == UHM_NODE_KIND_DEFAULT)
+                    ? UHM_SEPARATED_FACTOR : UHM_SEPARATED_SCHUR;
+  }
+}
+
+// element.cxx:288-334: factor and schur nodes sorted by global offset
+void Element_::arrange_nodes() {
+  factor.clear();
+  schur.clear();
+  std::map<int, Node> f, s;
+  for (auto& kv : nodes) {
+    if (!kv.first->get_n_dof()) continue;
+    if (kv.second == UHM_SEPARATED_FACTOR) f.insert({kv.first->get_offset(), kv.first});
+    else if (kv.second == UHM_SEPARATED_SCHUR) s.insert({kv.first->get_offset(), kv.first});
+  }
+  int o = 0;
+  for (auto& kv : f) { factor.push_back({kv.second, o}); o += kv.second->get_n_dof(); }
+  o = 0;
+  for (auto& kv : s) { schur.push_back({kv.second, o}); o += kv.second->get_n_dof(); }
+}
+
+// element.cxx:336-360
+void Element_::merge_nodes_from_children() {
+  if (is_leaf()) return;
+  nodes.clear();
+  for (Element c : children) merge_nodes(c);
+}
+
+void Element_::merge_nodes(Element c) {
+  for (auto& kv : c->nodes)
+    if (kv.second == UHM_SEPARATED_SCHUR) {
+      add_node(kv.first);
+      kv.first->remove_owner(c);
+    }
+}
+
+// element.cxx:362-381
+void Element_::restore_connectivity() {
+  if (!is_leaf()) return;
+  for (auto& kv : nodes) {
+    kv.second = UHM_NOT_SEPARATED;
+    kv.first->clean_connectivity();
+    kv.first->add_owner(this);
+  }
+  factor.clear();
+  schur.clear();
+}
+
+// element.cxx:383-392 (node-id order: deterministic)
+void Element_::numbering(int64_t& g) {
+  for (auto& kv : nodes)
+    if (kv.second == UHM_SEPARATED_FACTOR) {
+      kv.first->set_offset((int)g);
+      g += kv.first->get_n_dof();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LAWN-41 (LINAL/src/util.cxx:60-116)
+// ---------------------------------------------------------------------------
+static inline double MUL(int c) { return c ? 6.0 : 1.0; }
+static inline double ADD(int c) { return c ? 2.0 : 1.0; }
+double get_flop_gemm(int c, int mm, int nn, int kk) {
+  double m = mm, n = nn, k = kk;
+  return MUL(c) * (m * n * k) + ADD(c) * (m * n * k);
+}
+double get_flop_syrk(int c, int kk, int nn) {
+  double k = kk, n = nn;
+  return MUL(c) * (0.5 * k * n * (n + 1.0)) + ADD(c) * (0.5 * k * n * (n + 1.0));
+}
+double get_flop_trsm_lower(int c, int mm, int nn) {
+  double m = mm, n = nn;
+  return MUL(c) * (0.5 * n * m * (m + 1.0)) + ADD(c) * (0.5 * n * m * (m - 1.0));
+}
+double get_flop_trsm_upper(int c, int mm, int nn) {
+  double m = mm, n = nn;
+  return MUL(c) * (0.5 * m * n * (n + 1.0)) + ADD(c) * (0.5 * m * n * (n - 1.0));
+}
+double get_flop_lu(int c, int mm, int nn) {
+  double m = mm, n = nn;
+  if (m > n)
+    return MUL(c) * (0.5 * m * n * n - (1.0 / 6.0) * n * n * n + 0.5 * m * n - 0.5 * n * n + (2.0 / 3.0) * n) +
+           ADD(c) * (0.5 * m * n * n - (1.0 / 6.0) * n * n * n - 0.5 * m * n + (1.0 / 6.0) * n);
+  return MUL(c) * (0.5 * n * m * m - (1.0 / 6.0) * m * m * m + 0.5 * n * m - 0.5 * m * m + (2.0 / 3.0) * m) +
+         ADD(c) * (0.5 * n * m * m - (1.0 / 6.0) * m * m * m - 0.5 * n * m + (1.0 / 6.0) * m);
+}
+double get_flop_chol(int c, int nn) {
+  double n = nn;
+  return MUL(c) * ((1.0 / 6.0) * n * n * n + 0.5 * n * n + (1.0 / 3.0) * n) +
+         ADD(c) * ((1.0 / 6.0) * n * n * n - (1.0 / 6.0) * n);
+}
+
+// element.cxx:128-195
+void Element_::estimate_cost(int method, int datatype, int n_rhs, double& dec, double& sol,
+                             unsigned& nnz, double& buffer) const {
+  const int c = datatype == UHM_COMPLEX;
+  const std::pair<int, int> d = get_n_dof();
+  const int fs = d.first, ss = d.second;
+  const double mem = c ? 16.0 : 8.0;
+  if (method == UHM_CHOL) {
+    dec = get_flop_chol(c, fs) + get_flop_trsm_lower(c, fs, ss) + get_flop_syrk(c, fs, ss);
+    buffer = mem * fs * fs + mem * ss * fs;
+    nnz = fs * fs + ss * fs;
+  } else {
+    dec = get_flop_lu(c, fs, fs) + get_flop_trsm_lower(c, fs, ss) + get_flop_trsm_upper(c, ss, fs) +
+          get_flop_gemm(c, ss, ss, fs);
+    buffer = mem * fs * fs + 2 * mem * ss * fs;
+    nnz = (unsigned)(fs * fs + 2.0 * ss * fs);
+  }
+  sol = get_flop_trsm_lower(c, fs, n_rhs) + get_flop_gemm(c, ss, n_rhs, fs) +
+        get_flop_trsm_upper(c, n_rhs, fs) + get_flop_gemm(c, fs, n_rhs, ss);
+}
+
+// ---------------------------------------------------------------------------
+// Mesh_
+// ---------------------------------------------------------------------------
+Mesh_::Mesh_() {}
+Mesh_::~Mesh_() { delete engine; }
+
+Engine& Mesh_::eng() {
+  if (!engine) engine = new Engine(this);
+  return *engine;
+}
+
+Node Mesh_::add_node(int id, int n_dof) { return add_node(std::make_pair(id, 0), n_dof, n_dof, 0); }
+Node Mesh_::add_node(int id, int n_dof, int p) { return add_node(std::make_pair(id, 0), n_dof, p, 0); }
+Node Mesh_::add_node(std::pair<int, int> id, int n_dof) { return add_node(id, n_dof, n_dof, 0); }
+Node Mesh_::add_node(std::pair<int, int> id, int n_dof, int p) { return add_node(id, n_dof, p, 0); }
+Node Mesh_::add_node(std::pair<int, int> id, int n_dof, int p, int kind) {
+  auto r = nodes.insert(std::make_pair(id, Node_(id, n_dof, p, kind)));
+  if (!r.second) {
+    Node_& n = r.first->second;
+    if (n.n_dof != n_dof || n.p != p || n.kind != kind)
+      throw std::invalid_argument("add_node: node exists with different attributes");
+  }
+  return &r.first->second;
+}
+
+Node Mesh_::find_node(int id) { return find_node(std::make_pair(id, 0)); }
+Node Mesh_::find_node(std::pair<int, int> id) {
+  auto it = nodes.find(id);
+  return it == nodes.end() ? nullptr : &it->second;
+}
+
+Element Mesh_::add_element() { return add_element(0); }
+Element Mesh_::add_element(int gen) {
+  auto r = elements.insert(std::make_pair(id_element, Element_(id_element, gen)));
+  ++id_element;
+  return &r.first->second;
+}
+
+Element Mesh_::find_element(int id) {
+  auto it = elements.find(id);
+  return it == elements.end() ? nullptr : &it->second;
+}
+
+Element Mesh_::get_root() {
+  if (elements.empty()) return nullptr;
+  Element e = &elements.begin()->second;
+  while (e->parent) e = e->parent;
+  return e;
+}
+
+// mesh.cxx:385-421 (non-binary branch)
+Element Mesh_::refine_element(int id, int n_children) {
+  Element e = find_element(id);
+  if (!e || n_children < 2) throw std::invalid_argument("refine_element");
+  for (int i = 0; i < n_children; ++i) {
+    Element c = add_element(e->get_generation() + 1);
+    c->set_parent(e);
+    e->add_child(c);
+  }
+  return e;
+}
+
+void Mesh_::reset() {
+  unlock();
+  delete engine;
+  engine = nullptr;
+  elements.clear();
+  nodes.clear();
+  id_element = 0;
+}
+
+// .uhm text format of Mesh_::import_file (UHM/src/mesh/mesh.cxx:511-579)
+bool Mesh_::import_file(const char* path) {
+  reset();
+  FILE* fp = std::fopen(path, "r");
+  if (!fp) return false;
+  char line[10000];
+  auto next = [&](char* buf) -> bool {
+    while (std::fgets(buf, sizeof(line), fp)) {
+      const char* p = buf;
+      while (*p == ' ' || *p == '\t') ++p;
+      if (*p == '#' || *p == '\n' || *p == 0) continue;
+      return true;
+    }
+    return false;
+  };
+  char fmt[32] = {0};
+  if (!next(line) || std::sscanf(line, "%31s", fmt) != 1 || std::strcmp(fmt, "UHM")) {
+    std::fclose(fp);
+    return false;
+  }
+  int n_nodes = 0, n_elements = 0;
+  if (!next(line) || std::sscanf(line, "%d", &n_nodes) != 1) { std::fclose(fp); return false; }
+  for (int i = 0; i < n_nodes; ++i) {
+    int id, phy, ndof, p, kind;
+    if (!next(line) || std::sscanf(line, "%d %d %d %d %d", &id, &phy, &ndof, &p, &kind) != 5) {
+      std::fclose(fp);
+      return false;
+    }
+    add_node(std::make_pair(id, phy), ndof, p, kind);
+  }
+  if (!next(line) || std::sscanf(line, "%d", &n_elements) != 1) { std::fclose(fp); return false; }
+  for (int i = 0; i < n_elements; ++i) {
+    int nn;
+    if (!next(line) || std::sscanf(line, "%d", &nn) != 1) { std::fclose(fp); return false; }
+    Element e = add_element();
+    for (int j = 0; j < nn; ++j) {
+      int id, phy;
+      if (!next(line) || std::sscanf(line, "%d %d", &id, &phy) != 2) { std::fclose(fp); return false; }
+      Node n = find_node(std::make_pair(id, phy));
+      if (!n) { std::fclose(fp); return false; }
+      e->add_node(n);
+    }
+  }
+  std::fclose(fp);
+  // remove orphan nodes (mesh.cxx:236-241)
+  for (auto it = nodes.begin(); it != nodes.end();) {
+    if (!it->second.get_n_owner()) it = nodes.erase(it);
+    else ++it;
+  }
+  return true;
+}
+
+// mesh.cxx:438-456
+void Mesh_::lock() {
+  unlock();
+  // Scheduler_::load: group by generation (leaf -> root = descending), id order inside
+  for (auto& kv : elements) {
+    by_generation[kv.second.get_generation()].push_back(&kv.second);
+    if (kv.second.is_leaf()) leaves.push_back(&kv.second);
+  }
+  for (Element e : leaves) e->restore_connectivity();
+  for (auto& g : by_generation)
+    for (Element e : g.second) {
+      e->merge_nodes_from_children();
+      e->separate_nodes();
+    }
+  int64_t goff = 0;
+  for (auto& g : by_generation)
+    for (Element e : g.second) e->numbering(goff);
+  n_dof_total = goff;
+  for (auto& g : by_generation)
+    for (Element e : g.second) e->arrange_nodes();
+  locker = 1;
+  if (engine) engine->invalidate_plan();
+}
+
+void Mesh_::unlock() {
+  by_generation.clear();
+  leaves.clear();
+  locker = 0;
+  if (engine) engine->invalidate_plan();
+}
+
+// matrix.cxx:64-90
+void Mesh_::create_matrix_without_buffer(int dt, int nrhs) {
+  if (dt != UHM_REAL) throw std::invalid_argument("only UHM_REAL (FP64) is supported");
+  datatype = dt;
+  n_rhs = nrhs;
+  for (auto& kv : elements) {
+    std::pair<int, int> d = kv.second.get_n_dof();
+    kv.second.hm = FrontHandle{d.first, d.second, nrhs, dt, true};
+  }
+  if (engine) engine->invalidate_plan();
+}
+
+// buffers live in the device arena, allocated at the first factorisation
+void Mesh_::create_matrix_buffer(int) {}
+void Mesh_::create_leaf_matrix_buffer() {}
+void Mesh_::create_element_matrix_buffer(int) {}
+void Mesh_::free_matrix() {
+  for (auto& kv : elements) kv.second.hm.created = false;
+  delete engine;
+  engine = nullptr;
+}
+
+void Mesh_::copy_in(Element elt, int dt, int m, int n, int* nods, int side, void* buffer) {
+  copy_in(elt, dt, m, n, UHM_PHYSICS_SINGLE, nods, side, buffer);
+}
+void Mesh_::copy_in(Element elt, int dt, int m, int n, int nod_disp, int* nods, int side, void* buffer) {
+  if (dt != UHM_REAL) throw std::invalid_argument("copy_in: only UHM_REAL is supported");
+  eng().copy_in(elt, m, n, nod_disp, nods, side, (const double*)buffer);
+}
+void Mesh_::copy_out(Element elt, int dt, int m, int n, int* nods, int side, void* buffer) {
+  copy_out(elt, dt, m, n, UHM_PHYSICS_SINGLE, nods, side, buffer);
+}
+void Mesh_::copy_out(Element elt, int dt, int m, int n, int nod_disp, int* nods, int side, void* buffer) {
+  if (dt != UHM_REAL) throw std::invalid_argument("copy_out: only UHM_REAL is supported");
+  eng().copy_out(elt, m, n, nod_disp, nods, side, (double*)buffer);
+}
+
+// matrix.cxx:54-62: the right-hand side is taken from the element rhs at solve time
+void Mesh_::set_rhs() {}
+
+void Mesh_::run_factor(int method, int) { eng().factor(method); }
+void Mesh_::run_solve(int method, int phase) { eng().solve(method, phase); }
+
+void Mesh_::chol_with_free() { run_factor(UHM_CHOL, 0); }
+void Mesh_::chol_without_free() { run_factor(UHM_CHOL, 1); }
+void Mesh_::solve_chol_1() { run_solve(UHM_CHOL, 1); }
+void Mesh_::solve_chol_2() { run_solve(UHM_CHOL, 2); }
+void Mesh_::solve_chol() { run_solve(UHM_CHOL, 3); }
+void Mesh_::check_chol() {}
+void Mesh_::lu_nopiv_with_free() { run_factor(UHM_LU_NOPIV, 0); }
+void Mesh_::lu_nopiv_without_free() { run_factor(UHM_LU_NOPIV, 1); }
+void Mesh_::solve_lu_nopiv_1() { run_solve(UHM_LU_NOPIV, 1); }
+void Mesh_::solve_lu_nopiv_2() { run_solve(UHM_LU_NOPIV, 2); }
+void Mesh_::solve_lu_nopiv() { run_solve(UHM_LU_NOPIV, 3); }
+void Mesh_::check_lu_nopiv() {}
+void Mesh_::lu_piv_with_free() { run_factor(UHM_LU_PIV, 0); }
+void Mesh_::lu_piv_without_free() { run_factor(UHM_LU_PIV, 1); }
+void Mesh_::solve_lu_piv_1() { run_solve(UHM_LU_PIV, 1); }
+void Mesh_::solve_lu_piv_2() { run_solve(UHM_LU_PIV, 2); }
+void Mesh_::solve_lu_piv() { run_solve(UHM_LU_PIV, 3); }
+void Mesh_::check_lu_piv() {}
+
+// The reference returns sum over fronts of ||rt||_1 of its factor-based
+// check (UHM/src/matrix/uhm/fla/matrix.cxx:222-234); here: ||b - A x||_1 of
+// the true residual on the unassembled element matrices.
+double Mesh_::get_residual() { return eng().residual_norm1(); }
+
+unsigned Mesh_::get_n_dof() {
+  unsigned n = 0;
+  for (auto& kv : elements) n += kv.second.get_n_dof().first;
+  return n;
+}
+unsigned Mesh_::get_n_nonzero() {
+  unsigned n = 0;
+  for (auto& kv : elements)
+    if (kv.second.is_leaf()) {
+      std::pair<int, int> d = kv.second.get_n_dof();
+      n += (d.first + d.second) * (d.first + d.second);
+    }
+  return n;
+}
+unsigned Mesh_::get_n_nonzero_factor() {
+  unsigned n = 0;
+  for (auto& kv : elements) {
+    std::pair<int, int> d = kv.second.get_n_dof();
+    n += d.first * d.first + d.first * d.second * 2;
+  }
+  return n;
+}
+void Mesh_::estimate_cost(int method, int dt, int nrhs, double& dec, double& sol, unsigned& nnz,
+                          double& buffer) {
+  dec = sol = buffer = 0;
+  nnz = 0;
+  for (auto& kv : elements) {
+    double a, b, c;
+    unsigned z;
+    kv.second.estimate_cost(method, dt, nrhs, a, b, z, c);
+    dec += a;
+    sol += b;
+    nnz += z;
+    buffer += c;
+  }
+}
+
+}  // namespace uhm

@@ -1,0 +1,213 @@
+// UHM mesh / element / node objects and the symbolic analysis (lock).
+//
+// Host-side restatement of the reference's topology layer, with the same
+// names, argument meaning and semantics as
+//   UHM/include/uhm/mesh/node.hxx:45-102     (Node_)
+//   UHM/include/uhm/mesh/element.hxx:48-163  (Element_)
+//   UHM/include/uhm/mesh/mesh.hxx:58-301     (Mesh_)
+// The numerical work behind Mesh_::*_with_free / solve_* is done by the
+// device engine (engine.hpp); Element_::hm is a thin handle into its arena.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <set>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace uhm {
+
+// UHM/include/uhm/const.hxx:58-88
+enum { UHM_PHYSICS_SINGLE = 1, UHM_PHYSICS_MULTI = 2 };
+enum { UHM_NODE_KIND_DEFAULT = 0, UHM_NODE_KIND_BOUNDARY = 1 };
+enum { UHM_LHS = 1, UHM_RHS = 2 };
+enum { UHM_CHOL = 1, UHM_LU_NOPIV = 2, UHM_LU_PIV = 3, UHM_LU_INCPIV = 4, UHM_QR = 5 };
+enum { UHM_NOT_SEPARATED = 0, UHM_SEPARATED_FACTOR = 1, UHM_SEPARATED_SCHUR = 2 };
+constexpr int UHM_REAL = 101;      // FLA_DOUBLE (UHM/include/uhm/wrapper/fort.f90:36)
+constexpr int UHM_COMPLEX = 103;   // FLA_DOUBLE_COMPLEX
+
+class Node_;
+class Element_;
+class Mesh_;
+class Engine;
+typedef Node_* Node;
+typedef Element_* Element;
+typedef Mesh_* Mesh;
+
+// Orders nodes by id so that every walk over an element's node map is
+// deterministic.  (The reference keys std::map<Node,int> by pointer,
+// UHM/include/uhm/mesh/element.hxx:58.)
+struct NodeIdLess {
+  bool operator()(const Node_* a, const Node_* b) const;
+};
+struct ElementIdLess {
+  bool operator()(const Element_* a, const Element_* b) const;
+};
+
+class Node_ {
+ public:
+  std::pair<int, int> id;
+  int n_dof = 0, p = 0, kind = 0, offset = 0, marker = -1;
+  std::set<Element, ElementIdLess> owner;
+
+  Node_() = default;
+  Node_(std::pair<int, int> id_, int n_dof_, int p_, int kind_)
+      : id(id_), n_dof(n_dof_), p(p_), kind(kind_) {}
+
+  std::pair<int, int> get_id() const { return id; }
+  int get_n_dof() const { return n_dof; }
+  int get_p() const { return p; }
+  int get_kind() const { return kind; }
+  int get_offset() const { return offset; }
+  int get_n_owner() const { return (int)owner.size(); }
+  void set_offset(int o) { offset = o; }
+  void add_owner(Element e) { owner.insert(e); }
+  void remove_owner(Element e) { owner.erase(e); }
+  void clean_connectivity();   // drop non-leaf owners (UHM/src/mesh/node.cxx:110-118)
+};
+
+// Per-element matrix handle: sizes and its slots in the device engine.
+struct FrontHandle {
+  int fs = 0, ss = 0, n_rhs = 0, datatype = UHM_REAL;
+  bool created = false;
+};
+
+class Element_ {
+ public:
+  int id = 0, generation = 0;
+  Element parent = nullptr;
+  std::vector<Element> children;
+  std::map<Node, int, NodeIdLess> nodes;       // node -> separation flag
+  std::vector<std::pair<Node, int>> factor, schur;
+  FrontHandle hm;
+  int slot = -1;                               // index in the engine's front table
+
+  Element_() = default;
+  Element_(int id_, int gen) : id(id_), generation(gen) {}
+
+  int get_id() const { return id; }
+  int get_generation() const { return generation; }
+  Element get_parent() const { return parent; }
+  Element get_child(int i) const { return children.at(i); }
+  int get_n_children() const { return (int)children.size(); }
+  int get_n_nodes() const { return (int)nodes.size(); }
+  int get_n_factor_nodes() const { return (int)factor.size(); }
+  int get_n_schur_nodes() const { return (int)schur.size(); }
+  bool is_orphan() const { return parent == nullptr; }
+  bool is_leaf() const { return children.empty(); }
+  bool is_matrix_created() const { return hm.created; }
+  std::pair<int, int> get_n_dof() const;       // (fs, ss), element.cxx:112-126
+  int get_height() const;
+
+  void set_parent(Element p);
+  void add_child(Element c) { children.push_back(c); }
+  void add_node(Node n) { add_node(n, UHM_NOT_SEPARATED); }
+  void add_node(Node n, int separated);
+  void update_generation();                    // element.cxx:63-72
+
+  // symbolic steps (element.cxx:272-392)
+  void separate_nodes();
+  void arrange_nodes();
+  void merge_nodes_from_children();
+  void merge_nodes(Element c);
+  void restore_connectivity();
+  void numbering(int64_t& g_offset);
+
+  void estimate_cost(int method, int datatype, int n_rhs, double& flop_decompose,
+                     double& flop_solve, unsigned& n_nonzero_factor, double& buffer) const;
+};
+
+// LAWN-41 flop counts (LINAL/src/util.cxx:60-116), real and complex.
+double get_flop_gemm(int is_complex, int m, int n, int k);
+double get_flop_syrk(int is_complex, int k, int n);
+double get_flop_trsm_lower(int is_complex, int m, int n);
+double get_flop_trsm_upper(int is_complex, int m, int n);
+double get_flop_lu(int is_complex, int m, int n);
+double get_flop_chol(int is_complex, int n);
+
+class Mesh_ {
+ public:
+  Mesh_();
+  ~Mesh_();
+
+  // --- topology (mesh.hxx:82-180) -------------------------------------
+  Node add_node(int id, int n_dof);
+  Node add_node(int id, int n_dof, int p);
+  Node add_node(std::pair<int, int> id, int n_dof);
+  Node add_node(std::pair<int, int> id, int n_dof, int p);
+  Node add_node(std::pair<int, int> id, int n_dof, int p, int kind);
+  Node find_node(int id);
+  Node find_node(std::pair<int, int> id);
+  Element add_element();
+  Element add_element(int gen);
+  Element find_element(int id);
+  Element get_root();
+  Element refine_element(int id, int n_children);
+  int get_n_nodes() const { return (int)nodes.size(); }
+  int get_n_elements() const { return (int)elements.size(); }
+  bool import_file(const char* full_path);
+  void reset();
+
+  // --- solving sequence (mesh.hxx:182-300) ----------------------------
+  void lock();
+  void unlock();
+  int is_locked() const { return locker; }
+  void create_matrix_without_buffer(int datatype, int n_rhs);
+  void create_matrix_buffer(int is_schur = 0);
+  void create_leaf_matrix_buffer();
+  void create_element_matrix_buffer(int is_schur = 0);
+  void free_matrix();
+
+  void copy_in(Element elt, int datatype, int m, int n, int* nods, int side, void* buffer);
+  void copy_in(Element elt, int datatype, int m, int n, int nod_disp, int* nods, int side,
+               void* buffer);
+  void copy_out(Element elt, int datatype, int m, int n, int* nods, int side, void* buffer);
+  void copy_out(Element elt, int datatype, int m, int n, int nod_disp, int* nods, int side,
+                void* buffer);
+  void set_rhs();
+
+  void chol_with_free();
+  void chol_without_free();
+  void solve_chol_1();
+  void solve_chol_2();
+  void solve_chol();
+  void check_chol();
+  void lu_nopiv_with_free();
+  void lu_nopiv_without_free();
+  void solve_lu_nopiv_1();
+  void solve_lu_nopiv_2();
+  void solve_lu_nopiv();
+  void check_lu_nopiv();
+  void lu_piv_with_free();
+  void lu_piv_without_free();
+  void solve_lu_piv_1();
+  void solve_lu_piv_2();
+  void solve_lu_piv();
+  void check_lu_piv();
+
+  double get_residual();
+  unsigned get_n_dof();
+  unsigned get_n_nonzero();
+  unsigned get_n_nonzero_factor();
+  void estimate_cost(int method, int datatype, int n_rhs, double& flop_decompose,
+                     double& flop_solve, unsigned& n_nonzero_factor, double& buffer);
+
+  // --- internals used by the engine -----------------------------------
+  std::map<std::pair<int, int>, Node_> nodes;
+  std::map<int, Element_> elements;
+  std::map<int, std::vector<Element>, std::greater<int>> by_generation;  // leaf -> root
+  std::vector<Element> leaves;
+  int id_element = 0;
+  int locker = 0;
+  int n_rhs = 1;
+  int datatype = UHM_REAL;
+  int64_t n_dof_total = 0;
+  Engine* engine = nullptr;
+
+  Engine& eng();
+  void run_factor(int method, int keep_schur);
+  void run_solve(int method, int phase);
+};
+
+}  // namespace uhm
