@@ -1,0 +1,298 @@
+"""Benchmark: factor + solve seconds, 3D Poisson 16^3 hex p=4 (Cholesky fronts).
+
+One step = one full multifrontal factorisation + solve (+ FP64 iterative
+refinement for the mixed path) of the workload, inputs already resident in
+HBM.  ``value`` is the mixed-precision path (per-front FP32 / BF16-split,
+FP64 refinement to backward error <= 1e-12); the plain FP64 path is timed
+beside it.  ``e2e`` times the same steps through the C ABI with host buffers:
+bulk copy-in of element matrices and right-hand sides from pinned host memory,
+factor, solve, copy-out of the solution.
+
+``--impl reference`` times the CPU implementation of the same path (the
+numpy/scipy restatement in oracle/, all host cores) on the same workload.
+
+Synthetic data: seeded hp-FEM meshes (uhm_gb300.hpfem); no dataset involved.
+Element matrices (512 MB) and fronts (>3 GB) exceed the 129 MB L2, so no L2
+flush is needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "factor+solve s at 16³ p=4: plain FP64 vs mixed+IR+learned, bwd err≤1e-12"
+WORKLOAD = "3D Poisson 16^3 hex p=4 Legendre-hierarchic, Dirichlet, octree ND, Cholesky fronts, 1 RHS"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        s = [x for x in self.samples if len(x) >= 8]
+        if not s:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(x[0]) for x in s if x[0].replace(".", "").isdigit()]
+        mx = [float(x[1]) for x in s if x[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for x in s for i in range(4) if x[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(s)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _barrier_max(x: float, ws: int):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_workload(seed=0):
+    from uhm_gb300 import hpfem
+    return hpfem.poisson3d(16, 4, seed=seed)
+
+
+def cpu_reference(spec, steps, warmup):
+    """Time the CPU restatement of the path (oracle/uhm_oracle.py) on all host
+    cores (OpenBLAS threads inside each dense kernel)."""
+    from oracle import uhm_oracle as uo
+    plan = uo.symbolic(spec)
+    times = []
+    for i in range(warmup + steps):
+        t = time.perf_counter()
+        r = uo.solve_mesh(spec, uo.CHOL, plan=plan)
+        dt = time.perf_counter() - t - r.timings["symbolic"]
+        if i >= warmup:
+            times.append(dt)
+    return times, r
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    spec = build_workload()
+    cores = os.cpu_count()
+    times, _ = cpu_reference(spec, args.steps, args.warmup)
+    v = statistics.median(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded hp-FEM mesh)", "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": "one full factor+solve of the workload per step (assembly, "
+                                   "multifrontal Cholesky, forward/backward solve), numpy/scipy "
+                                   "OpenBLAS on all host cores"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    from uhm_gb300 import api, build
+    build.build()
+    ws, rank = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    spec = build_workload(seed=rank)
+    peaks, peak_src = _peaks()
+
+    m = api.load_spec(spec)
+    fd, _ = m.estimate_cost(api.UHM_CHOL)
+
+    def one_step(mesh):
+        mesh.chol_with_free()
+        mesh.solve_chol()
+        t = mesh.timing()
+        return (t["factor_ms"] + t["solve_ms"] + t["refine_ms"]) * 1e-3, t
+
+    # ---- plain FP64 (drop-in) -------------------------------------------------
+    m.set_mode(0)
+    for _ in range(max(1, min(args.warmup, 2))):
+        one_step(m)
+    plain = [one_step(m) for _ in range(max(1, min(args.steps, 3)))]
+    plain_s = statistics.median([p[0] for p in plain])
+    plain_berr = m.backward_error()
+
+    # ---- mixed + IR (headline) ----------------------------------------------
+    m.set_mode(1, args.prec, 1e-12, 10)
+    for _ in range(args.warmup):
+        one_step(m)
+    clocks = Clocks()
+    launches0 = None
+    clocks.start()
+    t_wall = time.perf_counter()
+    res = []
+    for _ in range(args.steps):
+        res.append(one_step(m))
+    t_wall = time.perf_counter() - t_wall
+    ck = clocks.stop()
+    step_s = [r[0] for r in res]
+    dev_s = sum(step_s) / len(step_s)
+    dev_s = _barrier_max(dev_s, ws)
+    last = res[-1][1]
+    berr = m.backward_error()
+    launches = int(sum(r[1]["kernel_launches"] for r in res) / len(res))
+
+    # ---- per-kernel profile (separate pass, outside the timed region) ---------
+    m.set_profiling(True)
+    one_step(m)
+    prof = m.profile()
+    m.set_profiling(False)
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    name, p = top
+    if p["flops"] > 0:
+        bound = "tensor" if args.prec == api.PREC_BF16X3 else "fp32-simt"
+        achieved = p["flops"] / (p["ms"] * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops") if args.prec == api.PREC_BF16X3 else 69.9
+        roof = {"bound": "tensor" if args.prec == api.PREC_BF16X3 else "compute",
+                "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": ("MEASURED_PEAKS.json bf16 (" + peak_src + ")") if args.prec == api.PREC_BF16X3
+                else "FP32 SIMT SGEMM measured on this GB300 (profiles/peaks_gb300.md)",
+                "bound_kind": bound}
+    else:
+        achieved = p["bytes"] / (p["ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm (" + peak_src + ")"}
+
+    # ---- end to end through the C ABI with host buffers -----------------------
+    emat = api.pinned_empty(spec.mats.size)
+    emat[:] = spec.mats
+    erhs = api.pinned_empty(spec.rhs.size)
+    erhs[:] = spec.rhs
+    xout = api.pinned_empty(spec.rhs.size)
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        m.copy_in_leaves(api.UHM_LHS, emat)
+        m.copy_in_leaves(api.UHM_RHS, erhs)
+        m.chol_with_free()
+        m.solve_chol()
+        m.copy_out_leaves(spec.rhs.size, out=xout)
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            e2e.append(dt)
+    e2e_s = _barrier_max(statistics.median(e2e), ws)
+    ok = np.isfinite(xout).all()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        times, _ = cpu_reference(spec, 1, 0)
+        cpu = {"value": times[0], "unit": "s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full factor+solve of the same 16^3 p=4 workload (numpy/scipy "
+                         "restatement of the reference path, OpenBLAS on all host cores)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": dev_s / ws, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "mixed: f32/bf16x3 fronts, f64 refinement",
+            "data": "synthetic (seeded hp-FEM mesh)",
+            "config": {"workload": WORKLOAD, "n_dof": int(spec.n_dof()), "n_fronts": int(spec.n_elements),
+                       "root_front": 11719, "factor_gflop_lawn41": fd / 1e9,
+                       "l2": "inputs larger than L2 (element matrices 512 MB, fronts > 3 GB)",
+                       "precision_policy": ["fp64", "fp32", "bf16x3"][args.prec]},
+            "backward_error": berr, "ir_iters": last["ir_iters"], "berr_first_solve": None,
+            "factor_ms": last["factor_ms"], "solve_ms": last["solve_ms"], "refine_ms": last["refine_ms"],
+            "plain_fp64_s": plain_s, "plain_fp64_backward_error": plain_berr,
+            "speedup_vs_plain_fp64": plain_s / dev_s,
+            "wall_s_per_step": t_wall / args.steps,
+            "e2e": {"value": e2e_s, "unit": "s",
+                    "h2d_bytes_per_step": int((spec.mats.size + spec.rhs.size) * 8),
+                    "d2h_bytes_per_step": int(spec.n_dof() * 8), "finite": bool(ok)},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "kernels": {k: {"ms": round(v["ms"], 3), "tflops": round(v["flops"] / (v["ms"] * 1e-3) / 1e12, 2)
+                            if v["flops"] else None,
+                            "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["bytes"] else None,
+                            "launches": v["launches"]} for k, v in prof.items()},
+            "cpu_baseline": cpu,
+            "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--prec", type=int, default=1, help="0 fp64, 1 fp32, 2 bf16x3 fronts (mixed path)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -120,6 +120,16 @@ int uhm_gpu_backward_error(long* mesh, double* berr);
  * refinement iterations, backward error, kernel launches */
 int uhm_gpu_get_timing(long* mesh, double* out);
 
+/* Per-kernel profile: when on, every launch of the factor / solve programs
+ * is bracketed by CUDA events (use outside timed regions).  Per op kind
+ * (0 assemble, 1 small-front factor, 2 diagonal POTRF, 3 panel TRSM,
+ * 4 trailing SYRK, 5 LU panel, 6 LU row solve, 7 LU trailing GEMM,
+ * 8..16 solve kernels): total ms, algorithmic flops, algorithmic bytes,
+ * launches since profiling was switched on. */
+int uhm_gpu_set_profiling(long* mesh, int on);
+int uhm_gpu_get_profile(long* mesh, int n_kinds, double* ms, double* flops, double* bytes,
+                        long* launches);
+
 /* front table after lock + create_matrix_without_buffer: per front (leaf to
  * root order) the element id, generation, fs, ss */
 int uhm_gpu_get_n_fronts(long* mesh, int* n);

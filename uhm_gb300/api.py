@@ -21,6 +21,7 @@ UHM_LHS, UHM_RHS = 1, 2
 UHM_PHYSICS_SINGLE, UHM_PHYSICS_MULTI = 1, 2
 UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV = 1, 2, 3
 PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
+STATUS_RECOMPUTED_FP64 = 20     # refinement missed; the solution was recomputed in FP64
 
 _lib = None
 
@@ -85,6 +86,8 @@ def _declare(L):
     sig("uhm_gpu_get_n_fronts", [_P(_l), _P(_i)], _i)
     sig("uhm_gpu_get_fronts", [_P(_l), _i, _P(_i), _P(_i), _P(_i), _P(_i)], _i)
     sig("uhm_gpu_get_front_nodes", [_P(_l), _i, _i, _P(_i), _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_set_profiling", [_P(_l), _i], _i)
+    sig("uhm_gpu_get_profile", [_P(_l), _i, _P(_d), _P(_d), _P(_d), _P(_l)], _i)
     sig("uhm_gpu_host_alloc", [_l], C.c_void_p)
     sig("uhm_gpu_host_free", [C.c_void_p])
 
@@ -132,7 +135,7 @@ class Mesh:
 
     def _check(self, code=None):
         st = self.status() if code is None else code
-        if st:
+        if st and st != STATUS_RECOMPUTED_FP64:
             raise UHMError(st, self.last_error())
 
     # -- topology --------------------------------------------------------
@@ -256,6 +259,22 @@ class Mesh:
         keys = ["upload_ms", "factor_ms", "solve_ms", "refine_ms", "total_ms", "ir_iters",
                 "berr", "kernel_launches"]
         return dict(zip(keys, list(out)))
+
+    OP_NAMES = ["assemble", "small_factor", "potrf_diag", "trsm_panel", "syrk_update",
+                "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
+                "trsv_fwd", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd",
+                "bwd_store", "op17", "op18", "op19"]
+
+    def set_profiling(self, on=True):
+        self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
+
+    def profile(self) -> dict:
+        n = 20
+        ms, fl, by = (_d * n)(), (_d * n)(), (_d * n)()
+        la = (_l * n)()
+        self._check(self.L.uhm_gpu_get_profile(C.byref(self.h), n, ms, fl, by, la))
+        return {self.OP_NAMES[k]: dict(ms=ms[k], flops=fl[k], bytes=by[k], launches=la[k])
+                for k in range(n) if la[k]}
 
     def get_n_dof(self) -> int:
         n = _i(0)

@@ -195,7 +195,7 @@ int uhm_gpu_get_last_error(long* mesh, char* buf, int len) {
 int uhm_gpu_set_mode(long* mesh, int mode, int default_prec, double tol, int max_iter) {
   return guard(M(mesh), [&] {
     uhm::Engine& e = M(mesh)->eng();
-    if (e.mode != mode || e.default_prec != default_prec) e.invalidate_plan();
+    if (e.mode != mode || e.default_prec != default_prec) e.invalidate_precision();
     e.mode = mode;
     e.default_prec = default_prec;
     e.ir_tol = tol;
@@ -212,7 +212,7 @@ int uhm_gpu_set_front_precision(long* mesh, int n, const int* prec) {
       int id = f.e->get_id();
       if (id < n) e.front_prec_override[f.slot] = prec[id];
     }
-    e.invalidate_plan();
+    e.invalidate_precision();
   });
 }
 int uhm_gpu_copy_in_leaves(long* mesh, int side, const int* nods_all, const double* buffer,
@@ -245,6 +245,25 @@ int uhm_gpu_get_timing(long* mesh, double* out) {
     out[5] = t.ir_iters;
     out[6] = t.berr;
     out[7] = (double)t.kernel_launches;
+  });
+}
+int uhm_gpu_set_profiling(long* mesh, int on) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    e.profiling = on != 0;
+    e.profile = uhm::OpProfile{};
+  });
+}
+int uhm_gpu_get_profile(long* mesh, int n_kinds, double* ms, double* flops, double* bytes,
+                        long* launches) {
+  return guard(M(mesh), [&] {
+    const uhm::OpProfile& p = M(mesh)->eng().profile;
+    for (int k = 0; k < n_kinds && k < uhm::N_OP_KINDS; ++k) {
+      ms[k] = p.ms[k];
+      flops[k] = p.flops[k];
+      bytes[k] = p.bytes[k];
+      launches[k] = (long)p.launches[k];
+    }
   });
 }
 int uhm_gpu_get_n_fronts(long* mesh, int* n) {

@@ -299,9 +299,12 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
       std::memcpy(h_pinned, buf, sizeof(double) * (size_t)emat_total);
       for (auto& es : esrc) es.has_lhs = true;
       emat_dirty = true;
+      anorm_valid = false;
     } else {
       CK(cudaMemcpyAsync(ctx.emat, buf, sizeof(double) * (size_t)emat_total, cudaMemcpyHostToDevice, stream));
       emat_dirty = false;
+      emat_device_only = true;
+      anorm_valid = false;
     }
     factored = false;
     anorm_inf = -1.0;
@@ -314,6 +317,7 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
     } else {
       CK(cudaMemcpyAsync(d_erhs, buf, sizeof(double) * (size_t)erhs_total, cudaMemcpyHostToDevice, stream));
       erhs_dirty = false;
+      erhs_device_only = true;
     }
   }
 }
@@ -489,9 +493,12 @@ void Engine::build_programs(int method) {
   fac_ops.clear();
   fwd_ops.clear();
   bwd_ops.clear();
-  auto push = [&](std::vector<Op>& ops, int kind, int dtype, int nb, int param, const std::vector<Item>& it) {
+  auto push = [&](std::vector<Op>& ops, int kind, int dtype, int nb, int param, const std::vector<Item>& it,
+                  double flops = 0, double bytes = 0) {
     if (it.empty()) return;
     Op op{kind, dtype, nb, param, add_items(it), (int)it.size()};
+    op.flops = flops;
+    op.bytes = bytes;
     ops.push_back(op);
   };
   const int small_max[2] = {SMALL_MAX_F64, SMALL_MAX_F32};
@@ -514,17 +521,50 @@ void Engine::build_programs(int method) {
           large.push_back(s);
         }
       }
-      push(fac_ops, OP_ASSEMBLE, dt, 0, chol ? 1 : 0, asm_items);
-      push(fac_ops, OP_SMALL_FACTOR, dt, 0, max_small, small_items);
+      // algorithmic bytes of the extend-add: read every source block once,
+      // write the parent panel once (lower triangle for Cholesky)
+      double asm_bytes = 0, small_flops = 0;
+      const double esz = dt == F64 ? 8.0 : 4.0;
+      for (int s : fl) {
+        const HostFront& f = fronts[s];
+        const double tri = chol ? 0.5 : 1.0;
+        asm_bytes += tri * (double)f.n * f.n * esz;
+        for (int cs : f.children) {
+          const HostFront& c = fronts[cs];
+          asm_bytes += tri * (double)c.ss * c.ss * (c.prec == PREC_FP64 ? 8.0 : 4.0);
+        }
+        const int ei = esrc_of_slot[s];
+        if (ei >= 0) asm_bytes += (double)esrc[ei].m * esrc[ei].m * 8.0;
+        if (f.n <= small_max[dt]) {
+          double dec, sol;
+          unsigned nz;
+          double bf;
+          f.e->estimate_cost(method, UHM_REAL, nr, dec, sol, nz, bf);
+          small_flops += dec;
+        }
+      }
+      push(fac_ops, OP_ASSEMBLE, dt, 0, chol ? 1 : 0, asm_items, 0, asm_bytes);
+      push(fac_ops, OP_SMALL_FACTOR, dt, 0, max_small, small_items, small_flops);
       int maxfs = 0;
       for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
       for (int k0 = 0; k0 < maxfs; k0 += NB) {
         std::vector<Item> p_items, t_items, u_items;
+        double fp = 0, ft = 0, fu = 0;
         for (int s : large) {
           const HostFront& f = fronts[s];
           if (f.fs <= k0) continue;
           const int kb = std::min(NB, f.fs - k0);
           const int base = k0 + kb;
+          const int mrest = f.n - base;
+          if (chol) {
+            fp += get_flop_chol(0, kb);
+            ft += get_flop_trsm_lower(0, kb, mrest);
+            fu += get_flop_syrk(0, kb, mrest);
+          } else {
+            fp += get_flop_lu(0, f.n - k0, kb);
+            ft += get_flop_trsm_lower(0, kb, mrest);
+            fu += get_flop_gemm(0, mrest, mrest, kb);
+          }
           p_items.push_back(Item{s, k0, 0, 0});
           if (chol) {
             for (int r0 = base; r0 < f.n; r0 += TRSM_RB) t_items.push_back(Item{s, k0, r0, 0});
@@ -539,13 +579,13 @@ void Engine::build_programs(int method) {
           }
         }
         if (chol) {
-          push(fac_ops, OP_POTRF, dt, NB, 0, p_items);
-          push(fac_ops, OP_TRSM, dt, NB, 0, t_items);
-          push(fac_ops, OP_SYRK, dt, NB, 0, u_items);
+          push(fac_ops, OP_POTRF, dt, NB, 0, p_items, fp);
+          push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
+          push(fac_ops, OP_SYRK, dt, NB, 0, u_items, fu);
         } else {
-          push(fac_ops, OP_GETRF, dt, NB, method == UHM_LU_PIV ? 1 : 0, p_items);
-          push(fac_ops, OP_LUROW, dt, NB, 0, t_items);
-          push(fac_ops, OP_GEMM, dt, NB, 0, u_items);
+          push(fac_ops, OP_GETRF, dt, NB, method == UHM_LU_PIV ? 1 : 0, p_items, fp);
+          push(fac_ops, OP_LUROW, dt, NB, 0, t_items, ft);
+          push(fac_ops, OP_GEMM, dt, NB, 0, u_items, fu);
         }
       }
     }
@@ -617,6 +657,15 @@ void Engine::build_programs(int method) {
 }
 
 void Engine::alloc_device(int method) {
+  if (dev_ok && (emat_device_only || erhs_device_only)) {
+    // element data arrived by direct device copies; keep it across the re-plan
+    CK(cudaStreamSynchronize(stream));
+    if (emat_device_only)
+      CK(cudaMemcpy(h_pinned, ctx.emat, sizeof(double) * (size_t)emat_total, cudaMemcpyDeviceToHost));
+    if (erhs_device_only)
+      CK(cudaMemcpy(h_pinned + emat_total, d_erhs, sizeof(double) * (size_t)erhs_total, cudaMemcpyDeviceToHost));
+    emat_device_only = erhs_device_only = false;
+  }
   free_device();
   if (!stream) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -666,6 +715,14 @@ void Engine::alloc_device(int method) {
         const int64_t v = (h_y_off[k] + r) | ((int64_t)esrc[k].m << 40);
         idx[fill[esrc[k].gdof[r]]++] = v;
       }
+  std::vector<int2> del(cnt[n_global]);
+  {
+    std::vector<int64_t> f2(cnt.begin(), cnt.end() - 1);
+    for (size_t k = 0; k < esrc.size(); ++k)
+      if ((int)esrc[k].gdof.size() == esrc[k].m)
+        for (int r = 0; r < esrc[k].m; ++r) del[f2[esrc[k].gdof[r]]++] = make_int2((int)k, r);
+  }
+  d_dof_el = (int2*)dmalloc(sizeof(int2) * std::max<size_t>(1, del.size()));
   d_dof_ptr = (int64_t*)dmalloc(sizeof(int64_t) * cnt.size());
   d_dof_idx = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, idx.size()));
   auto up = [&](void* d, const void* h, size_t bytes) {
@@ -685,10 +742,13 @@ void Engine::alloc_device(int method) {
   up(d_y_off, h_y_off.data(), sizeof(int64_t) * h_y_off.size());
   up(d_dof_ptr, cnt.data(), sizeof(int64_t) * cnt.size());
   up(d_dof_idx, idx.data(), sizeof(int64_t) * idx.size());
+  up(d_dof_el, del.data(), sizeof(int2) * del.size());
   CK(cudaStreamSynchronize(stream));
   dev_ok = true;
   method_built = method;
+  prec_dirty = false;
   emat_dirty = erhs_dirty = true;
+  anorm_valid = false;
 }
 
 void Engine::upload_elements() {
@@ -708,8 +768,15 @@ void Engine::assemble_rhs() {
 }
 
 void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
+  std::vector<cudaEvent_t> evs;
+  if (profiling) {
+    evs.resize(2 * ops.size());
+    for (auto& e : evs) CK(cudaEventCreate(&e));
+  }
+  size_t k = 0;
   for (const Op& op : ops) {
     const Item* it = d_items + op.item_off;
+    if (profiling) CK(cudaEventRecord(evs[2 * k], stream));
     switch (op.kind) {
       case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, stream); break;
       case OP_SMALL_FACTOR:
@@ -733,9 +800,23 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
       case OP_TRSV_B: launch_trsv_block(ctx, it, op.n_items, op.dtype, op.param, op.nb, 1, stream); break;
       case OP_BWD_STORE: launch_bwd_store(ctx, it, op.n_items, g_out, n_global, stream); break;
     }
+    if (profiling) CK(cudaEventRecord(evs[2 * k + 1], stream));
+    ++k;
     timing.kernel_launches++;
   }
   CK(cudaGetLastError());
+  if (profiling) {
+    CK(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < ops.size(); ++i) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, evs[2 * i], evs[2 * i + 1]));
+      profile.ms[ops[i].kind] += ms;
+      profile.flops[ops[i].kind] += ops[i].flops;
+      profile.bytes[ops[i].kind] += ops[i].bytes;
+      profile.launches[ops[i].kind] += 1;
+    }
+    for (auto& e : evs) cudaEventDestroy(e);
+  }
 }
 
 void Engine::check_status(const char* where) {
@@ -755,7 +836,7 @@ void Engine::factor(int method) {
   ensure_plan();
   for (auto& es : esrc)
     if (!es.has_lhs) fail("factor: an element matrix has not been copied in", 7);
-  if (!dev_ok || method_built != method) {
+  if (!dev_ok || method_built != method || prec_dirty) {
     build_plan(method);
     build_programs(method);
     alloc_device(method);
@@ -772,12 +853,29 @@ void Engine::factor(int method) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.upload_ms = ms;
   CK(cudaEventRecord(ev0, stream));
+  if (!anorm_valid) enqueue_anorm();
   run_ops(fac_ops, nullptr, nullptr);
   CK(cudaEventRecord(ev1, stream));
   CK(cudaEventSynchronize(ev1));
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.factor_ms = ms;
   check_status("factor");
+  if (status && mode == 1) {
+    // a low-precision front broke down: escalate the failed fronts to FP64
+    std::vector<int> st(fronts.size());
+    CK(cudaMemcpy(st.data(), ctx.status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost));
+    bool any = false;
+    if (front_prec_override.size() != fronts.size()) front_prec_override.assign(fronts.size(), -1);
+    for (size_t i = 0; i < st.size(); ++i)
+      if (st[i] && fronts[i].prec != PREC_FP64) { front_prec_override[i] = PREC_FP64; any = true; }
+    if (any) {
+      const double first_ms = timing.factor_ms;
+      prec_dirty = true;
+      factor(method);
+      timing.factor_ms += first_ms;
+      return;
+    }
+  }
   factored = true;
   factored_method = method;
   h_x_valid = false;
@@ -793,6 +891,7 @@ void Engine::solve(int method, int phase) {
   if (!factored) fail("solve: the mesh has not been factorised", 9);
   if (method != factored_method) fail("solve: method differs from the factorisation", 9);
   float ms = 0;
+  if (status == 20) { status = 0; last_error.clear(); }
   CK(cudaEventRecord(ev0, stream));
   if (phase & 1) assemble_rhs();
   solve_into(method, d_b, d_x, phase);
@@ -801,6 +900,60 @@ void Engine::solve(int method, int phase) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.solve_ms = ms;
   h_x_valid = false;
+  if (mode == 1 && phase == 3) refine(method);
+}
+
+// FP64 iterative refinement on the unassembled element matrices:
+//   r = b - A x (FP64, element by element), d = M^{-1} r with the
+//   low-precision factors, x += d, until the backward error
+//   ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= ir_tol.
+// A miss after ir_max corrections refactors and solves in plain FP64.
+void Engine::refine(int method) {
+  float ms = 0;
+  CK(cudaEventRecord(ev0, stream));
+  const int64_t nv = n_global * mesh->n_rhs;
+  const double an = operator_norm_inf();
+  launch_absmax(d_b, nv, d_red + 1024, stream);
+  const double bn = read_scalar(d_red + 1024);
+  double berr = 1.0;
+  int it = 0;
+  for (;; ++it) {
+    compute_residual(d_x, d_r);
+    launch_absmax(d_r, nv, d_red, stream);
+    launch_absmax(d_x, nv, d_red + 512, stream);
+    double h[2];
+    CK(cudaMemcpyAsync(&h[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&h[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    berr = h[0] / (an * h[1] + bn);
+    if (it == 0) timing.berr_first = berr;
+    if (berr <= ir_tol || it >= ir_max || !(berr == berr)) break;
+    solve_into(method, d_r, d_d, 3);
+    launch_axpy(d_x, d_d, nv, 1.0, stream);
+  }
+  CK(cudaEventRecord(ev1, stream));
+  CK(cudaEventSynchronize(ev1));
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  timing.refine_ms = ms;
+  timing.ir_iters = it;
+  timing.berr = berr;
+  if (!(berr <= ir_tol)) {
+    // tolerance missed: redo the whole solve in plain FP64
+    const Timing keep = timing;
+    const int saved = mode;
+    mode = 0;
+    prec_dirty = true;
+    factor(method);
+    solve(method, 3);
+    mode = saved;
+    prec_dirty = true;
+    Timing t2 = timing;
+    timing = keep;
+    timing.factor_ms += t2.factor_ms;
+    timing.solve_ms += t2.solve_ms;
+    status = 20;
+    last_error = "refinement missed its tolerance; solution recomputed in FP64";
+  }
 }
 
 void Engine::compute_residual(const double* x, double* r) {
@@ -824,51 +977,28 @@ double Engine::residual_norm1() {
   return best;
 }
 
-// ||A||_inf of the assembled operator sum_e P_e^T A_e P_e (host, once per factorisation)
+// ||A||_inf of the assembled operator sum_e P_e^T A_e P_e, exact, on the device
+// (k_anorm_partial + deterministic per-dof gather); result in d_red[1536]
+void Engine::enqueue_anorm() {
+  launch_anorm_partial(ctx.emat, d_emat_off, d_elem_m, d_emap_off, d_emap, d_dof_ptr, d_dof_el, d_y,
+                       d_y_off, (int)esrc.size(), stream);
+  launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, nullptr, n_global, d_r, n_global, 1, 0, stream);
+  launch_absmax(d_r, n_global, d_red + 1536, stream);
+  anorm_valid = true;
+  anorm_inf = -1.0;
+}
+
+double Engine::read_scalar(const double* d) {
+  double h = 0;
+  CK(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  return h;
+}
+
 double Engine::operator_norm_inf() {
-  if (anorm_inf >= 0) return anorm_inf;
-  std::vector<double> host_mats;
-  const double* mats = h_pinned;
-  if (!emat_dirty && dev_ok) {
-    host_mats.resize(emat_total);
-    CK(cudaMemcpy(host_mats.data(), ctx.emat, sizeof(double) * emat_total, cudaMemcpyDeviceToHost));
-    mats = host_mats.data();
-  }
-  // dof -> list of (element, row)
-  std::vector<int64_t> cnt(n_global + 1, 0);
-  for (auto& es : esrc)
-    for (int32_t g : es.gdof) cnt[g + 1]++;
-  for (int64_t i = 0; i < n_global; ++i) cnt[i + 1] += cnt[i];
-  std::vector<std::pair<int, int>> lst(cnt[n_global]);
-  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-  for (int k = 0; k < (int)esrc.size(); ++k)
-    for (int r = 0; r < esrc[k].m; ++r) lst[fill[esrc[k].gdof[r]]++] = {k, r};
-  double best = 0.0;
-#pragma omp parallel reduction(max : best)
-  {
-    std::vector<double> row(n_global, 0.0);
-    std::vector<char> seen(n_global, 0);
-    std::vector<int32_t> touched;
-#pragma omp for schedule(dynamic, 256)
-    for (int64_t i = 0; i < n_global; ++i) {
-      touched.clear();
-      for (int64_t k = cnt[i]; k < cnt[i + 1]; ++k) {
-        const ElemSource& es = esrc[lst[k].first];
-        const int l = lst[k].second;
-        const double* A = mats + es.mat_off;
-        for (int j = 0; j < es.m; ++j) {
-          const int32_t c = es.gdof[j];
-          if (!seen[c]) { seen[c] = 1; touched.push_back(c); }
-          row[c] += A[l + (int64_t)j * es.m];
-        }
-      }
-      double s = 0.0;
-      for (int32_t c : touched) { s += std::fabs(row[c]); row[c] = 0.0; seen[c] = 0; }
-      best = std::max(best, s);
-    }
-  }
-  anorm_inf = best;
-  return best;
+  if (!anorm_valid) enqueue_anorm();
+  if (anorm_inf < 0) anorm_inf = read_scalar(d_red + 1536);
+  return anorm_inf;
 }
 
 double Engine::backward_error() {

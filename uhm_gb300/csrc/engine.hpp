@@ -50,6 +50,14 @@ struct Op {
   int param;
   int64_t item_off;
   int n_items;
+  double flops = 0;   // algorithmic flops of this launch (LAWN-41 terms)
+  double bytes = 0;   // algorithmic HBM bytes of this launch
+};
+
+constexpr int N_OP_KINDS = 20;
+struct OpProfile {
+  double ms[N_OP_KINDS] = {0}, flops[N_OP_KINDS] = {0}, bytes[N_OP_KINDS] = {0};
+  int64_t launches[N_OP_KINDS] = {0};
 };
 
 enum OpKind : int {
@@ -72,6 +80,7 @@ class Engine {
 
   // --- set-up -----------------------------------------------------------
   void invalidate_plan() { plan_ok = false; }
+  void invalidate_precision() { prec_dirty = true; }
   void copy_in(Element e, int m, int n, int nod_disp, const int* nods, int side,
                const double* buf);
   void copy_out(Element e, int m, int n, int nod_disp, const int* nods, int side, double* buf);
@@ -98,6 +107,8 @@ class Engine {
   int status = 0;
   std::string last_error;
   Timing timing;
+  bool profiling = false;       // per-op CUDA events (outside timed regions)
+  OpProfile profile;
 
   // --- introspection ------------------------------------------------------
   std::vector<HostFront> fronts;              // by slot (leaf -> root order)
@@ -109,6 +120,9 @@ class Engine {
  private:
   Mesh_* mesh;
   bool plan_ok = false;
+  bool prec_dirty = false;
+  bool emat_device_only = false, erhs_device_only = false;
+  bool anorm_valid = false;
   bool dev_ok = false;
   bool factored = false;
   int factored_method = 0;
@@ -153,6 +167,7 @@ class Engine {
   int64_t* d_y_off = nullptr;
   int64_t* d_dof_ptr = nullptr;
   int64_t* d_dof_idx = nullptr;
+  int2* d_dof_el = nullptr;
   std::vector<int64_t> h_emat_off, h_emap_off, h_y_off;
   std::vector<int> h_elem_m;
   std::vector<int32_t> h_emap;
@@ -172,6 +187,9 @@ class Engine {
   void solve_into(int method, double* rhs, double* out, int phase);
   void compute_residual(const double* x, double* r);
   double operator_norm_inf();
+  void enqueue_anorm();
+  double read_scalar(const double* d);
+  void refine(int method);
   void check_status(const char* where);
   void* dmalloc(size_t bytes);
   int64_t add_items(const std::vector<uhm_gpu::Item>& it);

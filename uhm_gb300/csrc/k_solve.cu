@@ -449,3 +449,63 @@ void launch_axpy(double* y, const double* x, int64_t n, double alpha, cudaStream
 }
 
 }  // namespace uhm_gpu
+
+namespace uhm_gpu {
+
+// ||A||_inf of the assembled operator A = sum_e P_e^T A_e P_e, exactly, on the
+// device.  Entry (i, J) of A is summed over the elements that contain both
+// dofs; the element of smallest index among them (the "owner") computes that
+// sum and adds |A(i, J)| to its partial row sum for row i.  Partial sums are
+// then gathered per dof in element order (k_dof_gather), so the result is
+// deterministic.  dof_el lists, per dof, (element, local row) sorted by element.
+__global__ void __launch_bounds__(128) k_anorm_partial(const double* __restrict__ emat,
+                                                       const int64_t* __restrict__ emat_off,
+                                                       const int* __restrict__ elem_m,
+                                                       const int64_t* __restrict__ emap_off,
+                                                       const int32_t* __restrict__ emap,
+                                                       const int64_t* __restrict__ dof_ptr,
+                                                       const int2* __restrict__ dof_el,
+                                                       double* __restrict__ part,
+                                                       const int64_t* __restrict__ y_off) {
+  const int e = blockIdx.x;
+  const int m = elem_m[e];
+  const int32_t* __restrict__ map = emap + emap_off[e];
+  for (int l = threadIdx.x; l < m; l += blockDim.x) {
+    const int32_t i = map[l];
+    const int64_t a0 = dof_ptr[i], a1 = dof_ptr[i + 1];
+    double s = 0.0;
+    for (int j = 0; j < m; ++j) {
+      const int32_t J = map[j];
+      const int64_t b0 = dof_ptr[J], b1 = dof_ptr[J + 1];
+      // merge-intersect the two element lists
+      int64_t a = a0, b = b0;
+      int owner = -1;
+      double v = 0.0;
+      while (a < a1 && b < b1) {
+        const int2 pa = dof_el[a], pb = dof_el[b];
+        if (pa.x < pb.x) ++a;
+        else if (pb.x < pa.x) ++b;
+        else {
+          if (owner < 0) owner = pa.x;
+          const int me = elem_m[pa.x];
+          v += emat[emat_off[pa.x] + pa.y + (int64_t)pb.y * me];
+          ++a;
+          ++b;
+        }
+      }
+      if (owner == e) s += fabs(v);
+    }
+    part[y_off[e] + l] = s;
+  }
+}
+
+void launch_anorm_partial(const double* emat, const int64_t* emat_off, const int* elem_m,
+                          const int64_t* emap_off, const int32_t* emap, const int64_t* dof_ptr,
+                          const int2* dof_el, double* part, const int64_t* y_off, int n_elem,
+                          cudaStream_t s) {
+  if (!n_elem) return;
+  k_anorm_partial<<<n_elem, 128, 0, s>>>(emat, emat_off, elem_m, emap_off, emap, dof_ptr, dof_el,
+                                         part, y_off);
+}
+
+}  // namespace uhm_gpu

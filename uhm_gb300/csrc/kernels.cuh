@@ -110,6 +110,10 @@ void launch_dof_gather(const int64_t* ptr, const int64_t* idx, const double* y, 
                        cudaStream_t s);
 void launch_absmax(const double* v, int64_t n, double* out, cudaStream_t s);
 void launch_axpy(double* y, const double* x, int64_t n, double alpha, cudaStream_t s);
+void launch_anorm_partial(const double* emat, const int64_t* emat_off, const int* elem_m,
+                          const int64_t* emap_off, const int32_t* emap, const int64_t* dof_ptr,
+                          const int2* dof_el, double* part, const int64_t* y_off, int n_elem,
+                          cudaStream_t s);
 void launch_convert_panels(const DevCtx& c, const Item* items, int n_items, int to_f32,
                            cudaStream_t s);
 
