@@ -104,9 +104,16 @@ def _barrier_max(x: float, ws: int):
     return float(t.item())
 
 
-def build_workload(seed=0):
-    from uhm_gb300 import hpfem
-    return hpfem.poisson3d(16, 4, seed=seed)
+WORKLOADS = {
+    "poisson3d_16_p4": (lambda seed: __import__("uhm_gb300.hpfem", fromlist=["x"]).poisson3d(16, 4, seed=seed),
+                        WORKLOAD),
+    "poisson3d_8_p4": (lambda seed: __import__("uhm_gb300.hpfem", fromlist=["x"]).poisson3d(8, 4, seed=seed),
+                       "3D Poisson 8^3 hex p=4 (small profiling case)"),
+}
+
+
+def build_workload(seed=0, name="poisson3d_16_p4"):
+    return WORKLOADS[name][0](seed)
 
 
 def cpu_reference(spec, steps, warmup):
@@ -154,8 +161,17 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    spec = build_workload(seed=rank)
+    spec = build_workload(seed=rank, name=args.workload)
     peaks, peak_src = _peaks()
+    if args.profile_only:
+        # one warm factor+solve of the mixed path, for external profilers
+        m = api.load_spec(spec)
+        m.set_mode(1, args.prec, 1e-12, 10)
+        for _ in range(args.steps + args.warmup):
+            m.chol_with_free()
+            m.solve_chol()
+        print(json.dumps({"profile_only": True, "workload": args.workload, "timing": m.timing()}))
+        return
 
     m = api.load_spec(spec)
     fd, _ = m.estimate_cost(api.UHM_CHOL)
@@ -287,6 +303,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--prec", type=int, default=1, help="0 fp64, 1 fp32, 2 bf16x3 fronts (mixed path)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="poisson3d_16_p4", choices=sorted(WORKLOADS))
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run the mixed path only (for ncu launch lists / captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

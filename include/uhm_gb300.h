@@ -116,8 +116,9 @@ int uhm_gpu_get_node_solution(long* mesh, int n_nodes, const int* node_ids, doub
 /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), A the assembled sum of
  * element matrices, evaluated in FP64 on the device */
 int uhm_gpu_backward_error(long* mesh, double* berr);
-/* out[0..7] = upload ms, factor ms, solve ms, refine ms, total ms,
- * refinement iterations, backward error, kernel launches */
+/* out[0..8] = upload ms, factor ms, solve ms, refine ms, total ms,
+ * refinement iterations, backward error, kernel launches, backward error of
+ * the first (unrefined) solve */
 int uhm_gpu_get_timing(long* mesh, double* out);
 
 /* Per-kernel profile: when on, every launch of the factor / solve programs

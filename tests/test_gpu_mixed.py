@@ -21,7 +21,7 @@ def _mixed(spec, method, prec, tol=TOL):
     return m, x
 
 
-@pytest.mark.parametrize("prec", [api.PREC_FP32, api.PREC_BF16X3])
+@pytest.mark.parametrize("prec", [api.PREC_FP32, api.PREC_BF16X3, api.PREC_BF16X6])
 @pytest.mark.parametrize("name,make,method", [
     ("3d_8_p4", lambda: hpfem.poisson3d(8, 4, seed=21), uo.CHOL),
     ("2d_16_p4", lambda: hpfem.poisson2d(16, 4, seed=22), uo.CHOL),
@@ -41,6 +41,18 @@ def test_mixed_refines_to_fp64(native_lib, name, make, method, prec):
     assert uo.backward_error(spec, x, A, b) <= 2 * TOL
     rel = np.abs(x - ref.x).max() / np.abs(ref.x).max()
     assert rel < 1e-6, rel
+
+
+@pytest.mark.parametrize("prec,first_tol", [(api.PREC_BF16X3, 1e-5), (api.PREC_BF16X6, 1e-6)])
+def test_tensor_core_schur_update_accuracy(native_lib, prec, first_tol):
+    """Large fronts (ss >= 128) take the tcgen05 path: the backward error of
+    the first solve shows the factor is accurate to split-BF16 level, and the
+    refinement then reaches 1e-12."""
+    spec = hpfem.poisson3d(8, 4, seed=27)
+    m, x = _mixed(spec, uo.CHOL, prec)
+    t = m.timing()
+    assert t["berr"] <= TOL
+    assert 0 < m.first_backward_error() < first_tol, m.first_backward_error()
 
 
 def test_backward_error_matches_oracle(native_lib):

@@ -20,7 +20,7 @@ UHM_REAL, UHM_COMPLEX = 101, 103
 UHM_LHS, UHM_RHS = 1, 2
 UHM_PHYSICS_SINGLE, UHM_PHYSICS_MULTI = 1, 2
 UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV = 1, 2, 3
-PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16X6 = 0, 1, 2, 3
 STATUS_RECOMPUTED_FP64 = 20     # refinement missed; the solution was recomputed in FP64
 
 _lib = None
@@ -253,8 +253,13 @@ class Mesh:
         a, p = _arr(prec_by_element_id, np.int32, _i)
         self._check(self.L.uhm_gpu_set_front_precision(C.byref(self.h), len(a), p))
 
+    def first_backward_error(self) -> float:
+        out = (_d * 9)()
+        self.L.uhm_gpu_get_timing(C.byref(self.h), out)
+        return out[8]
+
     def timing(self) -> dict:
-        out = (_d * 8)()
+        out = (_d * 9)()
         self.L.uhm_gpu_get_timing(C.byref(self.h), out)
         keys = ["upload_ms", "factor_ms", "solve_ms", "refine_ms", "total_ms", "ir_iters",
                 "berr", "kernel_launches"]
@@ -262,14 +267,15 @@ class Mesh:
 
     OP_NAMES = ["assemble", "small_factor", "potrf_diag", "trsm_panel", "syrk_update",
                 "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
-                "trsv_fwd", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd",
-                "bwd_store", "op17", "op18", "op19"]
+                "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
+                "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags"] + \
+               [f"op{k}" for k in range(21, 32)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
 
     def profile(self) -> dict:
-        n = 20
+        n = 32
         ms, fl, by = (_d * n)(), (_d * n)(), (_d * n)()
         la = (_l * n)()
         self._check(self.L.uhm_gpu_get_profile(C.byref(self.h), n, ms, fl, by, la))

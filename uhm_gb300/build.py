@@ -24,6 +24,7 @@ SOURCES = [
     "engine.cu",
     "k_factor.cu",
     "k_solve.cu",
+    "k_tc_gemm.cu",
 ]
 
 

@@ -245,6 +245,7 @@ int uhm_gpu_get_timing(long* mesh, double* out) {
     out[5] = t.ir_iters;
     out[6] = t.berr;
     out[7] = (double)t.kernel_launches;
+    out[8] = t.berr_first;
   });
 }
 int uhm_gpu_set_profiling(long* mesh, int on) {

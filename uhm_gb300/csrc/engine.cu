@@ -19,7 +19,8 @@ static constexpr int SMALL_MAX_F32 = 224;
 static constexpr int NB = 64;               // panel width of the blocked kernels
 static constexpr int ASM_TJ = 16;           // assembly column tile (k_factor.cu)
 static constexpr int TRSM_RB = 64;
-static constexpr int GEMV_RB = 256;
+static constexpr int FWD_RB = 256;            // k_solve.cu
+static constexpr int BWD_RB = 512;
 static constexpr int LUROW_CB = 64;
 static constexpr int TILE = 64;             // trailing-update tile (k_tile_update)
 
@@ -63,12 +64,16 @@ void* Engine::dmalloc(size_t bytes) {
 
 void Engine::free_device() {
   if (stream) cudaStreamSynchronize(stream);
+  clear_graphs();
   for (void* p : allocations) cudaFree(p);
   allocations.clear();
   dev_ok = false;
   ctx = DevCtx{};
   d_items = nullptr;
-  d_b = d_x = d_r = d_d = d_erhs = d_y = d_red = nullptr;
+  d_b = d_x = d_r = d_d = d_erhs = d_y = d_red = d_scratch = nullptr;
+  d_ws = nullptr;
+  d_ws_off = d_ws_stride = nullptr;
+  d_err = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -366,7 +371,6 @@ int64_t Engine::add_items(const std::vector<Item>& it) {
 }
 
 void Engine::build_plan(int method) {
-  (void)method;
   const int nr = mesh->n_rhs;
   // precision per front
   for (auto& f : fronts) {
@@ -377,8 +381,17 @@ void Engine::build_plan(int method) {
         p = front_prec_override[f.slot];
     }
     f.prec = p;
+    f.tc = (p == PREC_BF16X3 || p == PREC_BF16X6) && f.n >= 512 && method == UHM_CHOL;
   }
   arena64_n = arena32_n = vec_n = piv_n = 0;
+  ws_total = 0;
+  for (auto& f : fronts) {
+    if (!f.tc) continue;
+    const int64_t mmax = f.n - std::min(TC_NBO, f.fs);
+    f.ws_off = ws_total;
+    f.ws_stride = mmax * TC_NBO;
+    ws_total += 3 * f.ws_stride;
+  }
   h_fronts.assign(fronts.size(), FrontDev{});
   h_srcs.clear();
   h_inv.clear();
@@ -395,9 +408,27 @@ void Engine::build_plan(int method) {
     f.off = an;
     an += ((int64_t)n * n + 63) / 64 * 64;
     f.voff = vec_n;
-    vec_n += (int64_t)n * nr;
+    vec_n += 2 * (int64_t)n * nr;          // z slab (forward) and y slab (solution)
     f.piv_off = piv_n;
     piv_n += f.fs;
+  }
+  // large Cholesky fronts: inverses of their 64 x 64 diagonal blocks and one
+  // completion flag per block for the flag-driven solves
+  dinv64_n = dinv32_n = flags_n = 0;
+  {
+    const int small_max_f[2] = {SMALL_MAX_F64, SMALL_MAX_F32};
+    for (auto& f : fronts) {
+      const int dt = f.prec == PREC_FP64 ? F64 : F32;
+      f.blocked = f.tc || f.n > small_max_f[dt];
+      f.flag_off = (int)flags_n;
+      f.dinv_off = 0;
+      if (!f.blocked || method != UHM_CHOL) continue;
+      const int nfb = (f.fs + NB - 1) / NB;
+      int64_t& dn = dt == F64 ? dinv64_n : dinv32_n;
+      f.dinv_off = dn;
+      dn += (int64_t)nfb * NB * NB;
+      flags_n += nfb;
+    }
   }
   // assembly sources in summation order: the element matrix (copy_in), then
   // the children in child order (op_merge, UHM/src/operation/element.cxx:150-162)
@@ -467,6 +498,8 @@ void Engine::build_plan(int method) {
     d.src0 = f.src0;
     d.nsrc = f.nsrc;
     d.status_slot = f.slot;
+    d.flag_off = f.flag_off;
+    d.dinv_off = f.dinv_off;
   }
   // element residual tables (elements with a matrix, in leaf order)
   h_emat_off.clear();
@@ -508,12 +541,16 @@ void Engine::build_programs(int method) {
       for (int s : lv)
         if (h_fronts[s].dtype == dt) fl.push_back(s);
       if (fl.empty()) continue;
+      std::vector<int> tcf;
+      for (int s : fl)
+        if (fronts[s].tc) tcf.push_back(s);
       std::vector<Item> asm_items, small_items;
       std::vector<int> large;
       int max_small = 1;
       for (int s : fl) {
         const int n = fronts[s].n;
         for (int J0 = 0; J0 < n; J0 += ASM_TJ) asm_items.push_back(Item{s, J0, 0, 0});
+        if (fronts[s].tc) continue;
         if (n <= small_max[dt]) {
           small_items.push_back(Item{s, 0, 0, 0});
           max_small = std::max(max_small, n);
@@ -588,6 +625,56 @@ void Engine::build_programs(int method) {
           push(fac_ops, OP_GEMM, dt, NB, 0, u_items, fu);
         }
       }
+      // tensor-core fronts: outer panels of TC_NBO columns; inside a panel the
+      // SIMT kernels factor 64 columns at a time and update only the panel's
+      // columns; the trailing block is then updated once per outer panel on
+      // the tensor cores (BF16-split operands, FP32 accumulation)
+      int maxfs_tc = 0;
+      for (int s : tcf) maxfs_tc = std::max(maxfs_tc, fronts[s].fs);
+      const int TB = tc_tile();
+      for (int K0 = 0; K0 < maxfs_tc; K0 += TC_NBO) {
+        for (int k0 = K0; k0 < K0 + TC_NBO && k0 < maxfs_tc; k0 += NB) {
+          std::vector<Item> p_items, t_items, u_items;
+          double fp = 0, ft = 0, fu = 0;
+          for (int s : tcf) {
+            const HostFront& f = fronts[s];
+            if (f.fs <= k0) continue;
+            const int kb = std::min(NB, f.fs - k0);
+            const int base = k0 + kb;
+            const int cmax = std::min(K0 + TC_NBO, f.fs);
+            p_items.push_back(Item{s, k0, 0, 0});
+            fp += get_flop_chol(0, kb);
+            for (int r0 = base; r0 < f.n; r0 += TRSM_RB) t_items.push_back(Item{s, k0, r0, 0});
+            ft += get_flop_trsm_lower(0, kb, f.n - base);
+            const int T = (f.n - base + TILE - 1) / TILE;
+            for (int ti = 0; ti < T; ++ti)
+              for (int tj = 0; tj <= ti; ++tj)
+                if (base + tj * TILE < cmax) u_items.push_back(Item{s, k0, ti, tj});
+            const double w = std::max(0, cmax - base), mr = f.n - base;
+            fu += 2.0 * kb * (w * mr - 0.5 * w * (w - 1));
+          }
+          push(fac_ops, OP_POTRF, dt, NB, 0, p_items, fp);
+          push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
+          push(fac_ops, OP_SYRK, dt, NB, TC_NBO, u_items, fu);
+        }
+        std::vector<Item> pk, tt;
+        double ftc = 0;
+        for (int s : tcf) {
+          const HostFront& f = fronts[s];
+          if (f.fs <= K0) continue;
+          const int KB = std::min(TC_NBO, f.fs - K0);
+          const int m = f.n - (K0 + KB);
+          if (m <= 0) continue;
+          for (int rb = 0; rb < (m + 63) / 64; ++rb) pk.push_back(Item{s, K0, rb, 0});
+          const int T = (m + TB - 1) / TB;
+          for (int ti = 0; ti < T; ++ti)
+            for (int tj = 0; tj <= ti; ++tj) tt.push_back(Item{s, K0, ti, tj});
+          ftc += get_flop_syrk(0, KB, m);
+        }
+        const int parts = fronts[tcf[0]].prec == PREC_BF16X6 ? 3 : 2;
+        push(fac_ops, OP_TC_PACK, dt, TC_NBO, parts, pk);
+        push(fac_ops, OP_TC_SYRK, dt, TC_NBO, parts, tt, ftc);
+      }
     }
   }
   // solve programs
@@ -608,19 +695,41 @@ void Engine::build_programs(int method) {
         else large.push_back(s);
       }
       push(fwd_ops, OP_FWD_SMALL, dt, 0, gm, sm);
+      if (chol && nr <= 4 && !large.empty()) {
+        // one flag-driven launch for every large front of this level
+        std::vector<Item> fi, ai;
+        int maxb = 0;
+        for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        for (int b = 0; b < maxb; ++b)
+          for (int s : large)
+            if (b < (fronts[s].fs + NB - 1) / NB) fi.push_back(Item{s, b, 0, 0});
+        for (int s : large) {
+          const HostFront& f = fronts[s];
+          const int nfb = (f.fs + NB - 1) / NB;
+          for (int k = 0; k * NB < f.ss; ++k) ai.push_back(Item{s, nfb + k, 0, 0});
+        }
+        fi.insert(fi.end(), ai.begin(), ai.end());
+        int f0 = 1 << 30, f1 = 0;
+        for (int s : large) {
+          f0 = std::min(f0, fronts[s].flag_off);
+          f1 = std::max(f1, fronts[s].flag_off + (fronts[s].fs + NB - 1) / NB);
+        }
+        Op op{OP_FWD_FLAGS, dt, f1 - f0, f0, add_items(fi), (int)fi.size()};
+        fwd_ops.push_back(op);
+        large.clear();
+      }
       int maxfs = 0;
       for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
       for (int k0 = 0; k0 < maxfs; k0 += NB) {
-        std::vector<Item> tv, gv;
+        std::vector<Item> fv;
         for (int s : large) {
           const HostFront& f = fronts[s];
           if (f.fs <= k0) continue;
           const int kb = std::min(NB, f.fs - k0);
-          tv.push_back(Item{s, k0, 0, 0});
-          for (int r0 = k0 + kb; r0 < f.n; r0 += GEMV_RB) gv.push_back(Item{s, k0, r0, 0});
+          const int nch = std::max(1, (f.n - k0 - kb + FWD_RB - 1) / FWD_RB);
+          for (int ch = 0; ch < nch; ++ch) fv.push_back(Item{s, k0, ch, 0});
         }
-        push(fwd_ops, OP_TRSV_F, dt, NB, gm, tv);
-        push(fwd_ops, OP_GEMV_F, dt, NB, gm, gv);
+        push(fwd_ops, OP_TRSV_F, dt, NB, gm, fv);
       }
     }
   }
@@ -638,15 +747,35 @@ void Engine::build_programs(int method) {
         else { large.push_back(s); st.push_back(Item{s, 0, 0, 0}); }
       }
       push(bwd_ops, OP_BWD_SMALL, dt, 0, gm, sm);
+      if (chol && nr <= 4 && !large.empty()) {
+        std::vector<Item> bi;
+        int maxb = 0;
+        for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        for (int b = maxb - 1; b >= 0; --b)
+          for (int s : large)
+            if (b < (fronts[s].fs + NB - 1) / NB) bi.push_back(Item{s, b, 0, 0});
+        int f0 = 1 << 30, f1 = 0;
+        for (int s : large) {
+          f0 = std::min(f0, fronts[s].flag_off);
+          f1 = std::max(f1, fronts[s].flag_off + (fronts[s].fs + NB - 1) / NB);
+        }
+        Op op{OP_BWD_FLAGS, dt, f1 - f0, f0, add_items(bi), (int)bi.size()};
+        bwd_ops.push_back(op);
+        large.clear();
+      }
       int maxfs = 0;
       for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
       int last = maxfs == 0 ? -1 : ((maxfs - 1) / NB) * NB;
       for (int k0 = last; k0 >= 0; k0 -= NB) {
-        std::vector<Item> tv;
-        for (int s : large)
-          if (fronts[s].fs > k0) tv.push_back(Item{s, k0, 0, 0});
-        push(bwd_ops, OP_GEMV_B, dt, NB, gm, tv);
-        push(bwd_ops, OP_TRSV_B, dt, NB, gm, tv);
+        std::vector<Item> bv;
+        for (int s : large) {
+          const HostFront& f = fronts[s];
+          if (f.fs <= k0) continue;
+          const int kb = std::min(NB, f.fs - k0);
+          const int nch = (f.n - k0 - kb + BWD_RB - 1) / BWD_RB;
+          for (int ch = 0; ch < std::max(1, nch); ++ch) bv.push_back(Item{s, k0, ch, nch});
+        }
+        push(bwd_ops, OP_TRSV_B, dt, NB, gm, bv);
       }
       push(bwd_ops, OP_BWD_STORE, dt, 0, gm, st);
     }
@@ -685,9 +814,46 @@ void Engine::alloc_device(int method) {
   ctx.emat = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, emat_total));
   ctx.vec = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, vec_n));
   ctx.status = (int*)dmalloc(sizeof(int) * fronts.size());
+  ctx.dinv64 = dinv64_n ? (double*)dmalloc(sizeof(double) * dinv64_n) : nullptr;
+  ctx.dinv32 = dinv32_n ? (float*)dmalloc(sizeof(float) * dinv32_n) : nullptr;
+  ctx.flags = (int*)dmalloc(sizeof(int) * std::max<int64_t>(1, flags_n));
+  d_ticket = (int*)dmalloc(sizeof(int));
   ctx.n_rhs = nr;
   ctx.symmetric = method == UHM_CHOL ? 1 : 0;
   d_items = (Item*)dmalloc(sizeof(Item) * std::max<size_t>(1, h_items.size()));
+  d_err = (int*)dmalloc(sizeof(int));
+  CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+  if (ws_total > 0) {
+    // one extra row block so tiles that run past the last part stay inside the tensor
+    d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * TC_NBO));
+    CK(cudaMemsetAsync(d_ws, 0, sizeof(uint16_t) * (size_t)(ws_total + 256 * TC_NBO), stream));
+    std::vector<int64_t> wo(fronts.size(), 0), wst(fronts.size(), 0);
+    for (auto& f : fronts) {
+      if (!f.tc) continue;
+      wo[f.slot] = f.ws_off;
+      wst[f.slot] = f.ws_stride;
+    }
+    if (!tc_encode_part(&ws_map, d_ws, ws_total / TC_NBO + 256, TC_NBO))
+      fail("tensor map encoding failed", 4);
+    d_ws_off = (int64_t*)dmalloc(sizeof(int64_t) * wo.size());
+    d_ws_stride = (int64_t*)dmalloc(sizeof(int64_t) * wst.size());
+    CK(cudaMemcpyAsync(d_ws_off, wo.data(), sizeof(int64_t) * wo.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_ws_stride, wst.data(), sizeof(int64_t) * wst.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  {
+    std::vector<int64_t> so(fronts.size());
+    int64_t tot = 0;
+    for (auto& f : fronts) {
+      so[f.slot] = tot;
+      tot += (int64_t)((f.n + BWD_RB - 1) / BWD_RB + 1) * nr * NB;
+    }
+    d_scratch = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, tot));
+    d_scr_off = (int64_t*)dmalloc(sizeof(int64_t) * so.size());
+    d_counters = (int*)dmalloc(sizeof(int) * fronts.size());
+    CK(cudaMemcpyAsync(d_scr_off, so.data(), sizeof(int64_t) * so.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(d_counters, 0, sizeof(int) * fronts.size(), stream));
+  }
   const size_t gv = sizeof(double) * (size_t)std::max<int64_t>(1, n_global) * nr;
   d_b = (double*)dmalloc(gv);
   d_x = (double*)dmalloc(gv);
@@ -767,7 +933,47 @@ void Engine::assemble_rhs() {
   launch_dof_gather(d_dof_ptr, d_dof_idx, d_erhs, nullptr, n_global, d_b, n_global, mesh->n_rhs, 0, stream);
 }
 
+void Engine::clear_graphs() {
+  for (auto& g : graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  graphs.clear();
+}
+
+// Replays a program as a CUDA graph: the first call runs it eagerly (kernel
+// attributes get set), the second captures and instantiates it, later calls
+// launch the instantiated graph (one launch for up to thousands of kernels).
 void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
+  if (!use_graphs || profiling || ops.empty()) {
+    launch_ops(ops, g_in, g_out);
+    return;
+  }
+  GraphEntry* ge = nullptr;
+  for (auto& g : graphs)
+    if (g.ops == &ops && g.gin == g_in && g.gout == g_out) ge = &g;
+  if (!ge) {
+    graphs.push_back(GraphEntry{&ops, g_in, g_out, 0, nullptr});
+    ge = &graphs.back();
+  }
+  if (!ge->exec && ge->eager_runs == 0) {
+    ge->eager_runs++;
+    launch_ops(ops, g_in, g_out);
+    return;
+  }
+  if (!ge->exec) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = timing.kernel_launches;
+    launch_ops(ops, g_in, g_out);
+    timing.kernel_launches = before;
+    CK(cudaStreamEndCapture(stream, &g));
+    CK(cudaGraphInstantiate(&ge->exec, g, 0));
+    cudaGraphDestroy(g);
+  }
+  CK(cudaGraphLaunch(ge->exec, stream));
+  timing.kernel_launches += (int64_t)ops.size();
+}
+
+void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
   std::vector<cudaEvent_t> evs;
   if (profiling) {
     evs.resize(2 * ops.size());
@@ -786,18 +992,31 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
         break;
       case OP_POTRF: launch_potrf_diag(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
-      case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
+      case OP_FWD_FLAGS:
+        launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, stream);
+        break;
+      case OP_BWD_FLAGS:
+        launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, stream);
+        break;
+      case OP_TC_PACK:
+        launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, stream);
+        break;
+      case OP_TC_SYRK:
+        launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, op.param == 3 ? 6 : 3,
+                       op.param == 3 ? TC_TERMS_BF16X6 : TC_TERMS_BF16X3, 1, d_err, stream);
+        break;
       case OP_GETRF: launch_getrf_panel(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
       case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
       case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
       case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, stream); break;
-      case OP_TRSV_F: launch_trsv_block(ctx, it, op.n_items, op.dtype, op.param, op.nb, 0, stream); break;
-      case OP_GEMV_F: launch_gemv_panel(ctx, it, op.n_items, op.dtype, op.param, op.nb, 0, stream); break;
+      case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;
       case OP_BWD_PREP: launch_bwd_prepare(ctx, it, op.n_items, 0, op.param, g_out, n_global, stream); break;
       case OP_BWD_SMALL: launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, stream); break;
-      case OP_GEMV_B: launch_gemv_panel(ctx, it, op.n_items, op.dtype, op.param, op.nb, 1, stream); break;
-      case OP_TRSV_B: launch_trsv_block(ctx, it, op.n_items, op.dtype, op.param, op.nb, 1, stream); break;
+      case OP_TRSV_B:
+        launch_bwd_step(ctx, it, op.n_items, op.dtype, op.param, d_scratch, d_scr_off, d_counters, stream);
+        break;
       case OP_BWD_STORE: launch_bwd_store(ctx, it, op.n_items, g_out, n_global, stream); break;
     }
     if (profiling) CK(cudaEventRecord(evs[2 * k + 1], stream));
@@ -810,6 +1029,7 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
     for (size_t i = 0; i < ops.size(); ++i) {
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, evs[2 * i], evs[2 * i + 1]));
+      if (ops[i].kind < 0 || ops[i].kind >= N_OP_KINDS) continue;
       profile.ms[ops[i].kind] += ms;
       profile.flops[ops[i].kind] += ops[i].flops;
       profile.bytes[ops[i].kind] += ops[i].bytes;
@@ -860,6 +1080,11 @@ void Engine::factor(int method) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.factor_ms = ms;
   check_status("factor");
+  {
+    int derr = 0;
+    CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (derr) fail("a tensor-core kernel gave up waiting (bounded wait expired)", 14);
+  }
   if (status && mode == 1) {
     // a low-precision front broke down: escalate the failed fronts to FP64
     std::vector<int> st(fronts.size());
@@ -887,6 +1112,12 @@ void Engine::solve_into(int method, double* rhs, double* out, int phase) {
   if (phase & 2) run_ops(bwd_ops, rhs, out);
 }
 
+void Engine::check_device_error(const char* where) {
+  int derr = 0;
+  CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (derr) fail(std::string(where) + ": a device wait gave up (bounded wait expired)", 14);
+}
+
 void Engine::solve(int method, int phase) {
   if (!factored) fail("solve: the mesh has not been factorised", 9);
   if (method != factored_method) fail("solve: method differs from the factorisation", 9);
@@ -900,6 +1131,7 @@ void Engine::solve(int method, int phase) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.solve_ms = ms;
   h_x_valid = false;
+  check_device_error("solve");
   if (mode == 1 && phase == 3) refine(method);
 }
 

@@ -13,12 +13,13 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "k_tc.cuh"
 #include "mesh.hpp"
 
 namespace uhm {
 
 // precision of a front's factorisation
-enum FrontPrec : int { PREC_FP64 = 0, PREC_FP32 = 1, PREC_BF16X3 = 2 };
+enum FrontPrec : int { PREC_FP64 = 0, PREC_FP32 = 1, PREC_BF16X3 = 2, PREC_BF16X6 = 3 };
 
 struct HostFront {
   Element e = nullptr;
@@ -27,6 +28,11 @@ struct HostFront {
   int parent = -1;
   std::vector<int> children;       // slots, in child order
   int prec = PREC_FP64;
+  bool tc = false;                 // trailing updates on tensor cores (BF16-split)
+  int64_t ws_off = 0, ws_stride = 0;
+  bool blocked = false;            // large front: blocked kernels, 64-col diagonal blocks
+  int flag_off = 0;
+  int64_t dinv_off = 0;
   int64_t off = 0, voff = 0, inv_off = 0, colptr_off = 0, sgi_off = 0, piv_off = 0;
   int src0 = 0, nsrc = 0;
 };
@@ -54,7 +60,7 @@ struct Op {
   double bytes = 0;   // algorithmic HBM bytes of this launch
 };
 
-constexpr int N_OP_KINDS = 20;
+constexpr int N_OP_KINDS = 32;
 struct OpProfile {
   double ms[N_OP_KINDS] = {0}, flops[N_OP_KINDS] = {0}, bytes[N_OP_KINDS] = {0};
   int64_t launches[N_OP_KINDS] = {0};
@@ -63,8 +69,9 @@ struct OpProfile {
 enum OpKind : int {
   OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
-  OP_TRSV_B, OP_BWD_STORE
+  OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_KIND_END
 };
+static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
 
 struct Timing {
   double upload_ms = 0, factor_ms = 0, solve_ms = 0, refine_ms = 0, total_ms = 0;
@@ -108,6 +115,7 @@ class Engine {
   std::string last_error;
   Timing timing;
   bool profiling = false;       // per-op CUDA events (outside timed regions)
+  bool use_graphs = true;       // replay factor / solve programs as CUDA graphs
   OpProfile profile;
 
   // --- introspection ------------------------------------------------------
@@ -149,6 +157,8 @@ class Engine {
   std::vector<uhm_gpu::Item> h_items;
   std::vector<Op> fac_ops, fwd_ops, bwd_ops;
   int64_t arena64_n = 0, arena32_n = 0, vec_n = 0, piv_n = 0;
+  int64_t dinv64_n = 0, dinv32_n = 0, flags_n = 0;
+  int* d_ticket = nullptr;
 
   // device memory
   uhm_gpu::DevCtx ctx{};
@@ -160,6 +170,15 @@ class Engine {
   double* d_erhs = nullptr;     // element rhs (FP64)
   double* d_y = nullptr;        // per-element A_e x_e
   double* d_red = nullptr;      // reduction scratch
+  double* d_scratch = nullptr;  // backward-solve partial sums
+  int64_t* d_scr_off = nullptr;
+  int* d_counters = nullptr;
+  void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
+  int64_t* d_ws_off = nullptr;
+  int64_t* d_ws_stride = nullptr;
+  CUtensorMap ws_map;                // one map over the whole BF16 workspace
+  int* d_err = nullptr;              // bounded-wait error flag of device kernels
+  int64_t ws_total = 0;
   int64_t* d_emat_off = nullptr;
   int* d_elem_m = nullptr;
   int64_t* d_emap_off = nullptr;
@@ -184,6 +203,16 @@ class Engine {
   void upload_elements();
   void assemble_rhs();
   void run_ops(const std::vector<Op>& ops, double* g_in, double* g_out);
+  void launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out);
+  struct GraphEntry {
+    const std::vector<Op>* ops;
+    double* gin;
+    double* gout;
+    int eager_runs;
+    cudaGraphExec_t exec;
+  };
+  std::vector<GraphEntry> graphs;
+  void clear_graphs();
   void solve_into(int method, double* rhs, double* out, int phase);
   void compute_residual(const double* x, double* r);
   double operator_norm_inf();
@@ -191,6 +220,7 @@ class Engine {
   double read_scalar(const double* d);
   void refine(int method);
   void check_status(const char* where);
+  void check_device_error(const char* where);
   void* dmalloc(size_t bytes);
   int64_t add_items(const std::vector<uhm_gpu::Item>& it);
   void fail(const std::string& msg, int code);

@@ -238,17 +238,35 @@ __global__ void __launch_bounds__(NT) k_potrf_diag(DevCtx c, const Item* __restr
     const int i = idx % kb, j = idx / kb;
     if (i >= j) G[i + (int64_t)j * n] = A[idx];
   }
+  // inverse of the lower-triangular diagonal block (for the flag-driven
+  // solves): column j of L^{-1} by forward substitution, one thread per column
+  if (nb == 64 && (sizeof(T) == 8 ? (void*)c.dinv64 : (void*)c.dinv32) != nullptr) {
+    T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32) + f.dinv_off + (int64_t)(k0 / 64) * 4096;
+    T* W = A + kb * kb;   // scratch 64 x 64
+    for (int idx = threadIdx.x; idx < 4096; idx += NT) W[idx] = T(0);
+    __syncthreads();
+    const int j = threadIdx.x;
+    if (j < kb) {
+      for (int i = j; i < kb; ++i) {
+        T s = i == j ? T(1) : T(0);
+        for (int t = j; t < i; ++t) s -= A[i + t * kb] * W[t + j * 64];
+        W[i + j * 64] = s / A[i + i * kb];
+      }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 4096; idx += NT) Dinv[idx] = W[idx];
+  }
 }
 
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s) {
   if (!n_items) return;
   if (dtype == F64) {
-    size_t sm = (size_t)nb * nb * sizeof(double);
+    size_t sm = (size_t)nb * nb * sizeof(double) + 4096 * sizeof(double);
     cudaFuncSetAttribute(k_potrf_diag<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_potrf_diag<double, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   } else {
-    size_t sm = (size_t)nb * nb * sizeof(float);
+    size_t sm = (size_t)nb * nb * sizeof(float) + 4096 * sizeof(float);
     cudaFuncSetAttribute(k_potrf_diag<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_potrf_diag<float, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   }
@@ -315,7 +333,7 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
 // item: front, a = k0, b = tile row, c = tile col (tiles counted from k0+kb)
 template <typename T, int BM, int BN, int BK, int TM, int TN, bool ROWPANEL>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
-k_tile_update(DevCtx c, const Item* __restrict__ items, int nb) {
+k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
@@ -325,6 +343,8 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb) {
   const int kb = min(nb, f.fs - k0);
   const int base = k0 + kb;
   const int R0 = base + it.b * BM, C0 = base + it.c * BN;
+  // nbo > 0: update only the columns of the current outer panel (two-level blocking)
+  const int cmax = nbo > 0 ? min((k0 / nbo) * nbo + nbo, f.fs) : n;
   T* __restrict__ G = arena<T>(c) + f.off;
   const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
   T acc[TM][TN];
@@ -373,7 +393,7 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       const int gc = C0 + tx + j * NTX;
-      if (gc >= n) continue;
+      if (gc >= cmax) continue;
       if (!ROWPANEL && gr < gc) continue;
       G[gr + (int64_t)gc * n] -= acc[i][j];
     }
@@ -381,17 +401,17 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb) {
 }
 
 void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
-                        cudaStream_t s) {
+                        int nbo, cudaStream_t s) {
   if (!n_items) return;
-  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb);
-  else k_tile_update<float, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb);
+  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
+  else k_tile_update<float, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
 }
 
 void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         cudaStream_t s) {
   if (!n_items) return;
-  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb);
-  else k_tile_update<float, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb);
+  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
+  else k_tile_update<float, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
 }
 
 // ---------------------------------------------------------------------------

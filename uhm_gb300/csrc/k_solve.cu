@@ -88,7 +88,13 @@ __global__ void __launch_bounds__(NT) k_fwd_small(DevCtx c, const Item* __restri
     }
     __syncthreads();
   }
-  for (int idx = threadIdx.x; idx < n * nr; idx += NT) zg[idx] = z[idx];
+  // y (second slab) receives the eliminated part, z keeps the updated bottom
+  double* __restrict__ yg = zg + (int64_t)n * nr;
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) {
+    const int i = idx % n;
+    if (i < fs) yg[idx] = z[idx];
+    else zg[idx] = z[idx];
+  }
 }
 
 void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
@@ -110,11 +116,11 @@ __global__ void __launch_bounds__(256) k_bwd_prepare(DevCtx c, const Item* __res
                                                      const double* __restrict__ g, int64_t ldg) {
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
-  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = c.vec + f.voff + (int64_t)f.n * c.n_rhs;
   const int32_t* __restrict__ sgi = c.sgi + f.sgi_off;
   for (int q = 0; q < c.n_rhs; ++q)
     for (int j = threadIdx.x; j < f.ss; j += blockDim.x)
-      z[f.fs + j + (int64_t)q * f.n] = g[sgi[j] + q * ldg];
+      y[f.fs + j + (int64_t)q * f.n] = g[sgi[j] + q * ldg];
 }
 
 void launch_bwd_prepare(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(NT) k_bwd_small(DevCtx c, const Item* __restri
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs;
   const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ zg = c.vec + f.voff;
+  double* __restrict__ zg = c.vec + f.voff + (int64_t)n * nr;   // y slab
   for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = zg[idx];
   __syncthreads();
   const bool chol = method == M_CHOL;
@@ -170,7 +176,6 @@ __global__ void __launch_bounds__(NT) k_bwd_small(DevCtx c, const Item* __restri
       __syncthreads();
     }
   }
-  for (int idx = threadIdx.x; idx < n * nr; idx += NT) zg[idx] = z[idx];
   for (int q = 0; q < nr; ++q)
     for (int i = threadIdx.x; i < fs; i += NT) g[(f.g0 + i) + q * ldg] = z[i + q * n];
 }
@@ -188,136 +193,202 @@ void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype
   }
 }
 
-// Large fronts, blocked by nb.  item: front, a = k0.
-// upper == 0: forward diagonal solve  z_k <- L_kk^{-1} z_k  (unit for LU)
-// upper == 1: backward diagonal solve z_k <- L_kk^{-T} z_k (Chol) / U_kk^{-1} z_k (LU)
+// ---------------------------------------------------------------------------
+// Large fronts, blocked by SB = 64 columns.
+// Forward step k (item: front, a = k0, b = row chunk): every CTA solves the
+// diagonal block x_k = L_kk^{-1} z_k (warp-synchronous substitution, unit
+// diagonal for LU), chunk 0 stores x_k in the y slab, and each CTA updates
+// its chunk of rows below:  z[r] -= L[r, k-block] x_k.  Step k reads only
+// z_k and writes only rows >= k0+kb and y_k, so CTAs never race.
+// Backward step k (item: front, a = k0, b = chunk, c = number of chunks):
+// each CTA forms partial dot products of its tail chunk (Chol: L^T, LU: U)
+// with y; the last CTA to arrive (threadfence reduction) sums the partials in
+// chunk order -- deterministic -- and solves the diagonal block into y_k.
+// ---------------------------------------------------------------------------
+constexpr int SB = 64;          // diagonal block of the blocked solves
+constexpr int FWD_RB = 256;     // rows per forward-update CTA
+constexpr int BWD_RB = 512;     // tail rows per backward partial CTA
+constexpr int NR_MAX = 16;      // right-hand sides of large fronts
+
+// lower-triangular substitution of one diagonal block by one warp;
+// x (shared, length kb) in, solution out
+template <typename T, typename CT>
+__device__ __forceinline__ void warp_lower_solve(const T* D, int kb, CT* x, bool unit) {
+  const int lane = threadIdx.x & 31;
+  CT v0 = lane < kb ? x[lane] : CT(0), v1 = lane + 32 < kb ? x[lane + 32] : CT(0);
+  for (int j = 0; j < kb; ++j) {
+    CT xj = __shfl_sync(0xffffffffu, j < 32 ? v0 : v1, j & 31);
+    if (!unit) xj /= (CT)D[j + j * SB];
+    if (lane == (j & 31)) { if (j < 32) v0 = xj; else v1 = xj; }
+    if (lane > j && lane < kb) v0 -= (CT)D[lane + j * SB] * xj;
+    if (lane + 32 > j && lane + 32 < kb) v1 -= (CT)D[lane + 32 + j * SB] * xj;
+  }
+  if (lane < kb) x[lane] = v0;
+  if (lane + 32 < kb) x[lane + 32] = v1;
+}
+
+// upper substitution: Chol uses L_kk^T (A(i,j) = D[j,i]), LU uses U_kk
+template <typename T, typename CT>
+__device__ __forceinline__ void warp_upper_solve(const T* D, int kb, CT* x, bool chol) {
+  const int lane = threadIdx.x & 31;
+  CT v0 = lane < kb ? x[lane] : CT(0), v1 = lane + 32 < kb ? x[lane + 32] : CT(0);
+  for (int j = kb - 1; j >= 0; --j) {
+    CT xj = __shfl_sync(0xffffffffu, j < 32 ? v0 : v1, j & 31);
+    xj /= (CT)D[j + j * SB];
+    if (lane == (j & 31)) { if (j < 32) v0 = xj; else v1 = xj; }
+    if (lane < j) v0 -= (CT)(chol ? D[j + lane * SB] : D[lane + j * SB]) * xj;
+    if (lane + 32 < j) v1 -= (CT)(chol ? D[j + (lane + 32) * SB] : D[lane + 32 + j * SB]) * xj;
+  }
+  if (lane < kb) x[lane] = v0;
+  if (lane + 32 < kb) x[lane + 32] = v1;
+}
+
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_trsv_block(DevCtx c, const Item* __restrict__ items,
-                                                   int method, int nb, int upper) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* D = reinterpret_cast<T*>(smem_raw);                   // kb x kb
-  double* z = reinterpret_cast<double*>(D + nb * nb);       // kb x n_rhs
+__global__ void __launch_bounds__(NT) k_fwd_step(DevCtx c, const Item* __restrict__ items, int method) {
+  using CT = T;   // compute in the storage precision of the factor
+  __shared__ T D[SB * SB];
+  __shared__ CT xk[SB * NR_MAX];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a, nr = c.n_rhs;
-  const int kb = min(nb, f.fs - k0);
+  const int kb = min(SB, f.fs - k0);
   const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ zg = c.vec + f.voff;
-  for (int idx = threadIdx.x; idx < kb * kb; idx += NT) {
-    const int i = idx % kb, j = idx / kb;
-    D[idx] = G[(k0 + i) + (int64_t)(k0 + j) * n];
+  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = z + (int64_t)n * nr;
+  for (int idx = threadIdx.x; idx < SB * kb; idx += NT) {
+    const int i = idx % SB, j = idx / SB;
+    D[idx] = i < kb ? G[(k0 + i) + (int64_t)(k0 + j) * n] : T(0);
   }
   for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
     const int i = idx % kb, q = idx / kb;
-    z[i + q * kb] = zg[(k0 + i) + (int64_t)q * n];
+    xk[i + q * SB] = (CT)z[(k0 + i) + (int64_t)q * n];
   }
   __syncthreads();
-  const bool chol = method == M_CHOL;
-  if (!upper) {
-    for (int j = 0; j < kb; ++j) {
-      if (chol && threadIdx.x < nr) z[j + threadIdx.x * kb] /= (double)D[j + j * kb];
-      __syncthreads();
-      const int h = kb - j - 1;
-      for (int idx = threadIdx.x; idx < h * nr; idx += NT) {
-        const int i = j + 1 + idx % h, q = idx / h;
-        z[i + q * kb] -= (double)D[i + j * kb] * z[j + q * kb];
-      }
-      __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  for (int q = warp; q < nr; q += NT / 32) warp_lower_solve<T, CT>(D, kb, xk + q * SB, method != M_CHOL);
+  __syncthreads();
+  if (it.b == 0)
+    for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
+      const int i = idx % kb, q = idx / kb;
+      y[(k0 + i) + (int64_t)q * n] = (double)xk[i + q * SB];
     }
-  } else {
-    for (int j = kb - 1; j >= 0; --j) {
-      if (threadIdx.x < nr) z[j + threadIdx.x * kb] /= (double)D[j + j * kb];
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < j * nr; idx += NT) {
-        const int i = idx % j, q = idx / j;
-        // chol: L^T(i, j) = L(j, i); LU: U(i, j)
-        const double a = chol ? (double)D[j + i * kb] : (double)D[i + j * kb];
-        z[i + q * kb] -= a * z[j + q * kb];
-      }
-      __syncthreads();
+  const int r0 = k0 + kb + it.b * FWD_RB;
+  const int r1 = min(r0 + FWD_RB, n);
+  for (int r = r0 + threadIdx.x; r < r1; r += NT) {
+    for (int q = 0; q < nr; ++q) {
+      CT acc = CT(0);
+      for (int t = 0; t < kb; ++t) acc += (CT)G[r + (int64_t)(k0 + t) * n] * xk[t + q * SB];
+      z[r + (int64_t)q * n] -= (double)acc;
     }
-  }
-  for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
-    const int i = idx % kb, q = idx / kb;
-    zg[(k0 + i) + (int64_t)q * n] = z[i + q * kb];
   }
 }
 
-void launch_trsv_block(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                       int nb, int upper, cudaStream_t s) {
-  if (!n_items) return;
-  if (dtype == F64) {
-    size_t sm = (size_t)nb * nb * sizeof(double) + (size_t)nb * c.n_rhs * sizeof(double);
-    cudaFuncSetAttribute(k_trsv_block<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_trsv_block<double, 256><<<n_items, 256, sm, s>>>(c, items, method, nb, upper);
-  } else {
-    size_t sm = (size_t)nb * nb * sizeof(float) + (size_t)nb * c.n_rhs * sizeof(double) + 16;
-    cudaFuncSetAttribute(k_trsv_block<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_trsv_block<float, 256><<<n_items, 256, sm, s>>>(c, items, method, nb, upper);
-  }
-}
-
-constexpr int GEMV_RB = 256;
-
-// upper == 0 (forward): item front, a = k0, b = r0:  z[r0..r0+RB) -= A[r0.., k0..k0+kb) z_k
-// upper == 1 (backward): item front, a = k0:  z_k -= A_tail^T z_tail (Chol: L[k0+kb:n, k]^T;
-//                        LU: U[k, k0+kb:n]) ; one CTA per step, reduction over the tail
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_gemv_panel(DevCtx c, const Item* __restrict__ items,
-                                                   int method, int nb, int upper) {
-  __shared__ double s_z[64 * 16];
-  __shared__ double s_red[NT / 32 + 1];
+__global__ void __launch_bounds__(NT) k_bwd_step(DevCtx c, const Item* __restrict__ items, int method,
+                                                 double* __restrict__ scratch,
+                                                 const int64_t* __restrict__ scr_off,
+                                                 int* __restrict__ counters) {
+  using CT = T;
+  // the diagonal block (last CTA) and the partial-sum tile (all CTAs) share storage
+  __shared__ __align__(16) unsigned char s_raw[sizeof(CT) * SB * (SB + 1)];
+  T* D = reinterpret_cast<T*>(s_raw);
+  CT (*tileT)[SB + 1] = reinterpret_cast<CT (*)[SB + 1]>(s_raw);
+  __shared__ CT part[4][SB];
+  __shared__ CT xk[SB * NR_MAX];
+  __shared__ CT ys[SB];
+  __shared__ int s_last;
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a, nr = c.n_rhs;
-  const int kb = min(nb, f.fs - k0);
+  const int kb = min(SB, f.fs - k0);
   const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ zg = c.vec + f.voff;
-  if (!upper) {
-    const int r0 = it.b;
-    for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
-      const int i = idx % kb, q = idx / kb;
-      s_z[i + q * 64] = zg[(k0 + i) + (int64_t)q * n];
-    }
-    __syncthreads();
-    for (int r = r0 + threadIdx.x; r < min(r0 + GEMV_RB, n); r += NT) {
-      for (int q = 0; q < nr; ++q) {
-        double acc = 0.0;
-        for (int t = 0; t < kb; ++t) acc += (double)G[r + (int64_t)(k0 + t) * n] * s_z[t + q * 64];
-        zg[r + (int64_t)q * n] -= acc;
-      }
-    }
-  } else {
-    const bool chol = method == M_CHOL;
-    const int t0 = k0 + kb;
+  double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
+  const int t0 = k0 + kb;
+  const int nch = it.c;
+  const bool chol = method == M_CHOL;
+  double* __restrict__ sc = scratch + scr_off[it.front];
+  if (nch > 0) {
+    const int c0 = t0 + it.b * BWD_RB, c1 = min(c0 + BWD_RB, n);
+    const int i = threadIdx.x % SB, g = threadIdx.x / SB;   // NT = 256: 4 groups
     for (int q = 0; q < nr; ++q) {
-      for (int i = 0; i < kb; ++i) {
-        double part = 0.0;
-        if (chol)
-          for (int r = t0 + threadIdx.x; r < n; r += NT)
-            part += (double)G[r + (int64_t)(k0 + i) * n] * zg[r + (int64_t)q * n];
-        else
-          for (int r = t0 + threadIdx.x; r < n; r += NT)
-            part += (double)G[(k0 + i) + (int64_t)r * n] * zg[r + (int64_t)q * n];
-        const double sum = block_sum<NT>(part, s_red);
-        if (threadIdx.x == 0) zg[(k0 + i) + (int64_t)q * n] -= sum;
+      CT acc = CT(0);
+      if (chol) {
+        // rows of the chunk in tiles of 64: load L[rows, k-block] coalesced
+        // along rows, then thread (i, g) sums 16 rows of column i
+        for (int t0r = c0; t0r < c1; t0r += SB) {
+          __syncthreads();
+          for (int idx = threadIdx.x; idx < SB * SB; idx += NT) {
+            const int rr = idx % SB, cc = idx / SB;
+            tileT[rr][cc] = (t0r + rr < c1 && cc < kb) ? (CT)G[(t0r + rr) + (int64_t)(k0 + cc) * n] : CT(0);
+          }
+          for (int rr = threadIdx.x; rr < SB; rr += NT)
+            ys[rr] = t0r + rr < c1 ? (CT)y[t0r + rr + (int64_t)q * n] : CT(0);
+          __syncthreads();
+#pragma unroll 4
+          for (int rr = g * 16; rr < g * 16 + 16; ++rr) acc += tileT[rr][i] * ys[rr];
+        }
+      } else if (i < kb) {
+        {
+          for (int cc = c0 + g; cc < c1; cc += 4)
+            acc += (CT)G[(k0 + i) + (int64_t)cc * n] * (CT)y[cc + (int64_t)q * n];
+        }
       }
+      part[g][i] = acc;
+      __syncthreads();
+      if (threadIdx.x < SB)
+        sc[((int64_t)it.b * nr + q) * SB + threadIdx.x] =
+            (double)(part[0][threadIdx.x] + part[1][threadIdx.x] + part[2][threadIdx.x] + part[3][threadIdx.x]);
+      __syncthreads();
     }
+    __threadfence();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&counters[it.front], 1) == nch - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) counters[it.front] = 0;
+  }
+  // last CTA (or the only one): sum partials in chunk order, solve the block
+  for (int idx = threadIdx.x; idx < SB * kb; idx += NT) {
+    const int ii = idx % SB, j = idx / SB;
+    D[idx] = ii < kb ? G[(k0 + ii) + (int64_t)(k0 + j) * n] : T(0);
+  }
+  for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
+    const int ii = idx % kb, q = idx / kb;
+    double s = 0.0;
+    for (int ch = 0; ch < nch; ++ch) s += sc[((int64_t)ch * nr + q) * SB + ii];
+    xk[ii + q * SB] = (CT)(y[(k0 + ii) + (int64_t)q * n] - s);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  for (int q = warp; q < nr; q += NT / 32) warp_upper_solve<T, CT>(D, kb, xk + q * SB, chol);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kb * nr; idx += NT) {
+    const int ii = idx % kb, q = idx / kb;
+    y[(k0 + ii) + (int64_t)q * n] = (double)xk[ii + q * SB];
   }
 }
 
-void launch_gemv_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                       int nb, int upper, cudaStream_t s) {
+void launch_fwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                     cudaStream_t s) {
   if (!n_items) return;
-  if (dtype == F64) k_gemv_panel<double, 256><<<n_items, 256, 0, s>>>(c, items, method, nb, upper);
-  else k_gemv_panel<float, 256><<<n_items, 256, 0, s>>>(c, items, method, nb, upper);
+  if (dtype == F64) k_fwd_step<double, 256><<<n_items, 256, 0, s>>>(c, items, method);
+  else k_fwd_step<float, 256><<<n_items, 256, 0, s>>>(c, items, method);
+}
+
+void launch_bwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                     double* scratch, const int64_t* scr_off, int* counters, cudaStream_t s) {
+  if (!n_items) return;
+  if (dtype == F64)
+    k_bwd_step<double, 256><<<n_items, 256, 0, s>>>(c, items, method, scratch, scr_off, counters);
+  else
+    k_bwd_step<float, 256><<<n_items, 256, 0, s>>>(c, items, method, scratch, scr_off, counters);
 }
 
 __global__ void __launch_bounds__(256) k_bwd_store(DevCtx c, const Item* __restrict__ items,
                                                    double* __restrict__ g, int64_t ldg) {
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
-  const double* __restrict__ z = c.vec + f.voff;
+  const double* __restrict__ z = c.vec + f.voff + (int64_t)f.n * c.n_rhs;   // y slab
   for (int q = 0; q < c.n_rhs; ++q)
     for (int i = threadIdx.x; i < f.fs; i += blockDim.x) g[(f.g0 + i) + q * ldg] = z[i + (int64_t)q * f.n];
 }
@@ -506,6 +577,228 @@ void launch_anorm_partial(const double* emat, const int64_t* emat_off, const int
   if (!n_elem) return;
   k_anorm_partial<<<n_elem, 128, 0, s>>>(emat, emat_off, elem_m, emap_off, emap, dof_ptr, dof_el,
                                          part, y_off);
+}
+
+}  // namespace uhm_gpu
+
+namespace uhm_gpu {
+
+// ===========================================================================
+// Flag-driven level solves of large Cholesky fronts.
+//
+// One launch covers every large front of a level.  The rows of a front are cut
+// into 64-row blocks: factor blocks [64b, min(64b+64, fs)) and ABL blocks
+// starting at fs.  A CTA takes a ticket (atomic counter) and processes the
+// item of that rank; items are ordered so that each CTA only waits for blocks
+// owned by CTAs with smaller tickets, which are already running -- progress
+// is guaranteed whatever the residency.  A finished block publishes its
+// solution (y slab), then a release-store of its flag; readers acquire the
+// flag before reading.  Every wait is bounded (error flag, no hang).
+// Forward:  x_b = L_bb^{-1} (z_b - sum_{j<b} L_bj x_j)
+// Backward: x_b = L_bb^{-T} (y_b - sum_{r > block b} L_rb^T x_r)
+// with L_bb^{-1} precomputed at factorisation (64 x 64, dinv arenas).
+// ===========================================================================
+constexpr int FB = 64;
+constexpr int SF_NR = 4;          // right-hand sides handled by these kernels
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool wait_flag(const int* p, int* err) {
+  for (uint32_t i = 0; i < (1u << 22); ++i) {
+    if (ld_acquire_gpu(p) == 1) return true;
+    __nanosleep(32);
+  }
+  atomicExch(err, 2);
+  return false;
+}
+
+template <typename T> __device__ __forceinline__ const T* dinv_arena(const DevCtx& c);
+template <> __device__ __forceinline__ const double* dinv_arena<double>(const DevCtx& c) { return c.dinv64; }
+template <> __device__ __forceinline__ const float* dinv_arena<float>(const DevCtx& c) { return c.dinv32; }
+
+// item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..)
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
+                                                   int* ticket, int* err) {
+  using CT = T;
+  __shared__ int s_t;
+  __shared__ CT red[4][FB][SF_NR];
+  __shared__ CT v[FB][SF_NR];
+  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
+  const int nfb = (fs + FB - 1) / FB;
+  const bool factor_block = b < nfb;
+  const int r0 = factor_block ? b * FB : fs + (b - nfb) * FB;
+  const int r1 = factor_block ? min(r0 + FB, fs) : min(r0 + FB, n);
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = z + (int64_t)n * nr;
+  const int* __restrict__ flg = c.flags + f.flag_off;
+  const int i = threadIdx.x % FB, g = threadIdx.x / FB;
+  const int row = r0 + i;
+  const bool rv = row < r1;
+  CT acc[SF_NR];
+#pragma unroll
+  for (int q = 0; q < SF_NR; ++q) acc[q] = CT(0);
+  const int jend = factor_block ? b : nfb;
+  for (int j = 0; j < jend; ++j) {
+    const int kbj = min(FB, fs - j * FB);
+    CT lv[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int cc = g * 16 + u;
+      lv[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
+    }
+    wait_flag(flg + j, err);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int cc = g * 16 + u;
+      if (cc < kbj)
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q)
+          if (q < nr) acc[q] += lv[u] * (CT)__ldcg(y + (j * FB + cc) + (int64_t)q * n);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
+  __syncthreads();
+  if (threadIdx.x < FB) {
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q)
+      v[i][q] = (rv && q < nr) ? (CT)z[row + (int64_t)q * n] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q])
+                               : CT(0);
+  }
+  __syncthreads();
+  if (factor_block) {
+    const int kb = r1 - r0;
+    const T* __restrict__ Di = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
+    if (threadIdx.x < FB && rv) {
+      CT x[SF_NR];
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q) x[q] = CT(0);
+      for (int t = 0; t <= i && t < kb; ++t) {
+        const CT d = (CT)Di[i + t * FB];
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q) x[q] += d * v[t][q];
+      }
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q)
+        if (q < nr) y[row + (int64_t)q * n] = (double)x[q];
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) st_release_gpu(c.flags + f.flag_off + b, 1);
+  } else if (threadIdx.x < FB && rv) {
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q)
+      if (q < nr) z[row + (int64_t)q * n] = (double)v[i][q];
+  }
+}
+
+// item: front, a = factor block index, tickets in descending block order
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restrict__ items,
+                                                   int* ticket, int* err) {
+  using CT = T;
+  __shared__ int s_t;
+  // the reduction tile [row lane][column] and, afterwards, the inverse diagonal block
+  __shared__ __align__(16) unsigned char s_raw[sizeof(CT) * FB * (FB + 1)];
+  CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(s_raw);
+  T* dsh = reinterpret_cast<T*>(s_raw);
+  __shared__ CT v[FB][SF_NR];
+  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
+  const int nfb = (fs + FB - 1) / FB;
+  const int c0 = b * FB, kb = min(FB, fs - c0);
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
+  const int* __restrict__ flg = c.flags + f.flag_off;
+  const int rl = threadIdx.x % FB, g = threadIdx.x / FB;   // row lane, column group
+  for (int q = 0; q < nr && q < SF_NR; ++q) {
+    CT acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = CT(0);
+    // rows below block b: the ABL part (known) first, then factor blocks
+    // from the last one down (they complete in that order)
+    for (int rs = fs; rs < n; rs += FB) {
+      const int r = rs + rl;
+      const CT xr = r < n ? (CT)y[r + (int64_t)q * n] : CT(0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int cc = g * 16 + u;
+        if (r < n && cc < kb) acc[u] += (CT)G[r + (int64_t)(c0 + cc) * n] * xr;
+      }
+    }
+    for (int j = nfb - 1; j > b; --j) {
+      const int r = j * FB + rl;
+      const bool in = r < min(j * FB + FB, fs);
+      CT lv[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int cc = g * 16 + u;
+        lv[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
+      }
+      wait_flag(flg + j, err);
+      const CT xr = in ? (CT)__ldcg(y + r + (int64_t)q * n) : CT(0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc[u] += lv[u] * xr;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) red[rl][g * 16 + u] = acc[u];
+    __syncthreads();
+    if (threadIdx.x < FB) {
+      CT s = CT(0);
+      for (int r = 0; r < FB; ++r) s += red[r][threadIdx.x];
+      v[threadIdx.x][q] = threadIdx.x < kb ? (CT)y[c0 + threadIdx.x + (int64_t)q * n] - s : CT(0);
+    }
+  }
+  const T* __restrict__ Di = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[idx] = Di[idx];
+  __syncthreads();
+  // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t
+  if (threadIdx.x < kb) {
+    const int ii = threadIdx.x;
+    for (int q = 0; q < nr && q < SF_NR; ++q) {
+      CT x = CT(0);
+      for (int t = ii; t < kb; ++t) x += (CT)dsh[t + ii * FB] * v[t][q];
+      y[c0 + ii + (int64_t)q * n] = (double)x;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) st_release_gpu(c.flags + f.flag_off + b, 1);
+}
+
+void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
+                      int* flag_base, int n_flags, int* err, cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
+  if (dtype == F64) k_fwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err);
+  else k_fwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err);
+}
+
+void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
+                      int* flag_base, int n_flags, int* err, cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
+  if (dtype == F64) k_bwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err);
+  else k_bwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err);
 }
 
 }  // namespace uhm_gpu

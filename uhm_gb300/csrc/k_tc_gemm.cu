@@ -1,0 +1,340 @@
+// Tensor-core Schur update for FP32 fronts: C -= A21 * A21^T (Cholesky) with
+// BF16-split operands on the 5th-generation tensor cores (tcgen05).
+//
+// The update restates the trailing SYRK of the front's blocked Cholesky
+// (LINAL/src/dense/chol.cxx:78-82 and the front-level syrk of
+// UHM/src/matrix/uhm/fla/chol/decompose.cxx:94-95).
+//
+// Split precision: every FP32 entry a = hi + lo + (mid) with hi, lo (, mid)
+// BF16 (round to nearest); the product a*b is taken as the sum of BF16
+// products hi*hi + hi*lo + lo*hi ("bf16x3", ~2^-17 relative) or, with three
+// parts, the six terms of order <= 2^-16 ("bf16x6", FP32-class).  Terms are
+// laid end to end along K, so one GEMM with K' = terms * KB accumulates them
+// all in FP32 in tensor memory.
+//
+// Kernel: one CTA per 128 x 128 output tile; warp 4 issues TMA loads
+// (128-byte swizzle) into a 4-stage shared-memory ring guarded by mbarriers,
+// one thread of warp 5 issues tcgen05.mma (M=128, N=128, K=16) into a
+// 128-column TMEM accumulator, warps 0-3 read TMEM back (tcgen05.ld) and
+// apply C -= acc to the FP32 panel.  Every wait is bounded: a wait that
+// gives up records an error flag and the CTA skips its stores.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <cstdio>
+
+#include "k_common.cuh"
+#include "k_tc.cuh"
+
+namespace uhm_gpu {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 4;
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 2;   // 16 KB (A and B tiles alike)
+constexpr uint32_t TC_CPAD = TC_BN + 1;                 // padded row of the staged C tile
+constexpr uint32_t TC_CTILE_BYTES = TC_BM * TC_CPAD * 4;
+constexpr uint32_t TC_SMEM = 1024 + TC_STAGES * 2 * TC_TILE_BYTES + 256 + TC_CTILE_BYTES;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false (and error flag) when the barrier never completes
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err) {
+  for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (i > 64) __nanosleep(64);
+  }
+  *abort_flag = 1;
+  if (err) atomicExch(err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// UMMA shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), descriptor version 1 (bits 46-47)
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;            // version
+  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, K-major both, M = N = 128
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+#define TC_LD32(taddr, v)                                                                        \
+  asm volatile(                                                                                  \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14," \
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"              \
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),      \
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),   \
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),            \
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),            \
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])             \
+      : "r"(taddr))
+
+// item: front, a = K0 (outer step start), b = tile row, c = tile col
+// (tiles counted from the trailing block's first row K0 + KB).
+// term_code: 2 bits per part index, 4 bits per term (A part, B part).
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_off,
+          const int64_t* __restrict__ ws_stride, const Item* __restrict__ items, int nbo, int nterms,
+          uint32_t term_code, int lower_only, int* err) {
+  extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* tilesA = smem;
+  uint8_t* tilesB = smem + TC_STAGES * TC_TILE_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * TC_STAGES * TC_TILE_BYTES);
+  // bars[0..S) full, bars[S..2S) empty, bars[2S] accumulator ready
+  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * TC_STAGES + 1);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 2);
+  float* s_c = reinterpret_cast<float*>(smem + 2 * TC_STAGES * TC_TILE_BYTES + 256);
+
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  // the whole BF16 workspace is one 2D tensor of rows of nbo elements;
+  // part p of this front starts at row (ws_off + p * ws_stride) / nbo
+  const int row0 = (int)(ws_off[it.front] / nbo);
+  const int prow = (int)(ws_stride[it.front] / nbo);
+  const int n = f.n, K0 = it.a;
+  const int KB = min(nbo, f.fs - K0);
+  const int base = K0 + KB;
+  const int R0 = base + it.b * TC_BM, C0 = base + it.c * TC_BN;
+  const int kpt = (KB + TC_BK - 1) / TC_BK;       // K chunks per term
+  const int nk = kpt * nterms;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[TC_STAGES + s]), 1);
+    }
+    mbar_init(smem_u32(&bars[2 * TC_STAGES]), 1);
+    *s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                 "r"(TC_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *s_tmem;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // TMA producer
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % TC_STAGES;
+        if (kc >= TC_STAGES &&
+            !mbar_wait(smem_u32(&bars[TC_STAGES + s]), ((kc / TC_STAGES) + 1) & 1, s_abort, err))
+          break;
+        const int term = kc / kpt, kk = kc % kpt;
+        const int pa = (term_code >> (4 * term)) & 3, pb = (term_code >> (4 * term + 2)) & 3;
+        const uint32_t fb = smem_u32(&bars[s]);
+        mbar_expect_tx(fb, 2 * TC_TILE_BYTES);
+        tma_load_2d(smem_u32(tilesA + s * TC_TILE_BYTES), &wsmap, kk * TC_BK, row0 + pa * prow + (R0 - base), fb);
+        tma_load_2d(smem_u32(tilesB + s * TC_TILE_BYTES), &wsmap, kk * TC_BK, row0 + pb * prow + (C0 - base), fb);
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t idesc = idesc_bf16_f32(TC_BM, TC_BN);
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % TC_STAGES;
+        if (!mbar_wait(smem_u32(&bars[s]), (kc / TC_STAGES) & 1, s_abort, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(tilesA + s * TC_TILE_BYTES);
+        const uint32_t b0 = smem_u32(tilesB + s * TC_TILE_BYTES);
+#pragma unroll
+        for (int k = 0; k < TC_BK / 16; ++k)
+          umma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc, (kc | k) != 0);
+        umma_commit(smem_u32(&bars[TC_STAGES + s]));
+      }
+      umma_commit(smem_u32(&bars[2 * TC_STAGES]));
+    }
+  } else {
+    // epilogue warps 0-3: TMEM lanes [32 warp, 32 warp + 32) = tile rows.
+    // While the mainloop runs, stage this thread's row of the C tile in
+    // shared memory (independent, coalesced loads), so that after the
+    // accumulator is ready only TMEM reads and stores remain.  Each thread
+    // reads back only the row it staged: no barrier needed.
+    float* __restrict__ G = c.a32 + f.off;
+    const int rl = warp * 32 + lane;
+    const int row = R0 + rl;
+    const int jmax = lower_only ? min(n, row + 1) : n;     // columns < jmax are stored
+    float* crow = s_c + rl * TC_CPAD;
+    // batches of 16 independent loads issued before any shared store (a
+    // shared store between them would order every load after the previous one)
+#pragma unroll 1
+    for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+      float t[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int col = C0 + j0 + u;
+        t[u] = (row < n && col < jmax) ? __ldcg(G + row + (int64_t)col * n) : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 16; ++u) crow[j0 + u] = t[u];
+    }
+    const bool ok = mbar_wait(smem_u32(&bars[2 * TC_STAGES]), 0, s_abort, err);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+    for (int cc = 0; cc < TC_BN / 32; ++cc) {
+      uint32_t v[32];
+      TC_LD32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (ok && !*s_abort && row < n) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = C0 + cc * 32 + j;
+          if (col < jmax) G[row + (int64_t)col * n] = crow[cc * 32 + j] - __uint_as_float(v[j]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+  }
+}
+
+// Split the panel A[K0+KB : n, K0 : K0+KB] (FP32, column-major, ld n) into
+// BF16 parts stored row-major with row length nbo (zero beyond KB):
+// part p row r = round-to-nearest BF16 of the p-th residual.
+// item: front, a = K0, b = row block (64 rows)
+__global__ void __launch_bounds__(256) k_tc_pack(DevCtx c, const Item* __restrict__ items, int nbo,
+                                                 int nparts, __nv_bfloat16* __restrict__ ws,
+                                                 const int64_t* __restrict__ ws_off,
+                                                 const int64_t* __restrict__ ws_stride) {
+  __shared__ float tile[64][65];
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, K0 = it.a;
+  const int KB = min(nbo, f.fs - K0);
+  const int base = K0 + KB;
+  const int r0 = it.b * 64;
+  const float* __restrict__ G = c.a32 + f.off;
+  __nv_bfloat16* __restrict__ W = ws + ws_off[it.front];
+  const int64_t pstride = ws_stride[it.front];
+  for (int k0 = 0; k0 < nbo; k0 += 64) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+      const int r = idx % 64, k = idx / 64;
+      const int gr = base + r0 + r, gk = k0 + k;
+      tile[r][k] = (gr < n && gk < KB) ? G[gr + (int64_t)(K0 + gk) * n] : 0.0f;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+      const int k = idx % 64, r = idx / 64;
+      if (base + r0 + r >= n) continue;
+      float x = tile[r][k];
+      for (int p = 0; p < nparts; ++p) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        W[p * pstride + (int64_t)(r0 + r) * nbo + k0 + k] = h;
+        x -= __bfloat162float(h);
+      }
+    }
+  }
+}
+
+// ---- host side ---------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static bool get_encoder() {
+  if (g_encode) return true;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return false;
+  }
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return true;
+}
+
+// 2D map over a row-major rows x nbo BF16 matrix, box 64 (K) x 128 (rows)
+bool tc_encode_part(CUtensorMap* map, void* base, int64_t rows, int nbo) {
+  if (!get_encoder()) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)nbo, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)nbo * 2};
+  cuuint32_t box[2] = {TC_BK, TC_BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+void launch_tc_pack(const DevCtx& c, const Item* items, int n_items, int nbo, int nparts, void* ws,
+                    const int64_t* ws_off, const int64_t* ws_stride, cudaStream_t s) {
+  if (!n_items) return;
+  k_tc_pack<<<n_items, 256, 0, s>>>(c, items, nbo, nparts, (__nv_bfloat16*)ws, ws_off, ws_stride);
+}
+
+void launch_tc_syrk(const DevCtx& c, const CUtensorMap& wsmap, const int64_t* ws_off,
+                    const int64_t* ws_stride, const Item* items, int n_items, int nbo, int nterms,
+                    uint32_t term_code, int lower_only, int* err, cudaStream_t s) {
+  if (!n_items) return;
+  cudaFuncSetAttribute(k_tc_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+  k_tc_syrk<<<n_items, TC_THREADS, TC_SMEM, s>>>(c, wsmap, ws_off, ws_stride, items, nbo, nterms, term_code,
+                                                 lower_only, err);
+}
+
+int tc_tile() { return TC_BM; }
+
+}  // namespace uhm_gpu

@@ -29,6 +29,8 @@ struct FrontDev {
   int g0;             // first global dof eliminated here
   int src0, nsrc;     // assembly sources [src0, src0 + nsrc)
   int status_slot;
+  int flag_off;       // first per-block flag of the flag-driven solves
+  int64_t dinv_off;   // inverses of the 64 x 64 diagonal blocks (element offset)
 };
 
 // An assembly source: an element matrix (full, FP64) or a child front's ABR.
@@ -62,6 +64,9 @@ struct DevCtx {
   double* emat;       // element matrices (FP64, retained for the residual)
   double* vec;        // per-front vector slabs
   int* status;        // per-front status
+  double* dinv64;     // inverted diagonal blocks of the factor (FP64 fronts)
+  float* dinv32;      // ... (FP32 fronts)
+  int* flags;         // per-block completion flags of the flag-driven solves
   int n_rhs;
   int symmetric;      // Cholesky: lower triangles only
 };
@@ -76,7 +81,7 @@ void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtyp
 void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s);
 void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
-                        cudaStream_t s);
+                        int nbo, cudaStream_t s);
 // LU (partial pivoting restricted to the factor rows, or none)
 void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         int pivot, cudaStream_t s);
@@ -92,10 +97,17 @@ void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype
                       cudaStream_t s);
 void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                       double* g, int64_t ldg, cudaStream_t s);
-void launch_trsv_block(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                       int nb, int upper, cudaStream_t s);
-void launch_gemv_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                       int nb, int upper, cudaStream_t s);
+// flag-driven level solves of large Cholesky fronts (one launch per level):
+// items ordered so that every CTA waits only on CTAs with smaller tickets
+void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
+                      int* flag_base, int n_flags, int* err, cudaStream_t s);
+void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
+                      int* flag_base, int n_flags, int* err, cudaStream_t s);
+// blocked solve steps of large fronts (64-column diagonal blocks)
+void launch_fwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                     cudaStream_t s);
+void launch_bwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
+                     double* scratch, const int64_t* scr_off, int* counters, cudaStream_t s);
 void launch_bwd_prepare(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                         const double* g, int64_t ldg, cudaStream_t s);
 void launch_bwd_store(const DevCtx& c, const Item* items, int n_items, double* g, int64_t ldg,
