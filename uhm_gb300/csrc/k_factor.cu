@@ -201,60 +201,92 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // blocked large-front Cholesky: diagonal block, panel TRSM, trailing update
 // item: front, a = k0 (step start), b = row block / tile row, c = tile col
 // ---------------------------------------------------------------------------
+// Cholesky of one diagonal block (kb <= 64) and the inverse of its factor, in
+// shared memory with 256 threads.  Right-looking, two barriers per column;
+// the trailing update is spread over all threads (column j = tid % 64, rows
+// j + tid / 64 + 4m).  Loads are issued in register batches before any
+// shared store.  The inverse L^{-1} (used by the panel TRSM and the
+// flag-driven solves) is formed row by row from the identity.  (Measured on
+// GB300: this plain formulation beat register-blocked and warp-serial
+// sub-block variants, whose long single-warp code paths ran slower.)
+constexpr int PLD = 65;   // padded leading dimension of the shared 64 x 64 tiles
+
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_potrf_diag(DevCtx c, const Item* __restrict__ items,
                                                    int nb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* A = reinterpret_cast<T*>(smem_raw);
+  static_assert(NT == 256, "256 threads");
+  extern __shared__ __align__(16) unsigned char potrf_dyn[];
+  T* A = reinterpret_cast<T*>(potrf_dyn);   // factor, column-major, ld PLD
+  T* W = A + 64 * PLD;                      // inverse of the factor
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  for (int idx = threadIdx.x; idx < kb * kb; idx += NT) {
-    const int i = idx % kb, j = idx / kb;
-    if (i >= j) A[idx] = G[i + (int64_t)j * n];
+  const int tid = threadIdx.x;
+  {
+    T t[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      t[u] = (i < kb && j < kb && i >= j) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      A[i + j * PLD] = t[u];
+    }
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int NW = NT / 32;
+  bool bad = false;
   for (int k = 0; k < kb; ++k) {
-    if (threadIdx.x == 0) {
-      T d = A[k + k * kb];
-      if (!(d > (T)0)) { set_status(c, it.front, d != d ? ST_NAN : ST_NOT_SPD); d = (T)1; }
-      A[k + k * kb] = my_sqrt<T>(d);
+    // the previous column's trailing update wrote this pivot: it is read
+    // after the barrier that ends that update, and the diagonal is
+    // overwritten only after the next barrier (every thread reads it first)
+    __syncthreads();
+    T piv = A[k + k * PLD];
+    if (!(piv > T(0))) { bad = true; piv = T(1); }
+    const T d = my_sqrt<T>(piv);
+    if (tid > k && tid < kb) A[tid + k * PLD] /= d;
+    __syncthreads();
+    if (tid == 0) A[k + k * PLD] = d;
+    const int j = tid & 63, g = tid >> 6;
+    if (j > k && j < kb) {
+      const T ajk = A[j + k * PLD];
+      for (int i = j + g; i < kb; i += 4) A[i + j * PLD] -= A[i + k * PLD] * ajk;
     }
+  }
+  if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+    if (i < kb && j < kb && i >= j) G[i + (int64_t)j * n] = A[i + j * PLD];
+  }
+  T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
+  if (nb != 64 || !Dinv) return;
+  Dinv += f.dinv_off + (int64_t)(k0 / 64) * 4096;
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+    W[i + j * PLD] = i == j ? T(1) : T(0);
+  }
+  __syncthreads();
+  for (int i = 0; i < kb; ++i) {
+    const T dii = A[i + i * PLD];
+    if (tid <= i) W[i + tid * PLD] /= dii;
     __syncthreads();
-    const T dkk = A[k + k * kb];
-    for (int i = k + 1 + threadIdx.x; i < kb; i += NT) A[i + k * kb] /= dkk;
-    __syncthreads();
-    for (int j = k + 1 + warp; j < kb; j += NW) {
-      const T ajk = A[j + k * kb];
-      for (int i = j + lane; i < kb; i += 32) A[i + j * kb] -= A[i + k * kb] * ajk;
+    const int cc = tid & 63, g = tid >> 6;
+    if (cc <= i) {
+      const T wic = W[i + cc * PLD];
+      for (int r = i + 1 + g; r < kb; r += 4) W[r + cc * PLD] -= A[r + i * PLD] * wic;
     }
     __syncthreads();
   }
-  for (int idx = threadIdx.x; idx < kb * kb; idx += NT) {
-    const int i = idx % kb, j = idx / kb;
-    if (i >= j) G[i + (int64_t)j * n] = A[idx];
-  }
-  // inverse of the lower-triangular diagonal block (for the flag-driven
-  // solves): column j of L^{-1} by forward substitution, one thread per column
-  if (nb == 64 && (sizeof(T) == 8 ? (void*)c.dinv64 : (void*)c.dinv32) != nullptr) {
-    T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32) + f.dinv_off + (int64_t)(k0 / 64) * 4096;
-    T* W = A + kb * kb;   // scratch 64 x 64
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) W[idx] = T(0);
-    __syncthreads();
-    const int j = threadIdx.x;
-    if (j < kb) {
-      for (int i = j; i < kb; ++i) {
-        T s = i == j ? T(1) : T(0);
-        for (int t = j; t < i; ++t) s -= A[i + t * kb] * W[t + j * 64];
-        W[i + j * 64] = s / A[i + i * kb];
-      }
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) Dinv[idx] = W[idx];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+    Dinv[idx] = (i < kb && j < kb) ? W[i + j * PLD] : T(0);
   }
 }
 
@@ -262,13 +294,13 @@ void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtyp
                        cudaStream_t s) {
   if (!n_items) return;
   if (dtype == F64) {
-    size_t sm = (size_t)nb * nb * sizeof(double) + 4096 * sizeof(double);
-    cudaFuncSetAttribute(k_potrf_diag<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_potrf_diag<double, 256><<<n_items, 256, sm, s>>>(c, items, nb);
+    const size_t dyn = 2 * 64 * PLD * sizeof(double);
+    cudaFuncSetAttribute(k_potrf_diag<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    k_potrf_diag<double, 256><<<n_items, 256, dyn, s>>>(c, items, nb);
   } else {
-    size_t sm = (size_t)nb * nb * sizeof(float) + 4096 * sizeof(float);
-    cudaFuncSetAttribute(k_potrf_diag<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_potrf_diag<float, 256><<<n_items, 256, sm, s>>>(c, items, nb);
+    const size_t dyn = 2 * 64 * PLD * sizeof(float);
+    cudaFuncSetAttribute(k_potrf_diag<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    k_potrf_diag<float, 256><<<n_items, 256, dyn, s>>>(c, items, nb);
   }
 }
 
@@ -284,8 +316,8 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
   const int n = f.n, k0 = it.a, r0 = it.b;
   const int kb = min(nb, f.fs - k0);
   const int rb = min(TRSM_RB, n - r0);
-  T* L = reinterpret_cast<T*>(smem_raw);        // kb x kb
-  T* X = L + nb * nb;                           // TRSM_RB x kb, ld TRSM_RB
+  T* L = reinterpret_cast<T*>(smem_raw);        // kb x kb (or 64 x 65 padded inverse)
+  T* X = L + 64 * 65;                           // TRSM_RB x kb, ld TRSM_RB
   T* __restrict__ G = arena<T>(c) + f.off;
   for (int idx = threadIdx.x; idx < kb * kb; idx += NT) {
     const int i = idx % kb, j = idx / kb;
@@ -296,6 +328,34 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
     X[idx] = i < rb ? G[(r0 + i) + (int64_t)(k0 + j) * n] : (T)0;
   }
   __syncthreads();
+  const T* Dinv = (sizeof(T) == 8 ? (const T*)c.dinv64 : (const T*)c.dinv32);
+  if (nb == 64 && Dinv) {
+    // X <- X * L11^{-T} as a product with the inverse computed by the
+    // diagonal-block kernel (stored column-major 64 x 64): no sequential sweep
+    Dinv += f.dinv_off + (int64_t)(k0 / 64) * 4096;
+    for (int idx = threadIdx.x; idx < 4096; idx += NT) {
+      // Dinv is column-major: Dinv[t * 64 + j] = Linv[j][t]; keep it as
+      // rows t of length 64 padded to 65, so that L[t * 65 + j] = Linv[j][t]
+      const int t = idx / 64, j = idx % 64;
+      L[t * 65 + j] = (t < kb && j < kb) ? Dinv[idx] : T(0);
+    }
+    __syncthreads();
+    const int i = threadIdx.x % TRSM_RB, jg = threadIdx.x / TRSM_RB;   // 4 column groups of 16
+    T acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = T(0);
+    for (int t = 0; t < kb; ++t) {
+      const T xv = X[i + t * TRSM_RB];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc[u] += xv * L[t * 65 + jg * 16 + u];
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int j = jg * 16 + u;
+      if (i < rb && j < kb) G[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
+    }
+    return;
+  }
   for (int j = 0; j < kb; ++j) {
     const T ljj = L[j + j * kb];
     for (int i = threadIdx.x; i < TRSM_RB; i += NT) X[i + j * TRSM_RB] /= ljj;
@@ -317,11 +377,11 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
                        cudaStream_t s) {
   if (!n_items) return;
   if (dtype == F64) {
-    size_t sm = (size_t)(nb * nb + TRSM_RB * nb) * sizeof(double);
+    size_t sm = (size_t)(64 * 65 + TRSM_RB * nb) * sizeof(double);
     cudaFuncSetAttribute(k_trsm_panel<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_trsm_panel<double, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   } else {
-    size_t sm = (size_t)(nb * nb + TRSM_RB * nb) * sizeof(float);
+    size_t sm = (size_t)(64 * 65 + TRSM_RB * nb) * sizeof(float);
     cudaFuncSetAttribute(k_trsm_panel<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_trsm_panel<float, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   }

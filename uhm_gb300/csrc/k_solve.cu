@@ -609,6 +609,37 @@ __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
 __device__ __forceinline__ void st_release_gpu(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Thread 0 waits (bounded) until flag[first] is set, extends the ready range
+// while further flags are set (step +1 or -1), issues one acquire fence for
+// all of them and returns the end of the range (exclusive) in *s_ready.
+__device__ __forceinline__ void ready_range(const int* flg, int first, int last, int step, int* s_ready,
+                                            int* err) {
+  if (threadIdx.x == 0) {
+    bool ok = false;
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+      if (ld_relaxed_gpu(flg + first) == 1) { ok = true; break; }
+      __nanosleep(32);
+    }
+    int k = first;
+    if (ok) {
+      k = first + step;
+      while (k != last && ld_relaxed_gpu(flg + k) == 1) k += step;
+    } else {
+      atomicExch(err, 2);
+      k = last;
+    }
+    __threadfence();
+    *s_ready = k;
+  }
+  __syncthreads();
+}
+
 __device__ __forceinline__ bool wait_flag(const int* p, int* err) {
   for (uint32_t i = 0; i < (1u << 22); ++i) {
     if (ld_acquire_gpu(p) == 1) return true;
@@ -630,6 +661,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   __shared__ int s_t;
   __shared__ CT red[4][FB][SF_NR];
   __shared__ CT v[FB][SF_NR];
+  __shared__ T dsh[FB * (FB + 1)];     // inverse diagonal block, staged before any wait
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
@@ -637,6 +669,10 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
   const int nfb = (fs + FB - 1) / FB;
   const bool factor_block = b < nfb;
+  if (factor_block) {
+    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
+    for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[(idx / FB) * (FB + 1) + idx % FB] = Dg[idx];
+  }
   const int r0 = factor_block ? b * FB : fs + (b - nfb) * FB;
   const int r1 = factor_block ? min(r0 + FB, fs) : min(r0 + FB, n);
   const T* __restrict__ G = arena<T>(c) + f.off;
@@ -650,23 +686,26 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) acc[q] = CT(0);
   const int jend = factor_block ? b : nfb;
-  for (int j = 0; j < jend; ++j) {
-    const int kbj = min(FB, fs - j * FB);
-    CT lv[16];
+  __shared__ int s_ready;
+  int done = 0;
+  while (done < jend) {
+    ready_range(flg, done, jend, 1, &s_ready, err);
+    const int upto = s_ready;
+    for (int j = done; j < upto; ++j) {
+      const int kbj = min(FB, fs - j * FB);
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int cc = g * 16 + u;
-      lv[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
+      for (int u = 0; u < 16; ++u) {
+        const int cc = g * 16 + u;
+        if (rv && cc < kbj) {
+          const CT l = (CT)G[row + (int64_t)(j * FB + cc) * n];
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q)
+            if (q < nr) acc[q] += l * (CT)__ldcg(y + (j * FB + cc) + (int64_t)q * n);
+        }
+      }
     }
-    wait_flag(flg + j, err);
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int cc = g * 16 + u;
-      if (cc < kbj)
-#pragma unroll
-        for (int q = 0; q < SF_NR; ++q)
-          if (q < nr) acc[q] += lv[u] * (CT)__ldcg(y + (j * FB + cc) + (int64_t)q * n);
-    }
+    done = upto;
+    __syncthreads();
   }
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
@@ -680,13 +719,12 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   __syncthreads();
   if (factor_block) {
     const int kb = r1 - r0;
-    const T* __restrict__ Di = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
     if (threadIdx.x < FB && rv) {
       CT x[SF_NR];
 #pragma unroll
       for (int q = 0; q < SF_NR; ++q) x[q] = CT(0);
       for (int t = 0; t <= i && t < kb; ++t) {
-        const CT d = (CT)Di[i + t * FB];
+        const CT d = (CT)dsh[t * (FB + 1) + i];     // Dinv[i][t], column t staged as row t
 #pragma unroll
         for (int q = 0; q < SF_NR; ++q) x[q] += d * v[t][q];
       }
@@ -710,11 +748,11 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
                                                    int* ticket, int* err) {
   using CT = T;
   __shared__ int s_t;
-  // the reduction tile [row lane][column] and, afterwards, the inverse diagonal block
-  __shared__ __align__(16) unsigned char s_raw[sizeof(CT) * FB * (FB + 1)];
-  CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(s_raw);
-  T* dsh = reinterpret_cast<T*>(s_raw);
+  extern __shared__ __align__(16) unsigned char bwd_dyn[];
+  CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(bwd_dyn);   // [row lane][column]
   __shared__ CT v[FB][SF_NR];
+  __shared__ int s_ready;
+  __shared__ T dsh[FB * (FB + 1)];
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
@@ -722,6 +760,10 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
   const int nfb = (fs + FB - 1) / FB;
   const int c0 = b * FB, kb = min(FB, fs - c0);
+  {
+    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
+    for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[(idx / FB) * (FB + 1) + idx % FB] = Dg[idx];
+  }
   const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
   const int* __restrict__ flg = c.flags + f.flag_off;
@@ -741,19 +783,24 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
         if (r < n && cc < kb) acc[u] += (CT)G[r + (int64_t)(c0 + cc) * n] * xr;
       }
     }
-    for (int j = nfb - 1; j > b; --j) {
-      const int r = j * FB + rl;
-      const bool in = r < min(j * FB + FB, fs);
-      CT lv[16];
+    int next = nfb - 1;
+    while (next > b) {
+      ready_range(flg, next, b, -1, &s_ready, err);
+      const int stop = s_ready;
+      for (int j = next; j > stop; --j) {
+        const int r = j * FB + rl;
+        const bool in = r < min(j * FB + FB, fs);
+        if (in) {
+          const CT xr = (CT)__ldcg(y + r + (int64_t)q * n);
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int cc = g * 16 + u;
-        lv[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
+          for (int u = 0; u < 16; ++u) {
+            const int cc = g * 16 + u;
+            if (cc < kb) acc[u] += (CT)G[r + (int64_t)(c0 + cc) * n] * xr;
+          }
+        }
       }
-      wait_flag(flg + j, err);
-      const CT xr = in ? (CT)__ldcg(y + r + (int64_t)q * n) : CT(0);
-#pragma unroll
-      for (int u = 0; u < 16; ++u) acc[u] += lv[u] * xr;
+      next = stop;
+      __syncthreads();
     }
     __syncthreads();
 #pragma unroll
@@ -765,16 +812,13 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
       v[threadIdx.x][q] = threadIdx.x < kb ? (CT)y[c0 + threadIdx.x + (int64_t)q * n] - s : CT(0);
     }
   }
-  const T* __restrict__ Di = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
   __syncthreads();
-  for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[idx] = Di[idx];
-  __syncthreads();
-  // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t
+  // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t   (column i of Dinv, staged at start)
   if (threadIdx.x < kb) {
     const int ii = threadIdx.x;
     for (int q = 0; q < nr && q < SF_NR; ++q) {
       CT x = CT(0);
-      for (int t = ii; t < kb; ++t) x += (CT)dsh[t + ii * FB] * v[t][q];
+      for (int t = ii; t < kb; ++t) x += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
       y[c0 + ii + (int64_t)q * n] = (double)x;
     }
   }
@@ -797,8 +841,15 @@ void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype
   if (!n_items) return;
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
   cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
-  if (dtype == F64) k_bwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err);
-  else k_bwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err);
+  if (dtype == F64) {
+    const size_t dyn = sizeof(double) * FB * (FB + 1);
+    cudaFuncSetAttribute(k_bwd_flags<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    k_bwd_flags<double><<<n_items, 256, dyn, s>>>(c, items, ticket, err);
+  } else {
+    const size_t dyn = sizeof(float) * FB * (FB + 1);
+    cudaFuncSetAttribute(k_bwd_flags<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    k_bwd_flags<float><<<n_items, 256, dyn, s>>>(c, items, ticket, err);
+  }
 }
 
 }  // namespace uhm_gpu
