@@ -1,0 +1,89 @@
+"""Runs the reference solver built by ``oracle/Makefile`` (TEST INFRASTRUCTURE).
+
+Writes a :class:`uhm_gb300.hpfem.MeshSpec` in the binary layout that
+``oracle/ref_driver.cpp`` reads, runs ``oracle/_ref/uhm_ref_driver`` and
+parses its output.  Only the fixture generator (``tests/golden/make_golden.py``)
+and tests that skip when the binary is absent use this module; the reference
+checkout is needed only to build the binary.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import tempfile
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DRIVER = os.path.join(HERE, "_ref", "uhm_ref_driver")
+
+
+@dataclass
+class RefResult:
+    x: np.ndarray          # (n_dof, n_rhs), node order of the spec, dofs of a node contiguous
+    fronts: np.ndarray     # (n_elements, 2): (factor dofs, schur dofs) per element
+    t_factor: float
+    t_solve: float
+    flop_decompose: float
+    flop_solve: float
+
+
+def available() -> bool:
+    return os.path.exists(DRIVER)
+
+
+def build(ref_root: str = "/root/reference", jobs: int = 16) -> bool:
+    """Compile the reference solver when its sources are present."""
+    if not os.path.isdir(os.path.join(ref_root, "UHM", "src")):
+        return available()
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", f"REF={ref_root}"], check=True)
+    return available()
+
+
+def write_spec(spec, method: int, path: str) -> None:
+    i32 = lambda a: np.asarray(a, dtype="<i4").tobytes()
+    with open(path, "wb") as f:
+        f.write(b"UHMS" + i32([1]))
+        f.write(i32([spec.n_nodes]))
+        f.write(i32(np.stack([spec.node_id, spec.node_ndof, spec.node_p, spec.node_kind], axis=1).ravel()))
+        f.write(i32([spec.n_elements, spec.n_leaves, spec.n_rhs, method]))
+        f.write(i32(spec.generation))
+        f.write(i32(spec.child_ptr))
+        f.write(i32(spec.child_idx))
+        f.write(i32(spec.elem_ptr))
+        f.write(i32(spec.elem_node))
+        for e in range(spec.n_leaves):
+            f.write(np.asarray(spec.element_matrix(e), dtype="<f8").ravel(order="F").tobytes())
+            f.write(np.asarray(spec.element_rhs(e), dtype="<f8").ravel(order="F").tobytes())
+
+
+def read_result(path: str, spec) -> RefResult:
+    buf = open(path, "rb").read()
+    if buf[:4] != b"UHMR":
+        raise ValueError("bad reference output")
+    p = 4
+    ver, n_nodes, n_rhs = np.frombuffer(buf, "<i4", 3, p)
+    p += 12
+    assert ver == 1 and n_nodes == spec.n_nodes
+    n_dof = int(spec.node_ndof.sum())
+    x = np.frombuffer(buf, "<f8", n_dof * n_rhs, p).reshape(n_dof, n_rhs).copy()
+    p += 8 * n_dof * n_rhs
+    n_el = int(np.frombuffer(buf, "<i4", 1, p)[0])
+    p += 4
+    fronts = np.frombuffer(buf, "<i4", 2 * n_el, p).reshape(n_el, 2).astype(np.int64)
+    p += 8 * n_el
+    tf, ts, fd, fs = np.frombuffer(buf, "<f8", 4, p)
+    return RefResult(x, fronts, float(tf), float(ts), float(fd), float(fs))
+
+
+def run(spec, method: int, threads: int = 1) -> RefResult:
+    if not available():
+        raise RuntimeError("reference solver not built (make -C oracle)")
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        write_spec(spec, method, fin)
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        subprocess.run([DRIVER, fin, fout, str(threads)], check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+        return read_result(fout, spec)
