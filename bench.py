@@ -215,23 +215,26 @@ def run_gpu(args):
     one_step(m)
     prof = m.profile()
     m.set_profiling(False)
-    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    name, p = top
-    if p["flops"] > 0:
-        bound = "tensor" if args.prec == api.PREC_BF16X3 else "fp32-simt"
+    # Roofline of the dominant tensor-core kernel: the BF16-split Schur update
+    # (tcgen05).  achieved = algorithmic Schur-update flops (one product per
+    # output, LAWN-41 SYRK count) / device time; the split evaluates 3 (BF16X3)
+    # or 6 (BF16X6) BF16 products per algorithmic one, reported as mma_frac.
+    tc_name = "tc_syrk_bf16"
+    if tc_name in prof and prof[tc_name]["ms"] > 0:
+        p = prof[tc_name]
+        terms = 6 if args.prec == api.PREC_BF16X6 else 3
         achieved = p["flops"] / (p["ms"] * 1e-3) / 1e12
-        peak = peaks.get("bf16_tflops") if args.prec == api.PREC_BF16X3 else 69.9
-        roof = {"bound": "tensor" if args.prec == api.PREC_BF16X3 else "compute",
-                "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None, "traffic": None,
-                "peak_source": ("MEASURED_PEAKS.json bf16 (" + peak_src + ")") if args.prec == api.PREC_BF16X3
-                else "FP32 SIMT SGEMM measured on this GB300 (profiles/peaks_gb300.md)",
-                "bound_kind": bound}
+        peak = float(peaks.get("bf16_tflops"))
+        roof = {"bound": "tensor", "kernel": tc_name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "mma_frac": terms * achieved / peak, "split_terms": terms,
+                "launches": p["launches"], "us_per_launch": 1e3 * p["ms"] / max(1, p["launches"]),
+                "traffic": None, "peak_source": f"bf16_tflops of MEASURED_PEAKS.json ({peak_src})"}
     else:
+        name, p = max(prof.items(), key=lambda kv: kv[1]["ms"])
         achieved = p["bytes"] / (p["ms"] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                "peak_source": "MEASURED_PEAKS.json hbm (" + peak_src + ")"}
+                "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_src})"}
 
     # ---- end to end through the C ABI with host buffers -----------------------
     emat = api.pinned_empty(spec.mats.size)
@@ -270,8 +273,8 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "n_dof": int(spec.n_dof()), "n_fronts": int(spec.n_elements),
                        "root_front": 11719, "factor_gflop_lawn41": fd / 1e9,
                        "l2": "inputs larger than L2 (element matrices 512 MB, fronts > 3 GB)",
-                       "precision_policy": ["fp64", "fp32", "bf16x3"][args.prec]},
-            "backward_error": berr, "ir_iters": last["ir_iters"], "berr_first_solve": None,
+                       "precision_policy": ["fp64", "fp32", "bf16x3", "bf16x6"][args.prec]},
+            "backward_error": berr, "ir_iters": last["ir_iters"], "berr_first_solve": last.get("berr_first"),
             "factor_ms": last["factor_ms"], "solve_ms": last["solve_ms"], "refine_ms": last["refine_ms"],
             "plain_fp64_s": plain_s, "plain_fp64_backward_error": plain_berr,
             "speedup_vs_plain_fp64": plain_s / dev_s,
@@ -301,7 +304,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", type=int, default=1, help="0 fp64, 1 fp32, 2 bf16x3 fronts (mixed path)")
+    ap.add_argument("--prec", type=int, default=2,
+                    help="front policy of the mixed path: 0 fp64, 1 fp32, 2 bf16x3, 3 bf16x6 "
+                         "(tensor-core split on fronts with n >= 512, fp32 below)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="poisson3d_16_p4", choices=sorted(WORKLOADS))
     ap.add_argument("--profile-only", action="store_true",

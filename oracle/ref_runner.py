@@ -83,7 +83,7 @@ def run(spec, method: int, threads: int = 1) -> RefResult:
     with tempfile.TemporaryDirectory() as d:
         fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
         write_spec(spec, method, fin)
-        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
         subprocess.run([DRIVER, fin, fout, str(threads)], check=True, env=env,
                        stdout=subprocess.DEVNULL)
         return read_result(fout, spec)

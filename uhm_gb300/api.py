@@ -262,7 +262,7 @@ class Mesh:
         out = (_d * 9)()
         self.L.uhm_gpu_get_timing(C.byref(self.h), out)
         keys = ["upload_ms", "factor_ms", "solve_ms", "refine_ms", "total_ms", "ir_iters",
-                "berr", "kernel_launches"]
+                "berr", "kernel_launches", "berr_first"]
         return dict(zip(keys, list(out)))
 
     OP_NAMES = ["assemble", "small_factor", "potrf_diag", "trsm_panel", "syrk_update",
