@@ -201,107 +201,153 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // blocked large-front Cholesky: diagonal block, panel TRSM, trailing update
 // item: front, a = k0 (step start), b = row block / tile row, c = tile col
 // ---------------------------------------------------------------------------
-// Cholesky of one diagonal block (kb <= 64) and the inverse of its factor, in
-// shared memory with 256 threads.  Right-looking, two barriers per column;
-// the trailing update is spread over all threads (column j = tid % 64, rows
-// j + tid / 64 + 4m).  Loads are issued in register batches before any
-// shared store.  The inverse L^{-1} (used by the panel TRSM and the
-// flag-driven solves) is formed row by row from the identity.  (Measured on
-// GB300: this plain formulation beat register-blocked and warp-serial
-// sub-block variants, whose long single-warp code paths ran slower.)
-constexpr int PLD = 65;   // padded leading dimension of the shared 64 x 64 tiles
+// Cholesky of one diagonal block (kb <= 64) and the inverse of its factor.
+// 64 threads; thread i keeps row i of the block in registers (fully unrolled,
+// compile-time register indices) and publishes every finished entry L[i][k]
+// into a row-major shared copy.  Left-looking: the entry (i, k) is
+//   L[i][k] = (A[i][k] - sum_{j<k} L[i][j] L[k][j]) / L[k][k],
+// with row k read from shared memory as 128-bit vectors.  One barrier per
+// column: before it, every thread has all terms j < k-1 (row k's entries up
+// to k-2 are visible since the previous barrier) and thread k has its pivot
+// (its own row is in registers); after it, the single missing term j = k-1
+// is added.  Blocks narrower than 64 are padded with the identity.  The
+// inverse L^{-1} (used by the panel TRSM and by the flag-driven solves) is
+// formed column per thread by forward substitution over the shared rows and
+// stored column-major with 128-bit stores.  FP32 pivots use rsqrt (the
+// factor is refined in FP64 by the mixed path); FP64 uses sqrt and a divide.
+template <typename T> struct PotrfVec;
+template <> struct PotrfVec<float> { using V = float4; static constexpr int W = 4, RL = 68; };
+template <> struct PotrfVec<double> { using V = double2; static constexpr int W = 2, RL = 66; };
 
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_potrf_diag(DevCtx c, const Item* __restrict__ items,
-                                                   int nb) {
-  static_assert(NT == 256, "256 threads");
-  extern __shared__ __align__(16) unsigned char potrf_dyn[];
-  T* A = reinterpret_cast<T*>(potrf_dyn);   // factor, column-major, ld PLD
-  T* W = A + 64 * PLD;                      // inverse of the factor
+template <typename T> __device__ __forceinline__ void pivot_root(T s, T& d, T& rd);
+template <> __device__ __forceinline__ void pivot_root<float>(float s, float& d, float& rd) {
+  rd = rsqrtf(s);
+  d = s * rd;
+}
+template <> __device__ __forceinline__ void pivot_root<double>(double s, double& d, double& rd) {
+  d = sqrt(s);
+  rd = 1.0 / d;
+}
+
+// s - sum_{j < CNT} x[j] * row[j]; row 16-byte aligned; W partial sums
+template <int CNT, typename T>
+__device__ __forceinline__ T potrf_dot(T s, const T (&x)[64], const T* __restrict__ row) {
+  constexpr int W = PotrfVec<T>::W;
+  using V = typename PotrfVec<T>::V;
+  T acc[W];
+#pragma unroll
+  for (int u = 0; u < W; ++u) acc[u] = T(0);
+#pragma unroll
+  for (int j = 0; j + W <= CNT; j += W) {
+    const V v = *reinterpret_cast<const V*>(row + j);
+    const T* pv = reinterpret_cast<const T*>(&v);
+#pragma unroll
+    for (int u = 0; u < W; ++u) acc[u] += x[j + u] * pv[u];
+  }
+#pragma unroll
+  for (int j = (CNT / W) * W; j < CNT; ++j) acc[0] += x[j] * row[j];
+  T t = acc[0];
+#pragma unroll
+  for (int u = 1; u < W; ++u) t += acc[u];
+  return s - t;
+}
+
+template <int K, typename T>
+struct PotrfColumn {
+  static __device__ __forceinline__ void run(T (&a)[64], T* Ls, T* sd, T* srd, int i, bool& bad) {
+    constexpr int RL = PotrfVec<T>::RL;
+    const T* rk = Ls + K * RL;
+    T s = potrf_dot<(K > 0 ? K - 1 : 0)>(a[K], a, rk);
+    if (i == K) {
+      if (K > 0) s -= a[K - 1] * a[K - 1];
+      T piv = s;
+      if (!(piv > T(0))) { bad = true; piv = T(1); }
+      T d, rd;
+      pivot_root<T>(piv, d, rd);
+      sd[K] = d;
+      srd[K] = rd;
+    }
+    __syncthreads();
+    if (K > 0) s -= a[K - 1] * rk[K - 1];
+    const T l = (i > K) ? s * srd[K] : (i == K ? sd[K] : T(0));
+    a[K] = l;
+    if (i > K) Ls[i * RL + K] = l;
+    PotrfColumn<K + 1, T>::run(a, Ls, sd, srd, i, bad);
+  }
+};
+template <typename T>
+struct PotrfColumn<64, T> {
+  static __device__ __forceinline__ void run(T (&)[64], T*, T*, T*, int, bool&) {}
+};
+
+template <int R, typename T>
+struct InverseRow {
+  static __device__ __forceinline__ void run(T (&x)[64], const T* Ls, const T* srd, int jc) {
+    constexpr int RL = PotrfVec<T>::RL;
+    x[R] = potrf_dot<R>((R == jc) ? T(1) : T(0), x, Ls + R * RL) * srd[R];
+    InverseRow<R + 1, T>::run(x, Ls, srd, jc);
+  }
+};
+template <typename T>
+struct InverseRow<64, T> {
+  static __device__ __forceinline__ void run(T (&)[64], const T*, const T*, int) {}
+};
+
+template <typename T>
+__global__ void __launch_bounds__(64) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
+  constexpr int RL = PotrfVec<T>::RL;
+  __shared__ __align__(16) T Ls[64 * RL];
+  __shared__ T sd[64], srd[64];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  const int tid = threadIdx.x;
+  const int i = threadIdx.x;
+  T a[64];
   {
-    T t[16];
+    const T* p = G + i;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-      t[u] = (i < kb && j < kb && i >= j) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
-    }
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-      A[i + j * PLD] = t[u];
+    for (int j = 0; j < 64; ++j) {
+      const bool in = i < kb && j < kb;
+      a[j] = in ? (j <= i ? p[(int64_t)j * n] : T(0)) : (i == j ? T(1) : T(0));
     }
   }
-  __syncthreads();
   bool bad = false;
-  for (int k = 0; k < kb; ++k) {
-    // the previous column's trailing update wrote this pivot: it is read
-    // after the barrier that ends that update, and the diagonal is
-    // overwritten only after the next barrier (every thread reads it first)
-    __syncthreads();
-    T piv = A[k + k * PLD];
-    if (!(piv > T(0))) { bad = true; piv = T(1); }
-    const T d = my_sqrt<T>(piv);
-    if (tid > k && tid < kb) A[tid + k * PLD] /= d;
-    __syncthreads();
-    if (tid == 0) A[k + k * PLD] = d;
-    const int j = tid & 63, g = tid >> 6;
-    if (j > k && j < kb) {
-      const T ajk = A[j + k * PLD];
-      for (int i = j + g; i < kb; i += 4) A[i + j * PLD] -= A[i + k * PLD] * ajk;
-    }
-  }
-  if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
-  __syncthreads();
+  PotrfColumn<0, T>::run(a, Ls, sd, srd, i, bad);
+  if (bad) set_status(c, it.front, ST_NOT_SPD);
+  {
+    T* p = G + i;
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-    if (i < kb && j < kb && i >= j) G[i + (int64_t)j * n] = A[i + j * PLD];
+    for (int j = 0; j < 64; ++j)
+      if (i < kb && j < kb && j <= i) p[(int64_t)j * n] = a[j];
   }
   T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
   if (nb != 64 || !Dinv) return;
-  Dinv += f.dinv_off + (int64_t)(k0 / 64) * 4096;
+  __syncthreads();   // every row of Ls is complete
+  const int jc = i;
+  T x[64];
+  InverseRow<0, T>::run(x, Ls, srd, jc);
+  using V = typename PotrfVec<T>::V;
+  constexpr int W = PotrfVec<T>::W;
+  V* D = reinterpret_cast<V*>(Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096 + jc * 64);
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-    W[i + j * PLD] = i == j ? T(1) : T(0);
-  }
-  __syncthreads();
-  for (int i = 0; i < kb; ++i) {
-    const T dii = A[i + i * PLD];
-    if (tid <= i) W[i + tid * PLD] /= dii;
-    __syncthreads();
-    const int cc = tid & 63, g = tid >> 6;
-    if (cc <= i) {
-      const T wic = W[i + cc * PLD];
-      for (int r = i + 1 + g; r < kb; r += 4) W[r + cc * PLD] -= A[r + i * PLD] * wic;
-    }
-    __syncthreads();
-  }
+  for (int r = 0; r < 64; r += W) {
+    V v;
+    T* pv = reinterpret_cast<T*>(&v);
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-    Dinv[idx] = (i < kb && j < kb) ? W[i + j * PLD] : T(0);
+    for (int u = 0; u < W; ++u) pv[u] = (r + u < kb && jc < kb) ? x[r + u] : T(0);
+    D[r / W] = v;
   }
 }
 
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s) {
   if (!n_items) return;
-  if (dtype == F64) {
-    const size_t dyn = 2 * 64 * PLD * sizeof(double);
-    cudaFuncSetAttribute(k_potrf_diag<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    k_potrf_diag<double, 256><<<n_items, 256, dyn, s>>>(c, items, nb);
-  } else {
-    const size_t dyn = 2 * 64 * PLD * sizeof(float);
-    cudaFuncSetAttribute(k_potrf_diag<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    k_potrf_diag<float, 256><<<n_items, 256, dyn, s>>>(c, items, nb);
-  }
+  if (dtype == F64)
+    k_potrf_diag<double><<<n_items, 64, 0, s>>>(c, items, nb);
+  else
+    k_potrf_diag<float><<<n_items, 64, 0, s>>>(c, items, nb);
 }
 
 constexpr int TRSM_RB = 64;   // rows per panel-TRSM block
