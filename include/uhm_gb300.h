@@ -139,6 +139,26 @@ int uhm_gpu_get_fronts(long* mesh, int n, int* elt_id, int* generation, int* fs,
 int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_factor,
                             int* n_schur);
 
+/* Solves (L L^T) x = b for a dense SPD matrix whose lower Cholesky factor L
+ * (n x n, column-major, leading dimension ld >= n, FP64) the caller already
+ * holds in device memory; x holds b on entry and the solution on return,
+ * also in device memory.  Nothing is allocated: this is for callers that may
+ * not call cudaMalloc (an application that owns all device memory through
+ * its own pool, a real-time loop that cannot take an allocation's implicit
+ * synchronisation).  It has no counterpart in the reference.
+ *   - n <= 262144; larger n returns 30, bad arguments return 7, a device
+ *     wait that gave up returns 14.
+ *   - Scratch: a fixed 32 KB device array inside this library (ticket, error
+ *     word, per-block completion flags), present on every GPU that loads the
+ *     library; each call clears the part it uses on `stream` first.
+ *   - The first call on a device looks up that array's device address (once
+ *     per device); make that first call before any stream capture.
+ *   - Calls share the array: calls that overlap on the GPU (other streams,
+ *     other host threads) race and must be serialised by the caller.
+ *   - The call waits for `stream` (it reads the error word back) and runs the
+ *     work on `stream` (NULL = the legacy default stream). */
+int uhm_gpu_dense_chol_solve_noalloc(const double* L, int n, int ld, double* x, void* stream);
+
 /* pinned host memory for the bulk transfers */
 void* uhm_gpu_host_alloc(long bytes);
 void uhm_gpu_host_free(void* p);

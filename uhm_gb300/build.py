@@ -25,6 +25,7 @@ SOURCES = [
     "k_factor.cu",
     "k_solve.cu",
     "k_tc_gemm.cu",
+    "k_noalloc.cu",
 ]
 
 
