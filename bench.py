@@ -2,9 +2,11 @@
 
 One step = one full multifrontal factorisation + solve (+ FP64 iterative
 refinement for the mixed path) of the workload, inputs already resident in
-HBM.  ``value`` is the mixed-precision path (per-front FP32 / BF16-split,
-FP64 refinement to backward error <= 1e-12); the plain FP64 path is timed
-beside it.  ``e2e`` times the same steps through the C ABI with host buffers:
+HBM.  ``value`` is the mixed-precision path with the learned per-front
+precision (FP64 / FP32 / BF16-split chosen by the selector network, FP64
+refinement to backward error <= 1e-12); the plain FP64 path and the fixed
+BF16-split policy are timed beside it.  The selector runs once, at the first
+factorisation (outside the timed steps; its wall time is reported).  ``e2e`` times the same steps through the C ABI with host buffers:
 bulk copy-in of element matrices and right-hand sides from pinned host memory,
 factor, solve, copy-out of the solution.
 
@@ -163,9 +165,17 @@ def run_gpu(args):
         dist.init_process_group("gloo")
     spec = build_workload(seed=rank, name=args.workload)
     peaks, peak_src = _peaks()
+    selector = None
+    if args.prec == api.PREC_LEARNED:
+        from uhm_gb300 import selector as sel
+        selector = sel.load_weights()
+        if selector is None:
+            raise RuntimeError("learned precision policy: uhm_gb300/selector_weights.npz is missing")
     if args.profile_only:
         # one warm factor+solve of the mixed path, for external profilers
         m = api.load_spec(spec)
+        if selector is not None:
+            m.set_selector(selector)
         m.set_mode(1, args.prec, 1e-12, 10)
         for _ in range(args.steps + args.warmup):
             m.chol_with_free()
@@ -190,9 +200,26 @@ def run_gpu(args):
     plain_s = statistics.median([p[0] for p in plain])
     plain_berr = m.backward_error()
 
-    # ---- mixed + IR (headline) ----------------------------------------------
+    # ---- fixed BF16X3 policy (the mixed path without the selector) -----------
+    fixed_s = None
+    if args.prec == api.PREC_LEARNED:
+        m.set_mode(1, api.PREC_BF16X3, 1e-12, 10)
+        for _ in range(max(1, min(args.warmup, 2))):
+            one_step(m)
+        fixed_s = statistics.median([one_step(m)[0] for _ in range(max(1, min(args.steps, 3)))])
+
+    # ---- mixed + IR (headline): learned per-front precision -------------------
+    if selector is not None:
+        m.set_selector(selector)
     m.set_mode(1, args.prec, 1e-12, 10)
-    for _ in range(args.warmup):
+    t_setup = time.perf_counter()
+    one_step(m)                               # first factorisation: features, selector, plan
+    t_setup = time.perf_counter() - t_setup
+    front_classes = None
+    if selector is not None:
+        _, cls = m.front_precision()
+        front_classes = dict(zip(["fp64", "fp32", "bf16"], np.bincount(cls[cls >= 0], minlength=3).tolist()))
+    for _ in range(max(0, args.warmup - 1)):
         one_step(m)
     clocks = Clocks()
     launches0 = None
@@ -268,16 +295,19 @@ def run_gpu(args):
             "metric": METRIC, "value": dev_s / ws, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "mixed: f32/bf16x3 fronts, f64 refinement",
+            "dtype": "mixed: per-front f64/f32/bf16x3 (learned), f64 refinement" if selector is not None
+                     else "mixed: f32/bf16x3 fronts, f64 refinement",
             "data": "synthetic (seeded hp-FEM mesh)",
             "config": {"workload": WORKLOAD, "n_dof": int(spec.n_dof()), "n_fronts": int(spec.n_elements),
                        "root_front": 11719, "factor_gflop_lawn41": fd / 1e9,
                        "l2": "inputs larger than L2 (element matrices 512 MB, fronts > 3 GB)",
-                       "precision_policy": ["fp64", "fp32", "bf16x3", "bf16x6"][args.prec]},
+                       "precision_policy": ["fp64", "fp32", "bf16x3", "bf16x6", "learned"][args.prec]},
             "backward_error": berr, "ir_iters": last["ir_iters"], "berr_first_solve": last.get("berr_first"),
             "factor_ms": last["factor_ms"], "solve_ms": last["solve_ms"], "refine_ms": last["refine_ms"],
             "plain_fp64_s": plain_s, "plain_fp64_backward_error": plain_berr,
             "speedup_vs_plain_fp64": plain_s / dev_s,
+            "fixed_bf16x3_s": fixed_s, "selector_front_classes": front_classes,
+            "first_step_wall_s": t_setup,
             "wall_s_per_step": t_wall / args.steps,
             "e2e": {"value": e2e_s, "unit": "s",
                     "h2d_bytes_per_step": int((spec.mats.size + spec.rhs.size) * 8),
@@ -304,9 +334,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--prec", type=int, default=2,
+    ap.add_argument("--prec", type=int, default=4,
                     help="front policy of the mixed path: 0 fp64, 1 fp32, 2 bf16x3, 3 bf16x6 "
-                         "(tensor-core split on fronts with n >= 512, fp32 below)")
+                         "(tensor-core split on fronts with n >= 512, fp32 below), 4 learned per front")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="poisson3d_16_p4", choices=sorted(WORKLOADS))
     ap.add_argument("--profile-only", action="store_true",

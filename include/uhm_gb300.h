@@ -95,7 +95,8 @@ int uhm_gpu_get_last_error(long* mesh, char* buf, int len);
 /* mode 0: plain FP64 fronts.  mode 1: mixed precision, fronts in
  * default_prec (0 FP64, 1 FP32, 2 BF16-split tensor-core Schur update) with
  * FP64 iterative refinement on the element matrices until the backward error
- * is <= tol or max_iter corrections have been applied. */
+ * is <= tol or max_iter corrections have been applied; default_prec 3 is the
+ * six-term BF16 split and 4 the learned per-front choice (below). */
 int uhm_gpu_set_mode(long* mesh, int mode, int default_prec, double tol, int max_iter);
 /* per-front precision, indexed by element id (-1 = default) */
 int uhm_gpu_set_front_precision(long* mesh, int n, const int* prec_by_element_id);
@@ -130,6 +131,9 @@ int uhm_gpu_get_timing(long* mesh, double* out);
 int uhm_gpu_set_profiling(long* mesh, int on);
 int uhm_gpu_get_profile(long* mesh, int n_kinds, double* ms, double* flops, double* bytes,
                         long* launches);
+/* every profiled launch in launch order: op kind, items (CTAs of work), ms;
+ * *n_out = number recorded (entries beyond cap are not written) */
+int uhm_gpu_get_op_log(long* mesh, int cap, int* kind, int* n_items, double* ms, int* n_out);
 
 /* front table after lock + create_matrix_without_buffer: per front (leaf to
  * root order) the element id, generation, fs, ss */
@@ -138,6 +142,31 @@ int uhm_gpu_get_fronts(long* mesh, int n, int* elt_id, int* generation, int* fs,
 /* node ids of one front, factor nodes then schur nodes, in front order */
 int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_factor,
                             int* n_schur);
+
+/* Learned per-front precision (uhm_gpu_set_mode default_prec = 4): a
+ * 12 -> 64 -> 64 -> 3 MLP (classes 0 FP64, 1 FP32, 2 BF16-split) reads per-front
+ * features computed from the element matrices and the tree and picks each
+ * front's precision before the first factorisation; a solve that misses the
+ * refinement tolerance is redone in FP64 (status 20).  Parameters: 5187
+ * floats, layout W1[64][12] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]. */
+int uhm_gpu_set_selector(long* mesh, const float* params, int n);
+/* per-front features (front order of uhm_gpu_get_fronts, 12 floats each),
+ * after the element matrices are copied in; method as for the factorisation */
+int uhm_gpu_get_front_features(long* mesh, int method, int n_fronts, float* out);
+/* per front: precision used by the last plan (0 FP64, 1 FP32, 2 BF16X3,
+ * 3 BF16X6) and the selector's class (-1 if it has not run) */
+int uhm_gpu_get_front_precision(long* mesh, int n_fronts, int* prec, int* learned_class);
+/* the selector network on caller samples X (N x 12, row-major, host memory):
+ * class and class probabilities; class-weighted cross-entropy gradient over
+ * all N samples (checks the training kernels); Adam training on shuffled
+ * minibatches, parameters updated in place, mean loss per epoch */
+int uhm_gpu_mlp_n_params(void);
+int uhm_gpu_mlp_n_features(void);
+int uhm_gpu_mlp_predict(const float* X, int N, const float* params, int* cls, float* prob);
+int uhm_gpu_mlp_gradient(const float* X, const int* Y, const float* class_weight, int N, const float* params,
+                         float* grad, float* loss);
+int uhm_gpu_mlp_train(const float* X, const int* Y, const float* class_weight, int N, float* params, int epochs,
+                      int batch, float lr, unsigned long long seed, float* loss_hist);
 
 /* Solves (L L^T) x = b for a dense SPD matrix whose lower Cholesky factor L
  * (n x n, column-major, leading dimension ld >= n, FP64) the caller already

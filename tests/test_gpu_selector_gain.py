@@ -1,0 +1,45 @@
+"""What the trained precision selector gains over the method without it.
+
+Held-out instances of the training mix (never used for training: instances
+400..511 of ``selector.sample_instances(512, seed=1)``), solved three ways to
+backward error 1e-12 with at most 3 refinement steps:
+
+* plain FP64 fronts (the drop-in, and the selector's fallback),
+* the fixed BF16-split policy (every front the cheapest precision, FP64 redo
+  on a miss),
+* the learned per-front precision (committed weights).
+
+The instances are ones where the fronts near the root are cheaper in FP32
+than split BF16 (8^3 and 16^3 meshes), so the learned choice must beat the
+fixed policy there; it must also be at least twice as fast as plain FP64.
+Every learned solve has to meet the target (with or without the redo).
+"""
+import numpy as np
+import pytest
+
+from uhm_gb300 import api
+from uhm_gb300 import selector as S
+
+pytestmark = pytest.mark.gpu
+
+HELD_OUT_SEEDS = (100475, 100486, 100488, 100459, 100466)
+
+
+def test_learned_precision_beats_fixed_policy(native_lib):
+    params = S.load_weights()
+    assert params is not None, "selector weights missing"
+    insts = {i.seed: i for i in S.sample_instances(512, 1)[400:]}
+    t = {"plain_fp64": 0.0, "fixed_bf16": 0.0, "learned": 0.0}
+    for seed in HELD_OUT_SEEDS:
+        inst = insts[seed]
+        assert inst.shift == 0.0
+        spec = S.make_mesh(inst)
+        m = api.load_spec(spec)
+        ev = S.evaluate_instance(m, spec, params)
+        assert ev["learned"]["ok"] or ev["learned"]["status"] == api.STATUS_RECOMPUTED_FP64
+        assert 0 <= ev["learned"]["berr"] <= S.TOL
+        for k in t:
+            t[k] += ev[k]["ms"]
+        del m
+    assert t["learned"] < 0.92 * t["fixed_bf16"], t
+    assert t["learned"] < 0.5 * t["plain_fp64"], t

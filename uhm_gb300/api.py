@@ -20,7 +20,7 @@ UHM_REAL, UHM_COMPLEX = 101, 103
 UHM_LHS, UHM_RHS = 1, 2
 UHM_PHYSICS_SINGLE, UHM_PHYSICS_MULTI = 1, 2
 UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV = 1, 2, 3
-PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16X6 = 0, 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16X6, PREC_LEARNED = 0, 1, 2, 3, 4
 STATUS_RECOMPUTED_FP64 = 20     # refinement missed; the solution was recomputed in FP64
 
 _lib = None
@@ -90,6 +90,16 @@ def _declare(L):
     sig("uhm_gpu_get_profile", [_P(_l), _i, _P(_d), _P(_d), _P(_d), _P(_l)], _i)
     sig("uhm_gpu_host_alloc", [_l], C.c_void_p)
     sig("uhm_gpu_host_free", [C.c_void_p])
+    _f = C.c_float
+    sig("uhm_gpu_set_selector", [_P(_l), _P(_f), _i], _i)
+    sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
+    sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
+    sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_mlp_n_params", [], _i)
+    sig("uhm_gpu_mlp_n_features", [], _i)
+    sig("uhm_gpu_mlp_predict", [_P(_f), _i, _P(_f), _P(_i), _P(_f)], _i)
+    sig("uhm_gpu_mlp_gradient", [_P(_f), _P(_i), _P(_f), _i, _P(_f), _P(_f), _P(_f)], _i)
+    sig("uhm_gpu_mlp_train", [_P(_f), _P(_i), _P(_f), _i, _P(_f), _i, _i, _f, C.c_ulonglong, _P(_f)], _i)
 
 
 class UHMError(RuntimeError):
@@ -313,6 +323,37 @@ class Mesh:
                                                    ids.ctypes.data_as(_P(_i)), C.byref(nf), C.byref(ns)))
         return ids[:nf.value], ids[nf.value:nf.value + ns.value]
 
+    def op_log(self, cap=1 << 16):
+        """Profiled launches in order: list of (op name, items, ms)."""
+        kind, items = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+        ms = np.zeros(cap, np.float64)
+        n = _i(0)
+        self._check(self.L.uhm_gpu_get_op_log(C.byref(self.h), cap, kind.ctypes.data_as(_P(_i)),
+                                              items.ctypes.data_as(_P(_i)), ms.ctypes.data_as(_P(_d)), C.byref(n)))
+        k = min(n.value, cap)
+        return [(self.OP_NAMES[kind[i]], int(items[i]), float(ms[i])) for i in range(k)]
+
+    # -- learned precision selector ------------------------------------------
+    def set_selector(self, params):
+        a, p = _arr(params, np.float32, C.c_float)
+        self._check(self.L.uhm_gpu_set_selector(C.byref(self.h), p, len(a)))
+
+    def front_features(self, method=UHM_CHOL):
+        """Selector features per front, in the order of fronts()."""
+        n = len(self.fronts()[0])
+        out = np.zeros((n, mlp_n_features()), np.float32)
+        self._check(self.L.uhm_gpu_get_front_features(C.byref(self.h), method, n,
+                                                      out.ctypes.data_as(_P(C.c_float))))
+        return out
+
+    def front_precision(self):
+        """(precision of each front in the last plan, selector class or -1)."""
+        n = len(self.fronts()[0])
+        prec, cls = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        self._check(self.L.uhm_gpu_get_front_precision(C.byref(self.h), n, prec.ctypes.data_as(_P(_i)),
+                                                       cls.ctypes.data_as(_P(_i))))
+        return prec, cls
+
     def node_solution(self, node_ids, ndof, n_rhs=1):
         ids, p = _arr(node_ids, np.int32, _i)
         rows = int(np.asarray(ndof)[ids].sum())
@@ -359,6 +400,57 @@ def pinned_empty(n: int, dtype=np.float64):
 
 
 _keep = {}
+
+
+def mlp_n_params() -> int:
+    return int(lib().uhm_gpu_mlp_n_params())
+
+
+def mlp_n_features() -> int:
+    return int(lib().uhm_gpu_mlp_n_features())
+
+
+def _mlp_check(code):
+    if code:
+        raise UHMError(code, "selector network call failed")
+
+
+def mlp_predict(X, params):
+    """Selector classes and probabilities for samples X (N x 12), on the device."""
+    X, px = _arr(X, np.float32, C.c_float)
+    P, pp = _arr(params, np.float32, C.c_float)
+    n = X.shape[0]
+    cls = np.zeros(n, np.int32)
+    prob = np.zeros((n, 3), np.float32)
+    _mlp_check(lib().uhm_gpu_mlp_predict(px, n, pp, cls.ctypes.data_as(_P(_i)), prob.ctypes.data_as(_P(C.c_float))))
+    return cls, prob
+
+
+def mlp_gradient(X, y, params, class_weight=None):
+    """(loss, gradient) of the class-weighted mean cross-entropy over all samples."""
+    X, px = _arr(X, np.float32, C.c_float)
+    y, py = _arr(y, np.int32, _i)
+    P, pp = _arr(params, np.float32, C.c_float)
+    w = None if class_weight is None else np.ascontiguousarray(class_weight, np.float32)
+    pw = None if w is None else w.ctypes.data_as(_P(C.c_float))
+    g = np.zeros(mlp_n_params(), np.float32)
+    loss = np.zeros(1, np.float32)
+    _mlp_check(lib().uhm_gpu_mlp_gradient(px, py, pw, X.shape[0], pp, g.ctypes.data_as(_P(C.c_float)),
+                                          loss.ctypes.data_as(_P(C.c_float))))
+    return float(loss[0]), g
+
+
+def mlp_train(X, y, params, epochs=20, batch=512, lr=1e-3, seed=0, class_weight=None):
+    """Adam on the device; returns (trained parameters, mean loss per epoch)."""
+    X, px = _arr(X, np.float32, C.c_float)
+    y, py = _arr(y, np.int32, _i)
+    P = np.array(params, dtype=np.float32, copy=True)
+    w = None if class_weight is None else np.ascontiguousarray(class_weight, np.float32)
+    pw = None if w is None else w.ctypes.data_as(_P(C.c_float))
+    hist = np.zeros(max(1, epochs), np.float32)
+    _mlp_check(lib().uhm_gpu_mlp_train(px, py, pw, X.shape[0], P.ctypes.data_as(_P(C.c_float)), epochs, batch,
+                                       float(lr), int(seed), hist.ctypes.data_as(_P(C.c_float))))
+    return P, hist[:epochs]
 
 
 def load_spec(spec, n_rhs=None, bulk=True, pinned=False):

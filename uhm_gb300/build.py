@@ -26,6 +26,7 @@ SOURCES = [
     "k_solve.cu",
     "k_tc_gemm.cu",
     "k_noalloc.cu",
+    "k_selector.cu",
 ]
 
 

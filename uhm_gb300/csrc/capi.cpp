@@ -215,6 +215,49 @@ int uhm_gpu_set_front_precision(long* mesh, int n, const int* prec) {
     e.invalidate_precision();
   });
 }
+int uhm_gpu_get_op_log(long* mesh, int cap, int* kind, int* n_items, double* ms, int* n_out) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    const int n = (int)e.op_log.size();
+    *n_out = n;
+    for (int i = 0; i < n && i < cap; ++i) {
+      kind[i] = e.op_log[i].kind;
+      n_items[i] = e.op_log[i].n_items;
+      ms[i] = e.op_log[i].ms;
+    }
+  });
+}
+int uhm_gpu_set_selector(long* mesh, const float* params, int n) {
+  return guard(M(mesh), [&] { M(mesh)->eng().set_selector(params, n); });
+}
+int uhm_gpu_get_front_features(long* mesh, int method, int n_fronts, float* out) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    e.prepare_device(method);
+    std::vector<float> f;
+    e.front_features(f);
+    if (n_fronts != (int)e.fronts.size()) {
+      e.status = 7;
+      throw std::invalid_argument("get_front_features: front count mismatch");
+    }
+    std::copy(f.begin(), f.end(), out);
+  });
+}
+int uhm_gpu_get_front_precision(long* mesh, int n_fronts, int* prec, int* learned_class) {
+  return guard(M(mesh), [&] {
+    uhm::Engine& e = M(mesh)->eng();
+    e.ensure_plan();
+    if (n_fronts != (int)e.fronts.size()) {
+      e.status = 7;
+      throw std::invalid_argument("get_front_precision: front count mismatch");
+    }
+    for (auto& f : e.fronts) {
+      if (prec) prec[f.slot] = f.prec;
+      if (learned_class)
+        learned_class[f.slot] = (int)e.learned_class.size() > f.slot ? e.learned_class[f.slot] : -1;
+    }
+  });
+}
 int uhm_gpu_copy_in_leaves(long* mesh, int side, const int* nods_all, const double* buffer,
                            long n_values) {
   return guard(M(mesh), [&] {
@@ -253,6 +296,7 @@ int uhm_gpu_set_profiling(long* mesh, int on) {
     uhm::Engine& e = M(mesh)->eng();
     e.profiling = on != 0;
     e.profile = uhm::OpProfile{};
+    e.op_log.clear();
   });
 }
 int uhm_gpu_get_profile(long* mesh, int n_kinds, double* ms, double* flops, double* bytes,

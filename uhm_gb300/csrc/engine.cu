@@ -1,6 +1,7 @@
 // Host side of the device engine: plan (front table, extend-add maps, launch
 // program), HBM arenas, element staging, factor / solve / residual drivers.
 #include "engine.hpp"
+#include "selector.hpp"
 
 #include <omp.h>
 
@@ -149,6 +150,7 @@ void Engine::ensure_plan() {
     h_pinned_bytes = need;
   }
   emat_dirty = erhs_dirty = true;
+  learned_valid = false;
   anorm_inf = -1.0;
   plan_ok = true;
   dev_ok = false;
@@ -279,6 +281,7 @@ void Engine::copy_in(Element e, int m, int n, int nod_disp, const int* nods, int
       for (int i = 0; i < m; ++i) dst[rowmap(i) + (int64_t)rowmap(j) * m] += buf[i + (int64_t)j * m];
     es.has_lhs = true;
     emat_dirty = true;
+    learned_valid = false;
     anorm_inf = -1.0;
     dev_ok = dev_ok && !first;   // maps change when an element appears
     factored = false;
@@ -311,6 +314,7 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
       emat_device_only = true;
       anorm_valid = false;
     }
+    learned_valid = false;
     factored = false;
     anorm_inf = -1.0;
   } else {
@@ -377,6 +381,11 @@ void Engine::build_plan(int method) {
     int p = PREC_FP64;
     if (mode == 1) {
       p = default_prec;
+      if (p == PREC_LEARNED) {
+        static const int cls2prec[3] = {PREC_FP64, PREC_FP32, PREC_BF16X3};
+        const int c = (int)learned_class.size() > f.slot ? learned_class[f.slot] : 1;
+        p = cls2prec[c >= 0 && c < 3 ? c : 1];
+      }
       if ((int)front_prec_override.size() > f.slot && front_prec_override[f.slot] >= 0)
         p = front_prec_override[f.slot];
     }
@@ -1030,6 +1039,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, evs[2 * i], evs[2 * i + 1]));
       if (ops[i].kind < 0 || ops[i].kind >= N_OP_KINDS) continue;
+      op_log.push_back(OpRecord{ops[i].kind, ops[i].n_items, ms});
       profile.ms[ops[i].kind] += ms;
       profile.flops[ops[i].kind] += ops[i].flops;
       profile.bytes[ops[i].kind] += ops[i].bytes;
@@ -1056,6 +1066,7 @@ void Engine::factor(int method) {
   ensure_plan();
   for (auto& es : esrc)
     if (!es.has_lhs) fail("factor: an element matrix has not been copied in", 7);
+  if (mode == 1 && default_prec == PREC_LEARNED && !learned_valid) apply_selector(method);
   if (!dev_ok || method_built != method || prec_dirty) {
     build_plan(method);
     build_programs(method);
@@ -1231,6 +1242,174 @@ double Engine::operator_norm_inf() {
   if (!anorm_valid) enqueue_anorm();
   if (anorm_inf < 0) anorm_inf = read_scalar(d_red + 1536);
   return anorm_inf;
+}
+
+// ---------------------------------------------------------------------------
+// learned precision selection
+// ---------------------------------------------------------------------------
+constexpr double SELECTOR_FP64_CONFIDENCE = 0.9;
+
+void Engine::prepare_device(int method) {
+  ensure_plan();
+  if (!dev_ok || method_built != method || prec_dirty) {
+    build_plan(method);
+    build_programs(method);
+    alloc_device(method);
+  }
+}
+
+void Engine::set_selector(const float* params, int n) {
+  if (n != uhm_gpu::SEL_NPARAMS) fail("set_selector: wrong parameter count", 7);
+  selector_params.assign(params, params + n);
+  learned_valid = false;
+  prec_dirty = true;
+}
+
+// Per front (slot order), SEL_F features from its sizes, its place in the tree
+// and statistics of the element matrices of its subtree and of the whole mesh:
+//   0 log2(n+1)/14   1 log2(fs+1)/14   2 log2(ss+1)/14   3 depth below the root / 8
+//   4 n >= 512 (tensor-core eligible)   5 log10(max/min mean |diagonal|) over the subtree / 6
+//   6 mean and 7 min over the subtree of sum(a)/sum|a|
+//   8 min column dominance over the subtree (clamped to [-4, 1]) / 4
+//   9 min of sum(a)/sum|a| over the mesh   10 log10(max/min mean |diagonal|) over the mesh / 6
+//   11 log10(LAWN-41 flops of the front + 1) / 13
+void Engine::front_features(std::vector<float>& feat) {
+  if (!dev_ok) fail("front features: no device data yet", 7);
+  upload_elements();
+  const int ne = (int)esrc.size();
+  std::vector<float> st((size_t)ne * 4, 0.f);
+  if (ne) {
+    float* d_st = nullptr;
+    CK(cudaMalloc(&d_st, sizeof(float) * 4 * (size_t)ne));
+    uhm_gpu::launch_elem_stats(ctx.emat, d_emat_off, d_elem_m, ne, d_st, stream);
+    CK(cudaMemcpyAsync(st.data(), d_st, sizeof(float) * st.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaFree(d_st));
+  }
+  struct Agg {
+    double cnt = 0, dmax = 0, dmin = 1e300, rsum = 0, rmin = 1e300, osum = 0, omin = 1e300;
+  };
+  const int nf = (int)fronts.size();
+  std::vector<Agg> agg(nf);
+  for (int s = 0; s < nf; ++s) {          // leaf -> root: children come first
+    Agg a;
+    const int ei = esrc_of_slot[s];
+    if (ei >= 0 && esrc[ei].has_lhs) {
+      const double dm = st[4 * ei + 0], r = st[4 * ei + 1];
+      const double o = std::max(-4.0, std::min(1.0, (double)st[4 * ei + 2]));
+      const double om = std::max(-4.0, std::min(1.0, (double)st[4 * ei + 3]));
+      a.cnt = 1;
+      a.dmax = dm;
+      a.dmin = dm;
+      a.rsum = r;
+      a.rmin = r;
+      a.osum = om;
+      a.omin = o;
+    }
+    for (int c : fronts[s].children) {
+      const Agg& b = agg[c];
+      a.cnt += b.cnt;
+      a.dmax = std::max(a.dmax, b.dmax);
+      a.dmin = std::min(a.dmin, b.dmin);
+      a.rsum += b.rsum;
+      a.rmin = std::min(a.rmin, b.rmin);
+      a.osum += b.osum;
+      a.omin = std::min(a.omin, b.omin);
+    }
+    agg[s] = a;
+  }
+  std::vector<int> depth(nf, 0);
+  for (int s = nf - 1; s >= 0; --s)
+    if (fronts[s].parent >= 0) depth[s] = depth[fronts[s].parent] + 1;
+  Agg all;
+  for (int s = 0; s < nf; ++s)
+    if (fronts[s].parent < 0) {
+      const Agg& b = agg[s];
+      all.cnt += b.cnt;
+      all.dmax = std::max(all.dmax, b.dmax);
+      all.dmin = std::min(all.dmin, b.dmin);
+      all.rmin = std::min(all.rmin, b.rmin);
+    }
+  feat.assign((size_t)nf * uhm_gpu::SEL_F, 0.f);
+  for (int s = 0; s < nf; ++s) {
+    const HostFront& f = fronts[s];
+    const Agg& a = agg[s];
+    float* x = &feat[(size_t)s * uhm_gpu::SEL_F];
+    const double cnt = std::max(1.0, a.cnt);
+    const double flops = get_flop_chol(0, f.fs) + get_flop_trsm_lower(0, f.fs, f.ss) + get_flop_syrk(0, f.fs, f.ss);
+    x[0] = (float)(std::log2(f.n + 1.0) / 14);
+    x[1] = (float)(std::log2(f.fs + 1.0) / 14);
+    x[2] = (float)(std::log2(f.ss + 1.0) / 14);
+    x[3] = (float)(depth[s] / 8.0);
+    x[4] = f.n >= 512 ? 1.f : 0.f;
+    x[5] = (float)(a.cnt > 0 && a.dmin > 0 ? std::log10(a.dmax / a.dmin) / 6 : 0.0);
+    x[6] = (float)(a.cnt > 0 ? a.rsum / cnt : 0.0);
+    x[7] = (float)(a.cnt > 0 ? a.rmin : 0.0);
+    x[8] = (float)(a.cnt > 0 ? a.omin / 4 : 0.0);
+    x[9] = (float)(all.cnt > 0 ? all.rmin : 0.0);
+    x[10] = (float)(all.cnt > 0 && all.dmin > 0 ? std::log10(all.dmax / all.dmin) / 6 : 0.0);
+    x[11] = (float)(std::log10(flops + 1.0) / 13);
+  }
+}
+
+// Runs the selector on the device and records one class per front; the
+// device buffers must exist (a provisional plan is built for that on the
+// first call), and the plan is rebuilt afterwards with the chosen precisions.
+// The per-front class probabilities are decoded per tree level from the mean
+// probabilities of its fronts (FP64 only above SELECTOR_FP64_CONFIDENCE), and
+// precision may only decrease with depth (class index non-decreasing from the
+// root down), which is the shape of the assignments the labels come from.
+void Engine::apply_selector(int method) {
+  if ((int)selector_params.size() != uhm_gpu::SEL_NPARAMS)
+    fail("learned precision requested but no selector parameters were set", 7);
+  if (!dev_ok || method_built != method) {
+    build_plan(method);
+    build_programs(method);
+    alloc_device(method);
+  }
+  std::vector<float> feat;
+  front_features(feat);
+  const int nf = (int)fronts.size();
+  float *d_feat = nullptr, *d_par = nullptr;
+  float* d_prob = nullptr;
+  CK(cudaMalloc(&d_feat, sizeof(float) * std::max<size_t>(1, feat.size())));
+  CK(cudaMalloc(&d_par, sizeof(float) * selector_params.size()));
+  CK(cudaMalloc(&d_prob, sizeof(float) * uhm_gpu::SEL_C * (size_t)std::max(1, nf)));
+  CK(cudaMemcpyAsync(d_feat, feat.data(), sizeof(float) * feat.size(), cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_par, selector_params.data(), sizeof(float) * selector_params.size(),
+                     cudaMemcpyHostToDevice, stream));
+  uhm_gpu::launch_mlp_infer(d_feat, nf, d_par, nullptr, d_prob, stream);
+  std::vector<float> prob((size_t)uhm_gpu::SEL_C * nf);
+  CK(cudaMemcpyAsync(prob.data(), d_prob, sizeof(float) * prob.size(), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  CK(cudaFree(d_feat));
+  CK(cudaFree(d_par));
+  CK(cudaFree(d_prob));
+  std::vector<int> depth(nf, 0);
+  int max_depth = 0;
+  for (int s = nf - 1; s >= 0; --s) {
+    if (fronts[s].parent >= 0) depth[s] = depth[fronts[s].parent] + 1;
+    max_depth = std::max(max_depth, depth[s]);
+  }
+  std::vector<double> lp((size_t)(max_depth + 1) * uhm_gpu::SEL_C, 0.0);
+  for (int s = 0; s < nf; ++s)
+    for (int c = 0; c < uhm_gpu::SEL_C; ++c) lp[(size_t)depth[s] * uhm_gpu::SEL_C + c] += prob[(size_t)s * uhm_gpu::SEL_C + c];
+  std::vector<int> lcls(max_depth + 1, 1);
+  for (int d = 0; d <= max_depth; ++d) {
+    const double* q = &lp[(size_t)d * uhm_gpu::SEL_C];
+    const double tot = q[0] + q[1] + q[2];
+    // FP64 costs a large multiple of FP32 on this GPU and a missed target is
+    // caught by the FP64 redo anyway: a level goes to FP64 only when the
+    // network is confident, otherwise the likelier of FP32 and BF16
+    const int best = (tot > 0 && q[0] > SELECTOR_FP64_CONFIDENCE * tot) ? 0 : (q[1] > q[2] ? 1 : 2);
+    lcls[d] = d > 0 ? std::max(best, lcls[d - 1]) : best;
+  }
+  std::vector<int> cls(nf, 1);
+  for (int s = 0; s < nf; ++s) cls[s] = lcls[depth[s]];
+  // new element matrices often leave the choice unchanged: re-plan only when it moved
+  if (cls != learned_class || !dev_ok) prec_dirty = true;
+  learned_class.swap(cls);
+  learned_valid = true;
 }
 
 double Engine::backward_error() {

@@ -18,8 +18,9 @@
 
 namespace uhm {
 
-// precision of a front's factorisation
-enum FrontPrec : int { PREC_FP64 = 0, PREC_FP32 = 1, PREC_BF16X3 = 2, PREC_BF16X6 = 3 };
+// precision of a front's factorisation; PREC_LEARNED (a default policy only)
+// lets the learned selector pick FP64 / FP32 / BF16X3 per front
+enum FrontPrec : int { PREC_FP64 = 0, PREC_FP32 = 1, PREC_BF16X3 = 2, PREC_BF16X6 = 3, PREC_LEARNED = 4 };
 
 struct HostFront {
   Element e = nullptr;
@@ -111,10 +112,23 @@ class Engine {
   double ir_tol = 1e-12;
   int ir_max = 10;
   std::vector<int> front_prec_override;       // by slot, -1 = default
+  std::vector<float> selector_params;         // MLP parameters for PREC_LEARNED
+  std::vector<int> learned_class;             // by slot: 0 FP64, 1 FP32, 2 BF16-split
+  void set_selector(const float* params, int n);
+  // device buffers for the current plan and precisions (no factorisation)
+  void prepare_device(int method);
+  // per-front selector features (slot order, SEL_F floats each); element
+  // matrices must have been copied in
+  void front_features(std::vector<float>& feat);
   int status = 0;
   std::string last_error;
   Timing timing;
   bool profiling = false;       // per-op CUDA events (outside timed regions)
+  struct OpRecord {
+    int kind, n_items;
+    float ms;
+  };
+  std::vector<OpRecord> op_log;  // every profiled launch, in launch order
   bool use_graphs = true;       // replay factor / solve programs as CUDA graphs
   OpProfile profile;
 
@@ -129,6 +143,8 @@ class Engine {
   Mesh_* mesh;
   bool plan_ok = false;
   bool prec_dirty = false;
+  bool learned_valid = false;
+  void apply_selector(int method);
   bool emat_device_only = false, erhs_device_only = false;
   bool anorm_valid = false;
   bool dev_ok = false;

@@ -194,13 +194,15 @@ def _merge_plan(n: int, merges):
     return plan
 
 
-def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, seed: int = 0,
+def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, react=None, seed: int = 0,
                n_rhs: int = 1, merges=None, h: float | None = None) -> MeshSpec:
     """Build a uniform quad (dim=2) or hex (dim=3) mesh of n^dim elements.
 
     p      : int, or an integer array of per-element orders (minimum rule)
     kappa  : None (1.0) or per-element diffusion coefficients
     beta   : None or a length-dim convection velocity (nonsymmetric matrices)
+    react  : None or per-element reaction coefficients c (adds c * mass; a
+             negative c shifts the operator towards its first eigenvalue)
     merges : per-level merge factors of the nested-dissection tree (product n);
              default: factors of 2 first, then odd primes.
     """
@@ -213,6 +215,7 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, seed: int = 0,
     p_el = np.broadcast_to(np.asarray(p, dtype=np.int64), (n_el,)).copy()
     assert p_el.min() >= 1
     kap = np.ones(n_el) if kappa is None else np.asarray(kappa, dtype=np.float64)
+    rea = None if react is None else np.broadcast_to(np.asarray(react, dtype=np.float64), (n_el,))
     symmetric = beta is None
 
     base, n_nodes = _entities(dim, nn)
@@ -286,18 +289,20 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, seed: int = 0,
             M, K, C = lobatto_1d(pe, pe + 1)
             if dim == 2:
                 diff = np.kron(M, K) + np.kron(K, M)
+                mass = (h / 2) ** 2 * np.kron(M, M)
                 conv = []
                 if beta is not None:
                     conv = [(h / 2) * np.kron(M, C), (h / 2) * np.kron(C, M)]
             else:
                 diff = (h / 2) * (np.kron(M, np.kron(M, K)) + np.kron(M, np.kron(K, M))
                                   + np.kron(K, np.kron(M, M)))
+                mass = (h / 2) ** 3 * np.kron(M, np.kron(M, M))
                 conv = []
                 if beta is not None:
                     s = (h / 2) ** 2
                     conv = [s * np.kron(M, np.kron(M, C)), s * np.kron(M, np.kron(C, M)),
                             s * np.kron(C, np.kron(M, M))]
-            cache[key] = (diff, conv)
+            cache[key] = (diff, conv, mass)
         return cache[key]
 
     mat_off = np.zeros(n_el, dtype=np.int64)
@@ -307,9 +312,11 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, seed: int = 0,
         off += int(elem_m[e]) ** 2
     mats = np.empty(off, dtype=np.float64)
     for e in range(n_el):
-        diff, conv = ref_mats(int(p_el[e]))
+        diff, conv, mass = ref_mats(int(p_el[e]))
         sel = sel_list[e]
         A = kap[e] * diff[np.ix_(sel, sel)]
+        if rea is not None and rea[e] != 0.0:
+            A = A + rea[e] * mass[np.ix_(sel, sel)]
         if beta is not None:
             for a in range(dim):
                 A = A + beta[a] * conv[a][np.ix_(sel, sel)]
