@@ -682,30 +682,56 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   const int i = threadIdx.x % FB, g = threadIdx.x / FB;
   const int row = r0 + i;
   const bool rv = row < r1;
-  CT acc[SF_NR];
+  CT acc[SF_NR], zr[SF_NR];
 #pragma unroll
-  for (int q = 0; q < SF_NR; ++q) acc[q] = CT(0);
+  for (int q = 0; q < SF_NR; ++q) {
+    acc[q] = CT(0);
+    zr[q] = (rv && q < nr && g == 0) ? (CT)z[row + (int64_t)q * n] : CT(0);   // before any wait
+  }
   const int jend = factor_block ? b : nfb;
   __shared__ int s_ready;
+  // The factor tile of block column j does not depend on any flag: it is
+  // loaded one block ahead, so that only the loads of y_j follow the wait.
+  CT tile[16];
+  auto load_tile = [&](int j) {
+    const int kbj = min(FB, fs - j * FB);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int cc = g * 16 + u;
+      tile[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
+    }
+  };
+  if (jend > 0) load_tile(0);
+  // y_j is read by every later block of the front at once: one warp per CTA
+  // stages it in shared memory (hundreds of CTAs hitting the same few lines
+  // with per-thread loads serialise in L2)
+  __shared__ CT ysh[SF_NR][FB];
   int done = 0;
   while (done < jend) {
     ready_range(flg, done, jend, 1, &s_ready, err);
     const int upto = s_ready;
     for (int j = done; j < upto; ++j) {
       const int kbj = min(FB, fs - j * FB);
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int cc = g * 16 + u;
-        if (rv && cc < kbj) {
-          const CT l = (CT)G[row + (int64_t)(j * FB + cc) * n];
-#pragma unroll
-          for (int q = 0; q < SF_NR; ++q)
-            if (q < nr) acc[q] += l * (CT)__ldcg(y + (j * FB + cc) + (int64_t)q * n);
+      if (threadIdx.x < 32) {
+        for (int q = 0; q < nr && q < SF_NR; ++q) {
+          const double* yj = y + j * FB + (int64_t)q * n;
+          for (int cc = threadIdx.x; cc < FB; cc += 32) ysh[q][cc] = cc < kbj ? (CT)__ldcg(yj + cc) : CT(0);
         }
       }
+      CT cur[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+      if (j + 1 < jend) load_tile(j + 1);
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q)
+          if (q < nr) acc[q] += cur[u] * ysh[q][g * 16 + u];
+      }
+      __syncthreads();
     }
     done = upto;
-    __syncthreads();
   }
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
@@ -713,8 +739,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   if (threadIdx.x < FB) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      v[i][q] = (rv && q < nr) ? (CT)z[row + (int64_t)q * n] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q])
-                               : CT(0);
+      v[i][q] = (rv && q < nr) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
   }
   __syncthreads();
   if (factor_block) {
@@ -772,31 +797,54 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     CT acc[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) acc[u] = CT(0);
-    // rows below block b: the ABL part (known) first, then factor blocks
+    // rows below block b: the ABL part (known) first, two row blocks per
+    // round with all loads issued before the arithmetic, then factor blocks
     // from the last one down (they complete in that order)
-    for (int rs = fs; rs < n; rs += FB) {
-      const int r = rs + rl;
-      const CT xr = r < n ? (CT)y[r + (int64_t)q * n] : CT(0);
+    for (int rs = fs; rs < n; rs += 2 * FB) {
+      CT xr[2], gv[2][16];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = rs + h * FB + rl;
+        xr[h] = r < n ? (CT)y[r + (int64_t)q * n] : CT(0);
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int cc = g * 16 + u;
+          gv[h][u] = (r < n && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int u = 0; u < 16; ++u) acc[u] += gv[h][u] * xr[h];
+    }
+    // the factor tile of row block j does not depend on any flag: loaded one
+    // block ahead, so that only the load of x_j follows the wait
+    CT tile[16];
+    auto load_tile = [&](int j) {
+      const int r = j * FB + rl;
+      const bool in = r < min(j * FB + FB, fs);
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int cc = g * 16 + u;
-        if (r < n && cc < kb) acc[u] += (CT)G[r + (int64_t)(c0 + cc) * n] * xr;
+        tile[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
       }
-    }
+    };
     int next = nfb - 1;
+    if (next > b) load_tile(next);
     while (next > b) {
       ready_range(flg, next, b, -1, &s_ready, err);
       const int stop = s_ready;
       for (int j = next; j > stop; --j) {
+        CT cur[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+        if (j - 1 > b) load_tile(j - 1);
         const int r = j * FB + rl;
         const bool in = r < min(j * FB + FB, fs);
         if (in) {
-          const CT xr = (CT)__ldcg(y + r + (int64_t)q * n);
+          const CT xr = (CT)__ldcg(y + r + (int64_t)q * n);   // one distinct value per lane
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const int cc = g * 16 + u;
-            if (cc < kb) acc[u] += (CT)G[r + (int64_t)(c0 + cc) * n] * xr;
-          }
+          for (int u = 0; u < 16; ++u) acc[u] += cur[u] * xr;
         }
       }
       next = stop;
