@@ -16,6 +16,7 @@
 // contributions, then children in child order), which is the reference's
 // summation order onto a zeroed parent; no atomics, bitwise reproducible.
 #include <cstdio>
+#include <stdexcept>
 #include "k_common.cuh"
 
 namespace uhm_gpu {
@@ -365,6 +366,46 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
   T* L = reinterpret_cast<T*>(smem_raw);        // kb x kb (or 64 x 65 padded inverse)
   T* X = L + 64 * 65;                           // TRSM_RB x kb, ld TRSM_RB
   T* __restrict__ G = arena<T>(c) + f.off;
+  const T* Dinv = (sizeof(T) == 8 ? (const T*)c.dinv64 : (const T*)c.dinv32);
+  if (nb == 64 && Dinv) {
+    // X <- X * L11^{-T} as a product with the inverse computed by the
+    // diagonal-block kernel (stored column-major 64 x 64): no sequential
+    // sweep.  Both tiles are loaded in one batch of registers.
+    static_assert(NT == 256 && TRSM_RB == 64, "64 x 64 tiles over 256 threads");
+    Dinv += f.dinv_off + (int64_t)(k0 / 64) * 4096;
+    T xv[16], dv[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = threadIdx.x + NT * u, i = idx % TRSM_RB, j = idx / TRSM_RB;
+      xv[u] = (i < rb && j < kb) ? G[(r0 + i) + (int64_t)(k0 + j) * n] : (T)0;
+      dv[u] = Dinv[idx];
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = threadIdx.x + NT * u;
+      // Dinv is column-major: Dinv[t * 64 + j] = Linv[j][t]; keep it as
+      // rows t of length 64 padded to 65, so that L[t * 65 + j] = Linv[j][t]
+      const int t = idx / 64, j = idx % 64;
+      X[idx] = xv[u];
+      L[t * 65 + j] = (t < kb && j < kb) ? dv[u] : T(0);
+    }
+    __syncthreads();
+    const int i = threadIdx.x % TRSM_RB, jg = threadIdx.x / TRSM_RB;   // 4 column groups of 16
+    T acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = T(0);
+    for (int t = 0; t < kb; ++t) {
+      const T x = X[i + t * TRSM_RB];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc[u] += x * L[t * 65 + jg * 16 + u];
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int j = jg * 16 + u;
+      if (i < rb && j < kb) G[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < kb * kb; idx += NT) {
     const int i = idx % kb, j = idx / kb;
     L[idx] = i >= j ? G[(k0 + i) + (int64_t)(k0 + j) * n] : (T)0;
@@ -374,34 +415,6 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
     X[idx] = i < rb ? G[(r0 + i) + (int64_t)(k0 + j) * n] : (T)0;
   }
   __syncthreads();
-  const T* Dinv = (sizeof(T) == 8 ? (const T*)c.dinv64 : (const T*)c.dinv32);
-  if (nb == 64 && Dinv) {
-    // X <- X * L11^{-T} as a product with the inverse computed by the
-    // diagonal-block kernel (stored column-major 64 x 64): no sequential sweep
-    Dinv += f.dinv_off + (int64_t)(k0 / 64) * 4096;
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) {
-      // Dinv is column-major: Dinv[t * 64 + j] = Linv[j][t]; keep it as
-      // rows t of length 64 padded to 65, so that L[t * 65 + j] = Linv[j][t]
-      const int t = idx / 64, j = idx % 64;
-      L[t * 65 + j] = (t < kb && j < kb) ? Dinv[idx] : T(0);
-    }
-    __syncthreads();
-    const int i = threadIdx.x % TRSM_RB, jg = threadIdx.x / TRSM_RB;   // 4 column groups of 16
-    T acc[16];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) acc[u] = T(0);
-    for (int t = 0; t < kb; ++t) {
-      const T xv = X[i + t * TRSM_RB];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) acc[u] += xv * L[t * 65 + jg * 16 + u];
-    }
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int j = jg * 16 + u;
-      if (i < rb && j < kb) G[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
-    }
-    return;
-  }
   for (int j = 0; j < kb; ++j) {
     const T ljj = L[j + j * kb];
     for (int i = threadIdx.x; i < TRSM_RB; i += NT) X[i + j * TRSM_RB] /= ljj;
@@ -458,23 +471,51 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = (T)0;
-  for (int kk = 0; kk < kb; kk += BK) {
-    for (int idx = threadIdx.x; idx < BK * BM; idx += NT) {
-      const int r = idx % BM, t = idx / BM;
+  // All K-chunks of both operands are loaded into registers in one batch
+  // (stores to shared memory between global loads would serialise them),
+  // then staged chunk by chunk.
+  constexpr int KCH = 4;                                  // chunks of BK (kb <= KCH * BK)
+  constexpr int PA = BK * BM / NT, PB = BK * BN / NT;    // elements per thread and chunk
+  static_assert(BK * BM % NT == 0 && BK * BN % NT == 0, "whole chunks per thread");
+  T ra[KCH][PA], rb[KCH][PB];
+#pragma unroll
+  for (int ch = 0; ch < KCH; ++ch) {
+    const int kk = ch * BK;
+#pragma unroll
+    for (int e = 0; e < PA; ++e) {
+      const int idx = threadIdx.x + NT * e, r = idx % BM, t = idx / BM;
       const int gr = R0 + r, gt = kk + t;
-      As[t][r] = (gr < n && gt < kb) ? G[gr + (int64_t)(k0 + gt) * n] : (T)0;
+      ra[ch][e] = (gr < n && gt < kb) ? G[gr + (int64_t)(k0 + gt) * n] : (T)0;
     }
-    if (!ROWPANEL) {
-      for (int idx = threadIdx.x; idx < BK * BN; idx += NT) {
+#pragma unroll
+    for (int e = 0; e < PB; ++e) {
+      const int idx = threadIdx.x + NT * e;
+      if (!ROWPANEL) {
         const int r = idx % BN, t = idx / BN;
         const int gr = C0 + r, gt = kk + t;
-        Bs[t][r] = (gr < n && gt < kb) ? G[gr + (int64_t)(k0 + gt) * n] : (T)0;
-      }
-    } else {
-      for (int idx = threadIdx.x; idx < BK * BN; idx += NT) {
+        rb[ch][e] = (gr < n && gt < kb) ? G[gr + (int64_t)(k0 + gt) * n] : (T)0;
+      } else {
         const int t = idx % BK, r = idx / BK;
         const int gr = C0 + r, gt = kk + t;
-        Bs[t][r] = (gr < n && gt < kb) ? G[(k0 + gt) + (int64_t)gr * n] : (T)0;
+        rb[ch][e] = (gr < n && gt < kb) ? G[(k0 + gt) + (int64_t)gr * n] : (T)0;
+      }
+    }
+  }
+  for (int kk = 0; kk < kb; kk += BK) {
+    const int ch = kk / BK;
+#pragma unroll
+    for (int cc = 0; cc < KCH; ++cc) {
+      if (cc != ch) continue;
+#pragma unroll
+      for (int e = 0; e < PA; ++e) {
+        const int idx = threadIdx.x + NT * e;
+        As[idx / BM][idx % BM] = ra[cc][e];
+      }
+#pragma unroll
+      for (int e = 0; e < PB; ++e) {
+        const int idx = threadIdx.x + NT * e;
+        if (!ROWPANEL) Bs[idx / BN][idx % BN] = rb[cc][e];
+        else Bs[idx % BK][idx / BK] = rb[cc][e];
       }
     }
     __syncthreads();
@@ -492,16 +533,26 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
     }
     __syncthreads();
   }
+  // C -= acc: every C value is read before any is written back
+  T cv[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     const int gr = R0 + ty + i * NTY;
-    if (gr >= n) continue;
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       const int gc = C0 + tx + j * NTX;
-      if (gc >= cmax) continue;
-      if (!ROWPANEL && gr < gc) continue;
-      G[gr + (int64_t)gc * n] -= acc[i][j];
+      const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
+      cv[i][j] = ok ? G[gr + (int64_t)gc * n] : (T)0;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int gr = R0 + ty + i * NTY;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int gc = C0 + tx + j * NTX;
+      const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
+      if (ok) G[gr + (int64_t)gc * n] = cv[i][j] - acc[i][j];
     }
   }
 }
@@ -509,12 +560,14 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
 void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         int nbo, cudaStream_t s) {
   if (!n_items) return;
+  if (nb > 64) throw std::invalid_argument("trailing update: panel width above 64");
   if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
   else k_tile_update<float, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
 }
 
 void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         cudaStream_t s) {
+  if (nb > 64) throw std::invalid_argument("trailing update: panel width above 64");
   if (!n_items) return;
   if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
   else k_tile_update<float, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
