@@ -109,6 +109,8 @@ def _barrier_max(x: float, ws: int):
 WORKLOADS = {
     "poisson3d_16_p4": (lambda seed: __import__("uhm_gb300.hpfem", fromlist=["x"]).poisson3d(16, 4, seed=seed),
                         WORKLOAD),
+    "poisson3d_12_p4": (lambda seed: __import__("uhm_gb300.hpfem", fromlist=["x"]).poisson3d(12, 4, seed=seed),
+                        "3D Poisson 12^3 hex p=4 (profiling case: root trailing block above L2 size)"),
     "poisson3d_8_p4": (lambda seed: __import__("uhm_gb300.hpfem", fromlist=["x"]).poisson3d(8, 4, seed=seed),
                        "3D Poisson 8^3 hex p=4 (small profiling case)"),
 }

@@ -12,11 +12,12 @@
 // laid end to end along K, so one GEMM with K' = terms * KB accumulates them
 // all in FP32 in tensor memory.
 //
-// Kernel: one CTA per 128 x 128 output tile; warp 4 issues TMA loads
-// (128-byte swizzle) into a 4-stage shared-memory ring guarded by mbarriers,
-// one thread of warp 5 issues tcgen05.mma (M=128, N=128, K=16) into a
-// 128-column TMEM accumulator, warps 0-3 read TMEM back (tcgen05.ld) and
-// apply C -= acc to the FP32 panel.  Every wait is bounded: a wait that
+// Kernel: one persistent CTA per SM walks the 128 x 128 output tiles; warp 4
+// issues TMA loads (128-byte swizzle) into a 4-stage shared-memory ring
+// guarded by mbarriers, one thread of warp 5 issues tcgen05.mma (M=128,
+// N=128, K=16) into one of two 128-column TMEM accumulators, warps 0-3 read
+// TMEM back (tcgen05.ld) and apply C -= acc to the FP32 panel while the next
+// tile accumulates in the other buffer.  Every wait is bounded: a wait that
 // gives up records an error flag and the CTA skips its stores.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -122,35 +123,35 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
         "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])             \
       : "r"(taddr))
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 // item: front, a = K0 (outer step start), b = tile row, c = tile col
 // (tiles counted from the trailing block's first row K0 + KB).
 // term_code: 2 bits per part index, 4 bits per term (A part, B part).
+//
+// Persistent: one CTA per SM walks the tile list with stride gridDim.x.  The
+// TMA ring (full / empty barriers) runs continuously across tiles; TMEM holds
+// two 128-column accumulators, so the epilogue of tile i (TMEM -> registers
+// -> C in global memory) overlaps the mainloop of tile i + 1.  acc_full[b]
+// is committed by the MMA thread when accumulator b holds a finished tile;
+// acc_empty[b] collects the 128 epilogue threads once they have read it.
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_off,
-          const int64_t* __restrict__ ws_stride, const Item* __restrict__ items, int nbo, int nterms,
-          uint32_t term_code, int lower_only, int* err) {
+          const int64_t* __restrict__ ws_stride, const Item* __restrict__ items, int n_items, int nbo,
+          int nterms, uint32_t term_code, int lower_only, int* err) {
   extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* tilesA = smem;
   uint8_t* tilesB = smem + TC_STAGES * TC_TILE_BYTES;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * TC_STAGES * TC_TILE_BYTES);
-  // bars[0..S) full, bars[S..2S) empty, bars[2S] accumulator ready
-  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * TC_STAGES + 1);
-  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 2);
+  // bars[0..S) full, bars[S..2S) empty, bars[2S..2S+2) acc_full, bars[2S+2..2S+4) acc_empty
+  uint64_t* acc_full = bars + 2 * TC_STAGES;
+  uint64_t* acc_empty = bars + 2 * TC_STAGES + 2;
+  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * TC_STAGES + 4);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
   float* s_c = reinterpret_cast<float*>(smem + 2 * TC_STAGES * TC_TILE_BYTES + 256);
-
-  const Item it = items[blockIdx.x];
-  const FrontDev f = c.fronts[it.front];
-  // the whole BF16 workspace is one 2D tensor of rows of nbo elements;
-  // part p of this front starts at row (ws_off + p * ws_stride) / nbo
-  const int row0 = (int)(ws_off[it.front] / nbo);
-  const int prow = (int)(ws_stride[it.front] / nbo);
-  const int n = f.n, K0 = it.a;
-  const int KB = min(nbo, f.fs - K0);
-  const int base = K0 + KB;
-  const int R0 = base + it.b * TC_BM, C0 = base + it.c * TC_BN;
-  const int kpt = (KB + TC_BK - 1) / TC_BK;       // K chunks per term
-  const int nk = kpt * nterms;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -158,96 +159,159 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       mbar_init(smem_u32(&bars[s]), 1);
       mbar_init(smem_u32(&bars[TC_STAGES + s]), 1);
     }
-    mbar_init(smem_u32(&bars[2 * TC_STAGES]), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), 128);
+    }
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
-                 "r"(TC_BN));
+                 "r"(2 * TC_BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *s_tmem;
 
+  // per-tile geometry, identical in every role
+  struct Tile {
+    int front, n, base, R0, C0, row0, prow, kpt, nk, off;
+  };
+  auto tile_of = [&](int t) {
+    const Item it = items[t];
+    const FrontDev f = c.fronts[it.front];
+    Tile T;
+    T.front = it.front;
+    T.n = f.n;
+    const int KB = min(nbo, f.fs - it.a);
+    T.base = it.a + KB;
+    T.R0 = T.base + it.b * TC_BM;
+    T.C0 = T.base + it.c * TC_BN;
+    // the whole BF16 workspace is one 2D tensor of rows of nbo elements;
+    // part p of this front starts at row (ws_off + p * ws_stride) / nbo
+    T.row0 = (int)(ws_off[it.front] / nbo);
+    T.prow = (int)(ws_stride[it.front] / nbo);
+    T.kpt = (KB + TC_BK - 1) / TC_BK;
+    T.nk = T.kpt * nterms;
+    T.off = (int)0;
+    (void)f;
+    return T;
+  };
+
   if (warp == 4) {
     if (lane == 0) {
       // TMA producer
-      for (int kc = 0; kc < nk; ++kc) {
-        const int s = kc % TC_STAGES;
-        if (kc >= TC_STAGES &&
-            !mbar_wait(smem_u32(&bars[TC_STAGES + s]), ((kc / TC_STAGES) + 1) & 1, s_abort, err))
-          break;
-        const int term = kc / kpt, kk = kc % kpt;
-        const int pa = (term_code >> (4 * term)) & 3, pb = (term_code >> (4 * term + 2)) & 3;
-        const uint32_t fb = smem_u32(&bars[s]);
-        mbar_expect_tx(fb, 2 * TC_TILE_BYTES);
-        tma_load_2d(smem_u32(tilesA + s * TC_TILE_BYTES), &wsmap, kk * TC_BK, row0 + pa * prow + (R0 - base), fb);
-        tma_load_2d(smem_u32(tilesB + s * TC_TILE_BYTES), &wsmap, kk * TC_BK, row0 + pb * prow + (C0 - base), fb);
+      uint32_t g = 0;       // chunks issued by this CTA so far
+      bool live = true;
+      for (int t = blockIdx.x; t < n_items && live; t += gridDim.x) {
+        const Tile T = tile_of(t);
+        for (int kc = 0; kc < T.nk; ++kc, ++g) {
+          const uint32_t s = g % TC_STAGES;
+          if (g >= TC_STAGES &&
+              !mbar_wait(smem_u32(&bars[TC_STAGES + s]), ((g / TC_STAGES) + 1) & 1, s_abort, err)) {
+            live = false;
+            break;
+          }
+          const int term = kc / T.kpt, kk = kc % T.kpt;
+          const int pa = (term_code >> (4 * term)) & 3, pb = (term_code >> (4 * term + 2)) & 3;
+          const uint32_t fb = smem_u32(&bars[s]);
+          mbar_expect_tx(fb, 2 * TC_TILE_BYTES);
+          tma_load_2d(smem_u32(tilesA + s * TC_TILE_BYTES), &wsmap, kk * TC_BK,
+                      T.row0 + pa * T.prow + (T.R0 - T.base), fb);
+          tma_load_2d(smem_u32(tilesB + s * TC_TILE_BYTES), &wsmap, kk * TC_BK,
+                      T.row0 + pb * T.prow + (T.C0 - T.base), fb);
+        }
       }
     }
   } else if (warp == 5) {
     if (lane == 0) {
       // MMA issuer
       const uint32_t idesc = idesc_bf16_f32(TC_BM, TC_BN);
-      for (int kc = 0; kc < nk; ++kc) {
-        const int s = kc % TC_STAGES;
-        if (!mbar_wait(smem_u32(&bars[s]), (kc / TC_STAGES) & 1, s_abort, err)) break;
+      uint32_t g = 0;
+      int i = 0;            // tiles processed by this CTA
+      bool live = true;
+      for (int t = blockIdx.x; t < n_items && live; t += gridDim.x, ++i) {
+        const Tile T = tile_of(t);
+        const int b = i & 1, u = i >> 1;
+        if (u >= 1 && !mbar_wait(smem_u32(&acc_empty[b]), (u - 1) & 1, s_abort, err)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a0 = smem_u32(tilesA + s * TC_TILE_BYTES);
-        const uint32_t b0 = smem_u32(tilesB + s * TC_TILE_BYTES);
+        const uint32_t acc = tmem + b * TC_BN;
+        for (int kc = 0; kc < T.nk; ++kc, ++g) {
+          const uint32_t s = g % TC_STAGES;
+          if (!mbar_wait(smem_u32(&bars[s]), (g / TC_STAGES) & 1, s_abort, err)) {
+            live = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a0 = smem_u32(tilesA + s * TC_TILE_BYTES);
+          const uint32_t b0 = smem_u32(tilesB + s * TC_TILE_BYTES);
 #pragma unroll
-        for (int k = 0; k < TC_BK / 16; ++k)
-          umma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc, (kc | k) != 0);
-        umma_commit(smem_u32(&bars[TC_STAGES + s]));
+          for (int k = 0; k < TC_BK / 16; ++k)
+            umma_bf16(acc, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc, (kc | k) != 0);
+          umma_commit(smem_u32(&bars[TC_STAGES + s]));
+        }
+        if (live) umma_commit(smem_u32(&acc_full[b]));
       }
-      umma_commit(smem_u32(&bars[2 * TC_STAGES]));
     }
   } else {
     // epilogue warps 0-3: TMEM lanes [32 warp, 32 warp + 32) = tile rows.
-    // While the mainloop runs, stage this thread's row of the C tile in
-    // shared memory (independent, coalesced loads), so that after the
-    // accumulator is ready only TMEM reads and stores remain.  Each thread
-    // reads back only the row it staged: no barrier needed.
-    float* __restrict__ G = c.a32 + f.off;
+    // The thread's row of the next C tile is staged in shared memory while
+    // the mainloop runs (independent, coalesced loads); each thread reads
+    // back only the row it staged, so no barrier is needed for s_c.
     const int rl = warp * 32 + lane;
-    const int row = R0 + rl;
-    const int jmax = lower_only ? min(n, row + 1) : n;     // columns < jmax are stored
     float* crow = s_c + rl * TC_CPAD;
-    // batches of 16 independent loads issued before any shared store (a
-    // shared store between them would order every load after the previous one)
+    int i = 0;
+    for (int t = blockIdx.x; t < n_items; t += gridDim.x, ++i) {
+      const Tile T = tile_of(t);
+      const FrontDev f = c.fronts[T.front];
+      float* __restrict__ G = c.a32 + f.off;
+      const int n = T.n;
+      const int row = T.R0 + rl;
+      const int jmax = lower_only ? min(n, row + 1) : n;     // columns < jmax are stored
 #pragma unroll 1
-    for (int j0 = 0; j0 < TC_BN; j0 += 16) {
-      float t[16];
+      for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+        float v[16];
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int col = C0 + j0 + u;
-        t[u] = (row < n && col < jmax) ? __ldcg(G + row + (int64_t)col * n) : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 16; ++u) crow[j0 + u] = t[u];
-    }
-    const bool ok = mbar_wait(smem_u32(&bars[2 * TC_STAGES]), 0, s_abort, err);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-    for (int cc = 0; cc < TC_BN / 32; ++cc) {
-      uint32_t v[32];
-      TC_LD32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (ok && !*s_abort && row < n) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int col = C0 + cc * 32 + j;
-          if (col < jmax) G[row + (int64_t)col * n] = crow[cc * 32 + j] - __uint_as_float(v[j]);
+        for (int q = 0; q < 16; ++q) {
+          const int col = T.C0 + j0 + q;
+          v[q] = (row < n && col < jmax) ? __ldcg(G + row + (int64_t)col * n) : 0.0f;
         }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) crow[j0 + q] = v[q];
+      }
+      const int b = i & 1, u = i >> 1;
+      const bool ok = mbar_wait(smem_u32(&acc_full[b]), u & 1, s_abort, err);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      float outv[TC_BN / 32][32];
+#pragma unroll
+      for (int cc = 0; cc < TC_BN / 32; ++cc) {
+        uint32_t v[32];
+        TC_LD32(tmem + ((uint32_t)(warp * 32) << 16) + b * TC_BN + cc * 32, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) outv[cc][j] = crow[cc * 32 + j] - __uint_as_float(v[j]);
+      }
+      // accumulator b may be overwritten from here on
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(smem_u32(&acc_empty[b]));
+      if (!*s_abort && row < n) {
+#pragma unroll
+        for (int cc = 0; cc < TC_BN / 32; ++cc)
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = T.C0 + cc * 32 + j;
+            if (col < jmax) G[row + (int64_t)col * n] = outv[cc][j];
+          }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BN));
   }
 }
 
@@ -330,9 +394,17 @@ void launch_tc_syrk(const DevCtx& c, const CUtensorMap& wsmap, const int64_t* ws
                     const int64_t* ws_stride, const Item* items, int n_items, int nbo, int nterms,
                     uint32_t term_code, int lower_only, int* err, cudaStream_t s) {
   if (!n_items) return;
+  static int n_sm = 0;
+  if (!n_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm <= 0) n_sm = 1;
+  }
   cudaFuncSetAttribute(k_tc_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-  k_tc_syrk<<<n_items, TC_THREADS, TC_SMEM, s>>>(c, wsmap, ws_off, ws_stride, items, nbo, nterms, term_code,
-                                                 lower_only, err);
+  const int grid = n_items < n_sm ? n_items : n_sm;   // one persistent CTA per SM
+  k_tc_syrk<<<grid, TC_THREADS, TC_SMEM, s>>>(c, wsmap, ws_off, ws_stride, items, n_items, nbo, nterms,
+                                              term_code, lower_only, err);
 }
 
 int tc_tile() { return TC_BM; }
