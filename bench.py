@@ -32,6 +32,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "factor+solve s at 16³ p=4: plain FP64 vs mixed+IR+learned, bwd err≤1e-12"
+# DRAM traffic of the tensor-core Schur update per algorithmic byte, from one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of its first
+# root-level launch on the 12^3 p=4 profiling case (trailing block above the
+# L2 size); scaled to the bench's launches by their algorithmic bytes
+TC_TRAFFIC_PER_ALG_BYTE = None
+TC_TRAFFIC_SOURCE = "not captured"
 WORKLOAD = "3D Poisson 16^3 hex p=4 Legendre-hierarchic, Dirichlet, octree ND, Cholesky fronts, 1 RHS"
 
 
@@ -244,20 +250,33 @@ def run_gpu(args):
     one_step(m)
     prof = m.profile()
     m.set_profiling(False)
-    # Roofline of the dominant tensor-core kernel: the BF16-split Schur update
-    # (tcgen05).  achieved = algorithmic Schur-update flops (one product per
-    # output, LAWN-41 SYRK count) / device time; the split evaluates 3 (BF16X3)
-    # or 6 (BF16X6) BF16 products per algorithmic one, reported as mma_frac.
+    # Roofline of the dominant contraction, the BF16-split Schur update
+    # (tcgen05).  With 256-wide outer panels every 128 x 128 tile does
+    # 2 * 256 algorithmic flops per 8 bytes of FP32 C read-modify-write (64
+    # flop/B, below the GPU's ~300 flop/B balance), so its bound is HBM:
+    # achieved = algorithmic bytes per launch (C lower triangle read + write,
+    # packed panel parts read once) / average launch time.  The tensor-pipe
+    # view is kept beside it: algorithmic flops / time against the BF16 peak,
+    # times the number of split products per algorithmic one.
     tc_name = "tc_syrk_bf16"
     if tc_name in prof and prof[tc_name]["ms"] > 0:
         p = prof[tc_name]
         terms = 6 if args.prec == api.PREC_BF16X6 else 3
-        achieved = p["flops"] / (p["ms"] * 1e-3) / 1e12
-        peak = float(peaks.get("bf16_tflops"))
-        roof = {"bound": "tensor", "kernel": tc_name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "mma_frac": terms * achieved / peak, "split_terms": terms,
-                "launches": p["launches"], "us_per_launch": 1e3 * p["ms"] / max(1, p["launches"]),
-                "traffic": None, "peak_source": f"bf16_tflops of MEASURED_PEAKS.json ({peak_src})"}
+        nl = max(1, p["launches"])
+        t_launch = p["ms"] * 1e-3 / nl
+        achieved = p["bytes"] / nl / t_launch / 1e9
+        tflops = p["flops"] / (p["ms"] * 1e-3) / 1e12
+        bf16_peak = float(peaks.get("bf16_tflops"))
+        traffic = None
+        if TC_TRAFFIC_PER_ALG_BYTE is not None:
+            traffic = TC_TRAFFIC_PER_ALG_BYTE * p["bytes"] / nl
+        roof = {"bound": "hbm", "kernel": tc_name, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "algorithmic_bytes_per_launch": p["bytes"] / nl, "us_per_launch": 1e6 * t_launch,
+                "launches": p["launches"], "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_src})",
+                "traffic_source": TC_TRAFFIC_SOURCE,
+                "tensor": {"achieved_tflops": tflops, "peak_tflops": bf16_peak, "frac": tflops / bf16_peak,
+                           "mma_frac": terms * tflops / bf16_peak, "split_terms": terms}}
     else:
         name, p = max(prof.items(), key=lambda kv: kv[1]["ms"])
         achieved = p["bytes"] / (p["ms"] * 1e-3) / 1e9

@@ -667,7 +667,7 @@ void Engine::build_programs(int method) {
           push(fac_ops, OP_SYRK, dt, NB, TC_NBO, u_items, fu);
         }
         std::vector<Item> pk, tt;
-        double ftc = 0;
+        double ftc = 0, btc = 0;
         for (int s : tcf) {
           const HostFront& f = fronts[s];
           if (f.fs <= K0) continue;
@@ -679,10 +679,14 @@ void Engine::build_programs(int method) {
           for (int ti = 0; ti < T; ++ti)
             for (int tj = 0; tj <= ti; ++tj) tt.push_back(Item{s, K0, ti, tj});
           ftc += get_flop_syrk(0, KB, m);
+          // algorithmic bytes: read and write the FP32 lower triangle of the
+          // trailing block once, read the packed panel parts once
+          const int np = fronts[s].prec == PREC_BF16X6 ? 3 : 2;
+          btc += 8.0 * 0.5 * (double)m * (m + 1) + 2.0 * np * (double)m * KB;
         }
         const int parts = fronts[tcf[0]].prec == PREC_BF16X6 ? 3 : 2;
         push(fac_ops, OP_TC_PACK, dt, TC_NBO, parts, pk);
-        push(fac_ops, OP_TC_SYRK, dt, TC_NBO, parts, tt, ftc);
+        push(fac_ops, OP_TC_SYRK, dt, TC_NBO, parts, tt, ftc, btc);
       }
     }
   }

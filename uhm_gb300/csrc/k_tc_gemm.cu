@@ -12,12 +12,13 @@
 // laid end to end along K, so one GEMM with K' = terms * KB accumulates them
 // all in FP32 in tensor memory.
 //
-// Kernel: one persistent CTA per SM walks the 128 x 128 output tiles; warp 4
+// Kernel: one persistent CTA per SM walks the 128 x 128 output tiles; warp 8
 // issues TMA loads (128-byte swizzle) into a 4-stage shared-memory ring
-// guarded by mbarriers, one thread of warp 5 issues tcgen05.mma (M=128,
-// N=128, K=16) into one of two 128-column TMEM accumulators, warps 0-3 read
-// TMEM back (tcgen05.ld) and apply C -= acc to the FP32 panel while the next
-// tile accumulates in the other buffer.  Every wait is bounded: a wait that
+// guarded by mbarriers, one thread of warp 9 issues tcgen05.mma (M=128,
+// N=128, K=16) into one of two 128-column TMEM accumulators, warps 0-7 read
+// TMEM back (tcgen05.ld; two warps per 32-lane quarter, one per column half)
+// and apply C -= acc to the FP32 panel while the next tile accumulates in
+// the other buffer.  Every wait is bounded: a wait that
 // gives up records an error flag and the CTA skips its stores.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -31,7 +32,8 @@
 namespace uhm_gpu {
 
 constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 4;
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 320;     // warps 0-7 epilogue, 8 TMA producer, 9 MMA issuer
+constexpr int TC_EPI_THREADS = 256;
 constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 2;   // 16 KB (A and B tiles alike)
 constexpr uint32_t TC_CPAD = TC_BN + 1;                 // padded row of the staged C tile
 constexpr uint32_t TC_CTILE_BYTES = TC_BM * TC_CPAD * 4;
@@ -136,7 +138,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 // two 128-column accumulators, so the epilogue of tile i (TMEM -> registers
 // -> C in global memory) overlaps the mainloop of tile i + 1.  acc_full[b]
 // is committed by the MMA thread when accumulator b holds a finished tile;
-// acc_empty[b] collects the 128 epilogue threads once they have read it.
+// acc_empty[b] collects the 256 epilogue threads once they have read it.
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_off,
           const int64_t* __restrict__ ws_stride, const Item* __restrict__ items, int n_items, int nbo,
@@ -161,7 +163,7 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&acc_full[b]), 1);
-      mbar_init(smem_u32(&acc_empty[b]), 128);
+      mbar_init(smem_u32(&acc_empty[b]), TC_EPI_THREADS);
     }
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -200,7 +202,7 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
     return T;
   };
 
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {
       // TMA producer
       uint32_t g = 0;       // chunks issued by this CTA so far
@@ -225,7 +227,7 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     if (lane == 0) {
       // MMA issuer
       const uint32_t idesc = idesc_bf16_f32(TC_BM, TC_BN);
@@ -256,12 +258,15 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       }
     }
   } else {
-    // epilogue warps 0-3: TMEM lanes [32 warp, 32 warp + 32) = tile rows.
-    // The thread's row of the next C tile is staged in shared memory while
-    // the mainloop runs (independent, coalesced loads); each thread reads
-    // back only the row it staged, so no barrier is needed for s_c.
-    const int rl = warp * 32 + lane;
-    float* crow = s_c + rl * TC_CPAD;
+    // epilogue warps 0-7: warp w reads TMEM lanes [32 (w % 4), +32) (its
+    // lane quarter = tile rows) and handles the columns [64 (w / 4), +64).
+    // The thread's half-row of the next C tile is staged in shared memory
+    // while the mainloop runs (independent, coalesced loads); each thread
+    // reads back only what it staged, so no barrier is needed for s_c.
+    const int quarter = warp & 3, half = warp >> 2;
+    const int rl = quarter * 32 + lane;
+    constexpr int HW = TC_BN / 2;
+    float* crow = s_c + rl * TC_CPAD + half * HW;
     int i = 0;
     for (int t = blockIdx.x; t < n_items; t += gridDim.x, ++i) {
       const Tile T = tile_of(t);
@@ -269,13 +274,14 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       float* __restrict__ G = c.a32 + f.off;
       const int n = T.n;
       const int row = T.R0 + rl;
+      const int cbase = T.C0 + half * HW;
       const int jmax = lower_only ? min(n, row + 1) : n;     // columns < jmax are stored
 #pragma unroll 1
-      for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+      for (int j0 = 0; j0 < HW; j0 += 16) {
         float v[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int col = T.C0 + j0 + q;
+          const int col = cbase + j0 + q;
           v[q] = (row < n && col < jmax) ? __ldcg(G + row + (int64_t)col * n) : 0.0f;
         }
 #pragma unroll
@@ -285,11 +291,11 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       const bool ok = mbar_wait(smem_u32(&acc_full[b]), u & 1, s_abort, err);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      float outv[TC_BN / 32][32];
+      float outv[HW / 32][32];
 #pragma unroll
-      for (int cc = 0; cc < TC_BN / 32; ++cc) {
+      for (int cc = 0; cc < HW / 32; ++cc) {
         uint32_t v[32];
-        TC_LD32(tmem + ((uint32_t)(warp * 32) << 16) + b * TC_BN + cc * 32, v);
+        TC_LD32(tmem + ((uint32_t)(quarter * 32) << 16) + b * TC_BN + half * HW + cc * 32, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 32; ++j) outv[cc][j] = crow[cc * 32 + j] - __uint_as_float(v[j]);
@@ -299,10 +305,10 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       mbar_arrive(smem_u32(&acc_empty[b]));
       if (!*s_abort && row < n) {
 #pragma unroll
-        for (int cc = 0; cc < TC_BN / 32; ++cc)
+        for (int cc = 0; cc < HW / 32; ++cc)
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int col = T.C0 + cc * 32 + j;
+            const int col = cbase + cc * 32 + j;
             if (col < jmax) G[row + (int64_t)col * n] = outv[cc][j];
           }
       }
