@@ -695,9 +695,29 @@ void Engine::build_programs(int method) {
   auto solve_small = [&](const HostFront& f, int dt) {
     return f.n <= small_max[dt] && (int64_t)f.n * nr <= 8192;
   };
+  // staged small-front solves (Cholesky): the launch's shared memory holds
+  // the largest front's factor panel, its right-hand sides and fs doubles;
+  // 0 selects the unstaged kernels (LU, or panels too large)
+  auto staged_bytes = [&](const std::vector<Item>& sm, int dt) {
+    if (!chol) return 0;
+    size_t mx = 0;
+    for (const Item& it : sm) {
+      const HostFront& f = fronts[it.front];
+      const size_t b = (size_t)f.n * nr * 8 + (size_t)f.fs * 8 + (size_t)f.n * f.fs * (dt == F64 ? 8 : 4);
+      mx = std::max(mx, b);
+    }
+    return mx <= 96 * 1024 ? (int)((mx + 15) / 16 * 16) : 0;
+  };
+  constexpr int GATHER_ROWS = 1024;   // rows per CTA of the forward gather (no pivots)
   for (auto& lv : levels) {
     std::vector<Item> g_items;
-    for (int s : lv) g_items.push_back(Item{s, 0, 0, 0});
+    for (int s : lv) {
+      if (gm == M_LU_PIV) {
+        g_items.push_back(Item{s, 0, 0, 0});
+      } else {
+        for (int r0 = 0; r0 < fronts[s].n; r0 += GATHER_ROWS) g_items.push_back(Item{s, r0, GATHER_ROWS, 0});
+      }
+    }
     push(fwd_ops, OP_FWD_GATHER, 0, 0, gm, g_items);
     for (int dt = 0; dt < 2; ++dt) {
       std::vector<Item> sm;
@@ -707,7 +727,7 @@ void Engine::build_programs(int method) {
         if (solve_small(fronts[s], dt)) sm.push_back(Item{s, 0, 0, 0});
         else large.push_back(s);
       }
-      push(fwd_ops, OP_FWD_SMALL, dt, 0, gm, sm);
+      push(fwd_ops, OP_FWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
       if (chol && nr <= 4 && !large.empty()) {
         // one flag-driven launch for every large front of this level
         std::vector<Item> fi, ai;
@@ -759,7 +779,7 @@ void Engine::build_programs(int method) {
         if (solve_small(fronts[s], dt)) sm.push_back(Item{s, 0, 0, 0});
         else { large.push_back(s); st.push_back(Item{s, 0, 0, 0}); }
       }
-      push(bwd_ops, OP_BWD_SMALL, dt, 0, gm, sm);
+      push(bwd_ops, OP_BWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
       if (chol && nr <= 4 && !large.empty()) {
         std::vector<Item> bi;
         int maxb = 0;
@@ -1023,10 +1043,12 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
       case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
       case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
-      case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, stream); break;
+      case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream); break;
       case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;
       case OP_BWD_PREP: launch_bwd_prepare(ctx, it, op.n_items, 0, op.param, g_out, n_global, stream); break;
-      case OP_BWD_SMALL: launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, stream); break;
+      case OP_BWD_SMALL:
+        launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, op.nb, stream);
+        break;
       case OP_TRSV_B:
         launch_bwd_step(ctx, it, op.n_items, op.dtype, op.param, d_scratch, d_scr_off, d_counters, stream);
         break;

@@ -27,8 +27,11 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
   const int n = f.n;
   double* __restrict__ z = c.vec + f.voff;
   const int32_t* __restrict__ inv = c.inv + f.inv_off;
+  // rows [it.a, it.a + it.b) of the front (it.b == 0: all rows; only then
+  // are pivots applied, which needs the whole gathered vector)
+  const int I0 = it.a, I1 = it.b > 0 ? min(n, it.a + it.b) : n;
   for (int q = 0; q < c.n_rhs; ++q) {
-    for (int I = threadIdx.x; I < n; I += blockDim.x) {
+    for (int I = I0 + threadIdx.x; I < I1; I += blockDim.x) {
       double acc = I < f.fs ? g[(f.g0 + I) + q * ldg] : 0.0;
       for (int s = 0; s < f.nsrc; ++s) {
         const SrcDev sd = c.srcs[f.src0 + s];
@@ -43,7 +46,7 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
     }
   }
   __syncthreads();
-  if (method == M_LU_PIV && threadIdx.x < c.n_rhs) {
+  if (method == M_LU_PIV && it.b == 0 && threadIdx.x < c.n_rhs) {
     // FLA_Apply_pivots(LEFT, NO_TRANSPOSE, p, xt): sequential interchanges
     const int q = threadIdx.x;
     const int32_t* __restrict__ piv = c.piv + f.piv_off;
@@ -97,9 +100,116 @@ __global__ void __launch_bounds__(NT) k_fwd_small(DevCtx c, const Item* __restri
   }
 }
 
+// Cholesky small fronts with the factor panel (n x fs) staged in shared
+// memory by one batch of loads: every column step then works on shared data
+// (one barrier per column instead of a global round trip per column).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_fwd_small_staged(DevCtx c, const Item* __restrict__ items) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs;
+  double* z = reinterpret_cast<double*>(smem_raw);
+  T* Ls = reinterpret_cast<T*>(z + (size_t)n * nr);
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ zg = c.vec + f.voff;
+  const int tot = n * fs;
+  for (int i0 = 0; i0 < tot; i0 += 8 * NT) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = i0 + threadIdx.x + u * NT;
+      v[u] = idx < tot ? G[idx] : T(0);        // columns 0..fs-1 are contiguous (ld n)
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = i0 + threadIdx.x + u * NT;
+      if (idx < tot) Ls[idx] = v[u];
+    }
+  }
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = zg[idx];
+  __syncthreads();
+  for (int j = 0; j < fs; ++j) {
+    if (threadIdx.x < nr) z[j + threadIdx.x * n] /= (double)Ls[j + j * n];
+    __syncthreads();
+    const int h = n - j - 1;
+    for (int idx = threadIdx.x; idx < h * nr; idx += NT) {
+      const int i = j + 1 + idx % h, q = idx / h;
+      z[i + q * n] -= (double)Ls[i + j * n] * z[j + q * n];
+    }
+    __syncthreads();
+  }
+  double* __restrict__ yg = zg + (int64_t)n * nr;
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) {
+    const int i = idx % n;
+    if (i < fs) yg[idx] = z[idx];
+    else zg[idx] = z[idx];
+  }
+}
+
+// x_F = L_FF^{-T} (y_F - L_SF^T x_S): the Schur-row products for all factor
+// columns at once, then the small triangular solve column by column.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_bwd_small_staged(DevCtx c, const Item* __restrict__ items,
+                                                         double* __restrict__ g, int64_t ldg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs;
+  double* z = reinterpret_cast<double*>(smem_raw);
+  double* w = z + (size_t)n * nr;
+  T* Ls = reinterpret_cast<T*>(w + fs);
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ zg = c.vec + f.voff + (int64_t)n * nr;   // y slab
+  const int tot = n * fs;
+  for (int i0 = 0; i0 < tot; i0 += 8 * NT) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = i0 + threadIdx.x + u * NT;
+      v[u] = idx < tot ? G[idx] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = i0 + threadIdx.x + u * NT;
+      if (idx < tot) Ls[idx] = v[u];
+    }
+  }
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = zg[idx];
+  __syncthreads();
+  for (int q = 0; q < nr; ++q) {
+    double* zq = z + q * n;
+    for (int j = threadIdx.x; j < fs; j += NT) {
+      double sacc = 0.0;
+      const T* col = Ls + (size_t)j * n;
+      for (int i = fs; i < n; ++i) sacc += (double)col[i] * zq[i];
+      w[j] = zq[j] - sacc;
+    }
+    __syncthreads();
+    for (int j = fs - 1; j >= 0; --j) {
+      const double xj = w[j] / (double)Ls[j + j * n];
+      for (int i = threadIdx.x; i < j; i += NT) w[i] -= (double)Ls[j + i * n] * xj;
+      if (threadIdx.x == 0) zq[j] = xj;
+      __syncthreads();
+    }
+  }
+  for (int q = 0; q < nr; ++q)
+    for (int i = threadIdx.x; i < fs; i += NT) g[(f.g0 + i) + q * ldg] = z[i + q * n];
+}
+
 void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                      cudaStream_t s) {
+                      int staged_bytes, cudaStream_t s) {
   if (!n_items) return;
+  if (method == M_CHOL && staged_bytes > 0) {
+    if (dtype == F64) {
+      cudaFuncSetAttribute(k_fwd_small_staged<double, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged_bytes);
+      k_fwd_small_staged<double, 128><<<n_items, 128, staged_bytes, s>>>(c, items);
+    } else {
+      cudaFuncSetAttribute(k_fwd_small_staged<float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged_bytes);
+      k_fwd_small_staged<float, 128><<<n_items, 128, staged_bytes, s>>>(c, items);
+    }
+    return;
+  }
   // the largest small front bounds the shared slab; 64 KB covers n*n_rhs <= 8192
   size_t sm = 8192 * sizeof(double);
   if (dtype == F64) {
@@ -181,8 +291,18 @@ __global__ void __launch_bounds__(NT) k_bwd_small(DevCtx c, const Item* __restri
 }
 
 void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                      double* g, int64_t ldg, cudaStream_t s) {
+                      double* g, int64_t ldg, int staged_bytes, cudaStream_t s) {
   if (!n_items) return;
+  if (method == M_CHOL && staged_bytes > 0) {
+    if (dtype == F64) {
+      cudaFuncSetAttribute(k_bwd_small_staged<double, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged_bytes);
+      k_bwd_small_staged<double, 128><<<n_items, 128, staged_bytes, s>>>(c, items, g, ldg);
+    } else {
+      cudaFuncSetAttribute(k_bwd_small_staged<float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, staged_bytes);
+      k_bwd_small_staged<float, 128><<<n_items, 128, staged_bytes, s>>>(c, items, g, ldg);
+    }
+    return;
+  }
   size_t sm = 8192 * sizeof(double);
   if (dtype == F64) {
     cudaFuncSetAttribute(k_bwd_small<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -340,21 +340,40 @@ __global__ void __launch_bounds__(256) k_tc_pack(DevCtx c, const Item* __restric
   __nv_bfloat16* __restrict__ W = ws + ws_off[it.front];
   const int64_t pstride = ws_stride[it.front];
   for (int k0 = 0; k0 < nbo; k0 += 64) {
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
-      const int r = idx % 64, k = idx / 64;
+    // one batch of 16 independent loads per thread (coalesced along the
+    // column), then the shared-memory transpose
+    float v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = threadIdx.x + 256 * u, r = idx % 64, k = idx / 64;
       const int gr = base + r0 + r, gk = k0 + k;
-      tile[r][k] = (gr < n && gk < KB) ? G[gr + (int64_t)(K0 + gk) * n] : 0.0f;
+      v[u] = (gr < n && gk < KB) ? G[gr + (int64_t)(K0 + gk) * n] : 0.0f;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
-      const int k = idx % 64, r = idx / 64;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = threadIdx.x + 256 * u, r = idx % 64, k = idx / 64;
+      tile[r][k] = v[u];
+    }
+    __syncthreads();
+    // each thread converts 8 consecutive k of one row and writes every part
+    // as one 16-byte store
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+      const int idx = threadIdx.x + 256 * h2, r = idx / 8, k8 = (idx % 8) * 8;
       if (base + r0 + r >= n) continue;
-      float x = tile[r][k];
+      float x[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) x[q] = tile[r][k8 + q];
       for (int p = 0; p < nparts; ++p) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        W[p * pstride + (int64_t)(r0 + r) * nbo + k0 + k] = h;
-        x -= __bfloat162float(h);
+        __align__(16) __nv_bfloat16 hb[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          hb[q] = __float2bfloat16_rn(x[q]);
+          x[q] -= __bfloat162float(hb[q]);
+        }
+        *reinterpret_cast<uint4*>(W + p * pstride + (int64_t)(r0 + r) * nbo + k0 + k8) =
+            *reinterpret_cast<const uint4*>(hb);
       }
     }
   }

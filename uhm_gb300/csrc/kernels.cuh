@@ -94,9 +94,9 @@ void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dty
 void launch_fwd_gather(const DevCtx& c, const Item* items, int n_items, const double* g,
                        int64_t ldg, int method, cudaStream_t s);
 void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                      cudaStream_t s);
+                      int staged_bytes, cudaStream_t s);
 void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
-                      double* g, int64_t ldg, cudaStream_t s);
+                      double* g, int64_t ldg, int staged_bytes, cudaStream_t s);
 // flag-driven level solves of large Cholesky fronts (one launch per level):
 // items ordered so that every CTA waits only on CTAs with smaller tickets
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
