@@ -9,11 +9,11 @@ backward error 1e-12 with at most 3 refinement steps:
   on a miss),
 * the learned per-front precision (committed weights).
 
-The instances are ones where the fronts near the root are cheaper in FP32
-than split BF16 (8^3 and 16^3 meshes), so the learned choice must beat the
-fixed policy there (the margin depends on the kernels' relative speeds at
-the time the labels were generated); it must also be at least twice as fast
-as plain FP64.
+The instances are 8^3 meshes where the fronts near the root are cheaper in
+FP32 than split BF16, so the learned choice must beat the fixed policy there
+by at least 8 % (observed 17-20 %; the margin depends on the kernels'
+relative speeds when the labels were generated); it must also be at least
+twice as fast as plain FP64.
 Every learned solve has to meet the target (with or without the redo).
 """
 import numpy as np
@@ -24,7 +24,7 @@ from uhm_gb300 import selector as S
 
 pytestmark = pytest.mark.gpu
 
-HELD_OUT_SEEDS = (100475, 100486, 100488, 100459, 100466)
+HELD_OUT_SEEDS = (100488, 100486, 100468, 100431, 100475)
 
 
 def test_learned_precision_beats_fixed_policy(native_lib):
@@ -43,5 +43,5 @@ def test_learned_precision_beats_fixed_policy(native_lib):
         for k in t:
             t[k] += ev[k]["ms"]
         del m
-    assert t["learned"] < 0.99 * t["fixed_bf16"], t
+    assert t["learned"] < 0.92 * t["fixed_bf16"], t
     assert t["learned"] < 0.5 * t["plain_fp64"], t

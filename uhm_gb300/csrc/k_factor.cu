@@ -202,24 +202,24 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // blocked large-front Cholesky: diagonal block, panel TRSM, trailing update
 // item: front, a = k0 (step start), b = row block / tile row, c = tile col
 // ---------------------------------------------------------------------------
-// Cholesky of one diagonal block (kb <= 64) and the inverse of its factor.
-// 64 threads; thread i keeps row i of the block in registers (fully unrolled,
-// compile-time register indices) and publishes every finished entry L[i][k]
-// into a row-major shared copy.  Left-looking: the entry (i, k) is
-//   L[i][k] = (A[i][k] - sum_{j<k} L[i][j] L[k][j]) / L[k][k],
-// with row k read from shared memory as 128-bit vectors.  One barrier per
-// column: before it, every thread has all terms j < k-1 (row k's entries up
-// to k-2 are visible since the previous barrier) and thread k has its pivot
-// (its own row is in registers); after it, the single missing term j = k-1
-// is added.  Blocks narrower than 64 are padded with the identity.  The
-// inverse L^{-1} (used by the panel TRSM and by the flag-driven solves) is
-// formed column per thread by forward substitution over the shared rows and
-// stored column-major with 128-bit stores.  FP32 pivots use rsqrt (the
-// factor is refined in FP64 by the mixed path); FP64 uses sqrt and a divide.
-template <typename T> struct PotrfVec;
-template <> struct PotrfVec<float> { using V = float4; static constexpr int W = 4, RL = 68; };
-template <> struct PotrfVec<double> { using V = double2; static constexpr int W = 2, RL = 66; };
-
+// Cholesky of one diagonal block (kb <= 64) and the inverse of its factor,
+// 256 threads.  Thread t owns the 4 x 4 tile (rows 4*(t%16).., columns
+// 4*(t/16)..) of the symmetric 64 x 64 block and the same tile of the inverse
+// X = L^{-1} being formed, both in registers.  Right-looking: phase p applies
+// column p of the factor to the trailing matrix,
+//   A[i][j] -= l_ip l_jp,   l_ip = v_p[i] / sqrt(v_p[p]),
+// where v_p (column p of the partially reduced block) was published to shared
+// memory by the 16 threads owning it at the end of phase p-1.  The same phase
+// applies step p-1 of the forward substitution L X = I,
+//   X[i][:] -= l_{i,p-1} x_{p-1}   (i > p-1),
+// and publishes row p of X scaled by 1/l_pp, so the factor and its inverse
+// take one barrier per column together.  Columns are walked four at a time so
+// that the register index inside a tile is a compile-time constant, and the
+// body stays a compact loop (a fully unrolled left-looking version with rows
+// in registers was bound by instruction fetch).  Blocks narrower than 64 are
+// padded with the identity.  FP32 pivots use rsqrt (the factor is refined in
+// FP64 by the mixed path); FP64 uses sqrt and a divide.  The inverse is stored
+// column-major (Dinv[j * 64 + i] = X[i][j]) with 128-bit stores.
 template <typename T> __device__ __forceinline__ void pivot_root(T s, T& d, T& rd);
 template <> __device__ __forceinline__ void pivot_root<float>(float s, float& d, float& rd) {
   rd = rsqrtf(s);
@@ -230,125 +230,136 @@ template <> __device__ __forceinline__ void pivot_root<double>(double s, double&
   rd = 1.0 / d;
 }
 
-// s - sum_{j < CNT} x[j] * row[j]; row 16-byte aligned; W partial sums
-template <int CNT, typename T>
-__device__ __forceinline__ T potrf_dot(T s, const T (&x)[64], const T* __restrict__ row) {
-  constexpr int W = PotrfVec<T>::W;
-  using V = typename PotrfVec<T>::V;
-  T acc[W];
-#pragma unroll
-  for (int u = 0; u < W; ++u) acc[u] = T(0);
-#pragma unroll
-  for (int j = 0; j + W <= CNT; j += W) {
-    const V v = *reinterpret_cast<const V*>(row + j);
-    const T* pv = reinterpret_cast<const T*>(&v);
-#pragma unroll
-    for (int u = 0; u < W; ++u) acc[u] += x[j + u] * pv[u];
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+  static __device__ __forceinline__ void ld(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
   }
-#pragma unroll
-  for (int j = (CNT / W) * W; j < CNT; ++j) acc[0] += x[j] * row[j];
-  T t = acc[0];
-#pragma unroll
-  for (int u = 1; u < W; ++u) t += acc[u];
-  return s - t;
-}
-
-template <int K, typename T>
-struct PotrfColumn {
-  static __device__ __forceinline__ void run(T (&a)[64], T* Ls, T* sd, T* srd, int i, bool& bad) {
-    constexpr int RL = PotrfVec<T>::RL;
-    const T* rk = Ls + K * RL;
-    T s = potrf_dot<(K > 0 ? K - 1 : 0)>(a[K], a, rk);
-    if (i == K) {
-      if (K > 0) s -= a[K - 1] * a[K - 1];
-      T piv = s;
-      if (!(piv > T(0))) { bad = true; piv = T(1); }
-      T d, rd;
-      pivot_root<T>(piv, d, rd);
-      sd[K] = d;
-      srd[K] = rd;
-    }
-    __syncthreads();
-    if (K > 0) s -= a[K - 1] * rk[K - 1];
-    const T l = (i > K) ? s * srd[K] : (i == K ? sd[K] : T(0));
-    a[K] = l;
-    if (i > K) Ls[i * RL + K] = l;
-    PotrfColumn<K + 1, T>::run(a, Ls, sd, srd, i, bad);
+  static __device__ __forceinline__ void st(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
   }
 };
-template <typename T>
-struct PotrfColumn<64, T> {
-  static __device__ __forceinline__ void run(T (&)[64], T*, T*, T*, int, bool&) {}
-};
-
-template <int R, typename T>
-struct InverseRow {
-  static __device__ __forceinline__ void run(T (&x)[64], const T* Ls, const T* srd, int jc) {
-    constexpr int RL = PotrfVec<T>::RL;
-    x[R] = potrf_dot<R>((R == jc) ? T(1) : T(0), x, Ls + R * RL) * srd[R];
-    InverseRow<R + 1, T>::run(x, Ls, srd, jc);
+template <> struct Vec4<double> {
+  static __device__ __forceinline__ void ld(const double* p, double (&v)[4]) {
+    const double2 q0 = *reinterpret_cast<const double2*>(p);
+    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
   }
-};
-template <typename T>
-struct InverseRow<64, T> {
-  static __device__ __forceinline__ void run(T (&)[64], const T*, const T*, int) {}
+  static __device__ __forceinline__ void st(double* p, const double (&v)[4]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+  }
 };
 
 template <typename T>
-__global__ void __launch_bounds__(64) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
-  constexpr int RL = PotrfVec<T>::RL;
-  __shared__ __align__(16) T Ls[64 * RL];
-  __shared__ T sd[64], srd[64];
+__global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
+  __shared__ __align__(16) T V[64][64];    // V[p][i]: column p of the reduced block (i >= p)
+  __shared__ __align__(16) T Xr[2][64];    // rows of the inverse, published scaled, double-buffered
+  __shared__ T sd[64], srd[64];            // l_pp and 1 / l_pp
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  const int i = threadIdx.x;
-  T a[64];
-  {
-    const T* p = G + i;
+  const int tid = threadIdx.x;
+  const int ti = tid & 15, tj = tid >> 4;
+  const int r0 = 4 * ti, c0 = 4 * tj;
+  // stage the lower triangle (coalesced column reads), identity padding
+#pragma unroll 4
+  for (int u = 0; u < 16; ++u) {
+    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+    if (i >= j) V[j][i] = (i < kb && j < kb) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
+  }
+  __syncthreads();
+  T a[4][4], x[4][4];
 #pragma unroll
-    for (int j = 0; j < 64; ++j) {
-      const bool in = i < kb && j < kb;
-      a[j] = in ? (j <= i ? p[(int64_t)j * n] : T(0)) : (i == j ? T(1) : T(0));
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = r0 + u, j = c0 + v;
+      a[u][v] = i >= j ? V[j][i] : V[i][j];
+      x[u][v] = i == j ? T(1) : T(0);
+    }
+  __syncthreads();   // column 0 of the staged block is v_0; later columns are republished
+  bool bad = false;
+  T rdq = T(0);      // 1 / l_{p-1,p-1}
+#pragma unroll 1
+  for (int q = 0; q < 16; ++q) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int p = 4 * q + s;
+      T piv = V[p][p];
+      if (!(piv > T(0))) { bad = true; piv = T(1); }
+      T d, rd;
+      pivot_root<T>(piv, d, rd);
+      if (tid == 0) { sd[p] = d; srd[p] = rd; }
+      T lr[4], lc[4];
+      Vec4<T>::ld(&V[p][r0], lr);
+      Vec4<T>::ld(&V[p][c0], lc);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) { lr[u] *= rd; lc[u] *= rd; }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) a[u][v] -= lr[u] * lc[v];
+      if (p > 0) {
+        T lq[4], xr[4];
+        Vec4<T>::ld(&V[p - 1][r0], lq);
+        Vec4<T>::ld(&Xr[(p - 1) & 1][c0], xr);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) lq[u] = (r0 + u > p - 1) ? lq[u] * rdq : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) x[u][v] -= lq[u] * xr[v];
+      }
+      // publish column p+1 of the reduced block (zero above its pivot)
+      const int CB = (s + 1) & 3;   // constant after unrolling
+      if (p + 1 < 64 && tj == q + (s + 1) / 4) {
+        T w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) w[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
+        Vec4<T>::st(&V[p + 1][r0], w);
+      }
+      // publish row p of the inverse, scaled by 1 / l_pp
+      if (ti == q) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) x[s][v] *= rd;
+        Vec4<T>::st(&Xr[p & 1][c0], x[s]);
+      }
+      rdq = rd;
+      __syncthreads();
     }
   }
-  bool bad = false;
-  PotrfColumn<0, T>::run(a, Ls, sd, srd, i, bad);
-  if (bad) set_status(c, it.front, ST_NOT_SPD);
-  {
-    T* p = G + i;
-#pragma unroll
-    for (int j = 0; j < 64; ++j)
-      if (i < kb && j < kb && j <= i) p[(int64_t)j * n] = a[j];
+  if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+  // factor: L[i][k] = v_k[i] / l_kk below the diagonal, l_kk on it
+#pragma unroll 4
+  for (int u = 0; u < 16; ++u) {
+    const int idx = tid + 256 * u, i = idx & 63, k = idx >> 6;
+    if (i >= k && i < kb && k < kb) G[i + (int64_t)k * n] = i == k ? sd[k] : V[k][i] * srd[k];
   }
   T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
   if (nb != 64 || !Dinv) return;
-  __syncthreads();   // every row of Ls is complete
-  const int jc = i;
-  T x[64];
-  InverseRow<0, T>::run(x, Ls, srd, jc);
-  using V = typename PotrfVec<T>::V;
-  constexpr int W = PotrfVec<T>::W;
-  V* D = reinterpret_cast<V*>(Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096 + jc * 64);
+  T* D = Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096;
 #pragma unroll
-  for (int r = 0; r < 64; r += W) {
-    V v;
-    T* pv = reinterpret_cast<T*>(&v);
+  for (int v = 0; v < 4; ++v) {
+    const int j = c0 + v;
+    T w[4];
 #pragma unroll
-    for (int u = 0; u < W; ++u) pv[u] = (r + u < kb && jc < kb) ? x[r + u] : T(0);
-    D[r / W] = v;
+    for (int u = 0; u < 4; ++u) w[u] = (r0 + u < kb && j < kb) ? x[u][v] : T(0);
+    Vec4<T>::st(D + (int64_t)j * 64 + r0, w);
   }
 }
 
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s) {
   if (!n_items) return;
+  if (nb > 64) throw std::invalid_argument("potrf_diag: block wider than 64");
   if (dtype == F64)
-    k_potrf_diag<double><<<n_items, 64, 0, s>>>(c, items, nb);
+    k_potrf_diag<double><<<n_items, 256, 0, s>>>(c, items, nb);
   else
-    k_potrf_diag<float><<<n_items, 64, 0, s>>>(c, items, nb);
+    k_potrf_diag<float><<<n_items, 256, 0, s>>>(c, items, nb);
 }
 
 constexpr int TRSM_RB = 64;   // rows per panel-TRSM block
