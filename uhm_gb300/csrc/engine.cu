@@ -75,6 +75,10 @@ void Engine::free_device() {
   d_ws = nullptr;
   d_ws_off = d_ws_stride = nullptr;
   d_err = nullptr;
+  d_dof_tree = nullptr;
+  d_tree_red = nullptr;
+  tree_bnorm.clear();
+  tree_anorm.clear();
 }
 
 // ---------------------------------------------------------------------------
@@ -895,6 +899,22 @@ void Engine::alloc_device(int method) {
   d_erhs = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, erhs_total));
   d_y = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, y_total));
   d_red = (double*)dmalloc(sizeof(double) * 2048);
+  {
+    // tree of every global dof (roots numbered in slot order)
+    std::vector<int> root_of(fronts.size(), -1);
+    n_trees = 0;
+    for (int s = (int)fronts.size() - 1; s >= 0; --s)
+      root_of[s] = fronts[s].parent < 0 ? n_trees++ : root_of[fronts[s].parent];
+    if (n_trees > 1) {
+      std::vector<int> dt(std::max<int64_t>(1, n_global), 0);
+      for (auto& f : fronts)
+        for (int k = 0; k < f.fs; ++k) dt[(size_t)f.g0 + k] = root_of[f.slot];
+      d_dof_tree = (int*)dmalloc(sizeof(int) * dt.size());
+      d_tree_red = (unsigned long long*)dmalloc(sizeof(unsigned long long) * 4 * n_trees);
+      CK(cudaMemcpyAsync(d_dof_tree, dt.data(), sizeof(int) * dt.size(), cudaMemcpyHostToDevice, stream));
+    }
+    n_trees = std::max(n_trees, 1);
+  }
   d_emat_off = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, h_emat_off.size()));
   d_elem_m = (int*)dmalloc(sizeof(int) * std::max<size_t>(1, h_elem_m.size()));
   d_emap_off = (int64_t*)dmalloc(sizeof(int64_t) * std::max<size_t>(1, h_emap_off.size()));
@@ -1081,7 +1101,8 @@ void Engine::check_status(const char* where) {
   for (size_t i = 0; i < st.size(); ++i)
     if (st[i]) {
       const char* what = st[i] == ST_NOT_SPD ? "front is not positive definite"
-                         : st[i] == ST_ZERO_PIVOT ? "zero pivot" : "NaN in front";
+                         : st[i] == ST_ZERO_PIVOT ? "zero pivot"
+                         : st[i] == ST_WAIT ? "a bounded wait inside a kernel gave up" : "NaN in front";
       status = 10 + st[i];
       last_error = std::string(where) + ": " + what + " (element " + std::to_string(fronts[i].e->get_id()) + ")";
       return;
@@ -1186,15 +1207,27 @@ void Engine::refine(int method) {
   const double bn = read_scalar(d_red + 1024);
   double berr = 1.0;
   int it = 0;
+  const bool forest = n_trees > 1;
+  if (forest) {
+    tree_max_async(d_b, nv, n_global, 2);
+    tree_bnorm = read_tree_slot(2);
+  }
   for (;; ++it) {
     compute_residual(d_x, d_r);
-    launch_absmax(d_r, nv, d_red, stream);
-    launch_absmax(d_x, nv, d_red + 512, stream);
-    double h[2];
-    CK(cudaMemcpyAsync(&h[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(&h[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    berr = h[0] / (an * h[1] + bn);
+    if (forest) {
+      tree_max_async(d_r, nv, n_global, 0);
+      tree_max_async(d_x, nv, n_global, 1);
+      const std::vector<double> rn = read_tree_slot(0);
+      berr = forest_berr(rn, read_tree_slot(1));
+    } else {
+      launch_absmax(d_r, nv, d_red, stream);
+      launch_absmax(d_x, nv, d_red + 512, stream);
+      double h[2];
+      CK(cudaMemcpyAsync(&h[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&h[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      berr = h[0] / (an * h[1] + bn);
+    }
     if (it == 0) timing.berr_first = berr;
     if (berr <= ir_tol || it >= ir_max || !(berr == berr)) break;
     solve_into(method, d_r, d_d, 3);
@@ -1253,8 +1286,10 @@ void Engine::enqueue_anorm() {
                        d_y_off, (int)esrc.size(), stream);
   launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, nullptr, n_global, d_r, n_global, 1, 0, stream);
   launch_absmax(d_r, n_global, d_red + 1536, stream);
+  if (n_trees > 1) tree_max_async(d_r, n_global, n_global, 3);
   anorm_valid = true;
   anorm_inf = -1.0;
+  tree_anorm.clear();
 }
 
 double Engine::read_scalar(const double* d) {
@@ -1262,6 +1297,37 @@ double Engine::read_scalar(const double* d) {
   CK(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
   return h;
+}
+
+void Engine::tree_max_async(const double* v, int64_t nv, int64_t ng, int slot) {
+  launch_absmax_tree(v, nv, ng, d_dof_tree, n_trees, d_tree_red + (size_t)slot * n_trees, stream);
+}
+
+std::vector<double> Engine::read_tree_slot(int slot) {
+  std::vector<unsigned long long> bits(n_trees);
+  CK(cudaMemcpyAsync(bits.data(), d_tree_red + (size_t)slot * n_trees, sizeof(unsigned long long) * n_trees,
+                     cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  std::vector<double> out(n_trees);
+  std::memcpy(out.data(), bits.data(), sizeof(double) * n_trees);
+  return out;
+}
+
+// worst per-tree ||b-Ax|| / (||A|| ||x|| + ||b||); NaN if any tree has a NaN
+double Engine::forest_berr(const std::vector<double>& rn, const std::vector<double>& xn) {
+  if (tree_anorm.empty()) {
+    operator_norm_inf();
+    tree_anorm = read_tree_slot(3);
+  }
+  double worst = 0.0;
+  bool nan = false;
+  for (int t = 0; t < n_trees; ++t) {
+    const double den = tree_anorm[t] * xn[t] + tree_bnorm[t];
+    const double b = den > 0 ? rn[t] / den : (rn[t] > 0 ? INFINITY : 0.0);
+    if (b != b) nan = true;
+    else if (b > worst) worst = b;
+  }
+  return nan ? NAN : worst;
 }
 
 double Engine::operator_norm_inf() {
@@ -1442,6 +1508,15 @@ double Engine::backward_error() {
   if (!factored) fail("backward_error: nothing solved", 9);
   compute_residual(d_x, d_r);
   const int64_t nv = n_global * mesh->n_rhs;
+  if (n_trees > 1) {
+    operator_norm_inf();
+    tree_max_async(d_b, nv, n_global, 2);
+    tree_bnorm = read_tree_slot(2);
+    tree_max_async(d_r, nv, n_global, 0);
+    tree_max_async(d_x, nv, n_global, 1);
+    const std::vector<double> rn = read_tree_slot(0);
+    return forest_berr(rn, read_tree_slot(1));
+  }
   launch_absmax(d_r, nv, d_red, stream);
   launch_absmax(d_x, nv, d_red + 512, stream);
   launch_absmax(d_b, nv, d_red + 1024, stream);

@@ -234,6 +234,16 @@ class Engine {
   double operator_norm_inf();
   void enqueue_anorm();
   double read_scalar(const double* d);
+  // forests (several independent trees, e.g. a batch of meshes): the
+  // backward error is taken per tree and the worst one is reported, so that
+  // every mesh of a batch meets the tolerance on its own operator
+  int n_trees = 1;
+  int* d_dof_tree = nullptr;                  // tree of each global dof
+  unsigned long long* d_tree_red = nullptr;   // 4 slots x n_trees: r, x, b, A maxima
+  std::vector<double> tree_bnorm, tree_anorm;
+  void tree_max_async(const double* v, int64_t nv, int64_t ng, int slot);
+  std::vector<double> read_tree_slot(int slot);
+  double forest_berr(const std::vector<double>& rn, const std::vector<double>& xn);
   void refine(int method);
   void check_status(const char* where);
   void check_device_error(const char* where);

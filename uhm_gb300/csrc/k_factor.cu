@@ -203,23 +203,30 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // item: front, a = k0 (step start), b = row block / tile row, c = tile col
 // ---------------------------------------------------------------------------
 // Cholesky of one diagonal block (kb <= 64) and the inverse of its factor,
-// 256 threads.  Thread t owns the 4 x 4 tile (rows 4*(t%16).., columns
-// 4*(t/16)..) of the symmetric 64 x 64 block and the same tile of the inverse
-// X = L^{-1} being formed, both in registers.  Right-looking: phase p applies
-// column p of the factor to the trailing matrix,
-//   A[i][j] -= l_ip l_jp,   l_ip = v_p[i] / sqrt(v_p[p]),
-// where v_p (column p of the partially reduced block) was published to shared
-// memory by the 16 threads owning it at the end of phase p-1.  The same phase
-// applies step p-1 of the forward substitution L X = I,
-//   X[i][:] -= l_{i,p-1} x_{p-1}   (i > p-1),
-// and publishes row p of X scaled by 1/l_pp, so the factor and its inverse
-// take one barrier per column together.  Columns are walked four at a time so
-// that the register index inside a tile is a compile-time constant, and the
-// body stays a compact loop (a fully unrolled left-looking version with rows
-// in registers was bound by instruction fetch).  Blocks narrower than 64 are
-// padded with the identity.  FP32 pivots use rsqrt (the factor is refined in
-// FP64 by the mixed path); FP64 uses sqrt and a divide.  The inverse is stored
-// column-major (Dinv[j * 64 + i] = X[i][j]) with 128-bit stores.
+// 256 threads = 8 warps.  Warp w owns the column block 8w..8w+7 of the
+// symmetric 64 x 64 block and of the inverse X = L^{-1} being formed; lane
+// (ti, h) keeps the 4 x 4 tile at rows 4 ti.., columns 8w + 4h.. of both in
+// registers.  Right-looking in column order; for each column p a warp
+//   (factor, p <= 8w+7) applies A[i][j] -= l_ip l_jp to its tile, where
+//     l_ip = v_p[i] / sqrt(v_p[p]) and v_p, column p of the partially reduced
+//     block, was published in shared memory by the warp owning column p;
+//   (inverse, p >= 8w) scales row p of its column block of X by 1 / l_pp and
+//     applies X[i][:] -= l_ip x_p for i > p.  Column blocks of X are
+//     independent, so this needs nothing from other warps but v_p.
+// The owner of column p+1 publishes it as soon as it has applied column p.
+// A hand-off inside a warp needs only __syncwarp; a column published by
+// another warp is awaited on its own mbarrier (16 arrivals, one per
+// publishing lane; arrive releases, try_wait acquires) with an iteration
+// limit, after which the front is flagged (status ST_WAIT) and the block
+// gives up.  The 64-pivot chain thus runs at warp-synchronous speed except at
+// the 7 hand-offs between warps, and each warp overlaps its trailing updates
+// and its part of the inverse with the chain; a warp does only the factor
+// steps that reach its columns and only the inverse steps whose rows are
+// nonzero in them.  Columns are walked four at a time so that register
+// indices inside a tile are compile-time constants.  Blocks narrower than 64
+// are padded with the identity.  FP32 pivots use rsqrt (the factor is refined
+// in FP64 by the mixed path); FP64 uses sqrt and a divide.  The inverse is
+// stored column-major (Dinv[j * 64 + i] = X[i][j]) with 128-bit stores.
 template <typename T> __device__ __forceinline__ void pivot_root(T s, T& d, T& rd);
 template <> __device__ __forceinline__ void pivot_root<float>(float s, float& d, float& rd) {
   rd = rsqrtf(s);
@@ -252,24 +259,66 @@ template <> struct Vec4<double> {
   }
 };
 
+constexpr uint32_t PD_WAIT_LIMIT = 1u << 20;
+
+__device__ __forceinline__ uint32_t pd_smem(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void pd_mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void pd_mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// bounded wait for phase 0 of a single-use barrier; false when it gave up
+// (here or, through *give_up, in another warp)
+__device__ __forceinline__ bool pd_mbar_wait(uint32_t bar, volatile int* give_up) {
+  for (uint32_t i = 0; i < PD_WAIT_LIMIT; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+        " selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar)
+        : "memory");
+    if (ok) return true;
+    if (*give_up) return false;
+  }
+  *give_up = 1;
+  return false;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
-  __shared__ __align__(16) T V[64][64];    // V[p][i]: column p of the reduced block (i >= p)
-  __shared__ __align__(16) T Xr[2][64];    // rows of the inverse, published scaled, double-buffered
+  __shared__ __align__(16) T V[64][64];    // V[p][i]: column p of the reduced block (zero above p)
+  __shared__ __align__(16) T XR[8][2][8];  // per warp: row p of its X block, scaled, double-buffered
   __shared__ T sd[64], srd[64];            // l_pp and 1 / l_pp
+  __shared__ __align__(8) unsigned long long mbar[64];   // column p published
+  __shared__ int s_give_up;
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  const int tid = threadIdx.x;
-  const int ti = tid & 15, tj = tid >> 4;
-  const int r0 = 4 * ti, c0 = 4 * tj;
-  // stage the lower triangle (coalesced column reads), identity padding
-#pragma unroll 4
-  for (int u = 0; u < 16; ++u) {
-    const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-    if (i >= j) V[j][i] = (i < kb && j < kb) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
+  const int tid = threadIdx.x, w = tid >> 5;
+  const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
+  const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
+  if (tid < 64) pd_mbar_init(pd_smem(&mbar[tid]), 16);
+  if (tid == 0) s_give_up = 0;
+  {
+    // stage the lower triangle (coalesced column reads, all loads in flight
+    // before the shared stores), identity padding
+    T g[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      g[u] = (i >= j && i < kb && j < kb) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      if (i >= j) V[j][i] = g[u];
+    }
   }
   __syncthreads();
   T a[4][4], x[4][4];
@@ -281,58 +330,66 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
       a[u][v] = i >= j ? V[j][i] : V[i][j];
       x[u][v] = i == j ? T(1) : T(0);
     }
-  __syncthreads();   // column 0 of the staged block is v_0; later columns are republished
-  bool bad = false;
-  T rdq = T(0);      // 1 / l_{p-1,p-1}
+  __syncthreads();   // tiles read before any column is republished; column 0 stays as staged
+  bool bad = false, gave_up = false;
 #pragma unroll 1
   for (int q = 0; q < 16; ++q) {
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int p = 4 * q + s;
+      if (p > 0 && (p >> 3) != w && !gave_up)
+        gave_up = !pd_mbar_wait(pd_smem(&mbar[p]), &s_give_up);
       T piv = V[p][p];
       if (!(piv > T(0))) { bad = true; piv = T(1); }
       T d, rd;
       pivot_root<T>(piv, d, rd);
       if (tid == 0) { sd[p] = d; srd[p] = rd; }
-      T lr[4], lc[4];
+      T lr[4];
       Vec4<T>::ld(&V[p][r0], lr);
-      Vec4<T>::ld(&V[p][c0], lc);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) { lr[u] *= rd; lc[u] *= rd; }
+      for (int u = 0; u < 4; ++u) lr[u] *= rd;
+      if (p <= cb0 + 7) {
+        T lc[4];
+        Vec4<T>::ld(&V[p][c0], lc);
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) a[u][v] -= lr[u] * lc[v];
-      if (p > 0) {
-        T lq[4], xr[4];
-        Vec4<T>::ld(&V[p - 1][r0], lq);
-        Vec4<T>::ld(&Xr[(p - 1) & 1][c0], xr);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) lq[u] = (r0 + u > p - 1) ? lq[u] * rdq : T(0);
+        for (int v = 0; v < 4; ++v) lc[v] *= rd;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-          for (int v = 0; v < 4; ++v) x[u][v] -= lq[u] * xr[v];
-      }
-      // publish column p+1 of the reduced block (zero above its pivot)
-      const int CB = (s + 1) & 3;   // constant after unrolling
-      if (p + 1 < 64 && tj == q + (s + 1) / 4) {
-        T w[4];
+          for (int v = 0; v < 4; ++v) a[u][v] -= lr[u] * lc[v];
+        if (p + 1 < 64 && ((p + 1) >> 3) == w) {
+          const int CB = (s + 1) & 3;   // constant after unrolling
+          if (tj == (p + 1) >> 2) {
+            T wv[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) w[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
-        Vec4<T>::st(&V[p + 1][r0], w);
+            for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
+            Vec4<T>::st(&V[p + 1][r0], wv);
+            pd_mbar_arrive(pd_smem(&mbar[p + 1]));
+          }
+          __syncwarp();
+        }
       }
-      // publish row p of the inverse, scaled by 1 / l_pp
-      if (ti == q) {
+      if (p >= cb0) {
+        if (ti == q) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) x[s][v] *= rd;
-        Vec4<T>::st(&Xr[p & 1][c0], x[s]);
+          for (int v = 0; v < 4; ++v) x[s][v] *= rd;
+          Vec4<T>::st(&XR[w][p & 1][4 * h], x[s]);
+        }
+        __syncwarp();
+        T xr[4];
+        Vec4<T>::ld(&XR[w][p & 1][4 * h], xr);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const T l = (r0 + u > p) ? lr[u] : T(0);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) x[u][v] -= l * xr[v];
+        }
       }
-      rdq = rd;
-      __syncthreads();
     }
   }
+  if (gave_up) set_status(c, it.front, ST_WAIT);
   if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+  __syncthreads();   // every column published, sd / srd complete
   // factor: L[i][k] = v_k[i] / l_kk below the diagonal, l_kk on it
 #pragma unroll 4
   for (int u = 0; u < 16; ++u) {
@@ -345,10 +402,10 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     const int j = c0 + v;
-    T w[4];
+    T wv[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) w[u] = (r0 + u < kb && j < kb) ? x[u][v] : T(0);
-    Vec4<T>::st(D + (int64_t)j * 64 + r0, w);
+    for (int u = 0; u < 4; ++u) wv[u] = (r0 + u < kb && j < kb) ? x[u][v] : T(0);
+    Vec4<T>::st(D + (int64_t)j * 64 + r0, wv);
   }
 }
 

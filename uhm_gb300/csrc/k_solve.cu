@@ -627,6 +627,44 @@ void launch_absmax(const double* v, int64_t n, double* out, cudaStream_t s) {
   k_absmax_final<<<1, 256, 0, s>>>(out + 1, np, out);
 }
 
+// Maximum |v| per tree of a forest.  v holds n_rhs columns of ng dofs;
+// tree[i] is the tree of dof i.  The dofs of one tree are not contiguous
+// (numbering runs generation by generation over all trees) but come in long
+// runs (a front's factor dofs are consecutive), so each thread scans 32
+// consecutive entries and flushes its running maximum with one atomicMax on
+// the bit pattern (non-negative doubles order like their bits; NaN, kept by
+// the comparison below, orders above every number) whenever the tree changes.
+// out[t] must be zeroed before the launch.
+__global__ void k_absmax_tree(const double* __restrict__ v, int64_t nv, int64_t ng,
+                              const int* __restrict__ tree, unsigned long long* __restrict__ out) {
+  const int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 32;
+  if (i0 >= nv) return;
+  const int64_t i1 = i0 + 32 < nv ? i0 + 32 : nv;
+  int64_t row = i0 % ng;
+  int cur = -1;
+  double m = 0.0;
+  for (int64_t i = i0; i < i1; ++i) {
+    const int t = tree[row];
+    if (t != cur) {
+      if (cur >= 0) atomicMax(&out[cur], (unsigned long long)__double_as_longlong(m));
+      cur = t;
+      m = 0.0;
+    }
+    const double a = fabs(v[i]);
+    if (a > m || a != a) m = a;
+    if (++row == ng) row = 0;
+  }
+  atomicMax(&out[cur], (unsigned long long)__double_as_longlong(m));
+}
+
+void launch_absmax_tree(const double* v, int64_t nv, int64_t ng, const int* tree, int n_trees,
+                        unsigned long long* out, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, sizeof(unsigned long long) * n_trees, s);
+  if (!nv) return;
+  const int64_t threads = (nv + 31) / 32;
+  k_absmax_tree<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(v, nv, ng, tree, out);
+}
+
 __global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, int64_t n, double a) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)

@@ -49,7 +49,7 @@ struct Item {
 };
 
 // Status words written by kernels (breakdown detection): per front.
-enum Status : int { ST_OK = 0, ST_NOT_SPD = 1, ST_ZERO_PIVOT = 2, ST_NAN = 3 };
+enum Status : int { ST_OK = 0, ST_NOT_SPD = 1, ST_ZERO_PIVOT = 2, ST_NAN = 3, ST_WAIT = 4 };
 
 struct DevCtx {
   FrontDev* fronts;
@@ -121,6 +121,9 @@ void launch_dof_gather(const int64_t* ptr, const int64_t* idx, const double* y, 
                        int64_t ldb, double* r, int64_t N, int n_rhs, int sub_from_b,
                        cudaStream_t s);
 void launch_absmax(const double* v, int64_t n, double* out, cudaStream_t s);
+// per-tree max |v| (forest of independent meshes); out: n_trees bit patterns
+void launch_absmax_tree(const double* v, int64_t nv, int64_t ng, const int* tree, int n_trees,
+                        unsigned long long* out, cudaStream_t s);
 void launch_axpy(double* y, const double* x, int64_t n, double alpha, cudaStream_t s);
 void launch_anorm_partial(const double* emat, const int64_t* emat_off, const int* elem_m,
                           const int64_t* emap_off, const int32_t* emap, const int64_t* dof_ptr,

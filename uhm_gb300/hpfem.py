@@ -37,7 +37,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = ["MeshSpec", "poisson2d", "poisson3d", "convdiff3d", "diffusion3d",
-           "build_mesh", "lobatto_1d"]
+           "build_mesh", "lobatto_1d", "forest", "batch3d"]
 
 
 # ----------------------------------------------------------------------------
@@ -441,3 +441,117 @@ def convdiff3d(n: int = 24, p: int = 3, seed: int = 0, pe: float = 100.0,
     beta = np.array([1.0, 0.5, 0.25]) * pe
     return build_mesh(3, n, p, kappa=kappa, beta=beta, seed=seed, n_rhs=n_rhs,
                       merges=merges)
+
+
+# ----------------------------------------------------------------------------
+# Many independent meshes as one forest
+# ----------------------------------------------------------------------------
+def forest(specs) -> MeshSpec:
+    """Join independent meshes into one MeshSpec whose tree is a forest.
+
+    The reference's Mesh_ holds any set of elements: ``lock`` groups them by
+    generation over the whole mesh (UHM/src/operation/scheduler.cxx:45-70) and
+    every element without a parent is a root whose nodes are all factored
+    (UHM/src/mesh/element.cxx:272-286), so a mesh made of several disjoint
+    trees factors and solves each tree independently.  Same-generation fronts
+    of all meshes then fall into the same level and share each launch.
+
+    Node ids of mesh k are shifted past those of meshes 0..k-1; the leaves of
+    all meshes come first (mesh by mesh), then the interior elements.  Every
+    spec must have the same ``n_rhs`` and symmetry.  ``info["parts"]`` lists,
+    per mesh, its node-id offset, number of nodes, leaf range and dofs.
+    """
+    specs = list(specs)
+    if not specs:
+        raise ValueError("forest: no meshes")
+    n_rhs = specs[0].n_rhs
+    sym = specs[0].symmetric
+    if any(s.n_rhs != n_rhs or s.symmetric != sym for s in specs):
+        raise ValueError("forest: meshes differ in n_rhs or symmetry")
+    leaf_base, int_base = [], []
+    nl = sum(s.n_leaves for s in specs)
+    lo, io = 0, nl
+    for s in specs:
+        leaf_base.append(lo)
+        int_base.append(io)
+        lo += s.n_leaves
+        io += s.n_elements - s.n_leaves
+
+    def remap(k, e):
+        s = specs[k]
+        e = np.asarray(e, dtype=np.int64)
+        return np.where(e < s.n_leaves, leaf_base[k] + e, int_base[k] + (e - s.n_leaves))
+
+    n_el = io
+    parent = np.full(n_el, -1, dtype=np.int64)
+    generation = np.zeros(n_el, dtype=np.int64)
+    children = [None] * n_el
+    node_id, node_ndof, node_p, node_kind = [], [], [], []
+    elem_node, elem_m, mats, rhs = [], [], [], []
+    parts = []
+    nid_off = 0
+    for k, s in enumerate(specs):
+        idx = remap(k, np.arange(s.n_elements))
+        par = s.parent
+        parent[idx] = np.where(par < 0, -1, remap(k, np.maximum(par, 0)))
+        generation[idx] = s.generation
+        for e in range(s.n_elements):
+            children[idx[e]] = remap(k, s.children(e))
+        node_id.append(s.node_id + nid_off)
+        node_ndof.append(s.node_ndof)
+        node_p.append(s.node_p)
+        node_kind.append(s.node_kind)
+        elem_node.append(s.elem_node + nid_off)
+        elem_m.append(s.elem_m)
+        mats.append(s.mats)
+        rhs.append(s.rhs)
+        parts.append(dict(node_off=nid_off, n_nodes=s.n_nodes, leaves=(leaf_base[k],
+                          leaf_base[k] + s.n_leaves), n_dof=s.n_dof(), info=s.info))
+        nid_off += int(s.node_id.max()) + 1
+    child_ptr = np.zeros(n_el + 1, dtype=np.int64)
+    for e in range(n_el):
+        child_ptr[e + 1] = child_ptr[e] + len(children[e])
+    child_idx = (np.concatenate([c for c in children if len(c)]).astype(np.int64)
+                 if child_ptr[-1] else np.zeros(0, dtype=np.int64))
+    elem_m = np.concatenate(elem_m)
+    sizes = elem_m.astype(np.int64)
+    mat_off = np.concatenate([[0], np.cumsum(sizes * sizes)[:-1]]).astype(np.int64)
+    rhs_off = np.concatenate([[0], np.cumsum(sizes * n_rhs)[:-1]]).astype(np.int64)
+    lens = np.concatenate([np.diff(s.elem_ptr) for s in specs])
+    elem_ptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    return MeshSpec(
+        dim=specs[0].dim,
+        node_id=np.concatenate(node_id).astype(np.int64),
+        node_ndof=np.concatenate(node_ndof),
+        node_p=np.concatenate(node_p),
+        node_kind=np.concatenate(node_kind),
+        elem_ptr=elem_ptr,
+        elem_node=np.concatenate(elem_node).astype(np.int64),
+        n_leaves=nl,
+        parent=parent,
+        generation=generation,
+        child_ptr=child_ptr,
+        child_idx=child_idx,
+        elem_m=elem_m,
+        mat_off=mat_off,
+        mats=np.concatenate(mats),
+        n_rhs=n_rhs,
+        rhs_off=rhs_off,
+        rhs=np.concatenate(rhs),
+        symmetric=sym,
+        info=dict(forest=len(specs), parts=parts, n_rhs=n_rhs),
+    )
+
+
+def batch3d(n_meshes: int, seed: int = 0, n_range=(8, 20), p_range=(2, 6), n_rhs: int = 16):
+    """The batched workload: independent 3D Poisson meshes with n uniform in
+    ``n_range`` (hexes per side) and p uniform in ``p_range``, ``n_rhs``
+    i.i.d. N(0,1) right-hand sides each, all drawn from ``seed``.  Returns
+    the list of specs (join them with :func:`forest`)."""
+    rng = np.random.default_rng(seed + 104729)
+    out = []
+    for k in range(n_meshes):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        p = int(rng.integers(p_range[0], p_range[1] + 1))
+        out.append(poisson3d(n, p, seed=seed * 100003 + k, n_rhs=n_rhs))
+    return out
