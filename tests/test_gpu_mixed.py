@@ -27,6 +27,7 @@ def _mixed(spec, method, prec, tol=TOL):
     ("2d_16_p4", lambda: hpfem.poisson2d(16, 4, seed=22), uo.CHOL),
     ("diff_6_p3_c1e4", lambda: hpfem.diffusion3d(6, 3, seed=23, merges=[3, 2]), uo.CHOL),
     ("cd_4_p3", lambda: hpfem.convdiff3d(4, 3, seed=24), uo.LU_PIV),
+    ("cd_12_p3_tall", lambda: hpfem.convdiff3d(12, 3, seed=25), uo.LU_PIV),
 ])
 def test_mixed_refines_to_fp64(native_lib, name, make, method, prec):
     spec = make()

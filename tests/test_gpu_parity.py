@@ -32,7 +32,12 @@ CASES = [
     ("cd_4_p3_lupiv", lambda: hpfem.convdiff3d(4, 3, seed=6), uo.LU_PIV),
     ("cd_6_p3_lupiv", lambda: hpfem.convdiff3d(6, 3, seed=7, merges=[3, 2]), uo.LU_PIV),
     ("cd_4_p2_lunopiv", lambda: hpfem.convdiff3d(4, 2, seed=8, pe=1.0), uo.LU_NOPIV),
+    # root front 6938 rows: LU panels on many CTAs (cooperative launch) + row interchanges
+    ("cd_12_p3_lupiv_tall", lambda: hpfem.convdiff3d(12, 3, seed=14), uo.LU_PIV),
     ("3d_4_p3_rhs4", lambda: hpfem.poisson3d(4, 3, seed=9, n_rhs=4), uo.CHOL),
+    # 16 right-hand sides through the flag-driven solves of the large fronts (four launches of four)
+    ("3d_8_p4_rhs16", lambda: hpfem.poisson3d(8, 4, seed=12, n_rhs=16), uo.CHOL),
+    ("3d_6_p3_rhs7", lambda: hpfem.poisson3d(6, 3, seed=13, n_rhs=7), uo.CHOL),
     ("diff_4_varp", lambda: hpfem.build_mesh(3, 4, np.random.default_rng(3).integers(2, 6, 64),
                                               seed=10), uo.CHOL),
 ]

@@ -278,8 +278,8 @@ class Mesh:
     OP_NAMES = ["assemble", "small_factor", "potrf_diag", "trsm_panel", "syrk_update",
                 "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
                 "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
-                "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags"] + \
-               [f"op{k}" for k in range(21, 32)]
+                "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
+                "laswp"] + [f"op{k}" for k in range(23, 32)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))

@@ -18,6 +18,7 @@ using namespace uhm_gpu;
 static constexpr int SMALL_MAX_F64 = 160;   // whole front in shared memory (200 KB)
 static constexpr int SMALL_MAX_F32 = 224;
 static constexpr int NB = 64;               // panel width of the blocked kernels
+static constexpr int GC_MIN_ROWS = 512;     // LU panels this tall run on many CTAs (k_getrf_coop)
 static constexpr int ASM_TJ = 16;           // assembly column tile (k_factor.cu)
 static constexpr int TRSM_RB = 64;
 static constexpr int FWD_RB = 256;            // k_solve.cu
@@ -77,6 +78,8 @@ void Engine::free_device() {
   d_err = nullptr;
   d_dof_tree = nullptr;
   d_tree_red = nullptr;
+  d_gc_xbuf = nullptr;
+  d_gc_ctr = nullptr;
   tree_bnorm.clear();
   tree_anorm.clear();
 }
@@ -535,6 +538,12 @@ void Engine::build_plan(int method) {
 void Engine::build_programs(int method) {
   const bool chol = method == UHM_CHOL;
   const int nr = mesh->n_rhs;
+  if (!n_sm) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    n_sm = std::max(1, n_sm);
+  }
   h_items.clear();
   fac_ops.clear();
   fwd_ops.clear();
@@ -633,7 +642,52 @@ void Engine::build_programs(int method) {
           push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
           push(fac_ops, OP_SYRK, dt, NB, 0, u_items, fu);
         } else {
-          push(fac_ops, OP_GETRF, dt, NB, method == UHM_LU_PIV ? 1 : 0, p_items, fp);
+          // tall panels (many rows below the diagonal) on many CTAs at once,
+          // the rest one CTA per front
+          const int piv = method == UHM_LU_PIV ? 1 : 0;
+          const int rcap = dt == F64 ? GC_RMAX_F64 : GC_RMAX_F32;
+          std::vector<Item> one, tall;
+          for (const Item& it : p_items)
+            (fronts[it.front].n - it.a >= GC_MIN_ROWS ? tall : one).push_back(it);
+          push(fac_ops, OP_GETRF, dt, NB, piv, one, tall.empty() ? fp : 0.0);
+          size_t i0 = 0;
+          while (i0 < tall.size()) {
+            // a group whose minimum CTA counts fit one cooperative launch
+            size_t i1 = i0;
+            int need = 0;
+            double rows_sum = 0;
+            while (i1 < tall.size()) {
+              const int rows = fronts[tall[i1].front].n - tall[i1].a;
+              const int mn = (rows + rcap - 1) / rcap;
+              if (i1 > i0 && need + mn > n_sm) break;
+              need += mn;
+              rows_sum += rows;
+              ++i1;
+            }
+            std::vector<Item> g;
+            int b = 0, rmax = 1;
+            const int spare = std::max(0, n_sm - need);
+            for (size_t i = i0; i < i1; ++i) {
+              const int rows = fronts[tall[i].front].n - tall[i].a;
+              int P = (rows + rcap - 1) / rcap + (int)(spare * (rows / rows_sum));
+              P = std::max(1, std::min(P, rows));
+              g.push_back(Item{tall[i].front, tall[i].a, b, P});
+              rmax = std::max(rmax, (rows + P - 1) / P);
+              b += P;
+            }
+            Op op{OP_GETRF_COOP, dt, NB, piv, add_items(g), (int)g.size()};
+            op.q0 = b;
+            op.aux = rmax;
+            if (i0 == 0) op.flops = fp;
+            fac_ops.push_back(op);
+            if (piv) {
+              std::vector<Item> sw;
+              for (const Item& it : g)
+                for (int c0 = 0; c0 < fronts[it.front].n; c0 += 256) sw.push_back(Item{it.front, it.a, c0, 0});
+              push(fac_ops, OP_LASWP, dt, NB, 0, sw);
+            }
+            i0 = i1;
+          }
           push(fac_ops, OP_LUROW, dt, NB, 0, t_items, ft);
           push(fac_ops, OP_GEMM, dt, NB, 0, u_items, fu);
         }
@@ -713,6 +767,7 @@ void Engine::build_programs(int method) {
     return mx <= 96 * 1024 ? (int)((mx + 15) / 16 * 16) : 0;
   };
   constexpr int GATHER_ROWS = 1024;   // rows per CTA of the forward gather (no pivots)
+  constexpr int NR_FLAGS_MAX = 16;    // right-hand sides taken by the flag-driven solves
   for (auto& lv : levels) {
     std::vector<Item> g_items;
     for (int s : lv) {
@@ -732,8 +787,9 @@ void Engine::build_programs(int method) {
         else large.push_back(s);
       }
       push(fwd_ops, OP_FWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
-      if (chol && nr <= 4 && !large.empty()) {
-        // one flag-driven launch for every large front of this level
+      if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
+        // one flag-driven launch for every large front of this level (per
+        // group of FLAG_NR right-hand sides)
         std::vector<Item> fi, ai;
         int maxb = 0;
         for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
@@ -751,8 +807,12 @@ void Engine::build_programs(int method) {
           f0 = std::min(f0, fronts[s].flag_off);
           f1 = std::max(f1, fronts[s].flag_off + (fronts[s].fs + NB - 1) / NB);
         }
-        Op op{OP_FWD_FLAGS, dt, f1 - f0, f0, add_items(fi), (int)fi.size()};
-        fwd_ops.push_back(op);
+        const int64_t io = add_items(fi);
+        for (int q0 = 0; q0 < nr; q0 += FLAG_NR) {
+          Op op{OP_FWD_FLAGS, dt, f1 - f0, f0, io, (int)fi.size()};
+          op.q0 = q0;
+          fwd_ops.push_back(op);
+        }
         large.clear();
       }
       int maxfs = 0;
@@ -784,7 +844,7 @@ void Engine::build_programs(int method) {
         else { large.push_back(s); st.push_back(Item{s, 0, 0, 0}); }
       }
       push(bwd_ops, OP_BWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
-      if (chol && nr <= 4 && !large.empty()) {
+      if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
         std::vector<Item> bi;
         int maxb = 0;
         for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
@@ -796,8 +856,12 @@ void Engine::build_programs(int method) {
           f0 = std::min(f0, fronts[s].flag_off);
           f1 = std::max(f1, fronts[s].flag_off + (fronts[s].fs + NB - 1) / NB);
         }
-        Op op{OP_BWD_FLAGS, dt, f1 - f0, f0, add_items(bi), (int)bi.size()};
-        bwd_ops.push_back(op);
+        const int64_t io = add_items(bi);
+        for (int q0 = 0; q0 < nr; q0 += (dt == F64 ? FLAG_NR_BWD_F64 : FLAG_NR)) {
+          Op op{OP_BWD_FLAGS, dt, f1 - f0, f0, io, (int)bi.size()};
+          op.q0 = q0;
+          bwd_ops.push_back(op);
+        }
         large.clear();
       }
       int maxfs = 0;
@@ -860,6 +924,10 @@ void Engine::alloc_device(int method) {
   d_items = (Item*)dmalloc(sizeof(Item) * std::max<size_t>(1, h_items.size()));
   d_err = (int*)dmalloc(sizeof(int));
   CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+  if (method != UHM_CHOL) {
+    d_gc_xbuf = (double*)dmalloc(sizeof(double) * (size_t)std::max(1, n_sm) * (2 * 66 + 2 * 64));
+    d_gc_ctr = (unsigned int*)dmalloc(2 * sizeof(unsigned int));
+  }
   if (ws_total > 0) {
     // one extra row block so tiles that run past the last part stay inside the tensor
     d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * TC_NBO));
@@ -1047,10 +1115,12 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
       case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
       case OP_FWD_FLAGS:
-        launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, stream);
+        launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                         stream);
         break;
       case OP_BWD_FLAGS:
-        launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, stream);
+        launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                         stream);
         break;
       case OP_TC_PACK:
         launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, stream);
@@ -1060,6 +1130,11 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
                        op.param == 3 ? TC_TERMS_BF16X6 : TC_TERMS_BF16X3, 1, d_err, stream);
         break;
       case OP_GETRF: launch_getrf_panel(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
+      case OP_GETRF_COOP:
+        launch_getrf_coop(ctx, it, op.n_items, op.q0, op.dtype, op.nb, op.param, op.aux, d_gc_xbuf, d_gc_ctr, d_err,
+                          stream);
+        break;
+      case OP_LASWP: launch_laswp(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
       case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
@@ -1141,7 +1216,7 @@ void Engine::factor(int method) {
   {
     int derr = 0;
     CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (derr) fail("a tensor-core kernel gave up waiting (bounded wait expired)", 14);
+    if (derr) fail("a kernel gave up waiting (bounded wait expired)", 14);
   }
   if (status && mode == 1) {
     // a low-precision front broke down: escalate the failed fronts to FP64

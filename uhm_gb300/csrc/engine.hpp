@@ -59,6 +59,8 @@ struct Op {
   int n_items;
   double flops = 0;   // algorithmic flops of this launch (LAWN-41 terms)
   double bytes = 0;   // algorithmic HBM bytes of this launch
+  int q0 = 0;         // first right-hand side (flag-driven solves) / CTAs (cooperative LU panel)
+  int aux = 0;        // rows per CTA (cooperative LU panel)
 };
 
 constexpr int N_OP_KINDS = 32;
@@ -70,7 +72,8 @@ struct OpProfile {
 enum OpKind : int {
   OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
-  OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_KIND_END
+  OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
+  OP_LASWP, OP_KIND_END
 };
 static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
 
@@ -194,6 +197,9 @@ class Engine {
   int64_t* d_ws_stride = nullptr;
   CUtensorMap ws_map;                // one map over the whole BF16 workspace
   int* d_err = nullptr;              // bounded-wait error flag of device kernels
+  double* d_gc_xbuf = nullptr;       // exchange buffer of the cooperative LU panel
+  unsigned int* d_gc_ctr = nullptr;  // its grid-barrier counter and abort word
+  int n_sm = 0;
   int64_t ws_total = 0;
   int64_t* d_emat_off = nullptr;
   int* d_elem_m = nullptr;

@@ -17,6 +17,7 @@
 // summation order onto a zeroed parent; no atomics, bitwise reproducible.
 #include <cstdio>
 #include <stdexcept>
+#include <string>
 #include "k_common.cuh"
 
 namespace uhm_gpu {
@@ -215,10 +216,11 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 //     independent, so this needs nothing from other warps but v_p.
 // The owner of column p+1 publishes it as soon as it has applied column p.
 // A hand-off inside a warp needs only __syncwarp; a column published by
-// another warp is awaited on its own mbarrier (16 arrivals, one per
-// publishing lane; arrive releases, try_wait acquires) with an iteration
-// limit, after which the front is flagged (status ST_WAIT) and the block
-// gives up.  The 64-pivot chain thus runs at warp-synchronous speed except at
+// another warp is awaited on its own mbarrier: after the warp barrier that
+// orders the 16 publishing lanes' stores, lane 0 arrives (release) and one
+// lane of each consuming warp waits (acquire, then a warp barrier), with an
+// iteration limit after which the front is flagged (status ST_WAIT) and the
+// block gives up.  The 64-pivot chain thus runs at warp-synchronous speed except at
 // the 7 hand-offs between warps, and each warp overlaps its trailing updates
 // and its part of the inverse with the chain; a warp does only the factor
 // steps that reach its columns and only the inverse steps whose rows are
@@ -288,22 +290,34 @@ __device__ __forceinline__ bool pd_mbar_wait(uint32_t bar, volatile int* give_up
   return false;
 }
 
-template <typename T>
+// hand-off of a published column to the other warps
+enum PotrfHandoff : int { PD_BLOCK_BARRIER = 0, PD_MBARRIER = 1, PD_FLAG_SPIN = 2 };
+constexpr int PD_HANDOFF = PD_BLOCK_BARRIER;
+
+__device__ __forceinline__ int pd_ld_volatile(const int* p) {
+  int v;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(v) : "r"(pd_smem(p)) : "memory");
+  return v;
+}
+
+template <typename T, int HO>
 __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
   __shared__ __align__(16) T V[64][64];    // V[p][i]: column p of the reduced block (zero above p)
   __shared__ __align__(16) T XR[8][2][8];  // per warp: row p of its X block, scaled, double-buffered
   __shared__ T sd[64], srd[64];            // l_pp and 1 / l_pp
-  __shared__ __align__(8) unsigned long long mbar[64];   // column p published
+  __shared__ __align__(8) unsigned long long mbar[64];   // column p published (PD_MBARRIER)
+  __shared__ int pflag[64];                               // column p published (PD_FLAG_SPIN)
   __shared__ int s_give_up;
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  const int tid = threadIdx.x, w = tid >> 5;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
   const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
-  if (tid < 64) pd_mbar_init(pd_smem(&mbar[tid]), 16);
+  if (HO == PD_MBARRIER && tid < 64) pd_mbar_init(pd_smem(&mbar[tid]), 1);
+  if (HO == PD_FLAG_SPIN && tid < 64) pflag[tid] = 0;
   if (tid == 0) s_give_up = 0;
   {
     // stage the lower triangle (coalesced column reads, all loads in flight
@@ -337,8 +351,22 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int p = 4 * q + s;
-      if (p > 0 && (p >> 3) != w && !gave_up)
-        gave_up = !pd_mbar_wait(pd_smem(&mbar[p]), &s_give_up);
+      if (HO != PD_BLOCK_BARRIER && p > 0 && (p >> 3) != w) {
+        // one lane waits (acquire), the warp barrier passes the ordering on
+        int ok = 1;
+        if (lane == 0 && !gave_up) {
+          if (HO == PD_MBARRIER) {
+            ok = pd_mbar_wait(pd_smem(&mbar[p]), &s_give_up);
+          } else {
+            ok = 0;
+            for (uint32_t i = 0; i < PD_WAIT_LIMIT; ++i)
+              if (pd_ld_volatile(&pflag[p])) { ok = 1; break; }
+            __threadfence_block();
+          }
+        }
+        __syncwarp();
+        gave_up = gave_up || !__shfl_sync(0xffffffffu, ok, 0);
+      }
       T piv = V[p][p];
       if (!(piv > T(0))) { bad = true; piv = T(1); }
       T d, rd;
@@ -364,9 +392,13 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
 #pragma unroll
             for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
             Vec4<T>::st(&V[p + 1][r0], wv);
-            pd_mbar_arrive(pd_smem(&mbar[p + 1]));
           }
-          __syncwarp();
+          __syncwarp();   // the column is visible to the warp; one lane releases it to the others
+          if (HO == PD_MBARRIER && lane == 0) pd_mbar_arrive(pd_smem(&mbar[p + 1]));
+          if (HO == PD_FLAG_SPIN && lane == 0) {
+            __threadfence_block();
+            *(volatile int*)&pflag[p + 1] = 1;
+          }
         }
       }
       if (p >= cb0) {
@@ -385,6 +417,7 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
           for (int v = 0; v < 4; ++v) x[u][v] -= l * xr[v];
         }
       }
+      if (HO == PD_BLOCK_BARRIER) __syncthreads();
     }
   }
   if (gave_up) set_status(c, it.front, ST_WAIT);
@@ -414,9 +447,9 @@ void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtyp
   if (!n_items) return;
   if (nb > 64) throw std::invalid_argument("potrf_diag: block wider than 64");
   if (dtype == F64)
-    k_potrf_diag<double><<<n_items, 256, 0, s>>>(c, items, nb);
+    k_potrf_diag<double, PD_HANDOFF><<<n_items, 256, 0, s>>>(c, items, nb);
   else
-    k_potrf_diag<float><<<n_items, 256, 0, s>>>(c, items, nb);
+    k_potrf_diag<float, PD_HANDOFF><<<n_items, 256, 0, s>>>(c, items, nb);
 }
 
 constexpr int TRSM_RB = 64;   // rows per panel-TRSM block
@@ -696,6 +729,257 @@ void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dty
   if (!n_items) return;
   if (dtype == F64) k_getrf_panel<double, 512><<<n_items, 512, 0, s>>>(c, items, nb, pivot);
   else k_getrf_panel<float, 512><<<n_items, 512, 0, s>>>(c, items, nb, pivot);
+}
+
+// ---------------------------------------------------------------------------
+// LU panel of a tall front on many CTAs (cooperative launch)
+// ---------------------------------------------------------------------------
+// The panel (rows k0..n-1, columns k0..k0+kb-1) of each item is split into
+// row chunks of R rows, one per CTA, held in shared memory (column-major,
+// leading dimension R).  For each column k of the panel, every CTA
+//   1. finds its candidate pivot: the largest |a| in column k among its rows
+//      in [k0+k, fs) (the reference searches the eliminated rows only), ties
+//      to the lowest row, and publishes value, row and the row's kb values
+//      in the exchange buffer; the CTA holding row k0+k also publishes that
+//      row;
+//   2. passes one grid barrier (the exchange buffers alternate by column
+//      parity, so a barrier per column is enough);
+//   3. picks the item's pivot from all its CTAs' candidates (same rule: the
+//      largest value, the lowest row on ties; this is the first maximum of a
+//      sequential search), swaps the two rows in its chunk when it holds
+//      them, and applies l_r = a_rk / a_kk, a_rj -= l_r u_j to its rows below
+//      the pivot row.
+// The result is the reference's partial pivoting (FLA_LU_piv inside the
+// eliminated block) exactly; only the panel's own columns are swapped here,
+// the other columns of the front by k_laswp afterwards.  Item: front,
+// a = k0, b = first CTA, c = number of CTAs.  The grid barrier is an arrival
+// counter with a bounded spin; a CTA that gives up raises the abort word and
+// the error flag, and every CTA then skips the remaining barriers.
+constexpr int GC_THREADS = 256;
+
+__device__ __forceinline__ unsigned int gc_ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// barrier number `round` (1, 2, ...) of a launch of `total` CTAs; false once
+// any CTA gave up
+__device__ __forceinline__ bool gc_grid_barrier(unsigned int* ctr, unsigned int round, unsigned int total,
+                                                int* err, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = *s_ok != 0;
+    if (ok) {
+      __threadfence();
+      atomicAdd(ctr, 1u);
+      const unsigned int target = round * total;
+      ok = false;
+      for (uint32_t i = 0; i < (1u << 22); ++i) {
+        if (gc_ld_acquire(ctr) >= target) { ok = true; break; }
+        if (gc_ld_acquire(ctr + 1)) break;          // another CTA gave up
+        __nanosleep(20);
+      }
+      if (!ok) {
+        atomicExch(ctr + 1, 1u);
+        atomicExch(err, 3);
+      }
+      __threadfence();
+    }
+    *s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(GC_THREADS) k_getrf_coop(DevCtx c, const Item* __restrict__ items, int n_items,
+                                                           int nb, int pivot, int rmax, double* __restrict__ xbuf,
+                                                           unsigned int* ctr, int* err) {
+  extern __shared__ __align__(16) unsigned char gc_smem[];
+  T* S = reinterpret_cast<T*>(gc_smem);        // chunk, column-major, leading dimension R
+  __shared__ T s_u[64], s_old[64];
+  __shared__ double s_cv[GC_THREADS / 32];
+  __shared__ int s_ci[GC_THREADS / 32];
+  __shared__ int s_ok, s_item, s_p, s_w;
+  const unsigned int total = gridDim.x;
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    int k = 0;
+    while (k + 1 < n_items && (int)blockIdx.x >= items[k + 1].b) ++k;
+    s_item = k;
+  }
+  __syncthreads();
+  const Item it = items[s_item];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, k0 = it.a;
+  const int kb = min(nb, fs - k0);
+  const int P = it.c, q = blockIdx.x - it.b;
+  const int rows = n - k0;
+  const int R = (rows + P - 1) / P;
+  const int rbeg = k0 + q * R, rend = min(rbeg + R, n);   // my rows [rbeg, rend)
+  const int nr_my = max(0, rend - rbeg);
+  T* __restrict__ G = arena<T>(c) + f.off;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // exchange buffer: per parity, per CTA {value, row, kb values}, then per item the row k0+k
+  constexpr int XS = 66;
+  auto cand = [&](int par, int b) { return xbuf + ((size_t)par * total + b) * XS; };
+  auto diag_row = [&](int par, int itx) { return xbuf + (size_t)2 * total * XS + ((size_t)par * n_items + itx) * 64; };
+  for (int idx = threadIdx.x; idx < nr_my * kb; idx += GC_THREADS) {
+    const int r = idx % nr_my, j = idx / nr_my;
+    S[j * rmax + r] = G[(rbeg + r) + (int64_t)(k0 + j) * n];
+  }
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    const int gk = k0 + k, par = k & 1;
+    // 1. candidate of this chunk
+    double bv = -1.0;
+    int bi = 0x7fffffff;
+    if (pivot) {
+      const int lo = max(rbeg, gk), hi = min(rend, fs);
+      for (int r = lo + threadIdx.x; r < hi; r += GC_THREADS) {
+        const double v = (double)my_abs<T>(S[k * rmax + (r - rbeg)]);
+        if (v > bv) { bv = v; bi = r; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (lane == 0) { s_cv[warp] = bv; s_ci[warp] = bi; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int w = 1; w < GC_THREADS / 32; ++w)
+          if (s_cv[w] > bv || (s_cv[w] == bv && s_ci[w] < bi)) { bv = s_cv[w]; bi = s_ci[w]; }
+        s_ci[0] = bi;
+        double* cb = cand(par, blockIdx.x);
+        cb[0] = bv;
+        cb[1] = (double)bi;
+      }
+      __syncthreads();
+      bi = s_ci[0];
+      if (bi != 0x7fffffff && threadIdx.x < kb) cand(par, blockIdx.x)[2 + threadIdx.x] = (double)S[threadIdx.x * rmax + (bi - rbeg)];
+    }
+    if (gk >= rbeg && gk < rend && threadIdx.x < kb)
+      diag_row(par, s_item)[threadIdx.x] = (double)S[threadIdx.x * rmax + (gk - rbeg)];
+    // 2. one grid barrier per column
+    if (!gc_grid_barrier(ctr, (unsigned int)(k + 1), total, err, &s_ok)) return;
+    // 3. the item's pivot
+    if (warp == 0) {
+      double v = -1.0;
+      int r = 0x7fffffff, w = -1;
+      if (pivot) {
+        for (int b = lane; b < P; b += 32) {
+          const double* cb = cand(par, it.b + b);
+          const double cv = __ldcg(cb);
+          const int ci = (int)__ldcg(cb + 1);
+          if (cv > v || (cv == v && ci < r)) { v = cv; r = ci; w = it.b + b; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const double ov = __shfl_down_sync(0xffffffffu, v, o);
+          const int oi = __shfl_down_sync(0xffffffffu, r, o);
+          const int ow = __shfl_down_sync(0xffffffffu, w, o);
+          if (ov > v || (ov == v && oi < r)) { v = ov; r = oi; w = ow; }
+        }
+      }
+      if (lane == 0) {
+        if (!pivot || r == 0x7fffffff) { r = gk; w = -1; }
+        s_p = r;
+        s_w = w;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (threadIdx.x < kb) {
+      const double* dr = diag_row(par, s_item);
+      s_old[threadIdx.x] = (T)__ldcg(dr + threadIdx.x);                        // old row gk
+      s_u[threadIdx.x] = p == gk ? s_old[threadIdx.x] : (T)__ldcg(cand(par, s_w) + 2 + threadIdx.x);
+    }
+    __syncthreads();
+    if (threadIdx.x < kb) {
+      if (gk >= rbeg && gk < rend) S[threadIdx.x * rmax + (gk - rbeg)] = s_u[threadIdx.x];
+      if (p != gk && p >= rbeg && p < rend) S[threadIdx.x * rmax + (p - rbeg)] = s_old[threadIdx.x];
+    }
+    if (q == 0 && threadIdx.x == 0) c.piv[f.piv_off + gk] = p;
+    __syncthreads();
+    T akk = s_u[k];
+    if (akk == (T)0 || akk != akk) {
+      if (q == 0 && threadIdx.x == 0) set_status(c, it.front, akk != akk ? ST_NAN : ST_ZERO_PIVOT);
+      akk = (T)1;
+    }
+    const T rinv = (T)1 / akk;
+    // rows below the pivot row: multiplier and rank-1 update of the panel's later columns
+    for (int r = max(rbeg, gk + 1) + threadIdx.x; r < rend; r += GC_THREADS) {
+      const int rl = r - rbeg;
+      const T l = S[k * rmax + rl] * rinv;
+      S[k * rmax + rl] = l;
+      for (int j = k + 1; j < kb; ++j) S[j * rmax + rl] -= l * s_u[j];
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < nr_my * kb; idx += GC_THREADS) {
+    const int r = idx % nr_my, j = idx / nr_my;
+    G[(rbeg + r) + (int64_t)(k0 + j) * n] = S[j * rmax + r];
+  }
+}
+
+void launch_getrf_coop(const DevCtx& c, const Item* items, int n_items, int n_ctas, int dtype, int nb, int pivot,
+                       int rmax, double* xbuf, unsigned int* ctr, int* err, cudaStream_t s) {
+  if (!n_items) return;
+  if (nb > 64) throw std::invalid_argument("getrf_coop: panel wider than 64");
+  cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned int), s);
+  const size_t smem = (size_t)rmax * nb * (dtype == F64 ? sizeof(double) : sizeof(float));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n_ctas);
+  cfg.blockDim = dim3(GC_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
+  if (dtype == F64) {
+    cudaFuncSetAttribute(k_getrf_coop<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaLaunchKernelEx(&cfg, k_getrf_coop<double>, c, items, n_items, nb, pivot, rmax, xbuf, ctr, err);
+  } else {
+    cudaFuncSetAttribute(k_getrf_coop<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaLaunchKernelEx(&cfg, k_getrf_coop<float>, c, items, n_items, nb, pivot, rmax, xbuf, ctr, err);
+  }
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("cooperative LU panel launch failed: ") + cudaGetErrorString(e));
+}
+
+// Row interchanges of a panel (pivots of rows k0..k0+kb-1, applied in order)
+// on the front's columns outside the panel.  Item: front, a = k0, b = first
+// column of a 256-column chunk; one thread per column.
+template <typename T>
+__global__ void __launch_bounds__(256) k_laswp(DevCtx c, const Item* __restrict__ items, int nb) {
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, k0 = it.a;
+  const int kb = min(nb, f.fs - k0);
+  const int j = it.b + threadIdx.x;
+  if (j >= n || (j >= k0 && j < k0 + kb)) return;
+  T* __restrict__ col = arena<T>(c) + f.off + (int64_t)j * n;
+  const int32_t* __restrict__ pv = c.piv + f.piv_off;
+  for (int k = k0; k < k0 + kb; ++k) {
+    const int p = pv[k];
+    if (p != k) {
+      const T t = col[k];
+      col[k] = col[p];
+      col[p] = t;
+    }
+  }
+}
+
+void launch_laswp(const DevCtx& c, const Item* items, int n_items, int dtype, int nb, cudaStream_t s) {
+  if (!n_items) return;
+  if (dtype == F64) k_laswp<double><<<n_items, 256, 0, s>>>(c, items, nb);
+  else k_laswp<float><<<n_items, 256, 0, s>>>(c, items, nb);
 }
 
 constexpr int LUROW_CB = 64;   // columns per row-panel block

@@ -757,7 +757,7 @@ namespace uhm_gpu {
 // with L_bb^{-1} precomputed at factorisation (64 x 64, dinv arenas).
 // ===========================================================================
 constexpr int FB = 64;
-constexpr int SF_NR = 4;          // right-hand sides handled by these kernels
+constexpr int SF_NR = FLAG_NR;    // right-hand sides handled by one launch
 
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
   int v;
@@ -811,10 +811,11 @@ template <typename T> __device__ __forceinline__ const T* dinv_arena(const DevCt
 template <> __device__ __forceinline__ const double* dinv_arena<double>(const DevCtx& c) { return c.dinv64; }
 template <> __device__ __forceinline__ const float* dinv_arena<float>(const DevCtx& c) { return c.dinv32; }
 
-// item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..)
+// item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
+// right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
 template <typename T>
 __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
-                                                   int* ticket, int* err) {
+                                                   int* ticket, int* err, int q0) {
   using CT = T;
   __shared__ int s_t;
   __shared__ CT red[4][FB][SF_NR];
@@ -844,7 +845,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) {
     acc[q] = CT(0);
-    zr[q] = (rv && q < nr && g == 0) ? (CT)z[row + (int64_t)q * n] : CT(0);   // before any wait
+    zr[q] = (rv && q0 + q < nr && g == 0) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);   // before any wait
   }
   const int jend = factor_block ? b : nfb;
   __shared__ int s_ready;
@@ -871,8 +872,8 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
     for (int j = done; j < upto; ++j) {
       const int kbj = min(FB, fs - j * FB);
       if (threadIdx.x < 32) {
-        for (int q = 0; q < nr && q < SF_NR; ++q) {
-          const double* yj = y + j * FB + (int64_t)q * n;
+        for (int q = 0; q < SF_NR && q0 + q < nr; ++q) {
+          const double* yj = y + j * FB + (int64_t)(q0 + q) * n;
           for (int cc = threadIdx.x; cc < FB; cc += 32) ysh[q][cc] = cc < kbj ? (CT)__ldcg(yj + cc) : CT(0);
         }
       }
@@ -885,7 +886,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
       for (int u = 0; u < 16; ++u) {
 #pragma unroll
         for (int q = 0; q < SF_NR; ++q)
-          if (q < nr) acc[q] += cur[u] * ysh[q][g * 16 + u];
+          if (q0 + q < nr) acc[q] += cur[u] * ysh[q][g * 16 + u];
       }
       __syncthreads();
     }
@@ -897,7 +898,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   if (threadIdx.x < FB) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      v[i][q] = (rv && q < nr) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
+      v[i][q] = (rv && q0 + q < nr) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
   }
   __syncthreads();
   if (factor_block) {
@@ -913,7 +914,7 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
       }
 #pragma unroll
       for (int q = 0; q < SF_NR; ++q)
-        if (q < nr) y[row + (int64_t)q * n] = (double)x[q];
+        if (q0 + q < nr) y[row + (int64_t)(q0 + q) * n] = (double)x[q];
     }
     __threadfence();
     __syncthreads();
@@ -921,19 +922,22 @@ __global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restr
   } else if (threadIdx.x < FB && rv) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      if (q < nr) z[row + (int64_t)q * n] = (double)v[i][q];
+      if (q0 + q < nr) z[row + (int64_t)(q0 + q) * n] = (double)v[i][q];
   }
 }
 
-// item: front, a = factor block index, tickets in descending block order
-template <typename T>
+// item: front, a = factor block index, tickets in descending block order;
+// right-hand sides q0 .. q0+NQ-1, accumulated in the same pass over the
+// factor tiles (a pass per right-hand side would put NQ-1 un-overlapped
+// re-reads of the whole block column on the chain of hand-offs)
+template <typename T, int NQ>
 __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restrict__ items,
-                                                   int* ticket, int* err) {
+                                                   int* ticket, int* err, int q0) {
   using CT = T;
   __shared__ int s_t;
   extern __shared__ __align__(16) unsigned char bwd_dyn[];
   CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(bwd_dyn);   // [row lane][column]
-  __shared__ CT v[FB][SF_NR];
+  __shared__ CT v[FB][NQ];
   __shared__ int s_ready;
   __shared__ T dsh[FB * (FB + 1)];
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
@@ -951,81 +955,94 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
   const int* __restrict__ flg = c.flags + f.flag_off;
   const int rl = threadIdx.x % FB, g = threadIdx.x / FB;   // row lane, column group
-  for (int q = 0; q < nr && q < SF_NR; ++q) {
-    CT acc[16];
+  CT acc[NQ][16];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) acc[u] = CT(0);
-    // rows below block b: the ABL part (known) first, two row blocks per
-    // round with all loads issued before the arithmetic, then factor blocks
-    // from the last one down (they complete in that order)
-    for (int rs = fs; rs < n; rs += 2 * FB) {
-      CT xr[2], gv[2][16];
+  for (int q = 0; q < NQ; ++q)
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int r = rs + h * FB + rl;
-        xr[h] = r < n ? (CT)y[r + (int64_t)q * n] : CT(0);
+    for (int u = 0; u < 16; ++u) acc[q][u] = CT(0);
+  // rows below block b: the ABL part (known) first, two row blocks per
+  // round with all loads issued before the arithmetic, then factor blocks
+  // from the last one down (they complete in that order)
+  for (int rs = fs; rs < n; rs += 2 * FB) {
+    CT xr[2][NQ], gv[2][16];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int cc = g * 16 + u;
-          gv[h][u] = (r < n && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
-        }
-      }
+    for (int h = 0; h < 2; ++h) {
+      const int r = rs + h * FB + rl;
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int u = 0; u < 16; ++u) acc[u] += gv[h][u] * xr[h];
-    }
-    // the factor tile of row block j does not depend on any flag: loaded one
-    // block ahead, so that only the load of x_j follows the wait
-    CT tile[16];
-    auto load_tile = [&](int j) {
-      const int r = j * FB + rl;
-      const bool in = r < min(j * FB + FB, fs);
+      for (int q = 0; q < NQ; ++q) xr[h][q] = (r < n && q0 + q < nr) ? (CT)y[r + (int64_t)(q0 + q) * n] : CT(0);
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int cc = g * 16 + u;
-        tile[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
+        gv[h][u] = (r < n && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
       }
-    };
-    int next = nfb - 1;
-    if (next > b) load_tile(next);
-    while (next > b) {
-      ready_range(flg, next, b, -1, &s_ready, err);
-      const int stop = s_ready;
-      for (int j = next; j > stop; --j) {
-        CT cur[16];
-#pragma unroll
-        for (int u = 0; u < 16; ++u) cur[u] = tile[u];
-        if (j - 1 > b) load_tile(j - 1);
-        const int r = j * FB + rl;
-        const bool in = r < min(j * FB + FB, fs);
-        if (in) {
-          const CT xr = (CT)__ldcg(y + r + (int64_t)q * n);   // one distinct value per lane
-#pragma unroll
-          for (int u = 0; u < 16; ++u) acc[u] += cur[u] * xr;
-        }
-      }
-      next = stop;
-      __syncthreads();
     }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q][u] += gv[h][u] * xr[h][q];
+  }
+  // the factor tile of row block j does not depend on any flag: loaded one
+  // block ahead, so that only the loads of x_j follow the wait
+  CT tile[16];
+  auto load_tile = [&](int j) {
+    const int r = j * FB + rl;
+    const bool in = r < min(j * FB + FB, fs);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int cc = g * 16 + u;
+      tile[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
+    }
+  };
+  int next = nfb - 1;
+  if (next > b) load_tile(next);
+  while (next > b) {
+    ready_range(flg, next, b, -1, &s_ready, err);
+    const int stop = s_ready;
+    for (int j = next; j > stop; --j) {
+      CT cur[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+      if (j - 1 > b) load_tile(j - 1);
+      const int r = j * FB + rl;
+      const bool in = r < min(j * FB + FB, fs);
+      if (in) {
+        CT xr[NQ];   // one distinct value per lane and right-hand side
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) xr[q] = q0 + q < nr ? (CT)__ldcg(y + r + (int64_t)(q0 + q) * n) : CT(0);
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) acc[q][u] += cur[u] * xr[q];
+      }
+    }
+    next = stop;
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
     __syncthreads();
 #pragma unroll
-    for (int u = 0; u < 16; ++u) red[rl][g * 16 + u] = acc[u];
+    for (int u = 0; u < 16; ++u) red[rl][g * 16 + u] = acc[q][u];
     __syncthreads();
     if (threadIdx.x < FB) {
       CT s = CT(0);
       for (int r = 0; r < FB; ++r) s += red[r][threadIdx.x];
-      v[threadIdx.x][q] = threadIdx.x < kb ? (CT)y[c0 + threadIdx.x + (int64_t)q * n] - s : CT(0);
+      v[threadIdx.x][q] = (threadIdx.x < kb && q0 + q < nr)
+                              ? (CT)y[c0 + threadIdx.x + (int64_t)(q0 + q) * n] - s : CT(0);
     }
   }
   __syncthreads();
   // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t   (column i of Dinv, staged at start)
   if (threadIdx.x < kb) {
     const int ii = threadIdx.x;
-    for (int q = 0; q < nr && q < SF_NR; ++q) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      if (q0 + q >= nr) break;
       CT x = CT(0);
       for (int t = ii; t < kb; ++t) x += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
-      y[c0 + ii + (int64_t)q * n] = (double)x;
+      y[c0 + ii + (int64_t)(q0 + q) * n] = (double)x;
     }
   }
   __threadfence();
@@ -1034,28 +1051,41 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
 }
 
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
-                      int* flag_base, int n_flags, int* err, cudaStream_t s) {
+                      int* flag_base, int n_flags, int* err, int q0, cudaStream_t s) {
   if (!n_items) return;
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
   cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
-  if (dtype == F64) k_fwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err);
-  else k_fwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err);
+  if (dtype == F64) k_fwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+  else k_fwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+}
+
+template <typename T, int NQ>
+static void bwd_flags_nq(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                         cudaStream_t s) {
+  const size_t dyn = sizeof(T) * FB * (FB + 1);
+  cudaFuncSetAttribute(k_bwd_flags<T, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  k_bwd_flags<T, NQ><<<n_items, 256, dyn, s>>>(c, items, ticket, err, q0);
+}
+
+template <typename T>
+static void bwd_flags_t(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                        int nq, cudaStream_t s) {
+  if (nq >= 4) bwd_flags_nq<T, 4>(c, items, n_items, ticket, err, q0, s);
+  else if (nq >= 2) bwd_flags_nq<T, 2>(c, items, n_items, ticket, err, q0, s);
+  else bwd_flags_nq<T, 1>(c, items, n_items, ticket, err, q0, s);
 }
 
 void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
-                      int* flag_base, int n_flags, int* err, cudaStream_t s) {
+                      int* flag_base, int n_flags, int* err, int q0, cudaStream_t s) {
   if (!n_items) return;
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
   cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
-  if (dtype == F64) {
-    const size_t dyn = sizeof(double) * FB * (FB + 1);
-    cudaFuncSetAttribute(k_bwd_flags<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    k_bwd_flags<double><<<n_items, 256, dyn, s>>>(c, items, ticket, err);
-  } else {
-    const size_t dyn = sizeof(float) * FB * (FB + 1);
-    cudaFuncSetAttribute(k_bwd_flags<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    k_bwd_flags<float><<<n_items, 256, dyn, s>>>(c, items, ticket, err);
-  }
+  // right-hand sides of this launch: FLAG_NR, or FLAG_NR_BWD_F64 in FP64
+  // (register budget of the NQ x 16 accumulators)
+  const int grp = dtype == F64 ? FLAG_NR_BWD_F64 : FLAG_NR;
+  const int nq = c.n_rhs - q0 < grp ? c.n_rhs - q0 : grp;
+  if (dtype == F64) bwd_flags_t<double>(c, items, n_items, ticket, err, q0, nq, s);
+  else bwd_flags_t<float>(c, items, n_items, ticket, err, q0, nq, s);
 }
 
 }  // namespace uhm_gpu

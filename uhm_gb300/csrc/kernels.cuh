@@ -83,6 +83,14 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
 void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         int nbo, cudaStream_t s);
 // LU (partial pivoting restricted to the factor rows, or none)
+// LU panel of tall fronts on many CTAs (cooperative launch of n_ctas CTAs;
+// item: front, a = k0, b = first CTA, c = CTAs; rmax = rows per CTA, at
+// most GC_RMAX_F64 / GC_RMAX_F32), then the panel's row interchanges on the
+// other columns (item: front, a = k0, b = first column of 256)
+constexpr int GC_RMAX_F64 = 384, GC_RMAX_F32 = 768;
+void launch_getrf_coop(const DevCtx& c, const Item* items, int n_items, int n_ctas, int dtype, int nb, int pivot,
+                       int rmax, double* xbuf, unsigned int* ctr, int* err, cudaStream_t s);
+void launch_laswp(const DevCtx& c, const Item* items, int n_items, int dtype, int nb, cudaStream_t s);
 void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                         int pivot, cudaStream_t s);
 void launch_lu_row_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
@@ -97,12 +105,15 @@ void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype
                       int staged_bytes, cudaStream_t s);
 void launch_bwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                       double* g, int64_t ldg, int staged_bytes, cudaStream_t s);
-// flag-driven level solves of large Cholesky fronts (one launch per level):
-// items ordered so that every CTA waits only on CTAs with smaller tickets
+// flag-driven level solves of large Cholesky fronts (one launch per level and
+// group of FLAG_NR right-hand sides, starting at column q0): items ordered so
+// that every CTA waits only on CTAs with smaller tickets
+constexpr int FLAG_NR = 4;
+constexpr int FLAG_NR_BWD_F64 = 2;   // backward FP64 launches take two
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
-                      int* flag_base, int n_flags, int* err, cudaStream_t s);
+                      int* flag_base, int n_flags, int* err, int q0, cudaStream_t s);
 void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
-                      int* flag_base, int n_flags, int* err, cudaStream_t s);
+                      int* flag_base, int n_flags, int* err, int q0, cudaStream_t s);
 // blocked solve steps of large fronts (64-column diagonal blocks)
 void launch_fwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                      cudaStream_t s);
