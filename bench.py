@@ -36,8 +36,10 @@ METRIC = "factor+solve s at 16³ p=4: plain FP64 vs mixed+IR+learned, bwd err≤
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of its first
 # root-level launch on the 12^3 p=4 profiling case (trailing block above the
 # L2 size); scaled to the bench's launches by their algorithmic bytes
-TC_TRAFFIC_PER_ALG_BYTE = None
-TC_TRAFFIC_SOURCE = "not captured"
+TC_TRAFFIC_PER_ALG_BYTE = 0.916
+TC_TRAFFIC_SOURCE = ("ncu --set full, k_tc_syrk first root-level launch of 3D Poisson 12^3 p=4 "
+                     "(578.8 MB DRAM read+write for 632.0 MB algorithmic), scaled by algorithmic bytes; "
+                     "profiles/tc_syrk_bf16_poisson3d_12_p4_root.md")
 WORKLOAD = "3D Poisson 16^3 hex p=4 Legendre-hierarchic, Dirichlet, octree ND, Cholesky fronts, 1 RHS"
 
 

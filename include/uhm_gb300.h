@@ -143,6 +143,19 @@ int uhm_gpu_get_fronts(long* mesh, int n, int* elt_id, int* generation, int* fs,
 int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_factor,
                             int* n_schur);
 
+/* Kernel-selection thresholds (no counterpart in the reference, whose block
+ * size is a compile-time knob, UHM/include/uhm/const.hxx): values[0] whole-front
+ * shared-memory factorisation up to n (FP64, at most 160), values[1] the same
+ * for FP32 (at most 224), values[2] tensor-core BF16-split fronts from n,
+ * values[3] LU panels on many CTAs from this many rows below the diagonal.
+ * uhm_gpu_autotune times candidate values on this mesh (element matrices and
+ * right-hand sides copied in; reps factor+solve runs per candidate, the
+ * fastest kept) and leaves the mesh factored and solved with the choice;
+ * n_timed returns how many candidates were timed. */
+int uhm_gpu_set_tunables(long* mesh, const int* values);
+int uhm_gpu_get_tunables(long* mesh, int* values);
+int uhm_gpu_autotune(long* mesh, int method, int reps, int* n_timed);
+
 /* Learned per-front precision (uhm_gpu_set_mode default_prec = 4): a
  * 12 -> 64 -> 64 -> 3 MLP (classes 0 FP64, 1 FP32, 2 BF16-split) reads per-front
  * features computed from the element matrices and the tree and picks each

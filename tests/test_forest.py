@@ -65,3 +65,18 @@ def test_native_lock_of_forest_matches_oracle(native_lib):
     plan = uo.symbolic(f)
     assert np.array_equal(got, plan.fs_ss())
     assert m.get_n_dof() == f.n_dof()
+
+
+def test_ragged_nested_dissection_structure(native_lib):
+    """n = 7 has no exact 2/3/5 merge plan: ceiling halving 7 -> 4 -> 2 -> 1,
+    with parents of fewer than 8 children at the far faces; the native
+    symbolic phase must give the oracle's fronts."""
+    spec = hpfem.poisson3d(7, 2, seed=6)
+    assert spec.info["merges"] == [2, 2, 2]
+    kids = np.diff(spec.child_ptr)[spec.n_leaves:]
+    assert kids.min() == 1 and kids.max() == 8
+    m = api.load_spec(spec)
+    eid, _, fs, ss = m.fronts()
+    got = np.zeros((spec.n_elements, 2), np.int64)
+    got[eid] = np.stack([fs, ss], axis=1)
+    assert np.array_equal(got, uo.symbolic(spec).fs_ss())

@@ -29,6 +29,7 @@ CASES = [
     ("3d_4_p3", lambda: hpfem.poisson3d(4, 3, seed=3), uo.CHOL),
     ("3d_8_p4", lambda: hpfem.poisson3d(8, 4, seed=4), uo.CHOL),
     ("3d_6_p2_merge32", lambda: hpfem.poisson3d(6, 2, seed=5, merges=[3, 2]), uo.CHOL),
+    ("3d_7_p3_ragged", lambda: hpfem.poisson3d(7, 3, seed=15), uo.CHOL),
     ("cd_4_p3_lupiv", lambda: hpfem.convdiff3d(4, 3, seed=6), uo.LU_PIV),
     ("cd_6_p3_lupiv", lambda: hpfem.convdiff3d(6, 3, seed=7, merges=[3, 2]), uo.LU_PIV),
     ("cd_4_p2_lunopiv", lambda: hpfem.convdiff3d(4, 2, seed=8, pe=1.0), uo.LU_NOPIV),

@@ -74,3 +74,16 @@ def test_symbolic_matches_reference(native_lib, case):
     fd, fsv = m.estimate_cost(method, spec.n_rhs)
     assert fd == pytest.approx(g["flops"][0], rel=1e-14)
     assert fsv == pytest.approx(g["flops"][1], rel=1e-14)
+
+
+def test_tunables_round_trip_and_limits(native_lib):
+    m = api.Mesh()
+    assert m.tunables() == dict(small_max_f64=160, small_max_f32=224, tc_min_n=512, gc_min_rows=512)
+    m.set_tunables(tc_min_n=768, small_max_f32=128)
+    assert m.tunables()["tc_min_n"] == 768 and m.tunables()["small_max_f32"] == 128
+    # whole-front shared-memory kernels hold at most 160 (FP64) / 224 (FP32) rows
+    with pytest.raises(api.UHMError):
+        m.set_tunables(small_max_f64=161)
+    with pytest.raises(api.UHMError):
+        m.set_tunables(small_max_f32=225)
+    assert m.tunables()["small_max_f32"] == 128

@@ -92,6 +92,9 @@ def _declare(L):
     sig("uhm_gpu_host_free", [C.c_void_p])
     _f = C.c_float
     sig("uhm_gpu_set_selector", [_P(_l), _P(_f), _i], _i)
+    sig("uhm_gpu_set_tunables", [_P(_l), _P(_i)], _i)
+    sig("uhm_gpu_get_tunables", [_P(_l), _P(_i)], _i)
+    sig("uhm_gpu_autotune", [_P(_l), _i, _i, _P(_i)], _i)
     sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
     sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
     sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
@@ -334,6 +337,28 @@ class Mesh:
         return [(self.OP_NAMES[kind[i]], int(items[i]), float(ms[i])) for i in range(k)]
 
     # -- learned precision selector ------------------------------------------
+    # -- kernel-selection thresholds --------------------------------------------
+    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows")
+
+    def tunables(self) -> dict:
+        v = np.zeros(len(self.TUNABLES), np.int32)
+        self._check(self.L.uhm_gpu_get_tunables(C.byref(self.h), v.ctypes.data_as(_P(_i))))
+        return dict(zip(self.TUNABLES, v.tolist()))
+
+    def set_tunables(self, **kw):
+        cur = self.tunables()
+        cur.update(kw)
+        v = np.asarray([cur[k] for k in self.TUNABLES], np.int32)
+        self._check(self.L.uhm_gpu_set_tunables(C.byref(self.h), v.ctypes.data_as(_P(_i))))
+
+    def autotune(self, method=UHM_CHOL, reps=2) -> dict:
+        """Time candidate thresholds on this mesh and keep the fastest
+        (uhm_gpu_autotune); returns the chosen values and the number of
+        candidates timed."""
+        n = _i(0)
+        self._check(self.L.uhm_gpu_autotune(C.byref(self.h), method, reps, C.byref(n)))
+        return dict(self.tunables(), timed=n.value)
+
     def set_selector(self, params):
         a, p = _arr(params, np.float32, C.c_float)
         self._check(self.L.uhm_gpu_set_selector(C.byref(self.h), p, len(a)))

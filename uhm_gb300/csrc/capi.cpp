@@ -227,6 +227,18 @@ int uhm_gpu_get_op_log(long* mesh, int cap, int* kind, int* n_items, double* ms,
     }
   });
 }
+int uhm_gpu_set_tunables(long* mesh, const int* values) {
+  return guard(M(mesh), [&] { M(mesh)->eng().set_tunables(values); });
+}
+int uhm_gpu_get_tunables(long* mesh, int* values) {
+  // a query: it cannot fail and does not report an earlier call's status
+  if (!M(mesh)) return 30;
+  M(mesh)->eng().get_tunables(values);
+  return 0;
+}
+int uhm_gpu_autotune(long* mesh, int method, int reps, int* n_timed) {
+  return guard(M(mesh), [&] { *n_timed = M(mesh)->eng().autotune(method, reps); });
+}
 int uhm_gpu_set_selector(long* mesh, const float* params, int n) {
   return guard(M(mesh), [&] { M(mesh)->eng().set_selector(params, n); });
 }

@@ -18,7 +18,6 @@ using namespace uhm_gpu;
 static constexpr int SMALL_MAX_F64 = 160;   // whole front in shared memory (200 KB)
 static constexpr int SMALL_MAX_F32 = 224;
 static constexpr int NB = 64;               // panel width of the blocked kernels
-static constexpr int GC_MIN_ROWS = 512;     // LU panels this tall run on many CTAs (k_getrf_coop)
 static constexpr int ASM_TJ = 16;           // assembly column tile (k_factor.cu)
 static constexpr int TRSM_RB = 64;
 static constexpr int FWD_RB = 256;            // k_solve.cu
@@ -397,7 +396,7 @@ void Engine::build_plan(int method) {
         p = front_prec_override[f.slot];
     }
     f.prec = p;
-    f.tc = (p == PREC_BF16X3 || p == PREC_BF16X6) && f.n >= 512 && method == UHM_CHOL;
+    f.tc = (p == PREC_BF16X3 || p == PREC_BF16X6) && f.n >= tune.tc_min_n && method == UHM_CHOL;
   }
   arena64_n = arena32_n = vec_n = piv_n = 0;
   ws_total = 0;
@@ -432,7 +431,7 @@ void Engine::build_plan(int method) {
   // completion flag per block for the flag-driven solves
   dinv64_n = dinv32_n = flags_n = 0;
   {
-    const int small_max_f[2] = {SMALL_MAX_F64, SMALL_MAX_F32};
+    const int small_max_f[2] = {tune.small_max_f64, tune.small_max_f32};
     for (auto& f : fronts) {
       const int dt = f.prec == PREC_FP64 ? F64 : F32;
       f.blocked = f.tc || f.n > small_max_f[dt];
@@ -556,7 +555,7 @@ void Engine::build_programs(int method) {
     op.bytes = bytes;
     ops.push_back(op);
   };
-  const int small_max[2] = {SMALL_MAX_F64, SMALL_MAX_F32};
+  const int small_max[2] = {tune.small_max_f64, tune.small_max_f32};
   for (auto& lv : levels) {
     for (int dt = 0; dt < 2; ++dt) {
       std::vector<int> fl;
@@ -648,7 +647,7 @@ void Engine::build_programs(int method) {
           const int rcap = dt == F64 ? GC_RMAX_F64 : GC_RMAX_F32;
           std::vector<Item> one, tall;
           for (const Item& it : p_items)
-            (fronts[it.front].n - it.a >= GC_MIN_ROWS ? tall : one).push_back(it);
+            (fronts[it.front].n - it.a >= tune.gc_min_rows ? tall : one).push_back(it);
           push(fac_ops, OP_GETRF, dt, NB, piv, one, tall.empty() ? fp : 0.0);
           size_t i0 = 0;
           while (i0 < tall.size()) {
@@ -1577,6 +1576,94 @@ void Engine::apply_selector(int method) {
   if (cls != learned_class || !dev_ok) prec_dirty = true;
   learned_class.swap(cls);
   learned_valid = true;
+}
+
+void Engine::set_tunables(const int* v) {
+  Tunables t;
+  t.small_max_f64 = v[0];
+  t.small_max_f32 = v[1];
+  t.tc_min_n = v[2];
+  t.gc_min_rows = v[3];
+  if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
+      t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64)
+    fail("set_tunables: value outside the kernels' limits", 7);
+  tune = t;
+  prec_dirty = true;
+  status = 0;          // a valid configuration clears an earlier configuration error
+  last_error.clear();
+}
+
+void Engine::get_tunables(int* v) const {
+  v[0] = tune.small_max_f64;
+  v[1] = tune.small_max_f32;
+  v[2] = tune.tc_min_n;
+  v[3] = tune.gc_min_rows;
+}
+
+int Engine::autotune(int method, int reps) {
+  if (reps < 1) reps = 1;
+  for (auto& es : esrc)
+    if (!es.has_lhs) fail("autotune: an element matrix has not been copied in", 7);
+  // launch programs as a signature: candidates that produce the same
+  // programs need no timing
+  auto signature = [&]() {
+    build_plan(method);
+    build_programs(method);
+    std::vector<int64_t> sig;
+    for (const auto* ops : {&fac_ops, &fwd_ops, &bwd_ops})
+      for (const Op& o : *ops) {
+        sig.push_back(o.kind);
+        sig.push_back(o.n_items);
+        sig.push_back(o.dtype);
+      }
+    return sig;
+  };
+  auto time_now = [&]() {
+    double best = 1e300;
+    for (int r = 0; r < reps + 1; ++r) {        // the first run builds graphs and is not counted
+      factor(method);
+      solve(method, 3);
+      const double t = timing.factor_ms + timing.solve_ms + timing.refine_ms;
+      if (r > 0 || reps == 0) best = std::min(best, t);
+    }
+    return best;
+  };
+  const bool lu = method != UHM_CHOL;
+  struct Knob { int* v; std::vector<int> cand; };
+  std::vector<Knob> knobs = {
+      {&tune.tc_min_n, {384, 512, 768, 1024, 1536, 1 << 30}},
+      {&tune.small_max_f32, {96, 128, 160, 192, 224}},
+      {&tune.small_max_f64, {64, 96, 128, 160}},
+  };
+  if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
+  int timed = 0;
+  prec_dirty = true;
+  double best_t = time_now();
+  ++timed;
+  for (Knob& k : knobs) {
+    const int keep = *k.v;
+    std::vector<std::vector<int64_t>> seen;
+    seen.push_back(signature());
+    int best_v = keep;
+    for (int c : k.cand) {
+      if (c == keep) continue;
+      *k.v = c;
+      const std::vector<int64_t> sg = signature();
+      bool dup = false;
+      for (auto& o : seen) dup = dup || o == sg;
+      if (dup) continue;
+      seen.push_back(sg);
+      prec_dirty = true;
+      const double t = time_now();
+      ++timed;
+      if (t < best_t) { best_t = t; best_v = c; }
+    }
+    *k.v = best_v;
+  }
+  prec_dirty = true;
+  factor(method);
+  solve(method, 3);
+  return timed;
 }
 
 double Engine::backward_error() {

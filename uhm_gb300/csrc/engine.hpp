@@ -84,6 +84,16 @@ struct Timing {
   int64_t kernel_launches = 0;
 };
 
+// Sizes at which the engine switches kernels for a front.  The defaults suit
+// the GB300 in general; Engine::autotune picks them per mesh by timing.
+struct Tunables {
+  int small_max_f64 = 160;   // whole front in shared memory up to this n (FP64; kernel limit 160)
+  int small_max_f32 = 224;   // same for FP32 fronts (kernel limit 224)
+  int tc_min_n = 512;        // BF16-split Cholesky fronts use the tensor cores from this n
+  int gc_min_rows = 512;     // LU panels with this many rows below the diagonal use many CTAs
+};
+constexpr int N_TUNABLES = 4;
+
 class Engine {
  public:
   explicit Engine(Mesh_* m);
@@ -118,6 +128,16 @@ class Engine {
   std::vector<float> selector_params;         // MLP parameters for PREC_LEARNED
   std::vector<int> learned_class;             // by slot: 0 FP64, 1 FP32, 2 BF16-split
   void set_selector(const float* params, int n);
+  Tunables tune;
+  void set_tunables(const int* v);            // N_TUNABLES values, checked against the kernel limits
+  void get_tunables(int* v) const;
+  // coordinate descent over candidate values of every tunable: each candidate
+  // whose launch programs differ from one already timed is timed over `reps`
+  // factor+solve(+refine) runs (minimum kept); the fastest is kept.  Element
+  // matrices and right-hand sides must have been copied in.  Returns the
+  // number of timed candidates; the mesh is left factored and solved with
+  // the chosen values.
+  int autotune(int method, int reps);
   // device buffers for the current plan and precisions (no factorisation)
   void prepare_device(int method);
   // per-front selector features (slot order, SEL_F floats each); element

@@ -814,7 +814,7 @@ template <> __device__ __forceinline__ const float* dinv_arena<float>(const DevC
 // item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
 // right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
+__global__ void __launch_bounds__(256, 3) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
                                                    int* ticket, int* err, int q0) {
   using CT = T;
   __shared__ int s_t;

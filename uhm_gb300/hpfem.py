@@ -174,7 +174,14 @@ def _entity_id(base, bub, coord):
 
 
 def _merge_plan(n: int, merges):
-    """Per-level merge factors reducing n cells to 1 along one axis."""
+    """Per-level merge factors reducing n cells to 1 along one axis.
+
+    When n factors into 2, 3 and 5 the plan is exact (smallest factors
+    first, 2s at the leaves).  Otherwise (a prime factor above 5, e.g. n = 11
+    or 14) exact merges would put a 7-, 11- or 13-way merge, and with it one
+    huge separator, at a single level; the plan then halves the cell count
+    with ceiling division at every level (nested dissection with a ragged
+    last block: 11 -> 6 -> 3 -> 2 -> 1), which build_mesh supports."""
     if merges is not None:
         assert int(np.prod(merges)) == n, (n, merges)
         return list(merges)
@@ -189,6 +196,8 @@ def _merge_plan(n: int, merges):
             f = 3
             while m % f:
                 f += 2
+            if f > 5:
+                return [2] * int(math.ceil(math.log2(n)))
             plan.append(f)
             m //= f
     return plan
@@ -356,7 +365,7 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, react=None, seed: 
     cur = {c: e for e, c in enumerate(el_coords)}
     cur_n = n
     for f in plan:
-        nxt_n = cur_n // f
+        nxt_n = -(-cur_n // f)         # the last block of a ragged halving is smaller
         blocks = list(itertools.product(*[range(nxt_n)] * dim))
         blocks = [tuple(reversed(b)) for b in blocks]
         nxt = {}
@@ -364,7 +373,9 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, react=None, seed: 
             kids = []
             for sub in itertools.product(*[range(f)] * dim):
                 sub = tuple(reversed(sub))
-                kids.append(cur[tuple(b[a] * f + sub[a] for a in range(dim))])
+                cc = tuple(b[a] * f + sub[a] for a in range(dim))
+                if all(x < cur_n for x in cc):
+                    kids.append(cur[cc])
             pid = len(parent)
             parent.append(-1)
             generation.append(min(generation[k] for k in kids) - 1)
