@@ -147,7 +147,9 @@ int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_fa
  * size is a compile-time knob, UHM/include/uhm/const.hxx): values[0] whole-front
  * shared-memory factorisation up to n (FP64, at most 160), values[1] the same
  * for FP32 (at most 224), values[2] tensor-core BF16-split fronts from n,
- * values[3] LU panels on many CTAs from this many rows below the diagonal.
+ * values[3] LU panels on many CTAs from this many rows below the diagonal,
+ * values[4] k: diagonal block and panel TRSM of a Cholesky step in one launch
+ * when that launch has at most k CTAs per SM (0: never).
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

@@ -282,7 +282,7 @@ class Mesh:
                 "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
                 "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
                 "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
-                "laswp"] + [f"op{k}" for k in range(23, 32)]
+                "laswp", "potrf_trsm"] + [f"op{k}" for k in range(24, 32)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
@@ -338,7 +338,7 @@ class Mesh:
 
     # -- learned precision selector ------------------------------------------
     # -- kernel-selection thresholds --------------------------------------------
-    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows")
+    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm")
 
     def tunables(self) -> dict:
         v = np.zeros(len(self.TUNABLES), np.int32)

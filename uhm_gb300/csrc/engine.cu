@@ -555,6 +555,30 @@ void Engine::build_programs(int method) {
     op.bytes = bytes;
     ops.push_back(op);
   };
+  // one Cholesky step's diagonal block + panel TRSM: fused (every CTA of the
+  // TRSM factors the block, the first writes its inverse) or two launches
+  auto push_potrf_trsm = [&](int dt, const std::vector<Item>& p_items, const std::vector<Item>& t_items,
+                             double fp, double ft) {
+    // every fused CTA repeats the latency-bound diagonal factorisation: fuse
+    // only while the launch fits fuse_potrf_trsm waves of one CTA per SM
+    const size_t n_fused = t_items.size() + p_items.size();
+    if (!tune.fuse_potrf_trsm || n_fused > (size_t)tune.fuse_potrf_trsm * n_sm) {
+      push(fac_ops, OP_POTRF, dt, NB, 0, p_items, fp);
+      push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
+      return;
+    }
+    std::vector<Item> fi;
+    for (const Item& d : p_items) {
+      bool first = true;
+      for (const Item& t : t_items)
+        if (t.front == d.front) {
+          fi.push_back(Item{t.front, t.a, t.b, first ? 1 : 0});
+          first = false;
+        }
+      if (first) fi.push_back(Item{d.front, d.a, fronts[d.front].n, 1});
+    }
+    push(fac_ops, OP_POTRF_TRSM, dt, NB, 0, fi, fp + ft);
+  };
   const int small_max[2] = {tune.small_max_f64, tune.small_max_f32};
   for (auto& lv : levels) {
     for (int dt = 0; dt < 2; ++dt) {
@@ -637,8 +661,7 @@ void Engine::build_programs(int method) {
           }
         }
         if (chol) {
-          push(fac_ops, OP_POTRF, dt, NB, 0, p_items, fp);
-          push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
+          push_potrf_trsm(dt, p_items, t_items, fp, ft);
           push(fac_ops, OP_SYRK, dt, NB, 0, u_items, fu);
         } else {
           // tall panels (many rows below the diagonal) on many CTAs at once,
@@ -719,8 +742,7 @@ void Engine::build_programs(int method) {
             const double w = std::max(0, cmax - base), mr = f.n - base;
             fu += 2.0 * kb * (w * mr - 0.5 * w * (w - 1));
           }
-          push(fac_ops, OP_POTRF, dt, NB, 0, p_items, fp);
-          push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
+          push_potrf_trsm(dt, p_items, t_items, fp, ft);
           push(fac_ops, OP_SYRK, dt, NB, TC_NBO, u_items, fu);
         }
         std::vector<Item> pk, tt;
@@ -1112,6 +1134,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
         break;
       case OP_POTRF: launch_potrf_diag(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_POTRF_TRSM: launch_potrf_trsm(ctx, it, op.n_items, op.dtype, stream); break;
       case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
       case OP_FWD_FLAGS:
         launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
@@ -1584,6 +1607,7 @@ void Engine::set_tunables(const int* v) {
   t.small_max_f32 = v[1];
   t.tc_min_n = v[2];
   t.gc_min_rows = v[3];
+  t.fuse_potrf_trsm = v[4] < 0 ? 0 : v[4];
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
       t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64)
     fail("set_tunables: value outside the kernels' limits", 7);
@@ -1598,6 +1622,7 @@ void Engine::get_tunables(int* v) const {
   v[1] = tune.small_max_f32;
   v[2] = tune.tc_min_n;
   v[3] = tune.gc_min_rows;
+  v[4] = tune.fuse_potrf_trsm;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -1635,6 +1660,7 @@ int Engine::autotune(int method, int reps) {
       {&tune.small_max_f32, {96, 128, 160, 192, 224}},
       {&tune.small_max_f64, {64, 96, 128, 160}},
   };
+  if (!lu) knobs.push_back({&tune.fuse_potrf_trsm, {0, 1, 2, 4}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;
   prec_dirty = true;

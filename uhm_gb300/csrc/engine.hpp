@@ -73,7 +73,7 @@ enum OpKind : int {
   OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
-  OP_LASWP, OP_KIND_END
+  OP_LASWP, OP_POTRF_TRSM, OP_KIND_END
 };
 static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
 
@@ -91,8 +91,10 @@ struct Tunables {
   int small_max_f32 = 224;   // same for FP32 fronts (kernel limit 224)
   int tc_min_n = 512;        // BF16-split Cholesky fronts use the tensor cores from this n
   int gc_min_rows = 512;     // LU panels with this many rows below the diagonal use many CTAs
+  int fuse_potrf_trsm = 2;   // Cholesky step: diagonal block + panel TRSM in one launch when it
+                             // has at most this many CTAs per SM (0: never)
 };
-constexpr int N_TUNABLES = 4;
+constexpr int N_TUNABLES = 5;
 
 class Engine {
  public:

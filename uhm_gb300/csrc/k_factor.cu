@@ -204,31 +204,27 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // item: front, a = k0 (step start), b = row block / tile row, c = tile col
 // ---------------------------------------------------------------------------
 // Cholesky of one diagonal block (kb <= 64) and the inverse of its factor,
-// 256 threads = 8 warps.  Warp w owns the column block 8w..8w+7 of the
-// symmetric 64 x 64 block and of the inverse X = L^{-1} being formed; lane
-// (ti, h) keeps the 4 x 4 tile at rows 4 ti.., columns 8w + 4h.. of both in
+// 256 threads = 8 warps (potrf_block, shared by k_potrf_diag and the fused
+// k_potrf_trsm).  Warp w owns the column block 8w..8w+7 of the symmetric
+// 64 x 64 block and of the inverse X = L^{-1} being formed; lane (ti, h)
+// keeps the 4 x 4 tile at rows 4 ti.., columns 8w + 4h.. of both in
 // registers.  Right-looking in column order; for each column p a warp
 //   (factor, p <= 8w+7) applies A[i][j] -= l_ip l_jp to its tile, where
 //     l_ip = v_p[i] / sqrt(v_p[p]) and v_p, column p of the partially reduced
-//     block, was published in shared memory by the warp owning column p;
+//     block, was published in shared memory by the 16 lanes owning it;
 //   (inverse, p >= 8w) scales row p of its column block of X by 1 / l_pp and
-//     applies X[i][:] -= l_ip x_p for i > p.  Column blocks of X are
-//     independent, so this needs nothing from other warps but v_p.
-// The owner of column p+1 publishes it as soon as it has applied column p.
-// A hand-off inside a warp needs only __syncwarp; a column published by
-// another warp is awaited on its own mbarrier: after the warp barrier that
-// orders the 16 publishing lanes' stores, lane 0 arrives (release) and one
-// lane of each consuming warp waits (acquire, then a warp barrier), with an
-// iteration limit after which the front is flagged (status ST_WAIT) and the
-// block gives up.  The 64-pivot chain thus runs at warp-synchronous speed except at
-// the 7 hand-offs between warps, and each warp overlaps its trailing updates
-// and its part of the inverse with the chain; a warp does only the factor
-// steps that reach its columns and only the inverse steps whose rows are
-// nonzero in them.  Columns are walked four at a time so that register
-// indices inside a tile are compile-time constants.  Blocks narrower than 64
-// are padded with the identity.  FP32 pivots use rsqrt (the factor is refined
-// in FP64 by the mixed path); FP64 uses sqrt and a divide.  The inverse is
-// stored column-major (Dinv[j * 64 + i] = X[i][j]) with 128-bit stores.
+//     applies X[i][:] -= l_ip x_p for i > p (column blocks of X are
+//     independent, so this needs nothing from other warps but v_p).
+// One block barrier per column publishes the next column.  A warp does only
+// the factor steps that reach its columns and only the inverse steps whose
+// rows are nonzero in them.  Columns are walked four at a time so that
+// register indices inside a tile are compile-time constants.  Blocks
+// narrower than 64 are padded with the identity.  FP32 pivots use rsqrt (the
+// factor is refined in FP64 by the mixed path); FP64 uses sqrt and a divide.
+// Measured alternatives: a fully unrolled left-looking version (one row per
+// thread, ~100 KB of straight-line code) was bound by instruction fetch;
+// warp-to-warp hand-offs on mbarriers or shared flags instead of the block
+// barrier were slower (their wake-up latency).
 template <typename T> __device__ __forceinline__ void pivot_root(T s, T& d, T& rd);
 template <> __device__ __forceinline__ void pivot_root<float>(float s, float& d, float& rd) {
   rd = rsqrtf(s);
@@ -261,64 +257,24 @@ template <> struct Vec4<double> {
   }
 };
 
-constexpr uint32_t PD_WAIT_LIMIT = 1u << 20;
+template <typename T>
+struct PotrfShared {
+  T V[64][64];      // V[p][i]: column p of the reduced block (zero above p)
+  T XR[8][2][8];    // per warp: row p of its block of X, scaled, double-buffered
+  T sd[64], srd[64];
+};
 
-__device__ __forceinline__ uint32_t pd_smem(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void pd_mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void pd_mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-// bounded wait for phase 0 of a single-use barrier; false when it gave up
-// (here or, through *give_up, in another warp)
-__device__ __forceinline__ bool pd_mbar_wait(uint32_t bar, volatile int* give_up) {
-  for (uint32_t i = 0; i < PD_WAIT_LIMIT; ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
-        " selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar)
-        : "memory");
-    if (ok) return true;
-    if (*give_up) return false;
-  }
-  *give_up = 1;
-  return false;
-}
-
-// hand-off of a published column to the other warps
-enum PotrfHandoff : int { PD_BLOCK_BARRIER = 0, PD_MBARRIER = 1, PD_FLAG_SPIN = 2 };
-constexpr int PD_HANDOFF = PD_BLOCK_BARRIER;
-
-__device__ __forceinline__ int pd_ld_volatile(const int* p) {
-  int v;
-  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(v) : "r"(pd_smem(p)) : "memory");
-  return v;
-}
-
-template <typename T, int HO>
-__global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
-  __shared__ __align__(16) T V[64][64];    // V[p][i]: column p of the reduced block (zero above p)
-  __shared__ __align__(16) T XR[8][2][8];  // per warp: row p of its X block, scaled, double-buffered
-  __shared__ T sd[64], srd[64];            // l_pp and 1 / l_pp
-  __shared__ __align__(8) unsigned long long mbar[64];   // column p published (PD_MBARRIER)
-  __shared__ int pflag[64];                               // column p published (PD_FLAG_SPIN)
-  __shared__ int s_give_up;
-  const Item it = items[blockIdx.x];
-  const FrontDev f = c.fronts[it.front];
-  const int n = f.n, k0 = it.a;
-  const int kb = min(nb, f.fs - k0);
-  T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
-  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+// Factor the 64 x 64 block at G (leading dimension n, kb <= 64 valid rows and
+// columns) in shared memory; on return x holds this thread's tile of
+// L^{-1}, sh.V / sh.sd / sh.srd the factor (L[i][k] = V[k][i] * srd[k] below
+// the diagonal, sd[k] on it), after a block barrier; bad is set when a pivot
+// was not positive.
+template <typename T>
+__device__ __forceinline__ void potrf_block(const T* __restrict__ G, int n, int kb, PotrfShared<T>& sh,
+                                            T (&x)[4][4], bool& bad) {
+  const int tid = threadIdx.x, w = tid >> 5;
   const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
   const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
-  if (HO == PD_MBARRIER && tid < 64) pd_mbar_init(pd_smem(&mbar[tid]), 1);
-  if (HO == PD_FLAG_SPIN && tid < 64) pflag[tid] = 0;
-  if (tid == 0) s_give_up = 0;
   {
     // stage the lower triangle (coalesced column reads, all loads in flight
     // before the shared stores), identity padding
@@ -331,85 +287,61 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-      if (i >= j) V[j][i] = g[u];
+      if (i >= j) sh.V[j][i] = g[u];
     }
   }
   __syncthreads();
-  T a[4][4], x[4][4];
+  T a[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int i = r0 + u, j = c0 + v;
-      a[u][v] = i >= j ? V[j][i] : V[i][j];
+      a[u][v] = i >= j ? sh.V[j][i] : sh.V[i][j];
       x[u][v] = i == j ? T(1) : T(0);
     }
   __syncthreads();   // tiles read before any column is republished; column 0 stays as staged
-  bool bad = false, gave_up = false;
+  bad = false;
 #pragma unroll 1
   for (int q = 0; q < 16; ++q) {
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int p = 4 * q + s;
-      if (HO != PD_BLOCK_BARRIER && p > 0 && (p >> 3) != w) {
-        // one lane waits (acquire), the warp barrier passes the ordering on
-        int ok = 1;
-        if (lane == 0 && !gave_up) {
-          if (HO == PD_MBARRIER) {
-            ok = pd_mbar_wait(pd_smem(&mbar[p]), &s_give_up);
-          } else {
-            ok = 0;
-            for (uint32_t i = 0; i < PD_WAIT_LIMIT; ++i)
-              if (pd_ld_volatile(&pflag[p])) { ok = 1; break; }
-            __threadfence_block();
-          }
-        }
-        __syncwarp();
-        gave_up = gave_up || !__shfl_sync(0xffffffffu, ok, 0);
-      }
-      T piv = V[p][p];
+      T piv = sh.V[p][p];
       if (!(piv > T(0))) { bad = true; piv = T(1); }
       T d, rd;
       pivot_root<T>(piv, d, rd);
-      if (tid == 0) { sd[p] = d; srd[p] = rd; }
+      if (tid == 0) { sh.sd[p] = d; sh.srd[p] = rd; }
       T lr[4];
-      Vec4<T>::ld(&V[p][r0], lr);
+      Vec4<T>::ld(&sh.V[p][r0], lr);
 #pragma unroll
       for (int u = 0; u < 4; ++u) lr[u] *= rd;
       if (p <= cb0 + 7) {
         T lc[4];
-        Vec4<T>::ld(&V[p][c0], lc);
+        Vec4<T>::ld(&sh.V[p][c0], lc);
 #pragma unroll
         for (int v = 0; v < 4; ++v) lc[v] *= rd;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
           for (int v = 0; v < 4; ++v) a[u][v] -= lr[u] * lc[v];
-        if (p + 1 < 64 && ((p + 1) >> 3) == w) {
+        if (p + 1 < 64 && ((p + 1) >> 3) == w && tj == (p + 1) >> 2) {
           const int CB = (s + 1) & 3;   // constant after unrolling
-          if (tj == (p + 1) >> 2) {
-            T wv[4];
+          T wv[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
-            Vec4<T>::st(&V[p + 1][r0], wv);
-          }
-          __syncwarp();   // the column is visible to the warp; one lane releases it to the others
-          if (HO == PD_MBARRIER && lane == 0) pd_mbar_arrive(pd_smem(&mbar[p + 1]));
-          if (HO == PD_FLAG_SPIN && lane == 0) {
-            __threadfence_block();
-            *(volatile int*)&pflag[p + 1] = 1;
-          }
+          for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
+          Vec4<T>::st(&sh.V[p + 1][r0], wv);
         }
       }
       if (p >= cb0) {
         if (ti == q) {
 #pragma unroll
           for (int v = 0; v < 4; ++v) x[s][v] *= rd;
-          Vec4<T>::st(&XR[w][p & 1][4 * h], x[s]);
+          Vec4<T>::st(&sh.XR[w][p & 1][4 * h], x[s]);
         }
         __syncwarp();
         T xr[4];
-        Vec4<T>::ld(&XR[w][p & 1][4 * h], xr);
+        Vec4<T>::ld(&sh.XR[w][p & 1][4 * h], xr);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const T l = (r0 + u > p) ? lr[u] : T(0);
@@ -417,21 +349,26 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
           for (int v = 0; v < 4; ++v) x[u][v] -= l * xr[v];
         }
       }
-      if (HO == PD_BLOCK_BARRIER) __syncthreads();
+      __syncthreads();
     }
   }
-  if (gave_up) set_status(c, it.front, ST_WAIT);
-  if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
-  __syncthreads();   // every column published, sd / srd complete
-  // factor: L[i][k] = v_k[i] / l_kk below the diagonal, l_kk on it
+}
+
+// L of the block into G (lower triangle; when G is not null) and its
+// inverse, column-major with 128-bit stores, into D (when not null)
+template <typename T>
+__device__ __forceinline__ void potrf_store(T* __restrict__ G, int n, int kb, const PotrfShared<T>& sh,
+                                            const T (&x)[4][4], T* __restrict__ D) {
+  const int tid = threadIdx.x;
+  if (G) {
 #pragma unroll 4
-  for (int u = 0; u < 16; ++u) {
-    const int idx = tid + 256 * u, i = idx & 63, k = idx >> 6;
-    if (i >= k && i < kb && k < kb) G[i + (int64_t)k * n] = i == k ? sd[k] : V[k][i] * srd[k];
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, k = idx >> 6;
+      if (i >= k && i < kb && k < kb) G[i + (int64_t)k * n] = i == k ? sh.sd[k] : sh.V[k][i] * sh.srd[k];
+    }
   }
-  T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
-  if (nb != 64 || !Dinv) return;
-  T* D = Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096;
+  if (!D) return;
+  const int r0 = 4 * (tid & 15), c0 = 4 * (tid >> 4);
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     const int j = c0 + v;
@@ -442,14 +379,30 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __restrict__ items, int nb) {
+  __shared__ __align__(16) PotrfShared<T> sh;
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, k0 = it.a;
+  const int kb = min(nb, f.fs - k0);
+  T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
+  T x[4][4];
+  bool bad;
+  potrf_block<T>(G, n, kb, sh, x, bad);
+  if (bad && threadIdx.x == 0) set_status(c, it.front, ST_NOT_SPD);
+  T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
+  potrf_store<T>(G, n, kb, sh, x, (nb == 64 && Dinv) ? Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096 : nullptr);
+}
+
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s) {
   if (!n_items) return;
   if (nb > 64) throw std::invalid_argument("potrf_diag: block wider than 64");
   if (dtype == F64)
-    k_potrf_diag<double, PD_HANDOFF><<<n_items, 256, 0, s>>>(c, items, nb);
+    k_potrf_diag<double><<<n_items, 256, 0, s>>>(c, items, nb);
   else
-    k_potrf_diag<float, PD_HANDOFF><<<n_items, 256, 0, s>>>(c, items, nb);
+    k_potrf_diag<float><<<n_items, 256, 0, s>>>(c, items, nb);
 }
 
 constexpr int TRSM_RB = 64;   // rows per panel-TRSM block
@@ -544,6 +497,92 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
     size_t sm = (size_t)(64 * 65 + TRSM_RB * nb) * sizeof(float);
     cudaFuncSetAttribute(k_trsm_panel<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_trsm_panel<float, 256><<<n_items, 256, sm, s>>>(c, items, nb);
+  }
+}
+
+// Diagonal block and panel TRSM of one 64-column step in one launch.  Every
+// CTA factors the diagonal block and forms its inverse itself (potrf_block;
+// the SMs would otherwise idle through that latency-bound step), then
+// applies X <- X L^{-T} = X (L^{-1})^T to its 64-row block of the panel.  The
+// CTA flagged in the item writes the inverse, which is how the factor's
+// diagonal block is kept: the flag-driven solves and this TRSM use only the
+// inverse, and writing L over the block in place would race with other
+// CTAs still reading A's block, so the arena keeps A's diagonal block.
+// Item: front, a = k0, b = first row of the block (n: none), c = 1 for the
+// writer.
+template <typename T>
+__global__ void __launch_bounds__(256) k_potrf_trsm(DevCtx c, const Item* __restrict__ items) {
+  extern __shared__ __align__(16) unsigned char pt_smem[];
+  PotrfShared<T>& sh = *reinterpret_cast<PotrfShared<T>*>(pt_smem);
+  T* Lt = reinterpret_cast<T*>(pt_smem + ((sizeof(PotrfShared<T>) + 15) / 16) * 16);   // 64 x 65
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, k0 = it.a, r0 = it.b;
+  const int kb = min(64, f.fs - k0);
+  T* __restrict__ A = arena<T>(c) + f.off;
+  T* __restrict__ G = A + k0 + (int64_t)k0 * n;
+  const int tid = threadIdx.x;
+  T x[4][4];
+  bool bad;
+  potrf_block<T>(G, n, kb, sh, x, bad);
+  const bool writer = it.c & 1;
+  if (writer) {
+    if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+    T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
+    potrf_store<T>(nullptr, n, kb, sh, x, Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096);
+  }
+  if (r0 >= n) return;
+  const int rb = min(TRSM_RB, n - r0);
+  // L^{-1} transposed into Lt (Lt[t * 65 + j] = Linv[j][t]); the panel
+  // block into V (its factor values are no longer needed once written)
+  {
+    const int ti = tid & 15, tj = tid >> 4;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int j = 4 * ti + u, t = 4 * tj + v;   // x[u][v] = Linv[j][t]
+        Lt[t * 65 + j] = (j < kb && t < kb) ? x[u][v] : T(0);
+      }
+  }
+  T* X = &sh.V[0][0];   // 64 x 64, column-major (V is free: nothing reads the factor any more)
+  {
+    T xv[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx % TRSM_RB, j = idx / TRSM_RB;
+      xv[u] = (i < rb && j < kb) ? A[(r0 + i) + (int64_t)(k0 + j) * n] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) X[tid + 256 * u] = xv[u];
+  }
+  __syncthreads();
+  const int i = tid % TRSM_RB, jg = tid / TRSM_RB;   // 4 column groups of 16
+  T acc[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) acc[u] = T(0);
+  for (int t = 0; t < kb; ++t) {
+    const T xv = X[i + t * TRSM_RB];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] += xv * Lt[t * 65 + jg * 16 + u];
+  }
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int j = jg * 16 + u;
+    if (i < rb && j < kb) A[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
+  }
+}
+
+void launch_potrf_trsm(const DevCtx& c, const Item* items, int n_items, int dtype, cudaStream_t s) {
+  if (!n_items) return;
+  if (dtype == F64) {
+    const size_t sm = ((sizeof(PotrfShared<double>) + 15) / 16) * 16 + sizeof(double) * 64 * 65;
+    cudaFuncSetAttribute(k_potrf_trsm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_potrf_trsm<double><<<n_items, 256, sm, s>>>(c, items);
+  } else {
+    const size_t sm = ((sizeof(PotrfShared<float>) + 15) / 16) * 16 + sizeof(float) * 64 * 65;
+    cudaFuncSetAttribute(k_potrf_trsm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_potrf_trsm<float><<<n_items, 256, sm, s>>>(c, items);
   }
 }
 

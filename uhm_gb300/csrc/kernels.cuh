@@ -76,6 +76,9 @@ void launch_assemble(const DevCtx& c, const Item* items, int n_items, int dtype,
                      cudaStream_t s);
 void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                          int max_n, cudaStream_t s);
+// diagonal block + panel TRSM of one 64-column step (every CTA factors the
+// block; item: front, a = k0, b = first row of the panel block, c = 1 writer)
+void launch_potrf_trsm(const DevCtx& c, const Item* items, int n_items, int dtype, cudaStream_t s);
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                        cudaStream_t s);
 void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
