@@ -149,7 +149,8 @@ int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_fa
  * for FP32 (at most 224), values[2] tensor-core BF16-split fronts from n,
  * values[3] LU panels on many CTAs from this many rows below the diagonal,
  * values[4] k: diagonal block and panel TRSM of a Cholesky step in one launch
- * when that launch has at most k CTAs per SM (0: never).
+ * when that launch has at most k CTAs per SM (0: never), values[5] outer
+ * panel width of tensor-core fronts (128, 256 or 512).
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

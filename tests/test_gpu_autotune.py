@@ -26,6 +26,7 @@ def test_autotune_keeps_valid_thresholds(native_lib, name, make, method, prec):
     assert r["tc_min_n"] in (384, 512, 768, 1024, 1536, 1 << 30)
     assert r["gc_min_rows"] in (256, 512, 1024, 2048, 1 << 30)
     assert r["fuse_potrf_trsm"] in (0, 1, 2, 4)
+    assert r["tc_nbo"] in (128, 256, 512)
     assert m.timing()["berr"] <= 1e-12
     m.factor(method)
     m.solve(method)

@@ -338,7 +338,7 @@ class Mesh:
 
     # -- learned precision selector ------------------------------------------
     # -- kernel-selection thresholds --------------------------------------------
-    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm")
+    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo")
 
     def tunables(self) -> dict:
         v = np.zeros(len(self.TUNABLES), np.int32)

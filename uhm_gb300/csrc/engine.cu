@@ -402,9 +402,9 @@ void Engine::build_plan(int method) {
   ws_total = 0;
   for (auto& f : fronts) {
     if (!f.tc) continue;
-    const int64_t mmax = f.n - std::min(TC_NBO, f.fs);
+    const int64_t mmax = f.n - std::min(tune.tc_nbo, f.fs);
     f.ws_off = ws_total;
-    f.ws_stride = mmax * TC_NBO;
+    f.ws_stride = mmax * tune.tc_nbo;
     ws_total += 3 * f.ws_stride;
   }
   h_fronts.assign(fronts.size(), FrontDev{});
@@ -714,15 +714,16 @@ void Engine::build_programs(int method) {
           push(fac_ops, OP_GEMM, dt, NB, 0, u_items, fu);
         }
       }
-      // tensor-core fronts: outer panels of TC_NBO columns; inside a panel the
+      // tensor-core fronts: outer panels of tc_nbo columns; inside a panel the
       // SIMT kernels factor 64 columns at a time and update only the panel's
       // columns; the trailing block is then updated once per outer panel on
       // the tensor cores (BF16-split operands, FP32 accumulation)
       int maxfs_tc = 0;
       for (int s : tcf) maxfs_tc = std::max(maxfs_tc, fronts[s].fs);
+      const int NBO = tune.tc_nbo;
       const int TB = tc_tile();
-      for (int K0 = 0; K0 < maxfs_tc; K0 += TC_NBO) {
-        for (int k0 = K0; k0 < K0 + TC_NBO && k0 < maxfs_tc; k0 += NB) {
+      for (int K0 = 0; K0 < maxfs_tc; K0 += NBO) {
+        for (int k0 = K0; k0 < K0 + NBO && k0 < maxfs_tc; k0 += NB) {
           std::vector<Item> p_items, t_items, u_items;
           double fp = 0, ft = 0, fu = 0;
           for (int s : tcf) {
@@ -730,7 +731,7 @@ void Engine::build_programs(int method) {
             if (f.fs <= k0) continue;
             const int kb = std::min(NB, f.fs - k0);
             const int base = k0 + kb;
-            const int cmax = std::min(K0 + TC_NBO, f.fs);
+            const int cmax = std::min(K0 + NBO, f.fs);
             p_items.push_back(Item{s, k0, 0, 0});
             fp += get_flop_chol(0, kb);
             for (int r0 = base; r0 < f.n; r0 += TRSM_RB) t_items.push_back(Item{s, k0, r0, 0});
@@ -743,14 +744,14 @@ void Engine::build_programs(int method) {
             fu += 2.0 * kb * (w * mr - 0.5 * w * (w - 1));
           }
           push_potrf_trsm(dt, p_items, t_items, fp, ft);
-          push(fac_ops, OP_SYRK, dt, NB, TC_NBO, u_items, fu);
+          push(fac_ops, OP_SYRK, dt, NB, NBO, u_items, fu);
         }
         std::vector<Item> pk, tt;
         double ftc = 0, btc = 0;
         for (int s : tcf) {
           const HostFront& f = fronts[s];
           if (f.fs <= K0) continue;
-          const int KB = std::min(TC_NBO, f.fs - K0);
+          const int KB = std::min(NBO, f.fs - K0);
           const int m = f.n - (K0 + KB);
           if (m <= 0) continue;
           for (int rb = 0; rb < (m + 63) / 64; ++rb) pk.push_back(Item{s, K0, rb, 0});
@@ -764,8 +765,8 @@ void Engine::build_programs(int method) {
           btc += 8.0 * 0.5 * (double)m * (m + 1) + 2.0 * np * (double)m * KB;
         }
         const int parts = fronts[tcf[0]].prec == PREC_BF16X6 ? 3 : 2;
-        push(fac_ops, OP_TC_PACK, dt, TC_NBO, parts, pk);
-        push(fac_ops, OP_TC_SYRK, dt, TC_NBO, parts, tt, ftc, btc);
+        push(fac_ops, OP_TC_PACK, dt, NBO, parts, pk);
+        push(fac_ops, OP_TC_SYRK, dt, NBO, parts, tt, ftc, btc);
       }
     }
   }
@@ -951,15 +952,15 @@ void Engine::alloc_device(int method) {
   }
   if (ws_total > 0) {
     // one extra row block so tiles that run past the last part stay inside the tensor
-    d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * TC_NBO));
-    CK(cudaMemsetAsync(d_ws, 0, sizeof(uint16_t) * (size_t)(ws_total + 256 * TC_NBO), stream));
+    d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * tune.tc_nbo));
+    CK(cudaMemsetAsync(d_ws, 0, sizeof(uint16_t) * (size_t)(ws_total + 256 * tune.tc_nbo), stream));
     std::vector<int64_t> wo(fronts.size(), 0), wst(fronts.size(), 0);
     for (auto& f : fronts) {
       if (!f.tc) continue;
       wo[f.slot] = f.ws_off;
       wst[f.slot] = f.ws_stride;
     }
-    if (!tc_encode_part(&ws_map, d_ws, ws_total / TC_NBO + 256, TC_NBO))
+    if (!tc_encode_part(&ws_map, d_ws, ws_total / tune.tc_nbo + 256, tune.tc_nbo))
       fail("tensor map encoding failed", 4);
     d_ws_off = (int64_t*)dmalloc(sizeof(int64_t) * wo.size());
     d_ws_stride = (int64_t*)dmalloc(sizeof(int64_t) * wst.size());
@@ -1608,8 +1609,10 @@ void Engine::set_tunables(const int* v) {
   t.tc_min_n = v[2];
   t.gc_min_rows = v[3];
   t.fuse_potrf_trsm = v[4] < 0 ? 0 : v[4];
+  t.tc_nbo = v[5];
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
-      t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64)
+      t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64 ||
+      (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512))
     fail("set_tunables: value outside the kernels' limits", 7);
   tune = t;
   prec_dirty = true;
@@ -1623,6 +1626,7 @@ void Engine::get_tunables(int* v) const {
   v[2] = tune.tc_min_n;
   v[3] = tune.gc_min_rows;
   v[4] = tune.fuse_potrf_trsm;
+  v[5] = tune.tc_nbo;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -1661,6 +1665,7 @@ int Engine::autotune(int method, int reps) {
       {&tune.small_max_f64, {64, 96, 128, 160}},
   };
   if (!lu) knobs.push_back({&tune.fuse_potrf_trsm, {0, 1, 2, 4}});
+  if (!lu) knobs.push_back({&tune.tc_nbo, {128, 256, 512}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;
   prec_dirty = true;

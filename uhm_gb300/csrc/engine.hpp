@@ -93,8 +93,9 @@ struct Tunables {
   int gc_min_rows = 512;     // LU panels with this many rows below the diagonal use many CTAs
   int fuse_potrf_trsm = 2;   // Cholesky step: diagonal block + panel TRSM in one launch when it
                              // has at most this many CTAs per SM (0: never)
+  int tc_nbo = 256;          // outer panel width of tensor-core fronts (128, 256 or 512)
 };
-constexpr int N_TUNABLES = 5;
+constexpr int N_TUNABLES = 6;
 
 class Engine {
  public:

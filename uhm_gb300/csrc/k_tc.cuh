@@ -6,7 +6,7 @@
 
 namespace uhm_gpu {
 
-constexpr int TC_NBO = 256;   // outer panel width of fronts updated on tensor cores
+constexpr int TC_NBO = 256;   // default outer panel width of fronts updated on tensor cores
 
 bool tc_encode_part(CUtensorMap* map, void* base, int64_t rows, int nbo);
 void launch_tc_pack(const DevCtx& c, const Item* items, int n_items, int nbo, int nparts, void* ws,
