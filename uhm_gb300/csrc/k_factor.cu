@@ -641,6 +641,24 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
       }
     }
   }
+  // FP32: the C tile does not depend on the arithmetic, so its loads go out
+  // with the operands' and their latency overlaps the products (FP64 keeps
+  // them after the products: the extra registers would halve its occupancy)
+  constexpr bool EARLY_C = sizeof(T) == 4;
+  T cv[TM][TN];
+  auto load_c = [&]() {
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int gr = R0 + ty + i * NTY;
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int gc = C0 + tx + j * NTX;
+        const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
+        cv[i][j] = ok ? G[gr + (int64_t)gc * n] : (T)0;
+      }
+    }
+  };
+  if constexpr (EARLY_C) load_c();
   for (int kk = 0; kk < kb; kk += BK) {
     const int ch = kk / BK;
 #pragma unroll
@@ -674,17 +692,7 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
     __syncthreads();
   }
   // C -= acc: every C value is read before any is written back
-  T cv[TM][TN];
-#pragma unroll
-  for (int i = 0; i < TM; ++i) {
-    const int gr = R0 + ty + i * NTY;
-#pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int gc = C0 + tx + j * NTX;
-      const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
-      cv[i][j] = ok ? G[gr + (int64_t)gc * n] : (T)0;
-    }
-  }
+  if constexpr (!EARLY_C) load_c();
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
     const int gr = R0 + ty + i * NTY;
