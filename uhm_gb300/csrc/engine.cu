@@ -19,6 +19,8 @@ static constexpr int SMALL_MAX_F64 = 160;   // whole front in shared memory (200
 static constexpr int SMALL_MAX_F32 = 224;
 static constexpr int NB = 64;               // panel width of the blocked kernels
 static constexpr int ASM_TJ = 16;           // assembly column tile (k_factor.cu)
+static constexpr int ASM_SCATTER_MIN = 2048;  // fronts this large: one column per CTA, shared-memory scatter
+static constexpr int ASM_SCATTER_MAX = 26624; // the FP64 column fits 208 KB of shared memory
 static constexpr int TRSM_RB = 64;
 static constexpr int FWD_RB = 256;            // k_solve.cu
 static constexpr int BWD_RB = 512;
@@ -410,6 +412,7 @@ void Engine::build_plan(int method) {
   h_fronts.assign(fronts.size(), FrontDev{});
   h_srcs.clear();
   h_inv.clear();
+  h_fwd.clear();
   h_colptr.clear();
   h_colsrc.clear();
   h_sgi.clear();
@@ -460,6 +463,9 @@ void Engine::build_plan(int method) {
       sd.dtype = F64;
       sd.is_child = 0;
       sd.slot = ei;
+      sd.m = es.m;
+      sd.fwd_off = (int64_t)h_fwd.size();
+      for (int r = 0; r < es.m; ++r) h_fwd.push_back(es.pos[r]);
       h_srcs.push_back(sd);
       std::vector<int32_t> inv(n, -1);
       for (int r = 0; r < es.m; ++r) inv[es.pos[r]] = r;
@@ -473,14 +479,20 @@ void Engine::build_plan(int method) {
       sd.dtype = c.prec == PREC_FP64 ? F64 : F32;
       sd.is_child = 1;
       sd.slot = cs;
-      h_srcs.push_back(sd);
+      sd.m = c.ss;
+      sd.fwd_off = (int64_t)h_fwd.size();
       std::vector<int32_t> inv(n, -1);
       int r = 0;
       for (auto& pr : c.e->schur) {
         auto it = fpos[f.slot].find(pr.first);
         if (it == fpos[f.slot].end()) fail("child schur node missing in parent", 6);
-        for (int k = 0; k < pr.first->get_n_dof(); ++k, ++r) inv[it->second + k] = r;
+        for (int k = 0; k < pr.first->get_n_dof(); ++k, ++r) {
+          inv[it->second + k] = r;
+          h_fwd.push_back(it->second + k);
+        }
       }
+      if (r != c.ss) fail("child schur rows do not match its schur size", 6);
+      h_srcs.push_back(sd);
       invs.push_back(std::move(inv));
     }
     f.nsrc = (int)invs.size();
@@ -592,9 +604,16 @@ void Engine::build_programs(int method) {
       std::vector<Item> asm_items, small_items;
       std::vector<int> large;
       int max_small = 1;
+      std::vector<Item> asm_big;
+      int n_big = 0;
       for (int s : fl) {
         const int n = fronts[s].n;
-        for (int J0 = 0; J0 < n; J0 += ASM_TJ) asm_items.push_back(Item{s, J0, 0, 0});
+        if (n >= ASM_SCATTER_MIN && n <= ASM_SCATTER_MAX) {
+          for (int J = 0; J < n; ++J) asm_big.push_back(Item{s, J, 0, 0});
+          n_big = std::max(n_big, n);
+        } else {
+          for (int J0 = 0; J0 < n; J0 += ASM_TJ) asm_items.push_back(Item{s, J0, 0, 0});
+        }
         if (fronts[s].tc) continue;
         if (n <= small_max[dt]) {
           small_items.push_back(Item{s, 0, 0, 0});
@@ -625,7 +644,8 @@ void Engine::build_programs(int method) {
           small_flops += dec;
         }
       }
-      push(fac_ops, OP_ASSEMBLE, dt, 0, chol ? 1 : 0, asm_items, 0, asm_bytes);
+      push(fac_ops, OP_ASSEMBLE, dt, 0, chol ? 1 : 0, asm_items, 0, asm_items.empty() ? 0.0 : asm_bytes);
+      push(fac_ops, OP_ASSEMBLE_SCATTER, dt, n_big, chol ? 1 : 0, asm_big, 0, asm_items.empty() ? asm_bytes : 0.0);
       push(fac_ops, OP_SMALL_FACTOR, dt, 0, max_small, small_items, small_flops);
       int maxfs = 0;
       for (int s : large) maxfs = std::max(maxfs, fronts[s].fs);
@@ -928,6 +948,7 @@ void Engine::alloc_device(int method) {
   ctx.fronts = (FrontDev*)dmalloc(sizeof(FrontDev) * h_fronts.size());
   ctx.srcs = (SrcDev*)dmalloc(sizeof(SrcDev) * std::max<size_t>(1, h_srcs.size()));
   ctx.inv = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_inv.size()));
+  ctx.fwd = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_fwd.size()));
   ctx.colptr = (int64_t*)dmalloc(sizeof(int64_t) * h_colptr.size());
   ctx.colsrc = (int2*)dmalloc(sizeof(int2) * std::max<size_t>(1, h_colsrc.size()));
   ctx.sgi = (int32_t*)dmalloc(sizeof(int32_t) * std::max<size_t>(1, h_sgi.size()));
@@ -1040,6 +1061,7 @@ void Engine::alloc_device(int method) {
   up(ctx.fronts, h_fronts.data(), sizeof(FrontDev) * h_fronts.size());
   up(ctx.srcs, h_srcs.data(), sizeof(SrcDev) * h_srcs.size());
   up(ctx.inv, h_inv.data(), sizeof(int32_t) * h_inv.size());
+  up(ctx.fwd, h_fwd.data(), sizeof(int32_t) * h_fwd.size());
   up(ctx.colptr, h_colptr.data(), sizeof(int64_t) * h_colptr.size());
   up(ctx.colsrc, h_colsrc.data(), sizeof(int2) * h_colsrc.size());
   up(ctx.sgi, h_sgi.data(), sizeof(int32_t) * h_sgi.size());
@@ -1128,6 +1150,9 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
     if (profiling) CK(cudaEventRecord(evs[2 * k], stream));
     switch (op.kind) {
       case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, stream); break;
+      case OP_ASSEMBLE_SCATTER:
+        launch_assemble_scatter(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream);
+        break;
       case OP_SMALL_FACTOR:
         launch_small_factor(ctx, it, op.n_items, op.dtype,
                             ctx.symmetric ? M_CHOL : (method_built == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV),

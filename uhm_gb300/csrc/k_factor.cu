@@ -63,6 +63,59 @@ __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restri
   }
 }
 
+// Extend-add of a large front, one parent column J per CTA.  The column is
+// accumulated in shared memory in FP64: zero, then each source holding
+// column J in source order (the element, then the children in child order)
+// scatters its column through its row map (an injective map, so a source
+// never hits the same entry twice and one barrier between sources keeps the
+// order); then the column is written once.  Every entry therefore gets the
+// same sum in the same order as in k_assemble (bit-identical), but each
+// source entry is read once instead of every parent row looking up every
+// source.
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble_scatter(DevCtx c, const Item* __restrict__ items,
+                                                          int lower) {
+  extern __shared__ double s_col[];
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, J = it.a;
+  const int istart = lower ? J : 0;
+  for (int I = istart + threadIdx.x; I < n; I += blockDim.x) s_col[I] = 0.0;
+  const int64_t* __restrict__ cp = c.colptr + f.colptr_off;
+  const int64_t k0 = cp[J], k1 = cp[J + 1];
+  __syncthreads();
+  for (int64_t k = k0; k < k1; ++k) {
+    const int2 cs = c.colsrc[k];
+    const SrcDev sd = c.srcs[f.src0 + cs.x];
+    const int32_t* __restrict__ fw = c.fwd + sd.fwd_off;
+#pragma unroll 4
+    for (int r = threadIdx.x; r < sd.m; r += blockDim.x) {
+      const int I = fw[r];
+      if (I >= istart) {
+        int rr = r, cc = cs.y;
+        if (sd.is_child && c.symmetric && rr < cc) { const int t = rr; rr = cc; cc = t; }
+        s_col[I] += load_src(c, sd, rr + (int64_t)cc * sd.ld);
+      }
+    }
+    __syncthreads();
+  }
+  T* __restrict__ P = arena<T>(c) + f.off + (int64_t)J * n;
+  for (int I = istart + threadIdx.x; I < n; I += blockDim.x) P[I] = (T)s_col[I];
+}
+
+void launch_assemble_scatter(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
+                             int n_max, cudaStream_t s) {
+  if (!n_items) return;
+  const size_t sm = sizeof(double) * (size_t)n_max;
+  if (dtype == F64) {
+    cudaFuncSetAttribute(k_assemble_scatter<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_assemble_scatter<double><<<n_items, 256, sm, s>>>(c, items, lower);
+  } else {
+    cudaFuncSetAttribute(k_assemble_scatter<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_assemble_scatter<float><<<n_items, 256, sm, s>>>(c, items, lower);
+  }
+}
+
 void launch_assemble(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
                      cudaStream_t s) {
   if (!n_items) return;

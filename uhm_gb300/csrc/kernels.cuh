@@ -40,6 +40,8 @@ struct SrcDev {
   int dtype;          // F64 / F32 (element matrices are F64)
   int is_child;       // 1: child ABR (lower triangle valid when symmetric)
   int slot;           // child front slot (or element index)
+  int m;              // rows (= columns) of the source block
+  int64_t fwd_off;    // its row map: source row -> parent position (DevCtx::fwd)
 };
 
 // Work item for per-front launches: front slot + tile / step data.
@@ -55,6 +57,7 @@ struct DevCtx {
   FrontDev* fronts;
   SrcDev* srcs;
   int32_t* inv;       // inverse maps
+  int32_t* fwd;       // forward maps (source row -> parent position)
   int64_t* colptr;    // per front: n+1 offsets into colsrc
   int2* colsrc;       // (source local index, source column)
   int32_t* sgi;       // schur-row global dofs
@@ -72,6 +75,10 @@ struct DevCtx {
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----------------------
+// extend-add of large fronts: one parent column per CTA, accumulated in
+// shared memory (item: front, a = column)
+void launch_assemble_scatter(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
+                             int n_max, cudaStream_t s);
 void launch_assemble(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
                      cudaStream_t s);
 void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
