@@ -814,7 +814,7 @@ template <> __device__ __forceinline__ const float* dinv_arena<float>(const DevC
 // item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
 // right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
                                                    int* ticket, int* err, int q0) {
   using CT = T;
   __shared__ int s_t;
@@ -902,19 +902,31 @@ __global__ void __launch_bounds__(256, 3) k_fwd_flags(DevCtx c, const Item* __re
   }
   __syncthreads();
   if (factor_block) {
+    // y = Dinv v on all 256 threads: column group g sums t in [16 g, 16 g + 16)
+    // (Dinv is lower triangular: t <= i), then the four partial sums are
+    // added in group order; this takes the 64-step dependent chain of one
+    // thread per row off the hand-off to the next block
     const int kb = r1 - r0;
-    if (threadIdx.x < FB && rv) {
-      CT x[SF_NR];
+    CT xp[SF_NR];
 #pragma unroll
-      for (int q = 0; q < SF_NR; ++q) x[q] = CT(0);
-      for (int t = 0; t <= i && t < kb; ++t) {
+    for (int q = 0; q < SF_NR; ++q) xp[q] = CT(0);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int t = g * 16 + u;
+      if (t <= i && t < kb) {
         const CT d = (CT)dsh[t * (FB + 1) + i];     // Dinv[i][t], column t staged as row t
 #pragma unroll
-        for (int q = 0; q < SF_NR; ++q) x[q] += d * v[t][q];
+        for (int q = 0; q < SF_NR; ++q) xp[q] += d * v[t][q];
       }
+    }
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q) red[g][i][q] = xp[q];
+    __syncthreads();
+    if (threadIdx.x < FB && rv) {
 #pragma unroll
       for (int q = 0; q < SF_NR; ++q)
-        if (q0 + q < nr) y[row + (int64_t)(q0 + q) * n] = (double)x[q];
+        if (q0 + q < nr)
+          y[row + (int64_t)(q0 + q) * n] = (double)(red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]);
     }
     __threadfence();
     __syncthreads();
@@ -1034,15 +1046,30 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     }
   }
   __syncthreads();
-  // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t   (column i of Dinv, staged at start)
+  // x = Dinv^T v : x_i = sum_{t >= i} Dinv[t, i] v_t   (column i of Dinv, staged at start),
+  // on all 256 threads: group gg sums t in [16 gg, 16 gg + 16), partial sums
+  // added in group order
+  {
+    const int ii = threadIdx.x % FB, gg = threadIdx.x / FB;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      CT xp = CT(0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int t = gg * 16 + u;
+        if (t >= ii && t < kb) xp += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
+      }
+      red[gg * NQ + q][ii] = xp;
+    }
+  }
+  __syncthreads();
   if (threadIdx.x < kb) {
     const int ii = threadIdx.x;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       if (q0 + q >= nr) break;
-      CT x = CT(0);
-      for (int t = ii; t < kb; ++t) x += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
-      y[c0 + ii + (int64_t)(q0 + q) * n] = (double)x;
+      y[c0 + ii + (int64_t)(q0 + q) * n] =
+          (double)(red[q][ii] + red[NQ + q][ii] + red[2 * NQ + q][ii] + red[3 * NQ + q][ii]);
     }
   }
   __threadfence();
