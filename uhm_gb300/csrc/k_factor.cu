@@ -261,22 +261,24 @@ void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dt
 // k_potrf_trsm).  Warp w owns the column block 8w..8w+7 of the symmetric
 // 64 x 64 block and of the inverse X = L^{-1} being formed; lane (ti, h)
 // keeps the 4 x 4 tile at rows 4 ti.., columns 8w + 4h.. of both in
-// registers.  Right-looking in column order; for each column p a warp
-//   (factor, p <= 8w+7) applies A[i][j] -= l_ip l_jp to its tile, where
-//     l_ip = v_p[i] / sqrt(v_p[p]) and v_p, column p of the partially reduced
-//     block, was published in shared memory by the 16 lanes owning it;
-//   (inverse, p >= 8w) scales row p of its column block of X by 1 / l_pp and
-//     applies X[i][:] -= l_ip x_p for i > p (column blocks of X are
-//     independent, so this needs nothing from other warps but v_p).
-// One block barrier per column publishes the next column.  A warp does only
-// the factor steps that reach its columns and only the inverse steps whose
-// rows are nonzero in them.  Columns are walked four at a time so that
-// register indices inside a tile are compile-time constants.  Blocks
-// narrower than 64 are padded with the identity.  FP32 pivots use rsqrt (the
-// factor is refined in FP64 by the mixed path); FP64 uses sqrt and a divide.
-// Measured alternatives: a fully unrolled left-looking version (one row per
+// registers.  Right-looking, four columns P..P+3 per phase: the columns, as
+// reduced by all earlier phases, were published in shared memory (V[P+j]);
+// every thread factors their 4 x 4 pivot block itself, forms the factor
+// entries of its 4 rows and 4 columns by a 4-step substitution
+//   l_rj = (v_{P+j}[r] - sum_{m<j} l_rm l_{P+j,P+m}) / l_{P+j,P+j},
+// and applies the rank-4 update A -= L_r L_c^T to its tile; the owners of
+// columns P+4..P+7 then publish them.  In the same phase the owners of rows
+// P..P+3 of X finish them with the pivot block's substitution and the other
+// rows take the rank-4 update X -= L[:, P:P+4] X[P:P+4, :] (column blocks of
+// X are independent, so rows go through shared memory per warp).  One block
+// barrier per phase, 16 in all.  A warp does only the factor work that
+// reaches its columns and only the inverse work whose rows are nonzero in
+// them.  Blocks narrower than 64 are padded with the identity.  FP32 pivots
+// use rsqrt (the factor is refined in FP64 by the mixed path); FP64 uses sqrt
+// and a divide.  Measured alternatives: one column per phase (64 barriers)
+// took 2x as long; a fully unrolled left-looking version (one row per
 // thread, ~100 KB of straight-line code) was bound by instruction fetch;
-// warp-to-warp hand-offs on mbarriers or shared flags instead of the block
+// hand-offs between warps on mbarriers or shared flags instead of the block
 // barrier were slower (their wake-up latency).
 template <typename T> __device__ __forceinline__ void pivot_root(T s, T& d, T& rd);
 template <> __device__ __forceinline__ void pivot_root<float>(float s, float& d, float& rd) {
@@ -313,18 +315,17 @@ template <> struct Vec4<double> {
 template <typename T>
 struct PotrfShared {
   T V[64][64];      // V[p][i]: column p of the reduced block (zero above p)
-  T XR[8][2][8];    // per warp: row p of its block of X, scaled, double-buffered
-  T sd[64], srd[64];
+  T XR[8][4][8];    // per warp: rows P..P+3 of its block of X, finished
 };
 
 // Factor the 64 x 64 block at G (leading dimension n, kb <= 64 valid rows and
-// columns) in shared memory; on return x holds this thread's tile of
-// L^{-1}, sh.V / sh.sd / sh.srd the factor (L[i][k] = V[k][i] * srd[k] below
-// the diagonal, sd[k] on it), after a block barrier; bad is set when a pivot
-// was not positive.
+// columns) in shared memory; on return x holds this thread's tile of L^{-1}
+// and, when Lout is not null, the lower triangle of L has been written there
+// (leading dimension n); bad is set when a pivot was not positive.  Ends
+// with a block barrier.
 template <typename T>
 __device__ __forceinline__ void potrf_block(const T* __restrict__ G, int n, int kb, PotrfShared<T>& sh,
-                                            T (&x)[4][4], bool& bad) {
+                                            T (&x)[4][4], bool& bad, T* __restrict__ Lout) {
   const int tid = threadIdx.x, w = tid >> 5;
   const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
   const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
@@ -353,74 +354,114 @@ __device__ __forceinline__ void potrf_block(const T* __restrict__ G, int n, int 
       a[u][v] = i >= j ? sh.V[j][i] : sh.V[i][j];
       x[u][v] = i == j ? T(1) : T(0);
     }
-  __syncthreads();   // tiles read before any column is republished; column 0 stays as staged
+  __syncthreads();   // tiles read before any column is republished; columns 0..3 stay as staged
   bad = false;
 #pragma unroll 1
   for (int q = 0; q < 16; ++q) {
+    const int P = 4 * q;
+    // the pivot block (every thread factors it) and this thread's rows / columns
+    T bk[4][4], lr[4][4], lc[4][4];   // bk[j][i] = v_{P+j}[P+i]; lr[u][j], lc[v][j]: factor entries
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      const int p = 4 * q + s;
-      T piv = sh.V[p][p];
-      if (!(piv > T(0))) { bad = true; piv = T(1); }
-      T d, rd;
-      pivot_root<T>(piv, d, rd);
-      if (tid == 0) { sh.sd[p] = d; sh.srd[p] = rd; }
-      T lr[4];
-      Vec4<T>::ld(&sh.V[p][r0], lr);
+    for (int j = 0; j < 4; ++j) {
+      T t4[4];
+      Vec4<T>::ld(&sh.V[P + j][P], bk[j]);
+      Vec4<T>::ld(&sh.V[P + j][r0], t4);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) lr[u] *= rd;
-      if (p <= cb0 + 7) {
-        T lc[4];
-        Vec4<T>::ld(&sh.V[p][c0], lc);
+      for (int u = 0; u < 4; ++u) lr[u][j] = t4[u];
+      Vec4<T>::ld(&sh.V[P + j][c0], t4);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) lc[v] *= rd;
+      for (int v = 0; v < 4; ++v) lc[v][j] = t4[v];
+    }
+    T lb[4][4], rd[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+    for (int j = 0; j < 4; ++j) {
+      T s = bk[j][j];
 #pragma unroll
-          for (int v = 0; v < 4; ++v) a[u][v] -= lr[u] * lc[v];
-        if (p + 1 < 64 && ((p + 1) >> 3) == w && tj == (p + 1) >> 2) {
-          const int CB = (s + 1) & 3;   // constant after unrolling
+      for (int m = 0; m < j; ++m) s -= lb[j][m] * lb[j][m];
+      if (!(s > T(0))) { bad = true; s = T(1); }
+      T d;
+      pivot_root<T>(s, d, rd[j]);
+      lb[j][j] = d;
+#pragma unroll
+      for (int i = j + 1; i < 4; ++i) {
+        T t = bk[j][i];
+#pragma unroll
+        for (int m = 0; m < j; ++m) t -= lb[i][m] * lb[j][m];
+        lb[i][j] = t * rd[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        T t = lr[u][j], tc = lc[u][j];
+#pragma unroll
+        for (int m = 0; m < j; ++m) { t -= lr[u][m] * lb[j][m]; tc -= lc[u][m] * lb[j][m]; }
+        lr[u][j] = t * rd[j];
+        lc[u][j] = tc * rd[j];
+      }
+    if (P <= cb0 + 3) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) a[u][v] -= lr[u][j] * lc[v][j];
+      if (P + 4 < 64 && tj == q + 1) {
+        // publish columns P+4..P+7 (zero above their diagonal)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
           T wv[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= p + 1) ? a[u][CB] : T(0);
-          Vec4<T>::st(&sh.V[p + 1][r0], wv);
+          for (int u = 0; u < 4; ++u) wv[u] = (r0 + u >= P + 4 + v) ? a[u][v] : T(0);
+          Vec4<T>::st(&sh.V[P + 4 + v][r0], wv);
         }
       }
-      if (p >= cb0) {
-        if (ti == q) {
+    }
+    if (Lout && tj == q) {
 #pragma unroll
-          for (int v = 0; v < 4; ++v) x[s][v] *= rd;
-          Vec4<T>::st(&sh.XR[w][p & 1][4 * h], x[s]);
-        }
-        __syncwarp();
-        T xr[4];
-        Vec4<T>::ld(&sh.XR[w][p & 1][4 * h], xr);
+      for (int j = 0; j < 4; ++j)
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const T l = (r0 + u > p) ? lr[u] : T(0);
+          const int i = r0 + u, k = P + j;
+          if (i >= k && i < kb && k < kb) Lout[i + (int64_t)k * n] = lr[u][j];
+        }
+    }
+    if (P + 3 >= cb0) {
+      if (ti == q) {
+        // rows P..P+3 of X: their last substitution, then published to the warp
 #pragma unroll
-          for (int v = 0; v < 4; ++v) x[u][v] -= l * xr[v];
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+          for (int m = 0; m < i; ++m)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) x[i][v] -= lb[i][m] * x[m][v];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) x[i][v] *= rd[i];
+          Vec4<T>::st(&sh.XR[w][i][4 * h], x[i]);
         }
       }
-      __syncthreads();
+      __syncwarp();
+      T xr[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Vec4<T>::ld(&sh.XR[w][j][4 * h], xr[j]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (r0 + u > P + 3) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) x[u][v] -= lr[u][j] * xr[j][v];
+        }
     }
+    __syncthreads();
   }
 }
 
-// L of the block into G (lower triangle; when G is not null) and its
-// inverse, column-major with 128-bit stores, into D (when not null)
+// the inverse, column-major with 128-bit stores (Dinv[j * 64 + i] = X[i][j]), into D
 template <typename T>
-__device__ __forceinline__ void potrf_store(T* __restrict__ G, int n, int kb, const PotrfShared<T>& sh,
-                                            const T (&x)[4][4], T* __restrict__ D) {
+__device__ __forceinline__ void potrf_store_inverse(int kb, const T (&x)[4][4], T* __restrict__ D) {
   const int tid = threadIdx.x;
-  if (G) {
-#pragma unroll 4
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx & 63, k = idx >> 6;
-      if (i >= k && i < kb && k < kb) G[i + (int64_t)k * n] = i == k ? sh.sd[k] : sh.V[k][i] * sh.srd[k];
-    }
-  }
-  if (!D) return;
   const int r0 = 4 * (tid & 15), c0 = 4 * (tid >> 4);
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
@@ -442,10 +483,11 @@ __global__ void __launch_bounds__(256) k_potrf_diag(DevCtx c, const Item* __rest
   T* __restrict__ G = arena<T>(c) + f.off + k0 + (int64_t)k0 * n;
   T x[4][4];
   bool bad;
-  potrf_block<T>(G, n, kb, sh, x, bad);
+  // L is written over the block in place: only this CTA reads it
+  potrf_block<T>(G, n, kb, sh, x, bad, G);
   if (bad && threadIdx.x == 0) set_status(c, it.front, ST_NOT_SPD);
   T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
-  potrf_store<T>(G, n, kb, sh, x, (nb == 64 && Dinv) ? Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096 : nullptr);
+  if (nb == 64 && Dinv) potrf_store_inverse<T>(kb, x, Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096);
 }
 
 void launch_potrf_diag(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
@@ -577,12 +619,12 @@ __global__ void __launch_bounds__(256) k_potrf_trsm(DevCtx c, const Item* __rest
   const int tid = threadIdx.x;
   T x[4][4];
   bool bad;
-  potrf_block<T>(G, n, kb, sh, x, bad);
+  potrf_block<T>(G, n, kb, sh, x, bad, nullptr);
   const bool writer = it.c & 1;
   if (writer) {
     if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
     T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
-    potrf_store<T>(nullptr, n, kb, sh, x, Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096);
+    potrf_store_inverse<T>(kb, x, Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096);
   }
   if (r0 >= n) return;
   const int rb = min(TRSM_RB, n - r0);
