@@ -579,15 +579,21 @@ void Engine::build_programs(int method) {
       push(fac_ops, OP_TRSM, dt, NB, 0, t_items, ft);
       return;
     }
+    // consecutive row blocks of a front grouped so that the launch is one wave
+    const int per_cta = std::max<int>(1, (int)((t_items.size() + n_sm - 1) / n_sm));
     std::vector<Item> fi;
     for (const Item& d : p_items) {
-      bool first = true;
+      std::vector<int> rows;
       for (const Item& t : t_items)
-        if (t.front == d.front) {
-          fi.push_back(Item{t.front, t.a, t.b, first ? 1 : 0});
-          first = false;
-        }
-      if (first) fi.push_back(Item{d.front, d.a, fronts[d.front].n, 1});
+        if (t.front == d.front) rows.push_back(t.b);
+      if (rows.empty()) {
+        fi.push_back(Item{d.front, d.a, fronts[d.front].n, 1});
+        continue;
+      }
+      for (size_t g0 = 0; g0 < rows.size(); g0 += per_cta) {
+        const int cnt = (int)std::min<size_t>(per_cta, rows.size() - g0);
+        fi.push_back(Item{d.front, d.a, rows[g0], (g0 == 0 ? 1 : 0) | (cnt << 1)});
+      }
     }
     push(fac_ops, OP_POTRF_TRSM, dt, NB, 0, fi, fp + ft);
   };

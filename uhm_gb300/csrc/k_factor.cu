@@ -512,8 +512,8 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
   const int n = f.n, k0 = it.a, r0 = it.b;
   const int kb = min(nb, f.fs - k0);
   const int rb = min(TRSM_RB, n - r0);
-  T* L = reinterpret_cast<T*>(smem_raw);        // kb x kb (or 64 x 65 padded inverse)
-  T* X = L + 64 * 65;                           // TRSM_RB x kb, ld TRSM_RB
+  T* L = reinterpret_cast<T*>(smem_raw);        // kb x kb (or 64 x 68 padded inverse)
+  T* X = L + 64 * 68;                           // TRSM_RB x kb, ld TRSM_RB
   T* __restrict__ G = arena<T>(c) + f.off;
   const T* Dinv = (sizeof(T) == 8 ? (const T*)c.dinv64 : (const T*)c.dinv32);
   if (nb == 64 && Dinv) {
@@ -533,10 +533,10 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
     for (int u = 0; u < 16; ++u) {
       const int idx = threadIdx.x + NT * u;
       // Dinv is column-major: Dinv[t * 64 + j] = Linv[j][t]; keep it as
-      // rows t of length 64 padded to 65, so that L[t * 65 + j] = Linv[j][t]
+      // rows t of length 64 padded to 68 (16-byte rows), L[t * 68 + j] = Linv[j][t]
       const int t = idx / 64, j = idx % 64;
       X[idx] = xv[u];
-      L[t * 65 + j] = (t < kb && j < kb) ? dv[u] : T(0);
+      L[t * 68 + j] = (t < kb && j < kb) ? dv[u] : T(0);
     }
     __syncthreads();
     const int i = threadIdx.x % TRSM_RB, jg = threadIdx.x / TRSM_RB;   // 4 column groups of 16
@@ -546,7 +546,12 @@ __global__ void __launch_bounds__(NT) k_trsm_panel(DevCtx c, const Item* __restr
     for (int t = 0; t < kb; ++t) {
       const T x = X[i + t * TRSM_RB];
 #pragma unroll
-      for (int u = 0; u < 16; ++u) acc[u] += x * L[t * 65 + jg * 16 + u];
+      for (int u4 = 0; u4 < 16; u4 += 4) {
+        T l4[4];
+        Vec4<T>::ld(&L[t * 68 + jg * 16 + u4], l4);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[u4 + e] += x * l4[e];
+      }
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
@@ -585,11 +590,11 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
                        cudaStream_t s) {
   if (!n_items) return;
   if (dtype == F64) {
-    size_t sm = (size_t)(64 * 65 + TRSM_RB * nb) * sizeof(double);
+    size_t sm = (size_t)(64 * 68 + TRSM_RB * nb) * sizeof(double);
     cudaFuncSetAttribute(k_trsm_panel<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_trsm_panel<double, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   } else {
-    size_t sm = (size_t)(64 * 65 + TRSM_RB * nb) * sizeof(float);
+    size_t sm = (size_t)(64 * 68 + TRSM_RB * nb) * sizeof(float);
     cudaFuncSetAttribute(k_trsm_panel<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_trsm_panel<float, 256><<<n_items, 256, sm, s>>>(c, items, nb);
   }
@@ -602,17 +607,20 @@ void launch_trsm_panel(const DevCtx& c, const Item* items, int n_items, int dtyp
 // CTA flagged in the item writes the inverse, which is how the factor's
 // diagonal block is kept: the flag-driven solves and this TRSM use only the
 // inverse, and writing L over the block in place would race with other
-// CTAs still reading A's block, so the arena keeps A's diagonal block.
-// Item: front, a = k0, b = first row of the block (n: none), c = 1 for the
-// writer.
+// CTAs still reading A's block, so the arena keeps A's diagonal block.  A CTA
+// takes several consecutive row blocks, so that a step's launch is one wave.
+// Item: front, a = k0, b = first row of the first block (n: none),
+// c = writer (bit 0) + 2 * number of row blocks.
+constexpr int PT_LD = 68;   // row length of the transposed inverse in shared memory (16-byte rows)
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_potrf_trsm(DevCtx c, const Item* __restrict__ items) {
   extern __shared__ __align__(16) unsigned char pt_smem[];
   PotrfShared<T>& sh = *reinterpret_cast<PotrfShared<T>*>(pt_smem);
-  T* Lt = reinterpret_cast<T*>(pt_smem + ((sizeof(PotrfShared<T>) + 15) / 16) * 16);   // 64 x 65
+  T* Lt = reinterpret_cast<T*>(pt_smem + ((sizeof(PotrfShared<T>) + 15) / 16) * 16);   // 64 x PT_LD
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
-  const int n = f.n, k0 = it.a, r0 = it.b;
+  const int n = f.n, k0 = it.a;
   const int kb = min(64, f.fs - k0);
   T* __restrict__ A = arena<T>(c) + f.off;
   T* __restrict__ G = A + k0 + (int64_t)k0 * n;
@@ -621,15 +629,15 @@ __global__ void __launch_bounds__(256) k_potrf_trsm(DevCtx c, const Item* __rest
   bool bad;
   potrf_block<T>(G, n, kb, sh, x, bad, nullptr);
   const bool writer = it.c & 1;
+  const int nrb = it.c >> 1;
   if (writer) {
     if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
     T* Dinv = (sizeof(T) == 8 ? (T*)c.dinv64 : (T*)c.dinv32);
     potrf_store_inverse<T>(kb, x, Dinv + f.dinv_off + (int64_t)(k0 / 64) * 4096);
   }
-  if (r0 >= n) return;
-  const int rb = min(TRSM_RB, n - r0);
-  // L^{-1} transposed into Lt (Lt[t * 65 + j] = Linv[j][t]); the panel
-  // block into V (its factor values are no longer needed once written)
+  if (it.b >= n || nrb == 0) return;
+  // L^{-1} transposed into Lt (Lt[t * PT_LD + j] = Linv[j][t]); the panel
+  // blocks into V in turn (its factor values are no longer needed)
   {
     const int ti = tid & 15, tj = tid >> 4;
 #pragma unroll
@@ -637,45 +645,56 @@ __global__ void __launch_bounds__(256) k_potrf_trsm(DevCtx c, const Item* __rest
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int j = 4 * ti + u, t = 4 * tj + v;   // x[u][v] = Linv[j][t]
-        Lt[t * 65 + j] = (j < kb && t < kb) ? x[u][v] : T(0);
+        Lt[t * PT_LD + j] = (j < kb && t < kb) ? x[u][v] : T(0);
       }
   }
-  T* X = &sh.V[0][0];   // 64 x 64, column-major (V is free: nothing reads the factor any more)
-  {
-    T xv[16];
+  T* X = &sh.V[0][0];   // 64 x 64, column-major
+  const int i = tid % TRSM_RB, jg = tid / TRSM_RB;   // 4 column groups of 16
+  for (int blk = 0; blk < nrb; ++blk) {
+    const int r0 = it.b + blk * TRSM_RB;
+    if (r0 >= n) break;
+    const int rb = min(TRSM_RB, n - r0);
+    {
+      T xv[16];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx % TRSM_RB, j = idx / TRSM_RB;
-      xv[u] = (i < rb && j < kb) ? A[(r0 + i) + (int64_t)(k0 + j) * n] : (T)0;
+      for (int u = 0; u < 16; ++u) {
+        const int idx = tid + 256 * u, ii = idx % TRSM_RB, j = idx / TRSM_RB;
+        xv[u] = (ii < rb && j < kb) ? A[(r0 + ii) + (int64_t)(k0 + j) * n] : (T)0;
+      }
+      __syncthreads();   // the previous block's reads of X are done
+#pragma unroll
+      for (int u = 0; u < 16; ++u) X[tid + 256 * u] = xv[u];
+    }
+    __syncthreads();
+    T acc[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[u] = T(0);
+    for (int t = 0; t < kb; ++t) {
+      const T xt = X[i + t * TRSM_RB];
+#pragma unroll
+      for (int u4 = 0; u4 < 16; u4 += 4) {
+        T l4[4];
+        Vec4<T>::ld(&Lt[t * PT_LD + jg * 16 + u4], l4);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[u4 + e] += xt * l4[e];
+      }
     }
 #pragma unroll
-    for (int u = 0; u < 16; ++u) X[tid + 256 * u] = xv[u];
-  }
-  __syncthreads();
-  const int i = tid % TRSM_RB, jg = tid / TRSM_RB;   // 4 column groups of 16
-  T acc[16];
-#pragma unroll
-  for (int u = 0; u < 16; ++u) acc[u] = T(0);
-  for (int t = 0; t < kb; ++t) {
-    const T xv = X[i + t * TRSM_RB];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) acc[u] += xv * Lt[t * 65 + jg * 16 + u];
-  }
-#pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int j = jg * 16 + u;
-    if (i < rb && j < kb) A[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
+    for (int u = 0; u < 16; ++u) {
+      const int j = jg * 16 + u;
+      if (i < rb && j < kb) A[(r0 + i) + (int64_t)(k0 + j) * n] = acc[u];
+    }
   }
 }
 
 void launch_potrf_trsm(const DevCtx& c, const Item* items, int n_items, int dtype, cudaStream_t s) {
   if (!n_items) return;
   if (dtype == F64) {
-    const size_t sm = ((sizeof(PotrfShared<double>) + 15) / 16) * 16 + sizeof(double) * 64 * 65;
+    const size_t sm = ((sizeof(PotrfShared<double>) + 15) / 16) * 16 + sizeof(double) * 64 * PT_LD;
     cudaFuncSetAttribute(k_potrf_trsm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_potrf_trsm<double><<<n_items, 256, sm, s>>>(c, items);
   } else {
-    const size_t sm = ((sizeof(PotrfShared<float>) + 15) / 16) * 16 + sizeof(float) * 64 * 65;
+    const size_t sm = ((sizeof(PotrfShared<float>) + 15) / 16) * 16 + sizeof(float) * 64 * PT_LD;
     cudaFuncSetAttribute(k_potrf_trsm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_potrf_trsm<float><<<n_items, 256, sm, s>>>(c, items);
   }
