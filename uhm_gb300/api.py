@@ -282,7 +282,7 @@ class Mesh:
                 "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
                 "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
                 "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
-                "laswp", "potrf_trsm", "assemble_scatter"] + [f"op{k}" for k in range(25, 32)]
+                "laswp", "potrf_trsm", "assemble_scatter", "tc_gemm_bf16"] + [f"op{k}" for k in range(26, 32)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))

@@ -398,7 +398,10 @@ void Engine::build_plan(int method) {
         p = front_prec_override[f.slot];
     }
     f.prec = p;
-    f.tc = (p == PREC_BF16X3 || p == PREC_BF16X6) && f.n >= tune.tc_min_n && method == UHM_CHOL;
+    // tensor-core Schur updates: Cholesky in BF16X3 / BF16X6, LU in BF16X3
+    // (its two operands take four packed parts)
+    f.tc = f.n >= tune.tc_min_n &&
+           (method == UHM_CHOL ? (p == PREC_BF16X3 || p == PREC_BF16X6) : p == PREC_BF16X3);
   }
   arena64_n = arena32_n = vec_n = piv_n = 0;
   ws_total = 0;
@@ -407,7 +410,7 @@ void Engine::build_plan(int method) {
     const int64_t mmax = f.n - std::min(tune.tc_nbo, f.fs);
     f.ws_off = ws_total;
     f.ws_stride = mmax * tune.tc_nbo;
-    ws_total += 3 * f.ws_stride;
+    ws_total += (method == UHM_CHOL ? 3 : 4) * f.ws_stride;
   }
   h_fronts.assign(fronts.size(), FrontDev{});
   h_srcs.clear();
@@ -597,6 +600,65 @@ void Engine::build_programs(int method) {
     }
     push(fac_ops, OP_POTRF_TRSM, dt, NB, 0, fi, fp + ft);
   };
+  // one LU step's 64-column panel: tall panels (many rows below the
+  // diagonal) on many CTAs at once (panel-only row swaps, then k_laswp for
+  // the other columns), the rest one CTA per front.  nbo > 0 (tensor-core
+  // fronts): rows are swapped only in columns below the outer panel's
+  // trailing block, whose swaps come after the outer panel
+  auto push_lu_panel = [&](int dt, const std::vector<Item>& p_items, double fp, int nbo) {
+    const int piv = method == UHM_LU_PIV ? 1 : 0;
+    const int rcap = dt == F64 ? GC_RMAX_F64 : GC_RMAX_F32;
+    auto col_end = [&](const Item& it) {
+      if (nbo <= 0) return 0;
+      return std::min((it.a / nbo) * nbo + nbo, fronts[it.front].fs);
+    };
+    std::vector<Item> one, tall;
+    for (const Item& it : p_items) {
+      if (fronts[it.front].n - it.a >= tune.gc_min_rows) tall.push_back(it);
+      else one.push_back(Item{it.front, it.a, col_end(it), 0});
+    }
+    push(fac_ops, OP_GETRF, dt, NB, piv, one, tall.empty() ? fp : 0.0);
+    size_t i0 = 0;
+    while (i0 < tall.size()) {
+      // a group whose minimum CTA counts fit one cooperative launch
+      size_t i1 = i0;
+      int need = 0;
+      double rows_sum = 0;
+      while (i1 < tall.size()) {
+        const int rows = fronts[tall[i1].front].n - tall[i1].a;
+        const int mn = (rows + rcap - 1) / rcap;
+        if (i1 > i0 && need + mn > n_sm) break;
+        need += mn;
+        rows_sum += rows;
+        ++i1;
+      }
+      std::vector<Item> g;
+      int b = 0, rmax = 1;
+      const int spare = std::max(0, n_sm - need);
+      for (size_t i = i0; i < i1; ++i) {
+        const int rows = fronts[tall[i].front].n - tall[i].a;
+        int P = (rows + rcap - 1) / rcap + (int)(spare * (rows / rows_sum));
+        P = std::max(1, std::min(P, rows));
+        g.push_back(Item{tall[i].front, tall[i].a, b, P});
+        rmax = std::max(rmax, (rows + P - 1) / P);
+        b += P;
+      }
+      Op op{OP_GETRF_COOP, dt, NB, piv, add_items(g), (int)g.size()};
+      op.q0 = b;
+      op.aux = rmax;
+      if (i0 == 0) op.flops = fp;
+      fac_ops.push_back(op);
+      if (piv) {
+        std::vector<Item> sw;
+        for (const Item& it : g) {
+          const int ce = col_end(it), lim = ce > 0 ? ce : fronts[it.front].n;
+          for (int c0 = 0; c0 < lim; c0 += 256) sw.push_back(Item{it.front, it.a, c0, ce});
+        }
+        push(fac_ops, OP_LASWP, dt, NB, 0, sw);
+      }
+      i0 = i1;
+    }
+  };
   const int small_max[2] = {tune.small_max_f64, tune.small_max_f32};
   for (auto& lv : levels) {
     for (int dt = 0; dt < 2; ++dt) {
@@ -690,52 +752,7 @@ void Engine::build_programs(int method) {
           push_potrf_trsm(dt, p_items, t_items, fp, ft);
           push(fac_ops, OP_SYRK, dt, NB, 0, u_items, fu);
         } else {
-          // tall panels (many rows below the diagonal) on many CTAs at once,
-          // the rest one CTA per front
-          const int piv = method == UHM_LU_PIV ? 1 : 0;
-          const int rcap = dt == F64 ? GC_RMAX_F64 : GC_RMAX_F32;
-          std::vector<Item> one, tall;
-          for (const Item& it : p_items)
-            (fronts[it.front].n - it.a >= tune.gc_min_rows ? tall : one).push_back(it);
-          push(fac_ops, OP_GETRF, dt, NB, piv, one, tall.empty() ? fp : 0.0);
-          size_t i0 = 0;
-          while (i0 < tall.size()) {
-            // a group whose minimum CTA counts fit one cooperative launch
-            size_t i1 = i0;
-            int need = 0;
-            double rows_sum = 0;
-            while (i1 < tall.size()) {
-              const int rows = fronts[tall[i1].front].n - tall[i1].a;
-              const int mn = (rows + rcap - 1) / rcap;
-              if (i1 > i0 && need + mn > n_sm) break;
-              need += mn;
-              rows_sum += rows;
-              ++i1;
-            }
-            std::vector<Item> g;
-            int b = 0, rmax = 1;
-            const int spare = std::max(0, n_sm - need);
-            for (size_t i = i0; i < i1; ++i) {
-              const int rows = fronts[tall[i].front].n - tall[i].a;
-              int P = (rows + rcap - 1) / rcap + (int)(spare * (rows / rows_sum));
-              P = std::max(1, std::min(P, rows));
-              g.push_back(Item{tall[i].front, tall[i].a, b, P});
-              rmax = std::max(rmax, (rows + P - 1) / P);
-              b += P;
-            }
-            Op op{OP_GETRF_COOP, dt, NB, piv, add_items(g), (int)g.size()};
-            op.q0 = b;
-            op.aux = rmax;
-            if (i0 == 0) op.flops = fp;
-            fac_ops.push_back(op);
-            if (piv) {
-              std::vector<Item> sw;
-              for (const Item& it : g)
-                for (int c0 = 0; c0 < fronts[it.front].n; c0 += 256) sw.push_back(Item{it.front, it.a, c0, 0});
-              push(fac_ops, OP_LASWP, dt, NB, 0, sw);
-            }
-            i0 = i1;
-          }
+          push_lu_panel(dt, p_items, fp, 0);
           push(fac_ops, OP_LUROW, dt, NB, 0, t_items, ft);
           push(fac_ops, OP_GEMM, dt, NB, 0, u_items, fu);
         }
@@ -748,7 +765,107 @@ void Engine::build_programs(int method) {
       for (int s : tcf) maxfs_tc = std::max(maxfs_tc, fronts[s].fs);
       const int NBO = tune.tc_nbo;
       const int TB = tc_tile();
-      for (int K0 = 0; K0 < maxfs_tc; K0 += NBO) {
+      for (int K0 = 0; !chol && K0 < maxfs_tc; K0 += NBO) {
+        // LU tensor-core fronts, standard blocked LU with an outer panel of
+        // NBO columns: inside it the 64-column steps swap rows and update
+        // only columns left of the panel's trailing block (first row /
+        // column B); then the panel's swaps for the columns right of it, the
+        // panel's rows of U there (row solve + rank-64 updates, block by
+        // block), and the trailing block C -= L21 U12 on the tensor cores
+        for (int k0 = K0; k0 < K0 + NBO && k0 < maxfs_tc; k0 += NB) {
+          std::vector<Item> p_items, t_items, u_items;
+          double fp = 0, ft = 0, fu = 0;
+          for (int s : tcf) {
+            const HostFront& f = fronts[s];
+            if (f.fs <= k0) continue;
+            const int kb = std::min(NB, f.fs - k0);
+            const int base = k0 + kb;
+            const int B = std::min(K0 + NBO, f.fs);
+            p_items.push_back(Item{s, k0, 0, 0});
+            fp += get_flop_lu(0, f.n - k0, kb);
+            for (int c0 = base; c0 < B; c0 += LUROW_CB) t_items.push_back(Item{s, k0, c0, B});
+            ft += get_flop_trsm_lower(0, kb, std::max(0, B - base));
+            const int T = (f.n - base + TILE - 1) / TILE;
+            for (int ti = 0; ti < T; ++ti)
+              for (int tj = 0; tj < T; ++tj)
+                if (base + tj * TILE < B) u_items.push_back(Item{s, k0, ti, tj});
+            fu += get_flop_gemm(0, f.n - base, std::max(0, B - base), kb);
+          }
+          push_lu_panel(dt, p_items, fp, NBO);
+          push(fac_ops, OP_LUROW, dt, NB, 0, t_items, ft);
+          {
+            Op op{OP_GEMM, dt, NB, 0, add_items(u_items), (int)u_items.size()};
+            op.q0 = NBO;
+            op.aux = 1;     // columns < B
+            op.flops = fu;
+            if (!u_items.empty()) fac_ops.push_back(op);
+          }
+        }
+        // the outer panel's row swaps on the columns >= B
+        if (method == UHM_LU_PIV) {
+          std::vector<Item> sw;
+          for (int s : tcf) {
+            const HostFront& f = fronts[s];
+            if (f.fs <= K0) continue;
+            const int B = std::min(K0 + NBO, f.fs);
+            for (int c0 = B; c0 < f.n; c0 += 256) sw.push_back(Item{s, K0, c0, 0});
+          }
+          push(fac_ops, OP_LASWP, dt, NBO, 0, sw);
+        }
+        // the outer panel's rows of U right of it, 64-row block by block
+        for (int k0 = K0; k0 < K0 + NBO && k0 < maxfs_tc; k0 += NB) {
+          std::vector<Item> t_items, u_items;
+          double ft = 0, fu = 0;
+          for (int s : tcf) {
+            const HostFront& f = fronts[s];
+            if (f.fs <= k0) continue;
+            const int kb = std::min(NB, f.fs - k0);
+            const int base = k0 + kb;
+            const int B = std::min(K0 + NBO, f.fs);
+            for (int c0 = B; c0 < f.n; c0 += LUROW_CB) t_items.push_back(Item{s, k0, c0, 0});
+            ft += get_flop_trsm_lower(0, kb, f.n - B);
+            const int T = (f.n - base + TILE - 1) / TILE;
+            for (int ti = 0; ti < T; ++ti) {
+              if (base + ti * TILE >= B) break;
+              for (int tj = 0; tj < T; ++tj)
+                if (base + (tj + 1) * TILE > B) u_items.push_back(Item{s, k0, ti, tj});
+            }
+            fu += get_flop_gemm(0, std::max(0, B - base), f.n - B, kb);
+          }
+          push(fac_ops, OP_LUROW, dt, NB, 0, t_items, ft);
+          Op op{OP_GEMM, dt, NB, 0, add_items(u_items), (int)u_items.size()};
+          op.q0 = NBO;
+          op.aux = 2;       // rows < B, columns >= B
+          op.flops = fu;
+          if (!u_items.empty()) fac_ops.push_back(op);
+        }
+        // trailing block on the tensor cores: L21 (parts 0-1) and U12^T (parts 2-3)
+        std::vector<Item> pk, tt;
+        double ftc = 0, btc = 0;
+        for (int s : tcf) {
+          const HostFront& f = fronts[s];
+          if (f.fs <= K0) continue;
+          const int KB = std::min(NBO, f.fs - K0);
+          const int m = f.n - (K0 + KB);
+          if (m <= 0) continue;
+          for (int rb = 0; rb < (m + 63) / 64; ++rb) pk.push_back(Item{s, K0, rb, 0});
+          const int T = (m + TB - 1) / TB;
+          for (int ti = 0; ti < T; ++ti)
+            for (int tj = 0; tj < T; ++tj) tt.push_back(Item{s, K0, ti, tj});
+          ftc += get_flop_gemm(0, m, m, KB);
+          btc += 8.0 * (double)m * m + 2.0 * 4 * (double)m * KB;
+        }
+        if (!pk.empty()) {
+          Op pa{OP_TC_PACK, dt, NBO, 2, add_items(pk), (int)pk.size()};
+          fac_ops.push_back(pa);
+          Op pb = pa;
+          pb.q0 = 1;        // transposed: U12^T
+          pb.aux = 2;       // into parts 2-3
+          fac_ops.push_back(pb);
+          push(fac_ops, OP_TC_GEMM, dt, NBO, 2, tt, ftc, btc);
+        }
+      }
+      for (int K0 = 0; chol && K0 < maxfs_tc; K0 += NBO) {
         for (int k0 = K0; k0 < K0 + NBO && k0 < maxfs_tc; k0 += NB) {
           std::vector<Item> p_items, t_items, u_items;
           double fp = 0, ft = 0, fu = 0;
@@ -1177,7 +1294,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
                          stream);
         break;
       case OP_TC_PACK:
-        launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, stream);
+        launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, op.q0, op.aux, stream);
         break;
       case OP_TC_SYRK:
         launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, op.param == 3 ? 6 : 3,
@@ -1190,7 +1307,11 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
         break;
       case OP_LASWP: launch_laswp(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
       case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
-      case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
+      case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, op.q0, op.aux, stream); break;
+      case OP_TC_GEMM:
+        launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, 3, TC_TERMS_LU_BF16X3, 0, d_err,
+                       stream);
+        break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
       case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream); break;
       case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;

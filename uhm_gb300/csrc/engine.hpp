@@ -73,7 +73,7 @@ enum OpKind : int {
   OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
-  OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_KIND_END
+  OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_KIND_END
 };
 static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
 

@@ -703,10 +703,14 @@ void launch_potrf_trsm(const DevCtx& c, const Item* items, int n_items, int dtyp
 // Trailing update of one BM x BN tile of the front:
 //   C[rows, cols] -= A[rows, k0:k0+kb] * B,  B = A[cols, k0:k0+kb]^T  (ROWPANEL=false: SYRK)
 //                                            B = A[k0:k0+kb, cols]    (ROWPANEL=true: LU GEMM)
-// item: front, a = k0, b = tile row, c = tile col (tiles counted from k0+kb)
+// item: front, a = k0, b = tile row, c = tile col (tiles counted from k0+kb).
+// With two-level blocking (nbo > 0) B = K0 + min(nbo, fs - K0) is the first
+// row / column of the current outer panel's trailing block, and region
+// selects what is updated: 0 every entry, 1 columns < B (inside the outer
+// panel), 2 rows < B and columns >= B (the outer panel's rows right of it).
 template <typename T, int BM, int BN, int BK, int TM, int TN, bool ROWPANEL>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
-k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
+k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo, int region) {
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
@@ -716,8 +720,10 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
   const int kb = min(nb, f.fs - k0);
   const int base = k0 + kb;
   const int R0 = base + it.b * BM, C0 = base + it.c * BN;
-  // nbo > 0: update only the columns of the current outer panel (two-level blocking)
-  const int cmax = nbo > 0 ? min((k0 / nbo) * nbo + nbo, f.fs) : n;
+  const int Bnd = nbo > 0 ? min((k0 / nbo) * nbo + nbo, f.fs) : n;
+  const int rmax = region == 2 ? Bnd : n;
+  const int cmin = region == 2 ? Bnd : 0;
+  const int cmax = region == 1 ? Bnd : n;
   T* __restrict__ G = arena<T>(c) + f.off;
   const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
   T acc[TM][TN];
@@ -767,7 +773,7 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
         const int gc = C0 + tx + j * NTX;
-        const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
+        const bool ok = gr < rmax && gc >= cmin && gc < cmax && (ROWPANEL || gr >= gc);
         cv[i][j] = ok ? G[gr + (int64_t)gc * n] : (T)0;
       }
     }
@@ -813,7 +819,7 @@ k_tile_update(DevCtx c, const Item* __restrict__ items, int nb, int nbo) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
       const int gc = C0 + tx + j * NTX;
-      const bool ok = gr < n && gc < cmax && (ROWPANEL || gr >= gc);
+      const bool ok = gr < rmax && gc >= cmin && gc < cmax && (ROWPANEL || gr >= gc);
       if (ok) G[gr + (int64_t)gc * n] = cv[i][j] - acc[i][j];
     }
   }
@@ -823,16 +829,17 @@ void launch_syrk_update(const DevCtx& c, const Item* items, int n_items, int dty
                         int nbo, cudaStream_t s) {
   if (!n_items) return;
   if (nb > 64) throw std::invalid_argument("trailing update: panel width above 64");
-  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
-  else k_tile_update<float, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo);
+  const int region = nbo > 0 ? 1 : 0;
+  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo, region);
+  else k_tile_update<float, 64, 64, 16, 4, 4, false><<<n_items, 256, 0, s>>>(c, items, nb, nbo, region);
 }
 
-void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
-                        cudaStream_t s) {
+void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb, int nbo,
+                        int region, cudaStream_t s) {
   if (nb > 64) throw std::invalid_argument("trailing update: panel width above 64");
   if (!n_items) return;
-  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
-  else k_tile_update<float, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, 0);
+  if (dtype == F64) k_tile_update<double, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, nbo, region);
+  else k_tile_update<float, 64, 64, 16, 4, 4, true><<<n_items, 256, 0, s>>>(c, items, nb, nbo, region);
 }
 
 // ---------------------------------------------------------------------------
@@ -848,6 +855,7 @@ __global__ void __launch_bounds__(NT) k_getrf_panel(DevCtx c, const Item* __rest
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, k0 = it.a;
   const int kb = min(nb, fs - k0);
+  const int jend = it.b > 0 ? min(it.b, n) : n;   // rows are swapped in columns < jend
   T* __restrict__ G = arena<T>(c) + f.off;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int NW = NT / 32;
@@ -862,7 +870,7 @@ __global__ void __launch_bounds__(NT) k_getrf_panel(DevCtx c, const Item* __rest
       const int p = block_argmax<T, NT>(best, bi, s_v, s_i);
       if (threadIdx.x == 0) c.piv[f.piv_off + k] = p;
       if (p != k)
-        for (int j = threadIdx.x; j < n; j += NT) {
+        for (int j = threadIdx.x; j < jend; j += NT) {
           T t = G[k + (int64_t)j * n];
           G[k + (int64_t)j * n] = G[p + (int64_t)j * n];
           G[p + (int64_t)j * n] = t;
@@ -1114,9 +1122,10 @@ void launch_getrf_coop(const DevCtx& c, const Item* items, int n_items, int n_ct
     throw std::runtime_error(std::string("cooperative LU panel launch failed: ") + cudaGetErrorString(e));
 }
 
-// Row interchanges of a panel (pivots of rows k0..k0+kb-1, applied in order)
-// on the front's columns outside the panel.  Item: front, a = k0, b = first
-// column of a 256-column chunk; one thread per column.
+// Row interchanges of a panel (pivots of rows k0..k0+kb-1, kb = min(nb,
+// fs - k0), applied in order) on the front's columns outside the panel and
+// below a column limit.  Item: front, a = k0, b = first column of a
+// 256-column chunk, c = column limit (0: n); one thread per column.
 template <typename T>
 __global__ void __launch_bounds__(256) k_laswp(DevCtx c, const Item* __restrict__ items, int nb) {
   const Item it = items[blockIdx.x];
@@ -1124,7 +1133,8 @@ __global__ void __launch_bounds__(256) k_laswp(DevCtx c, const Item* __restrict_
   const int n = f.n, k0 = it.a;
   const int kb = min(nb, f.fs - k0);
   const int j = it.b + threadIdx.x;
-  if (j >= n || (j >= k0 && j < k0 + kb)) return;
+  const int jend = it.c > 0 ? min(it.c, n) : n;
+  if (j >= jend || (j >= k0 && j < k0 + kb)) return;
   T* __restrict__ col = arena<T>(c) + f.off + (int64_t)j * n;
   const int32_t* __restrict__ pv = c.piv + f.piv_off;
   for (int k = k0; k < k0 + kb; ++k) {
@@ -1145,7 +1155,8 @@ void launch_laswp(const DevCtx& c, const Item* items, int n_items, int dtype, in
 
 constexpr int LUROW_CB = 64;   // columns per row-panel block
 
-// A[k0:k0+kb, cols] <- L11^{-1} A[k0:k0+kb, cols]  (unit lower), cols >= k0+kb
+// A[k0:k0+kb, cols] <- L11^{-1} A[k0:k0+kb, cols]  (unit lower), cols >= k0+kb;
+// item: front, a = k0, b = first column of the chunk, c = column limit (0: n)
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_lu_row_update(DevCtx c, const Item* __restrict__ items,
                                                       int nb) {
@@ -1154,7 +1165,8 @@ __global__ void __launch_bounds__(NT) k_lu_row_update(DevCtx c, const Item* __re
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, k0 = it.a, c0 = it.b;
   const int kb = min(nb, f.fs - k0);
-  const int cb = min(LUROW_CB, n - c0);
+  const int cend = it.c > 0 ? min(it.c, n) : n;    // columns < cend (item c; 0: all)
+  const int cb = min(LUROW_CB, cend - c0);
   T* L = reinterpret_cast<T*>(smem_raw);      // kb x kb
   T* X = L + nb * nb;                         // kb x LUROW_CB, ld nb
   T* __restrict__ G = arena<T>(c) + f.off;

@@ -325,10 +325,13 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
 // BF16 parts stored row-major with row length nbo (zero beyond KB):
 // part p row r = round-to-nearest BF16 of the p-th residual.
 // item: front, a = K0, b = row block (64 rows)
+// trans = 1 packs U12^T instead: row r is column base + r of the front, rows
+// K0..K0+KB (the LU panel's U block right of the outer panel), into parts
+// poff.. (the B operand of the LU trailing update).
 __global__ void __launch_bounds__(256) k_tc_pack(DevCtx c, const Item* __restrict__ items, int nbo,
                                                  int nparts, __nv_bfloat16* __restrict__ ws,
                                                  const int64_t* __restrict__ ws_off,
-                                                 const int64_t* __restrict__ ws_stride) {
+                                                 const int64_t* __restrict__ ws_stride, int trans, int poff) {
   __shared__ float tile[64][65];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
@@ -345,14 +348,17 @@ __global__ void __launch_bounds__(256) k_tc_pack(DevCtx c, const Item* __restric
     float v[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      const int idx = threadIdx.x + 256 * u, r = idx % 64, k = idx / 64;
+      const int idx = threadIdx.x + 256 * u;
+      const int r = trans ? idx / 64 : idx % 64, k = trans ? idx % 64 : idx / 64;
       const int gr = base + r0 + r, gk = k0 + k;
-      v[u] = (gr < n && gk < KB) ? G[gr + (int64_t)(K0 + gk) * n] : 0.0f;
+      v[u] = (gr < n && gk < KB) ? (trans ? G[(K0 + gk) + (int64_t)gr * n] : G[gr + (int64_t)(K0 + gk) * n])
+                                 : 0.0f;
     }
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      const int idx = threadIdx.x + 256 * u, r = idx % 64, k = idx / 64;
+      const int idx = threadIdx.x + 256 * u;
+      const int r = trans ? idx / 64 : idx % 64, k = trans ? idx % 64 : idx / 64;
       tile[r][k] = v[u];
     }
     __syncthreads();
@@ -372,7 +378,7 @@ __global__ void __launch_bounds__(256) k_tc_pack(DevCtx c, const Item* __restric
           hb[q] = __float2bfloat16_rn(x[q]);
           x[q] -= __bfloat162float(hb[q]);
         }
-        *reinterpret_cast<uint4*>(W + p * pstride + (int64_t)(r0 + r) * nbo + k0 + k8) =
+        *reinterpret_cast<uint4*>(W + (p + poff) * pstride + (int64_t)(r0 + r) * nbo + k0 + k8) =
             *reinterpret_cast<const uint4*>(hb);
       }
     }
@@ -410,9 +416,9 @@ bool tc_encode_part(CUtensorMap* map, void* base, int64_t rows, int nbo) {
 }
 
 void launch_tc_pack(const DevCtx& c, const Item* items, int n_items, int nbo, int nparts, void* ws,
-                    const int64_t* ws_off, const int64_t* ws_stride, cudaStream_t s) {
+                    const int64_t* ws_off, const int64_t* ws_stride, int trans, int poff, cudaStream_t s) {
   if (!n_items) return;
-  k_tc_pack<<<n_items, 256, 0, s>>>(c, items, nbo, nparts, (__nv_bfloat16*)ws, ws_off, ws_stride);
+  k_tc_pack<<<n_items, 256, 0, s>>>(c, items, nbo, nparts, (__nv_bfloat16*)ws, ws_off, ws_stride, trans, poff);
 }
 
 void launch_tc_syrk(const DevCtx& c, const CUtensorMap& wsmap, const int64_t* ws_off,

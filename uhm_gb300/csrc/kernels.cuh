@@ -105,8 +105,9 @@ void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dty
                         int pivot, cudaStream_t s);
 void launch_lu_row_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
                           int pivot, cudaStream_t s);
-void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb,
-                        cudaStream_t s);
+// LU trailing GEMM tiles; nbo / region as for k_tile_update (0 / 0: every entry)
+void launch_gemm_update(const DevCtx& c, const Item* items, int n_items, int dtype, int nb, int nbo,
+                        int region, cudaStream_t s);
 
 // tree solves over the global vector g (N x n_rhs, column-major, ld N)
 void launch_fwd_gather(const DevCtx& c, const Item* items, int n_items, const double* g,

@@ -5,7 +5,8 @@
     up to 1e4), beta = (1, .5, .25) * 100, nested-dissection merges 3, 2, 2, 2
     (leaves to root; root front 14,911): LU with partial pivoting inside
     each eliminated block (the reference's Mesh_::lu_piv_with_free /
-    solve_lu_piv path).  Plain FP64 fronts against FP32 fronts with FP64
+    solve_lu_piv path).  Plain FP64 fronts against FP32 (or, --prec 2,
+    BF16-split with tensor-core trailing updates) fronts with FP64
     element-wise refinement to backward error 1e-12; seconds per
     factor+solve(+refine), GFLOP/s over the LAWN-41 count, backward errors.
 
@@ -42,7 +43,7 @@ def _step(m, method):
     return (t["factor_ms"] + t["solve_ms"] + t["refine_ms"]) * 1e-3, t
 
 
-def convdiff(n=24, p=3, seed=0, steps=3, warmup=1, plain_steps=1, merges=(3, 2, 2, 2)):
+def convdiff(n=24, p=3, seed=0, steps=3, warmup=1, plain_steps=1, merges=(3, 2, 2, 2), prec=api.PREC_FP32):
     t0 = time.perf_counter()
     spec = hpfem.convdiff3d(n, p, seed=seed, merges=list(merges) if merges else None)
     t_gen = time.perf_counter() - t0
@@ -61,18 +62,20 @@ def convdiff(n=24, p=3, seed=0, steps=3, warmup=1, plain_steps=1, merges=(3, 2, 
                          "factor_ms": pl[-1][1]["factor_ms"], "solve_ms": pl[-1][1]["solve_ms"],
                          "backward_error": m.backward_error()}
     out["plain_fp64"]["factor_gflops"] = fd / 1e9 / (pl[-1][1]["factor_ms"] * 1e-3)
-    m.set_mode(1, api.PREC_FP32, TOL, 10)
+    m.set_mode(1, prec, TOL, 10)
     for _ in range(warmup):
         _step(m, method)
     mx = [_step(m, method) for _ in range(steps)]
     last = mx[-1][1]
-    out["mixed_fp32_ir"] = {"s": statistics.median([r[0] for r in mx]),
+    key = {api.PREC_FP32: "mixed_fp32_ir", api.PREC_BF16X3: "mixed_bf16x3_ir"}.get(prec, "mixed_ir")
+    out["mixed_precision"] = key
+    out[key] = {"s": statistics.median([r[0] for r in mx]),
                             "factor_ms": last["factor_ms"], "solve_ms": last["solve_ms"],
                             "refine_ms": last["refine_ms"], "ir_iters": last["ir_iters"],
                             "berr_first_solve": last.get("berr_first"), "backward_error": last["berr"],
                             "status": m.status()}
-    out["mixed_fp32_ir"]["factor_gflops"] = fd / 1e9 / (last["factor_ms"] * 1e-3)
-    out["speedup_mixed_vs_plain"] = out["plain_fp64"]["s"] / out["mixed_fp32_ir"]["s"]
+    out[key]["factor_gflops"] = fd / 1e9 / (last["factor_ms"] * 1e-3)
+    out["speedup_mixed_vs_plain"] = out["plain_fp64"]["s"] / out[key]["s"]
     return out
 
 
@@ -151,6 +154,8 @@ def main(argv=None):
     c.add_argument("--steps", type=int, default=3)
     c.add_argument("--seed", type=int, default=0)
     c.add_argument("--merges", type=int, nargs="*", default=[3, 2, 2, 2])
+    c.add_argument("--prec", type=int, default=api.PREC_FP32,
+                   help="front precision of the mixed path: 1 FP32, 2 BF16X3 (tensor-core trailing updates)")
     b = sub.add_parser("batch")
     b.add_argument("--meshes", type=int, default=64)
     b.add_argument("--n-range", type=int, nargs=2, default=(8, 12))
@@ -163,7 +168,7 @@ def main(argv=None):
     b.add_argument("--no-separate", action="store_true")
     a = ap.parse_args(argv)
     if a.what == "convdiff":
-        r = convdiff(a.n, a.p, a.seed, a.steps, merges=a.merges or None)
+        r = convdiff(a.n, a.p, a.seed, a.steps, merges=a.merges or None, prec=a.prec)
     else:
         r = batch(a.meshes, a.seed, tuple(a.n_range), tuple(a.p_range), a.rhs, a.prec, a.max_dofs,
                   a.steps, separate=not a.no_separate)
