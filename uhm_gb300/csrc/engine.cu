@@ -1251,7 +1251,17 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int64_t before = timing.kernel_launches;
-    launch_ops(ops, g_in, g_out);
+    try {
+      launch_ops(ops, g_in, g_out);
+    } catch (...) {
+      // a launcher refused (bad arguments, a launch the device cannot take):
+      // close the capture so that the stream stays usable, then report
+      cudaGraph_t broken = nullptr;
+      cudaStreamEndCapture(stream, &broken);
+      if (broken) cudaGraphDestroy(broken);
+      cudaGetLastError();
+      throw;
+    }
     timing.kernel_launches = before;
     CK(cudaStreamEndCapture(stream, &g));
     CK(cudaGraphInstantiate(&ge->exec, g, 0));
