@@ -143,6 +143,25 @@ int uhm_gpu_get_fronts(long* mesh, int n, int* elt_id, int* generation, int* fs,
 int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_factor,
                             int* n_schur);
 
+/* Element matrices generated on the device instead of copied in (no
+ * counterpart in the reference, which takes element matrices from its caller
+ * through copy_in, UHM/src/mesh/interf.cxx:108-204): uniform quad (dim 2) or
+ * hex (dim 3) meshes with integrated-Legendre (Lobatto) modes.  Per element
+ * (leaf order, as uhm_gpu_copy_in_leaves): order p_el (1..7), diffusion
+ * coefficient kappa, optional reaction react (or NULL) and, for all elements,
+ * optional convection velocity beta[dim] (or NULL); its retained tensor modes
+ * sel[sel_ptr[e] .. sel_ptr[e+1]) (flat index mi[0] + mi[1] (p+1) + mi[2]
+ * (p+1)^2, in the element's row order).  ref holds, from ref_off[p], the
+ * (p+1) x (p+1) 1D mass, stiffness and convection matrices (row-major) of
+ * order p.  hh = h/2; cmass, cconv: the mass and convection scale factors
+ * ((h/2)^dim and (h/2)^(dim-1)).  The element node lists must be known: a
+ * uhm_gpu_copy_in_leaves with nods_all (e.g. of the right-hand sides) gives
+ * them.  method as for the factorisation. */
+int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh, double cmass, double cconv,
+                                      int n_el, const double* ref, const long* ref_off, int n_ref_off,
+                                      const int* p_el, const double* kappa, const double* react,
+                                      const double* beta, const long* sel_ptr, const int* sel);
+
 /* Kernel-selection thresholds (no counterpart in the reference, whose block
  * size is a compile-time knob, UHM/include/uhm/const.hxx): values[0] whole-front
  * shared-memory factorisation up to n (FP64, at most 160), values[1] the same

@@ -95,6 +95,8 @@ def _declare(L):
     sig("uhm_gpu_set_tunables", [_P(_l), _P(_i)], _i)
     sig("uhm_gpu_get_tunables", [_P(_l), _P(_i)], _i)
     sig("uhm_gpu_autotune", [_P(_l), _i, _i, _P(_i)], _i)
+    sig("uhm_gpu_generate_lobatto_elements", [_P(_l), _i, _i, _d, _d, _d, _i, _P(_d), _P(_l), _i, _P(_i),
+                                              _P(_d), _P(_d), _P(_d), _P(_l), _P(_i)], _i)
     sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
     sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
     sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
@@ -337,6 +339,27 @@ class Mesh:
         return [(self.OP_NAMES[kind[i]], int(items[i]), float(ms[i])) for i in range(k)]
 
     # -- learned precision selector ------------------------------------------
+    # -- element matrices generated on the device -------------------------------
+    def generate_elements(self, recipe, method=UHM_CHOL):
+        """Build every leaf's element matrix on the device from
+        hpfem.element_recipe(spec) (uhm_gpu_generate_lobatto_elements)
+        instead of copying it in; the element node lists must be known (a
+        bulk copy_in_leaves with node lists, e.g. of the right-hand sides)."""
+        r = recipe
+        keep = []
+
+        def ptr(a, dt, ct):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data_as(_P(ct))
+        self._check(self.L.uhm_gpu_generate_lobatto_elements(
+            C.byref(self.h), method, r["dim"], r["hh"], r["cmass"], r["cconv"], r["n_el"],
+            ptr(r["ref"], np.float64, _d), ptr(r["ref_off"], np.int64, _l), len(r["ref_off"]),
+            ptr(r["p_el"], np.int32, _i), ptr(r["kappa"], np.float64, _d), ptr(r["react"], np.float64, _d),
+            ptr(r["beta"], np.float64, _d), ptr(r["sel_ptr"], np.int64, _l), ptr(r["sel"], np.int32, _i)))
+
     # -- kernel-selection thresholds --------------------------------------------
     TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo")
 
@@ -478,7 +501,7 @@ def mlp_train(X, y, params, epochs=20, batch=512, lr=1e-3, seed=0, class_weight=
     return P, hist[:epochs]
 
 
-def load_spec(spec, n_rhs=None, bulk=True, pinned=False):
+def load_spec(spec, n_rhs=None, bulk=True, pinned=False, lhs=True):
     """Feed a uhm_gb300.hpfem.MeshSpec through the Mesh API: nodes, leaf
     elements (add_element + element_add_node), the tree through
     add_element(gen) / set_parent / add_child, lock,
@@ -502,7 +525,11 @@ def load_spec(spec, n_rhs=None, bulk=True, pinned=False):
     m.lock()
     m.create_matrix_without_buffer(UHM_REAL, n_rhs)
     m._elts = elts
-    if bulk:
+    if not lhs:
+        # right-hand sides (and the element node lists) only: the element
+        # matrices come from the device generator (generate_elements)
+        m.copy_in_leaves(UHM_RHS, spec.rhs, spec.elem_node.astype(np.int32))
+    elif bulk:
         nods_all = spec.elem_node.astype(np.int32)
         m.copy_in_leaves(UHM_LHS, spec.mats, nods_all)
         m.copy_in_leaves(UHM_RHS, spec.rhs)

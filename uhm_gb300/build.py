@@ -27,6 +27,7 @@ SOURCES = [
     "k_tc_gemm.cu",
     "k_noalloc.cu",
     "k_selector.cu",
+    "k_elements.cu",
 ]
 
 

@@ -227,6 +227,18 @@ int uhm_gpu_get_op_log(long* mesh, int cap, int* kind, int* n_items, double* ms,
     }
   });
 }
+int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh, double cmass, double cconv,
+                                      int n_el, const double* ref, const long* ref_off, int n_ref_off,
+                                      const int* p_el, const double* kappa, const double* react,
+                                      const double* beta, const long* sel_ptr, const int* sel) {
+  static_assert(sizeof(long) == sizeof(int64_t), "long is 64-bit");
+  return guard(M(mesh), [&] {
+    M(mesh)->eng().generate_lobatto_elements(method, dim, hh, cmass, cconv, n_el, ref,
+                                             reinterpret_cast<const int64_t*>(ref_off), n_ref_off, p_el, kappa,
+                                             react, beta, reinterpret_cast<const int64_t*>(sel_ptr),
+                                             reinterpret_cast<const int32_t*>(sel));
+  });
+}
 int uhm_gpu_set_tunables(long* mesh, const int* values) {
   return guard(M(mesh), [&] { M(mesh)->eng().set_tunables(values); });
 }

@@ -339,6 +339,66 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
   }
 }
 
+void Engine::generate_lobatto_elements(int method, int dim, double hh, double cmass, double cconv, int n_el,
+                                       const double* ref, const int64_t* ref_off, int n_ref_off, const int* p_el,
+                                       const double* kappa, const double* react, const double* beta,
+                                       const int64_t* sel_ptr, const int32_t* sel) {
+  ensure_plan();
+  if (dim != 2 && dim != 3) fail("generate_lobatto_elements: dim must be 2 or 3", 7);
+  if (n_el != (int)esrc.size()) fail("generate_lobatto_elements: element count differs from the mesh's leaves", 7);
+  int pmax = 0;
+  for (int e = 0; e < n_el; ++e) {
+    const int64_t m = sel_ptr[e + 1] - sel_ptr[e];
+    const int p = p_el[e];
+    if (p < 1 || p > 7 || p >= n_ref_off) fail("generate_lobatto_elements: order outside 1..7", 7);
+    if (esrc[e].node_order.empty())
+      fail("generate_lobatto_elements: element node lists unknown (copy_in_leaves with node lists first)", 7);
+    if (m != esrc[e].m) fail("generate_lobatto_elements: retained modes differ from the element's dofs", 7);
+    pmax = std::max(pmax, p);
+  }
+  // the assembly programs list an element source only for leaves that carry a
+  // matrix, so mark them before the programs are built
+  for (auto& es : esrc) es.has_lhs = true;
+  prepare_device(method);
+  const int64_t n_sel = sel_ptr[n_el];
+  const int64_t n_ref = ref_off[pmax] + 3 * (int64_t)(pmax + 1) * (pmax + 1);
+  std::vector<int64_t> off(n_el);
+  for (int e = 0; e < n_el; ++e) off[e] = esrc[e].mat_off;
+  // temporaries for the recipe, freed on every way out (cudaFree waits for the kernel)
+  struct Temps {
+    std::vector<void*> v;
+    ~Temps() {
+      for (void* d : v) cudaFree(d);
+    }
+  } tmp;
+  auto up = [&](const void* src, size_t bytes) -> void* {
+    void* d = nullptr;
+    CK(cudaMalloc(&d, std::max<size_t>(bytes, 16)));
+    tmp.v.push_back(d);
+    if (bytes) CK(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, stream));
+    return d;
+  };
+  auto* d_off = (int64_t*)up(off.data(), sizeof(int64_t) * n_el);
+  auto* d_p = (int*)up(p_el, sizeof(int) * n_el);
+  auto* d_kap = (double*)up(kappa, sizeof(double) * n_el);
+  auto* d_rea = react ? (double*)up(react, sizeof(double) * n_el) : nullptr;
+  auto* d_beta = beta ? (double*)up(beta, sizeof(double) * dim) : nullptr;
+  auto* d_sp = (int64_t*)up(sel_ptr, sizeof(int64_t) * (n_el + 1));
+  auto* d_sel = (int32_t*)up(sel, sizeof(int32_t) * n_sel);
+  auto* d_ref = (double*)up(ref, sizeof(double) * n_ref);
+  auto* d_roff = (int64_t*)up(ref_off, sizeof(int64_t) * n_ref_off);
+  uhm_gpu::launch_gen_lobatto(ctx.emat, d_off, n_el, d_p, d_kap, d_rea, d_beta, d_sp, d_sel, d_ref, d_roff, dim, hh,
+                              cmass, cconv, stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(stream));
+  emat_dirty = false;
+  emat_device_only = true;
+  anorm_valid = false;
+  learned_valid = false;
+  factored = false;
+  anorm_inf = -1.0;
+}
+
 void Engine::copy_out(Element e, int m, int n, int nod_disp, const int* nods, int side, double* buf) {
   ensure_plan();
   if (side != UHM_RHS) fail("copy_out: only the solution (UHM_RHS) is supported", 7);

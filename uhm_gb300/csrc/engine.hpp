@@ -112,6 +112,12 @@ class Engine {
   // m_e x m_e column-major in the element's own node order, back to back
   void copy_in_leaves(int side, const double* buf, int64_t n_values);
   void copy_out_leaves(double* buf, int64_t n_values);
+  // element matrices of all leaves generated on the device (hp-FEM Lobatto
+  // modes, k_elements.cu) instead of copied in; leaf order as copy_in_leaves
+  void generate_lobatto_elements(int method, int dim, double hh, double cmass, double cconv, int n_el,
+                                 const double* ref, const int64_t* ref_off, int n_ref_off, const int* p_el,
+                                 const double* kappa, const double* react, const double* beta,
+                                 const int64_t* sel_ptr, const int32_t* sel);
   // element maps of all leaves from their node lists (leaf order, single physics)
   void set_leaf_nodes(const int* nods_all);
   void node_solution(int n_nodes, const int* ids, double* out, int64_t n_values);

@@ -37,7 +37,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = ["MeshSpec", "poisson2d", "poisson3d", "convdiff3d", "diffusion3d",
-           "build_mesh", "lobatto_1d", "forest", "batch3d"]
+           "build_mesh", "lobatto_1d", "forest", "batch3d", "element_recipe"]
 
 
 # ----------------------------------------------------------------------------
@@ -412,7 +412,14 @@ def build_mesh(dim: int, n: int, p, *, kappa=None, beta=None, react=None, seed: 
         rhs=rhs,
         symmetric=symmetric,
         info=dict(dim=dim, n=n, p=(int(p_el[0]) if np.all(p_el == p_el[0]) else "var"),
-                  merges=plan, seed=seed, n_rhs=n_rhs, h=h),
+                  merges=plan, seed=seed, n_rhs=n_rhs, h=h,
+                  # what a device-side generator needs to rebuild the element
+                  # matrices (element_recipe): per element its order,
+                  # coefficients and retained tensor modes
+                  recipe=dict(p_el=p_el, kappa=kap, react=rea, beta=beta,
+                              sel_ptr=np.concatenate([[0], np.cumsum([len(v) for v in sel_list])]).astype(np.int64),
+                              sel=(np.concatenate(sel_list).astype(np.int32) if sel_list
+                                   else np.zeros(0, np.int32)))),
     )
 
 
@@ -566,3 +573,41 @@ def batch3d(n_meshes: int, seed: int = 0, n_range=(8, 20), p_range=(2, 6), n_rhs
         p = int(rng.integers(p_range[0], p_range[1] + 1))
         out.append(poisson3d(n, p, seed=seed * 100003 + k, n_rhs=n_rhs))
     return out
+
+
+def element_recipe(spec: MeshSpec) -> dict:
+    """Inputs of the device-side element-matrix generator
+    (uhm_gpu_generate_lobatto_elements) for a mesh from build_mesh: the
+    1D Lobatto matrices (M, K, C) of every order in use, stored back to back
+    with per-order offsets, and per element its order, coefficients and
+    retained tensor modes (flat index mi[0] + mi[1] (p+1) + mi[2] (p+1)^2)
+    in the element's row order.  The generator combines them exactly as
+    build_mesh does (same products and sums in the same order, no fused
+    multiply-add), so the matrices come out bit-identical."""
+    r = spec.info.get("recipe")
+    if r is None:
+        raise ValueError("element_recipe: the mesh was not built by build_mesh")
+    dim, h = spec.dim, spec.info["h"]
+    pmax = int(r["p_el"].max())
+    ref_off = np.zeros(pmax + 2, np.int64)
+    parts = []
+    for p in range(1, pmax + 1):
+        M, K, C = lobatto_1d(p, p + 1)
+        ref_off[p] = sum(x.size for x in parts)
+        parts += [M.ravel(order="C"), K.ravel(order="C"), C.ravel(order="C")]
+    ref = np.concatenate(parts)
+    n_el = spec.n_leaves
+    react = r["react"]
+    beta = r["beta"]
+    # scale factors exactly as build_mesh forms them
+    hh = h / 2
+    cmass = (h / 2) ** 3 if dim == 3 else (h / 2) ** 2
+    cconv = (h / 2) ** 2 if dim == 3 else (h / 2)
+    return dict(dim=dim, h=float(h), hh=float(hh), cmass=float(cmass), cconv=float(cconv),
+                n_el=n_el, ref=ref, ref_off=ref_off,
+                p_el=np.ascontiguousarray(r["p_el"], np.int32),
+                kappa=np.ascontiguousarray(r["kappa"], np.float64),
+                react=None if react is None else np.ascontiguousarray(react, np.float64),
+                beta=None if beta is None else np.ascontiguousarray(beta, np.float64),
+                sel_ptr=np.ascontiguousarray(r["sel_ptr"], np.int64),
+                sel=np.ascontiguousarray(r["sel"], np.int32))

@@ -10,6 +10,12 @@
     element-wise refinement to backward error 1e-12; seconds per
     factor+solve(+refine), GFLOP/s over the LAWN-41 count, backward errors.
 
+``python -m uhm_gb300.measure elements``
+    Element matrices of 3D Poisson 16^3 hex p=4 generated on the device
+    (uhm_gpu_generate_lobatto_elements, recipe upload included) against the
+    host mesh build (numpy); also checks that the solution from generated
+    matrices has the same bits as from copied-in ones.
+
 ``python -m uhm_gb300.measure batch``
     Many independent 3D Poisson meshes (n hexes per side and order p drawn
     uniformly from the given ranges, 16 right-hand sides each) joined into
@@ -145,6 +151,40 @@ def batch(n_meshes=64, seed=0, n_range=(8, 12), p_range=(2, 4), n_rhs=16, prec=a
     return out
 
 
+def elements(n=16, p=4, seed=0, reps=3):
+    t0 = time.perf_counter()
+    spec = hpfem.poisson3d(n, p, seed=seed)
+    t_host = time.perf_counter() - t0          # the whole host mesh build, element matrices included
+    recipe = hpfem.element_recipe(spec)
+    m_copy = api.load_spec(spec)
+    m_copy.set_mode(1, api.PREC_BF16X3, TOL, 10)
+    m_copy.chol_with_free()
+    m_copy.solve_chol()
+    x_copy = m_copy.node_solution(spec.node_id.astype(np.int32), spec.node_ndof)
+    m = api.load_spec(spec, lhs=False)
+    m.set_mode(1, api.PREC_BF16X3, TOL, 10)
+    m.generate_elements(recipe)
+    m.chol_with_free()
+    m.solve_chol()
+    gen = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        m.generate_elements(recipe)            # returns after the kernel has finished
+        gen.append(time.perf_counter() - t)
+    cp = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        m_copy.copy_in_leaves(api.UHM_LHS, spec.mats)   # pageable host buffer -> device element buffer
+        cp.append(time.perf_counter() - t)
+    m.chol_with_free()
+    m.solve_chol()
+    x_gen = m.node_solution(spec.node_id.astype(np.int32), spec.node_ndof)
+    return {"workload": f"3D Poisson {n}^3 hex p={p} element matrices ({spec.mats.nbytes / 1e6:.0f} MB)",
+            "host_mesh_build_s": t_host, "device_generation_s": statistics.median(gen),
+            "copy_in_s": statistics.median(cp),
+            "same_solution_bits": bool(np.array_equal(x_gen, x_copy))}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m uhm_gb300.measure")
     sub = ap.add_subparsers(dest="what", required=True)
@@ -156,6 +196,9 @@ def main(argv=None):
     c.add_argument("--merges", type=int, nargs="*", default=[3, 2, 2, 2])
     c.add_argument("--prec", type=int, default=api.PREC_FP32,
                    help="front precision of the mixed path: 1 FP32, 2 BF16X3 (tensor-core trailing updates)")
+    el = sub.add_parser("elements")
+    el.add_argument("--n", type=int, default=16)
+    el.add_argument("--p", type=int, default=4)
     b = sub.add_parser("batch")
     b.add_argument("--meshes", type=int, default=64)
     b.add_argument("--n-range", type=int, nargs=2, default=(8, 12))
@@ -167,9 +210,11 @@ def main(argv=None):
     b.add_argument("--seed", type=int, default=0)
     b.add_argument("--no-separate", action="store_true")
     a = ap.parse_args(argv)
-    if a.what == "convdiff":
+    if a.what == "elements":
+        r = elements(a.n, a.p)
+    elif a.what == "convdiff":
         r = convdiff(a.n, a.p, a.seed, a.steps, merges=a.merges or None, prec=a.prec)
-    else:
+    elif a.what == "batch":
         r = batch(a.meshes, a.seed, tuple(a.n_range), tuple(a.p_range), a.rhs, a.prec, a.max_dofs,
                   a.steps, separate=not a.no_separate)
     print(json.dumps(r))
