@@ -156,7 +156,9 @@ int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* n_fa
  * order p.  hh = h/2; cmass, cconv: the mass and convection scale factors
  * ((h/2)^dim and (h/2)^(dim-1)).  The element node lists must be known: a
  * uhm_gpu_copy_in_leaves with nods_all (e.g. of the right-hand sides) gives
- * them.  method as for the factorisation. */
+ * them.  method as for the factorisation.  Afterwards, until the next
+ * factorisation, uhm_gpu_get_timing's out[0] is the generation kernel's
+ * device time in ms. */
 int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh, double cmass, double cconv,
                                       int n_el, const double* ref, const long* ref_off, int n_ref_off,
                                       const int* p_el, const double* kappa, const double* react,

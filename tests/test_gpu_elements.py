@@ -2,7 +2,8 @@
 instead of built on the host and copied in.  The generator forms every entry
 with the host generator's products and sums in the same order, so the FP64
 solutions must be bit-identical to those from copied-in matrices, for
-diffusion, convection-diffusion (LU), 2D, variable-order and reaction meshes;
+diffusion, convection-diffusion (LU), 2D, variable-order and reaction meshes
+(and 2D convection with reaction);
 generating over copied-in matrices gives the same solution too."""
 import numpy as np
 import pytest
@@ -18,6 +19,7 @@ CASES = [
     ("2d_8_p4", lambda: hpfem.poisson2d(8, 4, seed=63), uo.CHOL),
     ("varp_3", lambda: hpfem.build_mesh(3, 3, np.random.default_rng(4).integers(2, 6, 27), seed=64), uo.CHOL),
     ("react_3_p3", lambda: hpfem.build_mesh(3, 3, 3, react=-3.0, seed=65), uo.CHOL),
+    ("cd2d_react_8_p3", lambda: hpfem.build_mesh(2, 8, 3, beta=(30.0, -20.0), react=0.5, seed=67), uo.LU_PIV),
 ]
 
 

@@ -81,6 +81,8 @@ void Engine::free_device() {
   d_tree_red = nullptr;
   d_gc_xbuf = nullptr;
   d_gc_ctr = nullptr;
+  d_gen = nullptr;
+  d_gen_bytes = 0;
   tree_bnorm.clear();
   tree_anorm.clear();
 }
@@ -346,7 +348,10 @@ void Engine::generate_lobatto_elements(int method, int dim, double hh, double cm
   ensure_plan();
   if (dim != 2 && dim != 3) fail("generate_lobatto_elements: dim must be 2 or 3", 7);
   if (n_el != (int)esrc.size()) fail("generate_lobatto_elements: element count differs from the mesh's leaves", 7);
-  int pmax = 0;
+  // every index the kernel derives from the recipe is checked here: modes
+  // inside the (p+1)^dim tensor grid, each order's 1D matrices inside ref
+  int64_t n_ref = 0;
+  if (sel_ptr[0] != 0) fail("generate_lobatto_elements: sel_ptr[0] must be 0", 7);
   for (int e = 0; e < n_el; ++e) {
     const int64_t m = sel_ptr[e + 1] - sel_ptr[e];
     const int p = p_el[e];
@@ -354,43 +359,76 @@ void Engine::generate_lobatto_elements(int method, int dim, double hh, double cm
     if (esrc[e].node_order.empty())
       fail("generate_lobatto_elements: element node lists unknown (copy_in_leaves with node lists first)", 7);
     if (m != esrc[e].m) fail("generate_lobatto_elements: retained modes differ from the element's dofs", 7);
-    pmax = std::max(pmax, p);
+    const int q = p + 1;
+    const int64_t grid = dim == 3 ? (int64_t)q * q * q : (int64_t)q * q;
+    if (m > grid) fail("generate_lobatto_elements: more retained modes than the element has", 7);
+    for (int64_t k = sel_ptr[e]; k < sel_ptr[e + 1]; ++k)
+      if (sel[k] < 0 || sel[k] >= grid) fail("generate_lobatto_elements: retained mode outside the tensor grid", 7);
+    if (ref_off[p] < 0) fail("generate_lobatto_elements: negative ref_off", 7);
+    n_ref = std::max<int64_t>(n_ref, ref_off[p] + 3 * (int64_t)q * q);
   }
   // the assembly programs list an element source only for leaves that carry a
   // matrix, so mark them before the programs are built
   for (auto& es : esrc) es.has_lhs = true;
   prepare_device(method);
   const int64_t n_sel = sel_ptr[n_el];
-  const int64_t n_ref = ref_off[pmax] + 3 * (int64_t)(pmax + 1) * (pmax + 1);
   std::vector<int64_t> off(n_el);
   for (int e = 0; e < n_el; ++e) off[e] = esrc[e].mat_off;
-  // temporaries for the recipe, freed on every way out (cudaFree waits for the kernel)
-  struct Temps {
-    std::vector<void*> v;
-    ~Temps() {
-      for (void* d : v) cudaFree(d);
-    }
-  } tmp;
-  auto up = [&](const void* src, size_t bytes) -> void* {
-    void* d = nullptr;
-    CK(cudaMalloc(&d, std::max<size_t>(bytes, 16)));
-    tmp.v.push_back(d);
-    if (bytes) CK(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, stream));
-    return d;
+  // the recipe in one device buffer (kept with the plan's allocations):
+  // each array at a 16-byte-aligned offset of one host staging block
+  std::vector<unsigned char> stage;
+  auto place = [&](const void* src, size_t bytes) -> size_t {
+    const size_t o = (stage.size() + 15) & ~size_t(15);
+    stage.resize(o + bytes);
+    if (bytes) std::memcpy(stage.data() + o, src, bytes);
+    return o;
   };
-  auto* d_off = (int64_t*)up(off.data(), sizeof(int64_t) * n_el);
-  auto* d_p = (int*)up(p_el, sizeof(int) * n_el);
-  auto* d_kap = (double*)up(kappa, sizeof(double) * n_el);
-  auto* d_rea = react ? (double*)up(react, sizeof(double) * n_el) : nullptr;
-  auto* d_beta = beta ? (double*)up(beta, sizeof(double) * dim) : nullptr;
-  auto* d_sp = (int64_t*)up(sel_ptr, sizeof(int64_t) * (n_el + 1));
-  auto* d_sel = (int32_t*)up(sel, sizeof(int32_t) * n_sel);
-  auto* d_ref = (double*)up(ref, sizeof(double) * n_ref);
-  auto* d_roff = (int64_t*)up(ref_off, sizeof(int64_t) * n_ref_off);
-  uhm_gpu::launch_gen_lobatto(ctx.emat, d_off, n_el, d_p, d_kap, d_rea, d_beta, d_sp, d_sel, d_ref, d_roff, dim, hh,
-                              cmass, cconv, stream);
+  const size_t o_off = place(off.data(), sizeof(int64_t) * n_el);
+  const size_t o_p = place(p_el, sizeof(int) * n_el);
+  const size_t o_kap = place(kappa, sizeof(double) * n_el);
+  const size_t o_rea = react ? place(react, sizeof(double) * n_el) : 0;
+  const size_t o_beta = beta ? place(beta, sizeof(double) * dim) : 0;
+  const size_t o_sp = place(sel_ptr, sizeof(int64_t) * (n_el + 1));
+  const size_t o_sel = place(sel, sizeof(int32_t) * n_sel);
+  const size_t o_ref = place(ref, sizeof(double) * n_ref);
+  // per-order tables (device only) after the staged arrays
+  bool used[8] = {};
+  for (int e = 0; e < n_el; ++e) used[p_el[e]] = true;
+  int64_t tab_off[8] = {}, n_tab = 0;
+  for (int p = 1; p <= 7; ++p)
+    if (used[p]) {
+      tab_off[p] = n_tab;
+      n_tab += uhm_gpu::gen_table_doubles(p, dim, react != nullptr, beta != nullptr);
+    }
+  const size_t o_toff = place(tab_off, sizeof(tab_off));
+  const size_t o_tab = (stage.size() + 15) & ~size_t(15);
+  const size_t need = o_tab + sizeof(double) * (size_t)n_tab;
+  if (need > d_gen_bytes) {
+    d_gen = (unsigned char*)dmalloc(need);
+    d_gen_bytes = need;
+  }
+  CK(cudaMemcpyAsync(d_gen, stage.data(), stage.size(), cudaMemcpyHostToDevice, stream));
+  unsigned char* g = d_gen;
+  auto* d_tab = (double*)(g + o_tab);
+  CK(cudaEventRecord(ev0, stream));
+  for (int p = 1; p <= 7; ++p)
+    if (used[p])
+      uhm_gpu::launch_gen_tables(d_tab + tab_off[p], (const double*)(g + o_ref) + ref_off[p], p, dim, hh, cmass,
+                                 cconv, react != nullptr, beta != nullptr, stream);
+  uhm_gpu::launch_gen_lobatto(ctx.emat, (const int64_t*)(g + o_off), n_el, (const int*)(g + o_p),
+                              (const double*)(g + o_kap), react ? (const double*)(g + o_rea) : nullptr,
+                              beta ? (const double*)(g + o_beta) : nullptr, (const int64_t*)(g + o_sp),
+                              (const int32_t*)(g + o_sel), d_tab, (const int64_t*)(g + o_toff), dim, stream);
   CK(cudaGetLastError());
+  CK(cudaEventRecord(ev1, stream));
   CK(cudaStreamSynchronize(stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  timing = Timing{};
+  timing.upload_ms = ms;   // the generation kernels' device time
+  int n_launch = 1;
+  for (int p = 1; p <= 7; ++p) n_launch += used[p];
+  timing.kernel_launches = n_launch;
   emat_dirty = false;
   emat_device_only = true;
   anorm_valid = false;

@@ -226,6 +226,8 @@ class Engine {
   int64_t* d_ws_stride = nullptr;
   CUtensorMap ws_map;                // one map over the whole BF16 workspace
   int* d_err = nullptr;              // bounded-wait error flag of device kernels
+  unsigned char* d_gen = nullptr;    // recipe of the element generator (one block)
+  size_t d_gen_bytes = 0;
   double* d_gc_xbuf = nullptr;       // exchange buffer of the cooperative LU panel
   unsigned int* d_gc_ctr = nullptr;  // its grid-barrier counter and abort word
   int n_sm = 0;

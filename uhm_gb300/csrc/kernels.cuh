@@ -138,10 +138,12 @@ void launch_bwd_store(const DevCtx& c, const Item* items, int n_items, double* g
 // element-wise residual r = b - sum_e P_e^T A_e P_e x, deterministic gather
 // hp-FEM element matrices generated on the device (k_elements.cu); hh = h/2,
 // cmass / cconv the mass and convection scale factors as the host computes them
+int64_t gen_table_doubles(int p, int dim, int has_react, int has_beta);
+void launch_gen_tables(double* tab, const double* ref_p, int p, int dim, double hh, double cmass, double cconv,
+                       int has_react, int has_beta, cudaStream_t s);
 void launch_gen_lobatto(double* emat, const int64_t* emat_off, int n_el, const int* p_el, const double* kappa,
                         const double* react, const double* beta, const int64_t* sel_ptr, const int32_t* sel,
-                        const double* ref, const int64_t* ref_off, int dim, double hh, double cmass,
-                        double cconv, cudaStream_t s);
+                        const double* tab, const int64_t* tab_off, int dim, cudaStream_t s);
 void launch_elem_gemv(const double* emat, const int64_t* emat_off, const int* elem_m,
                       const int64_t* emap_off, const int32_t* emap, const double* x, int64_t ldx,
                       double* y, const int64_t* y_off, int n_elem, int n_rhs, cudaStream_t s);
