@@ -86,6 +86,23 @@ int uhm_gpu_add_element_with_generation(long* mesh, int* gen, long* elt);
 int uhm_gpu_element_set_parent(long* elt, long* parent);
 int uhm_gpu_element_add_child(long* elt, long* child);
 
+/* Factor reuse.  The reference has these as C++ only (Mesh_::backup and
+ * Mesh_::check_reuse, UHM/src/mesh/mesh.cxx:113-225; Element_::set_reuse and
+ * is_matrix_reusable, UHM/src/mesh/element.cxx:75,216).  backup copies the
+ * connectivity of mesh into the mesh backup (another handle from
+ * uhm_mesh_create_); check_reuse flags the elements of mesh whose factor and
+ * schur nodes are unchanged since, clearing the flag up the tree from any
+ * that changed.  A factorisation then keeps, instead of redoing, every front
+ * whose element is flagged, whose factor from the previous factorisation of
+ * the same locked mesh is still held, whose element matrix was not copied in
+ * since, and whose children are all kept.  uhm_gpu_get_n_refactored gives the
+ * number of fronts the last factorisation redid. */
+int uhm_gpu_element_set_reuse(long* elt, int flag);
+int uhm_gpu_element_get_reuse(long* elt, int* flag);
+int uhm_gpu_mesh_backup(long* mesh, long* backup);
+int uhm_gpu_mesh_check_reuse(long* mesh, long* backup);
+int uhm_gpu_get_n_refactored(long* mesh, int* n);
+
 /* 0 = ok; 4 = device allocation failed; 5..9 = API misuse; 11 = front not
  * positive definite; 12 = zero pivot; 13 = NaN; 20 = refinement missed its
  * tolerance (solution redone in FP64); 30 = unsupported call. */

@@ -97,6 +97,11 @@ def _declare(L):
     sig("uhm_gpu_autotune", [_P(_l), _i, _i, _P(_i)], _i)
     sig("uhm_gpu_generate_lobatto_elements", [_P(_l), _i, _i, _d, _d, _d, _i, _P(_d), _P(_l), _i, _P(_i),
                                               _P(_d), _P(_d), _P(_d), _P(_l), _P(_i)], _i)
+    sig("uhm_gpu_element_set_reuse", [_P(_l), _i], _i)
+    sig("uhm_gpu_element_get_reuse", [_P(_l), _P(_i)], _i)
+    sig("uhm_gpu_mesh_backup", [_P(_l), _P(_l)], _i)
+    sig("uhm_gpu_mesh_check_reuse", [_P(_l), _P(_l)], _i)
+    sig("uhm_gpu_get_n_refactored", [_P(_l), _P(_i)], _i)
     sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
     sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
     sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
@@ -176,6 +181,26 @@ class Mesh:
 
     def add_child(self, elt, child):
         self.L.uhm_gpu_element_add_child(C.byref(_l(elt)), C.byref(_l(child)))
+
+    # -- factor reuse (Mesh_::backup / check_reuse, Element_::set_reuse) ----
+    def set_reuse(self, elt, flag=True):
+        self.L.uhm_gpu_element_set_reuse(C.byref(_l(elt)), int(bool(flag)))
+
+    def get_reuse(self, elt) -> bool:
+        f = _i(0)
+        self.L.uhm_gpu_element_get_reuse(C.byref(_l(elt)), C.byref(f))
+        return bool(f.value)
+
+    def backup(self, other: "Mesh"):
+        self._check(self.L.uhm_gpu_mesh_backup(C.byref(self.h), C.byref(other.h)))
+
+    def check_reuse(self, other: "Mesh"):
+        self._check(self.L.uhm_gpu_mesh_check_reuse(C.byref(self.h), C.byref(other.h)))
+
+    def n_refactored(self) -> int:
+        n = _i(0)
+        self._check(self.L.uhm_gpu_get_n_refactored(C.byref(self.h), C.byref(n)))
+        return n.value
 
     def lock(self):
         self.L.uhm_lock_(C.byref(self.h))

@@ -179,6 +179,23 @@ int uhm_gpu_element_add_child(long* elt, long* child) {
   reinterpret_cast<Element>(*elt)->add_child(reinterpret_cast<Element>(*child));
   return 0;
 }
+int uhm_gpu_element_set_reuse(long* elt, int flag) {
+  reinterpret_cast<Element>(*elt)->set_reuse(flag);
+  return 0;
+}
+int uhm_gpu_element_get_reuse(long* elt, int* flag) {
+  *flag = reinterpret_cast<Element>(*elt)->is_matrix_reusable() ? 1 : 0;
+  return 0;
+}
+int uhm_gpu_mesh_backup(long* mesh, long* backup) {
+  return guard(M(mesh), [&] { M(mesh)->backup(M(backup)); });
+}
+int uhm_gpu_mesh_check_reuse(long* mesh, long* backup) {
+  return guard(M(mesh), [&] { M(mesh)->check_reuse(M(backup)); });
+}
+int uhm_gpu_get_n_refactored(long* mesh, int* n) {
+  return guard(M(mesh), [&] { *n = M(mesh)->eng().n_refactored; });
+}
 int uhm_gpu_get_status(long* mesh) {
   Mesh m = M(mesh);
   return m && m->engine ? m->engine->status : 0;

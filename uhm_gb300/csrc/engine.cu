@@ -83,6 +83,11 @@ void Engine::free_device() {
   d_gc_ctr = nullptr;
   d_gen = nullptr;
   d_gen_bytes = 0;
+  d_items_part = nullptr;
+  d_items_part_cap = 0;
+  fac_ops_part.clear();
+  part_mask.clear();
+  front_kept.clear();
   tree_bnorm.clear();
   tree_anorm.clear();
 }
@@ -146,6 +151,8 @@ void Engine::ensure_plan() {
     esrc_of_slot[e->slot] = (int)esrc.size();
     esrc.push_back(std::move(es));
   }
+  leaf_changed.assign(esrc.size(), 1);
+  front_kept.assign(fronts.size(), 0);
   size_t need = (size_t)(emat_total + erhs_total) * sizeof(double);
   if (need > h_pinned_bytes || !h_pinned) {
     release_staging();
@@ -284,6 +291,18 @@ void Engine::copy_in(Element e, int m, int n, int nod_disp, const int* nods, int
     for (int r = 0; r < m; ++r) perm[r] = row_of[pos[r]];
   }
   auto rowmap = [&](int r) { return perm.empty() ? r : perm[r]; };
+  // copy_in adds into the host staging copy: fetch it first when the
+  // current data only exist on the device (bulk device copy, generated)
+  if (dev_ok && side == UHM_LHS && emat_device_only) {
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemcpy(h_pinned, ctx.emat, sizeof(double) * (size_t)emat_total, cudaMemcpyDeviceToHost));
+    emat_device_only = false;
+  }
+  if (dev_ok && side != UHM_LHS && erhs_device_only) {
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemcpy(h_pinned + emat_total, d_erhs, sizeof(double) * (size_t)erhs_total, cudaMemcpyDeviceToHost));
+    erhs_device_only = false;
+  }
   if (side == UHM_LHS) {
     double* dst = h_pinned + es.mat_off;
     if (!es.has_lhs) std::memset(dst, 0, sizeof(double) * (size_t)m * m);
@@ -291,7 +310,9 @@ void Engine::copy_in(Element e, int m, int n, int nod_disp, const int* nods, int
       for (int i = 0; i < m; ++i) dst[rowmap(i) + (int64_t)rowmap(j) * m] += buf[i + (int64_t)j * m];
     es.has_lhs = true;
     emat_dirty = true;
+    leaf_changed[ei] = 1;
     learned_valid = false;
+    anorm_valid = false;
     anorm_inf = -1.0;
     dev_ok = dev_ok && !first;   // maps change when an element appears
     factored = false;
@@ -313,6 +334,7 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
     if (es.node_order.empty()) fail("copy_in_leaves: element maps unknown (call uhm_gpu_set_leaf_nodes first)", 7);
   if (side == UHM_LHS) {
     if (n_values != emat_total) fail("copy_in_leaves: size mismatch", 7);
+    std::fill(leaf_changed.begin(), leaf_changed.end(), 1);
     if (!dev_ok) {
       std::memcpy(h_pinned, buf, sizeof(double) * (size_t)emat_total);
       for (auto& es : esrc) es.has_lhs = true;
@@ -370,6 +392,7 @@ void Engine::generate_lobatto_elements(int method, int dim, double hh, double cm
   // the assembly programs list an element source only for leaves that carry a
   // matrix, so mark them before the programs are built
   for (auto& es : esrc) es.has_lhs = true;
+  std::fill(leaf_changed.begin(), leaf_changed.end(), 1);
   prepare_device(method);
   const int64_t n_sel = sel_ptr[n_el];
   std::vector<int64_t> off(n_el);
@@ -762,7 +785,7 @@ void Engine::build_programs(int method) {
     for (int dt = 0; dt < 2; ++dt) {
       std::vector<int> fl;
       for (int s : lv)
-        if (h_fronts[s].dtype == dt) fl.push_back(s);
+        if (h_fronts[s].dtype == dt && (!fac_mask || (*fac_mask)[s])) fl.push_back(s);
       if (fl.empty()) continue;
       std::vector<int> tcf;
       for (int s : fl)
@@ -1011,6 +1034,7 @@ void Engine::build_programs(int method) {
       }
     }
   }
+  if (fac_mask) return;   // a partial factor program (build_partial) needs no solves
   // solve programs
   const int gm = chol ? M_CHOL : (method == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV);
   auto solve_small = [&](const HostFront& f, int dt) {
@@ -1369,7 +1393,7 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
   timing.kernel_launches += (int64_t)ops.size();
 }
 
-void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
+void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out, const uhm_gpu::Item* base) {
   std::vector<cudaEvent_t> evs;
   if (profiling) {
     evs.resize(2 * ops.size());
@@ -1377,7 +1401,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out)
   }
   size_t k = 0;
   for (const Op& op : ops) {
-    const Item* it = d_items + op.item_off;
+    const Item* it = (base ? base : d_items) + op.item_off;
     if (profiling) CK(cudaEventRecord(evs[2 * k], stream));
     switch (op.kind) {
       case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, stream); break;
@@ -1488,9 +1512,29 @@ void Engine::factor(int method) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.upload_ms = ms;
+  // factor reuse (operation/element.cxx:202-205 skips the merge and the
+  // factorisation of a reusable element): keep a front when its element is
+  // flagged, its factor from the last factorisation of this plan is held,
+  // its element matrix was not copied in since and all its children are kept
+  std::vector<char> act(fronts.size(), 1);
+  int n_keep = 0;
+  if (front_kept.size() == fronts.size() && leaf_changed.size() == esrc.size())
+    for (auto& lv : levels)   // leaves first: children before parents
+      for (int s : lv) {
+        const HostFront& f = fronts[s];
+        bool keep = front_kept[s] && f.e->is_matrix_reusable();
+        const int ei = esrc_of_slot[s];
+        if (ei >= 0 && leaf_changed[ei]) keep = false;
+        for (int c : f.children) keep = keep && !act[c];
+        act[s] = keep ? 0 : 1;
+        n_keep += keep ? 1 : 0;
+      }
+  if (n_keep > 0 && act != part_mask) build_partial(method, act);
+  n_refactored = (int)fronts.size() - n_keep;
   CK(cudaEventRecord(ev0, stream));
   if (!anorm_valid) enqueue_anorm();
-  run_ops(fac_ops, nullptr, nullptr);
+  if (n_keep > 0) launch_ops(fac_ops_part, nullptr, nullptr, d_items_part);
+  else run_ops(fac_ops, nullptr, nullptr);
   CK(cudaEventRecord(ev1, stream));
   CK(cudaEventSynchronize(ev1));
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
@@ -1520,6 +1564,49 @@ void Engine::factor(int method) {
   factored = true;
   factored_method = method;
   h_x_valid = false;
+  // every front's factor now belongs to the current element matrices
+  front_kept.assign(fronts.size(), status == 0 ? 1 : 0);
+  if (status == 0) leaf_changed.assign(esrc.size(), 0);
+}
+
+// The factor program over the fronts marked in act only: build_programs with
+// a mask, its items in their own device array; the full programs (and their
+// CUDA graphs) are left as they are.
+void Engine::build_partial(int method, const std::vector<char>& act) {
+  std::vector<uhm_gpu::Item> items_full = std::move(h_items);
+  std::vector<Op> fac_full = std::move(fac_ops), fwd_full = std::move(fwd_ops), bwd_full = std::move(bwd_ops);
+  auto restore = [&]() {
+    fac_mask = nullptr;
+    h_items = std::move(items_full);
+    fac_ops = std::move(fac_full);
+    fwd_ops = std::move(fwd_full);
+    bwd_ops = std::move(bwd_full);
+  };
+  h_items.clear();
+  fac_ops.clear();
+  fwd_ops.clear();
+  bwd_ops.clear();
+  fac_mask = &act;
+  std::vector<uhm_gpu::Item> items_part;
+  try {
+    build_programs(method);
+  } catch (...) {
+    restore();
+    throw;
+  }
+  fac_ops_part = std::move(fac_ops);
+  items_part = std::move(h_items);
+  restore();
+  part_mask.clear();
+  if (items_part.size() > d_items_part_cap) {
+    d_items_part = (uhm_gpu::Item*)dmalloc(sizeof(uhm_gpu::Item) * items_part.size());
+    d_items_part_cap = items_part.size();
+  }
+  if (!items_part.empty())
+    CK(cudaMemcpyAsync(d_items_part, items_part.data(), sizeof(uhm_gpu::Item) * items_part.size(),
+                       cudaMemcpyHostToDevice, stream));
+  CK(cudaStreamSynchronize(stream));
+  part_mask = act;
 }
 
 void Engine::solve_into(int method, double* rhs, double* out, int phase) {
@@ -1910,6 +1997,7 @@ int Engine::autotune(int method, int reps) {
   auto time_now = [&]() {
     double best = 1e300;
     for (int r = 0; r < reps + 1; ++r) {        // the first run builds graphs and is not counted
+      std::fill(front_kept.begin(), front_kept.end(), 0);   // time whole factorisations
       factor(method);
       solve(method, 3);
       const double t = timing.factor_ms + timing.solve_ms + timing.refine_ms;

@@ -153,6 +153,7 @@ class Engine {
   // matrices must have been copied in
   void front_features(std::vector<float>& feat);
   int status = 0;
+  int n_refactored = 0;         // fronts the last factorisation redid (the rest were kept)
   std::string last_error;
   Timing timing;
   bool profiling = false;       // per-op CUDA events (outside timed regions)
@@ -204,6 +205,16 @@ class Engine {
   std::vector<int2> h_colsrc;
   std::vector<uhm_gpu::Item> h_items;
   std::vector<Op> fac_ops, fwd_ops, bwd_ops;
+  // factor reuse: fronts whose factor from the last factorisation of this
+  // plan is held (by slot), leaves whose element matrix changed since (by
+  // element source), and the factor program over the fronts to redo
+  std::vector<char> front_kept, leaf_changed;
+  std::vector<Op> fac_ops_part;
+  std::vector<char> part_mask;
+  const std::vector<char>* fac_mask = nullptr;   // build_programs: factor only these slots
+  uhm_gpu::Item* d_items_part = nullptr;
+  size_t d_items_part_cap = 0;
+  void build_partial(int method, const std::vector<char>& act);
   int64_t arena64_n = 0, arena32_n = 0, vec_n = 0, piv_n = 0;
   int64_t dinv64_n = 0, dinv32_n = 0, flags_n = 0;
   int* d_ticket = nullptr;
@@ -256,7 +267,8 @@ class Engine {
   void upload_elements();
   void assemble_rhs();
   void run_ops(const std::vector<Op>& ops, double* g_in, double* g_out);
-  void launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out);
+  // items of the ops at base (d_items when null)
+  void launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out, const uhm_gpu::Item* base = nullptr);
   struct GraphEntry {
     const std::vector<Op>* ops;
     double* gin;

@@ -254,6 +254,47 @@ void Mesh_::reset() {
   id_element = 0;
 }
 
+// mesh.cxx:113-154: connectivity only, by element id; each factor / schur
+// node is kept as (its address in this mesh, n_dof + p + kind)
+void Mesh_::backup(Mesh_* b) {
+  if (!b || b == this) throw std::invalid_argument("backup: needs another mesh");
+  b->reset();
+  for (auto& kv : elements) {
+    const Element_& a = kv.second;
+    Element_& c = b->elements.insert(std::make_pair(a.id, Element_(a.id, a.generation))).first->second;
+    for (const auto& pr : a.factor)
+      c.factor.emplace_back(pr.first, pr.first->get_n_dof() + pr.first->get_p() + pr.first->get_kind());
+    for (const auto& pr : a.schur)
+      c.schur.emplace_back(pr.first, pr.first->get_n_dof() + pr.first->get_p() + pr.first->get_kind());
+  }
+  b->id_element = id_element;
+}
+
+// mesh.cxx:156-225, in the same element order (by id): an element keeps its
+// factorisation when an element of its id is in the backup with the same
+// factor and schur nodes (same node, same n_dof + p + kind, same order);
+// one that does not clears the flag on itself and every ancestor
+void Mesh_::check_reuse(Mesh_* b) {
+  if (!b || b == this) throw std::invalid_argument("check_reuse: needs the backup mesh");
+  for (auto& kv : elements) kv.second.set_reuse(1);
+  auto same = [](const std::vector<std::pair<Node, int>>& x, const std::vector<std::pair<Node, int>>& y) {
+    if (x.size() != y.size()) return false;
+    for (size_t i = 0; i < x.size(); ++i) {
+      const Node n = x[i].first;
+      if (n != y[i].first || n->get_n_dof() + n->get_p() + n->get_kind() != y[i].second) return false;
+    }
+    return true;
+  };
+  for (auto& kv : elements) {
+    Element a = &kv.second;
+    Element bb = b->find_element(a->get_id());
+    const bool flag = bb && same(a->factor, bb->factor) && same(a->schur, bb->schur);
+    a->set_reuse(flag);
+    if (!a->is_matrix_reusable())
+      for (Element u = a; u; u = u->get_parent()) u->set_reuse(0);
+  }
+}
+
 // .uhm text format of Mesh_::import_file (UHM/src/mesh/mesh.cxx:511-579)
 bool Mesh_::import_file(const char* path) {
   reset();

@@ -82,6 +82,7 @@ class Element_ {
   std::vector<std::pair<Node, int>> factor, schur;
   FrontHandle hm;
   int slot = -1;                               // index in the engine's front table
+  int reuse = 0;                               // keep the last factorisation (element.hxx:66)
 
   Element_() = default;
   Element_(int id_, int gen) : id(id_), generation(gen) {}
@@ -97,6 +98,8 @@ class Element_ {
   bool is_orphan() const { return parent == nullptr; }
   bool is_leaf() const { return children.empty(); }
   bool is_matrix_created() const { return hm.created; }
+  void set_reuse(int flag) { reuse = flag; }   // element.cxx:75
+  bool is_matrix_reusable() const { return reuse != 0; }
   std::pair<int, int> get_n_dof() const;       // (fs, ss), element.cxx:112-126
   int get_height() const;
 
@@ -148,6 +151,11 @@ class Mesh_ {
   int get_n_elements() const { return (int)elements.size(); }
   bool import_file(const char* full_path);
   void reset();
+  // factor reuse (mesh.cxx:113-225): backup keeps each element's factor and
+  // schur nodes with n_dof + p + kind; check_reuse flags the elements whose
+  // lists are unchanged and clears the flag up the tree from any that changed
+  void backup(Mesh_* b);
+  void check_reuse(Mesh_* b);
 
   // --- solving sequence (mesh.hxx:182-300) ----------------------------
   void lock();
