@@ -103,6 +103,26 @@ int uhm_gpu_mesh_backup(long* mesh, long* backup);
 int uhm_gpu_mesh_check_reuse(long* mesh, long* backup);
 int uhm_gpu_get_n_refactored(long* mesh, int* n);
 
+/* The assembled operator as a sparse matrix for external solvers: the
+ * reference's DSparse_ (UHM/include/uhm/interf/sparse.hxx:99-129,
+ * UHM/src/interf/sparse.cxx:188-460) over every leaf, in leaf order.  Entries
+ * are keyed by global (row, col), or (col, row) when cs, with global dofs as
+ * the mesh numbers them (uhm_gpu_get_node_offsets); contributions to one
+ * entry are added in leaf order (axpy = 1) or the first kept (axpy = 0).
+ * compress = 0: triplets in key order, rows in ia, columns in ja
+ * (DSparse_::triplet); compress = 1: compressed rows (cs = 0: ia pointers,
+ * ja columns) or columns (cs = 1: ja pointers, ia rows) (DSparse_::compress).
+ * is_sym keeps the entries whose key has second >= first; fort adds 1 to
+ * every index and pointer.  b is the assembled right-hand sides, column-major
+ * (n_dof x n_rhs).  Call once with ia, ja, a, b NULL for the lengths
+ * (len_ia, len_ja, n_nz), then with arrays of those lengths.  n_dof is the
+ * number of dofs (the reference's triplet reports its last index instead). */
+int uhm_gpu_export_sparse(long* mesh, int is_sym, int fort, int cs, int compress, int axpy, int* n_dof,
+                          int* n_rhs, long* len_ia, long* len_ja, long* n_nz, int* ia, int* ja, double* a,
+                          double* b);
+/* the first global dof of each node (single physics ids) in the locked mesh */
+int uhm_gpu_get_node_offsets(long* mesh, int n, const int* ids, int* offsets);
+
 /* 0 = ok; 4 = device allocation failed; 5..9 = API misuse; 11 = front not
  * positive definite; 12 = zero pivot; 13 = NaN; 20 = refinement missed its
  * tolerance (solution redone in FP64); 30 = unsupported call. */

@@ -102,6 +102,9 @@ def _declare(L):
     sig("uhm_gpu_mesh_backup", [_P(_l), _P(_l)], _i)
     sig("uhm_gpu_mesh_check_reuse", [_P(_l), _P(_l)], _i)
     sig("uhm_gpu_get_n_refactored", [_P(_l), _P(_i)], _i)
+    sig("uhm_gpu_export_sparse", [_P(_l), _i, _i, _i, _i, _i, _P(_i), _P(_i), _P(_l), _P(_l), _P(_l),
+                                  _P(_i), _P(_i), _P(_d), _P(_d)], _i)
+    sig("uhm_gpu_get_node_offsets", [_P(_l), _i, _P(_i), _P(_i)], _i)
     sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
     sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
     sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
@@ -201,6 +204,31 @@ class Mesh:
         n = _i(0)
         self._check(self.L.uhm_gpu_get_n_refactored(C.byref(self.h), C.byref(n)))
         return n.value
+
+    # -- sparse export (DSparse_::import_element + triplet / compress) --------
+    def export_sparse(self, is_sym=False, fort=False, cs=False, compress=False, axpy=True) -> dict:
+        nd, nr = _i(0), _i(0)
+        lia, lja, nnz = _l(0), _l(0), _l(0)
+        flags = [int(bool(v)) for v in (is_sym, fort, cs, compress, axpy)]
+        self._check(self.L.uhm_gpu_export_sparse(C.byref(self.h), *flags, C.byref(nd), C.byref(nr),
+                                                 C.byref(lia), C.byref(lja), C.byref(nnz),
+                                                 None, None, None, None))
+        ia = np.zeros(lia.value, np.int32)
+        ja = np.zeros(lja.value, np.int32)
+        a = np.zeros(nnz.value)
+        b = np.zeros(nd.value * nr.value)
+        self._check(self.L.uhm_gpu_export_sparse(C.byref(self.h), *flags, C.byref(nd), C.byref(nr),
+                                                 C.byref(lia), C.byref(lja), C.byref(nnz),
+                                                 ia.ctypes.data_as(_P(_i)), ja.ctypes.data_as(_P(_i)),
+                                                 a.ctypes.data_as(_P(_d)), b.ctypes.data_as(_P(_d))))
+        return dict(n_dof=nd.value, n_rhs=nr.value, ia=ia, ja=ja, a=a, b=b.reshape(nr.value, nd.value).T)
+
+    def node_offsets(self, ids) -> np.ndarray:
+        ids = np.ascontiguousarray(ids, np.int32)
+        out = np.zeros(len(ids), np.int32)
+        self._check(self.L.uhm_gpu_get_node_offsets(C.byref(self.h), len(ids), ids.ctypes.data_as(_P(_i)),
+                                                    out.ctypes.data_as(_P(_i))))
+        return out
 
     def lock(self):
         self.L.uhm_lock_(C.byref(self.h))

@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = [
     "mesh.cpp",
+    "sparse.cpp",
     "capi.cpp",
     "engine.cu",
     "k_factor.cu",

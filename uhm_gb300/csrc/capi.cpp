@@ -193,6 +193,34 @@ int uhm_gpu_mesh_backup(long* mesh, long* backup) {
 int uhm_gpu_mesh_check_reuse(long* mesh, long* backup) {
   return guard(M(mesh), [&] { M(mesh)->check_reuse(M(backup)); });
 }
+int uhm_gpu_export_sparse(long* mesh, int is_sym, int fort, int cs, int compress, int axpy, int* n_dof,
+                          int* n_rhs, long* len_ia, long* len_ja, long* n_nz, int* ia, int* ja, double* a,
+                          double* b) {
+  return guard(M(mesh), [&] {
+    uhm::Engine::SparseOut o;
+    M(mesh)->eng().export_sparse(is_sym, fort, cs, compress, axpy, o);
+    *n_dof = o.n_dof;
+    *n_rhs = o.n_rhs;
+    *len_ia = (long)o.ia.size();
+    *len_ja = (long)o.ja.size();
+    *n_nz = (long)o.a.size();
+    if (ia) std::memcpy(ia, o.ia.data(), sizeof(int) * o.ia.size());
+    if (ja) std::memcpy(ja, o.ja.data(), sizeof(int) * o.ja.size());
+    if (a) std::memcpy(a, o.a.data(), sizeof(double) * o.a.size());
+    if (b) std::memcpy(b, o.b.data(), sizeof(double) * o.b.size());
+  });
+}
+int uhm_gpu_get_node_offsets(long* mesh, int n, const int* ids, int* offsets) {
+  return guard(M(mesh), [&] {
+    uhm::Mesh_* m = M(mesh);
+    if (!m->is_locked()) throw std::invalid_argument("node offsets: the mesh is not locked");
+    for (int i = 0; i < n; ++i) {
+      uhm::Node nd = m->find_node(ids[i]);
+      if (!nd) throw std::invalid_argument("node offsets: unknown node");
+      offsets[i] = nd->get_offset();
+    }
+  });
+}
 int uhm_gpu_get_n_refactored(long* mesh, int* n) {
   return guard(M(mesh), [&] { *n = M(mesh)->eng().n_refactored; });
 }

@@ -120,6 +120,18 @@ class Engine {
                                  const int64_t* sel_ptr, const int32_t* sel);
   // element maps of all leaves from their node lists (leaf order, single physics)
   void set_leaf_nodes(const int* nods_all);
+  // The assembled operator and right-hand sides as a sparse matrix, the
+  // reference's DSparse_ (UHM/src/interf/sparse.cxx:188-460): every leaf's
+  // element matrix added in leaf order into entries keyed by global
+  // (row, col) -- (col, row) when cs -- then listed in key order as
+  // triplets or compressed rows (columns when cs); is_sym keeps col >= row
+  // of the key; fort adds 1 to every index.  sparse.cpp.
+  struct SparseOut {
+    int n_dof = 0, n_rhs = 0;
+    std::vector<int> ia, ja;
+    std::vector<double> a, b;
+  };
+  void export_sparse(int is_sym, int fort, int cs, int compress, int axpy, SparseOut& out);
   void node_solution(int n_nodes, const int* ids, double* out, int64_t n_values);
 
   // --- numerics -----------------------------------------------------------
