@@ -56,6 +56,11 @@ extern "C" {
                                              double* flop_decompose, double* flop_solve,
                                              unsigned* n_nonzero_factor, double* buffer);
 /* fort.hxx:120-121*/ void uhm_mesh_import_(long* mesh, char* filename);
+/* fort.hxx:122: the reference partitions with METIS (build_tree.cxx:52-54,
+ * build_tree_var4.cxx); here the heavy-edge matching of its
+ * build_tree_var1.cxx:53-181 over the elements without a parent (ties by
+ * element and node id; one tree per connected part; new elements that would
+ * eliminate nothing are left out) */
 /* fort.hxx:122   */ void uhm_build_tree_(long* mesh);
 /* fort.hxx:123-125*/ void uhm_create_matrix_without_buffer_(long* mesh, int* datatype, int* n_rhs);
 /* fort.hxx:126   */ void uhm_create_leaf_matrix_buffer_(long* mesh);
@@ -102,6 +107,13 @@ int uhm_gpu_element_get_reuse(long* elt, int* flag);
 int uhm_gpu_mesh_backup(long* mesh, long* backup);
 int uhm_gpu_mesh_check_reuse(long* mesh, long* backup);
 int uhm_gpu_get_n_refactored(long* mesh, int* n);
+
+/* The element tree: every element (id order) with its parent (-1 for a
+ * root) and generation; n is set to the element count, and nothing else is
+ * written when cap < n.  uhm_gpu_get_children: an element's children in
+ * child order. */
+int uhm_gpu_get_tree(long* mesh, int cap, int* elt_id, int* parent_id, int* generation, int* n);
+int uhm_gpu_get_children(long* mesh, int elt_id, int cap, int* child_id, int* n);
 
 /* The assembled operator as a sparse matrix for external solvers: the
  * reference's DSparse_ (UHM/include/uhm/interf/sparse.hxx:99-129,

@@ -105,6 +105,8 @@ def _declare(L):
     sig("uhm_gpu_export_sparse", [_P(_l), _i, _i, _i, _i, _i, _P(_i), _P(_i), _P(_l), _P(_l), _P(_l),
                                   _P(_i), _P(_i), _P(_d), _P(_d)], _i)
     sig("uhm_gpu_get_node_offsets", [_P(_l), _i, _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_get_tree", [_P(_l), _i, _P(_i), _P(_i), _P(_i), _P(_i)], _i)
+    sig("uhm_gpu_get_children", [_P(_l), _i, _i, _P(_i), _P(_i)], _i)
     sig("uhm_gpu_get_op_log", [_P(_l), _i, _P(_i), _P(_i), _P(_d), _P(_i)], _i)
     sig("uhm_gpu_get_front_features", [_P(_l), _i, _i, _P(_f)], _i)
     sig("uhm_gpu_get_front_precision", [_P(_l), _i, _P(_i), _P(_i)], _i)
@@ -222,6 +224,27 @@ class Mesh:
                                                  ia.ctypes.data_as(_P(_i)), ja.ctypes.data_as(_P(_i)),
                                                  a.ctypes.data_as(_P(_d)), b.ctypes.data_as(_P(_d))))
         return dict(n_dof=nd.value, n_rhs=nr.value, ia=ia, ja=ja, a=a, b=b.reshape(nr.value, nd.value).T)
+
+    def build_tree(self):
+        self.L.uhm_build_tree_(C.byref(self.h))
+        self._check()
+
+    def tree(self):
+        """(element ids, parent ids (-1 for roots), generations, {id: children})"""
+        n = _i(0)
+        self._check(self.L.uhm_gpu_get_tree(C.byref(self.h), 0, None, None, None, C.byref(n)))
+        eid, par, gen = (np.zeros(n.value, np.int32) for _ in range(3))
+        self._check(self.L.uhm_gpu_get_tree(C.byref(self.h), n.value, eid.ctypes.data_as(_P(_i)),
+                                            par.ctypes.data_as(_P(_i)), gen.ctypes.data_as(_P(_i)),
+                                            C.byref(n)))
+        kids = {}
+        buf = np.zeros(1 << 16, np.int32)
+        for e in eid.tolist():
+            k = _i(0)
+            self._check(self.L.uhm_gpu_get_children(C.byref(self.h), e, len(buf),
+                                                    buf.ctypes.data_as(_P(_i)), C.byref(k)))
+            kids[e] = buf[:k.value].tolist()
+        return eid, par, gen, kids
 
     def node_offsets(self, ids) -> np.ndarray:
         ids = np.ascontiguousarray(ids, np.int32)

@@ -123,8 +123,7 @@ void uhm_mesh_import_(long* mesh, char* filename) {
   });
 }
 void uhm_build_tree_(long* mesh) {
-  set_err(M(mesh), "build_tree: METIS-based tree construction is not part of this library; "
-                   "build the tree with uhm_gpu_add_element_with_generation / uhm_gpu_element_set_parent", 30);
+  guard(M(mesh), [&] { M(mesh)->build_tree(); });
 }
 void uhm_create_matrix_without_buffer_(long* mesh, int* dt, int* n_rhs) {
   guard(M(mesh), [&] { M(mesh)->create_matrix_without_buffer(*dt, *n_rhs); });
@@ -219,6 +218,28 @@ int uhm_gpu_get_node_offsets(long* mesh, int n, const int* ids, int* offsets) {
       if (!nd) throw std::invalid_argument("node offsets: unknown node");
       offsets[i] = nd->get_offset();
     }
+  });
+}
+int uhm_gpu_get_tree(long* mesh, int cap, int* elt_id, int* parent_id, int* generation, int* n) {
+  return guard(M(mesh), [&] {
+    uhm::Mesh_* m = M(mesh);
+    *n = (int)m->elements.size();
+    if (cap < *n) return;
+    int i = 0;
+    for (auto& kv : m->elements) {
+      elt_id[i] = kv.first;
+      parent_id[i] = kv.second.parent ? kv.second.parent->get_id() : -1;
+      generation[i] = kv.second.get_generation();
+      ++i;
+    }
+  });
+}
+int uhm_gpu_get_children(long* mesh, int elt_id, int cap, int* child_id, int* n) {
+  return guard(M(mesh), [&] {
+    uhm::Element e = M(mesh)->find_element(elt_id);
+    if (!e) throw std::invalid_argument("get_children: unknown element");
+    *n = e->get_n_children();
+    for (int i = 0; i < *n && i < cap; ++i) child_id[i] = e->get_child(i)->get_id();
   });
 }
 int uhm_gpu_get_n_refactored(long* mesh, int* n) {

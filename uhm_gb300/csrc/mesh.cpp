@@ -10,6 +10,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <set>
 #include <stdexcept>
 
 #include "engine.hpp"
@@ -293,6 +295,117 @@ void Mesh_::check_reuse(Mesh_* b) {
     if (!a->is_matrix_reusable())
       for (Element u = a; u; u = u->get_parent()) u->set_reuse(0);
   }
+}
+
+// Heavy-edge matching, level by level (build_tree_var1.cxx:53-181).  Each
+// round visits the elements without a parent in order and, through their
+// schur nodes, every pair of them that shares a node.  A pair's weight is
+// (dofs of the nodes only the two of them own, minus the dofs of every
+// other schur node of either); pairs are merged under a new parent from the
+// heaviest down (equal weights: the later-listed pair first, as a reverse
+// walk of the reference's multimap), each element at most once per round.
+// The new parents and the unmerged elements make the next round's list.
+// Differences, all deterministic: elements and nodes are ordered by id
+// where the reference compares addresses; a round that merges nothing ends
+// the build (each connected part of the mesh becomes its own tree, where
+// the reference would not stop); and a new element that eliminates no node
+// is taken out again, its children moved to its parent in its place (its
+// parent merges the same nodes), so every interior front factors something.
+int Mesh_::build_tree() {
+  unlock();
+  // the subtrees already present, children before parents
+  std::vector<Element> orphan;
+  for (auto& kv : elements)
+    if (kv.second.is_orphan()) orphan.push_back(&kv.second);
+  std::vector<Element> post;
+  std::function<void(Element)> visit = [&](Element e) {
+    for (Element c : e->children) visit(c);
+    post.push_back(e);
+  };
+  for (Element e : orphan) visit(e);
+  for (Element e : post)
+    if (e->is_leaf()) e->restore_connectivity();
+  for (Element e : post) {
+    e->merge_nodes_from_children();
+    e->separate_nodes();
+  }
+  std::vector<Element> created;
+  while (orphan.size() > 1) {
+    std::set<std::pair<int, int>> seen;
+    struct Cand {
+      int w0, w1;
+      size_t order;
+      Element a, b;
+    };
+    std::vector<Cand> cand;
+    for (Element o : orphan)
+      for (auto& kv : o->nodes) {
+        if (kv.second != UHM_SEPARATED_SCHUR) continue;
+        for (Element nb : kv.first->owner) {
+          if (nb == o) continue;
+          Element a = o, b = nb;
+          if (a->id > b->id) std::swap(a, b);
+          if (!seen.insert({a->id, b->id}).second) continue;
+          int w0 = 0, w1 = 0;
+          const Element pr[2] = {a, b};
+          for (int i = 0; i < 2; ++i)
+            for (auto& nn : pr[i]->nodes) {
+              if (nn.second != UHM_SEPARATED_SCHUR) continue;
+              const Node n = nn.first;
+              if (n->get_n_owner() == 2 && n->owner.count(pr[1 - i])) {
+                if (i == 0) w0 += n->get_n_dof();
+              } else {
+                w1 -= n->get_n_dof();
+              }
+            }
+          cand.push_back(Cand{w0, w1, cand.size(), a, b});
+        }
+      }
+    std::stable_sort(cand.begin(), cand.end(),
+                     [](const Cand& x, const Cand& y) { return x.w0 != y.w0 ? x.w0 < y.w0 : x.w1 < y.w1; });
+    std::vector<Element> next;
+    for (auto it = cand.rbegin(); it != cand.rend(); ++it) {
+      Element a = it->a, b = it->b;
+      if (!a->is_orphan() || !b->is_orphan()) continue;
+      Element p = add_element(std::min(a->get_generation(), b->get_generation()) - 1);
+      p->add_child(a);
+      a->set_parent(p);
+      p->add_child(b);
+      b->set_parent(p);
+      p->merge_nodes_from_children();
+      p->separate_nodes();
+      next.push_back(p);
+      created.push_back(p);
+    }
+    if (next.empty()) break;   // no two parts share a node: one tree per part
+    for (Element o : orphan)
+      if (o->is_orphan()) next.push_back(o);
+    orphan.swap(next);
+  }
+  // take out new elements that eliminate nothing (their parent merges the
+  // same nodes from their children)
+  for (Element p : created) {
+    if (!p->parent || p->get_n_dof().first > 0) continue;
+    Element q = p->parent;
+    std::vector<Element> kids;
+    for (Element c : q->children) {
+      if (c != p) {
+        kids.push_back(c);
+        continue;
+      }
+      for (Element g : p->children) {
+        g->parent = q;
+        kids.push_back(g);
+      }
+    }
+    q->children.swap(kids);
+    for (auto& kv : p->nodes) kv.first->remove_owner(p);
+    elements.erase(p->id);
+  }
+  int roots = 0;
+  for (auto& kv : elements) roots += kv.second.is_orphan() ? 1 : 0;
+  if (engine) engine->invalidate_plan();
+  return roots;
 }
 
 // .uhm text format of Mesh_::import_file (UHM/src/mesh/mesh.cxx:511-579)

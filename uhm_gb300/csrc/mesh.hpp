@@ -156,6 +156,10 @@ class Mesh_ {
   // lists are unchanged and clears the flag up the tree from any that changed
   void backup(Mesh_* b);
   void check_reuse(Mesh_* b);
+  // assembly tree over the elements without a parent, built by heavy-edge
+  // matching (UHM/src/operation/build_tree_var1.cxx:53-181); returns the
+  // number of roots (one per connected part of the mesh)
+  int build_tree();
 
   // --- solving sequence (mesh.hxx:182-300) ----------------------------
   void lock();
