@@ -10,9 +10,8 @@
  * error that uhm_gpu_get_status / uhm_gpu_get_last_error report.
  *
  * Part 2 (uhm_gpu_*) adds what the device path needs and the reference has
- * no call for: tree construction through the Element API (the reference
- * builds trees with METIS, which this path does not use), status codes,
- * precision / refinement control, bulk transfers and timings.
+ * no call for: explicit tree construction through the Element API, status
+ * codes, precision / refinement control, bulk transfers and timings.
  *
  * Constants (UHM/include/uhm/wrapper/fort.f90:33-53):
  *   UHM_REAL = 101, UHM_COMPLEX = 103 (unsupported), UHM_LHS = 1, UHM_RHS = 2,
@@ -20,6 +19,30 @@
  */
 #ifndef UHM_GB300_H
 #define UHM_GB300_H
+
+/* the constants above, for C callers (the reference defines them for
+ * Fortran in fort.f90 and for C++ in UHM/include/uhm/const.hxx; C++ callers
+ * of this library have them in uhm_gb300/csrc/mesh.hpp) */
+#ifndef __cplusplus
+#ifndef UHM_REAL
+#define UHM_REAL 101
+#endif
+#ifndef UHM_COMPLEX
+#define UHM_COMPLEX 103
+#endif
+#ifndef UHM_LHS
+#define UHM_LHS 1
+#endif
+#ifndef UHM_RHS
+#define UHM_RHS 2
+#endif
+#ifndef UHM_PHYSICS_SINGLE
+#define UHM_PHYSICS_SINGLE 1
+#endif
+#ifndef UHM_PHYSICS_MULTI
+#define UHM_PHYSICS_MULTI 2
+#endif
+#endif
 
 #ifdef __cplusplus
 extern "C" {
