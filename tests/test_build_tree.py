@@ -115,3 +115,63 @@ def test_built_mesh_takes_the_usual_calls(native_lib):
     m.copy_in_leaves(api.UHM_RHS, spec.rhs)
     assert m.status() == 0
     assert m.get_n_dof() == spec.n_dof()
+
+
+def _write_uhm(spec, path, extra_node=False):
+    """the leaves of a spec in the .uhm text format Mesh_::import_file reads
+    (UHM/src/mesh/mesh.cxx:511-579): nodes "id phy n_dof p kind", then per
+    element its node count and "id phy" lines"""
+    lines = ["# written for the import test", "UHM", str(spec.n_nodes + (1 if extra_node else 0))]
+    for i, d, p, k in zip(spec.node_id, spec.node_ndof, spec.node_p, spec.node_kind):
+        lines.append(f"{int(i)} 0 {int(d)} {int(p)} {int(k)}")
+    if extra_node:
+        lines.append(f"{int(spec.node_id.max()) + 1} 0 5 2 0")     # owned by no element: dropped
+    lines.append(str(spec.n_leaves))
+    for e in range(spec.n_leaves):
+        nl = spec.element_nodes(e)
+        lines.append(str(len(nl)))
+        lines += [f"{int(n)} 0" for n in nl]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def test_import_then_build_tree(native_lib, tmp_path):
+    """The reference's file-driven flow: import_file (leaves only), build_tree,
+    lock, create_matrix, copy_in -- fronts equal the oracle's on the built tree."""
+    spec = hpfem.convdiff3d(3, 2, seed=10)
+    f = tmp_path / "mesh.uhm"
+    _write_uhm(spec, f, extra_node=True)
+    m = api.Mesh()
+    m.import_file(str(f))
+    m.build_tree()
+    m.lock()
+    m.create_matrix_without_buffer(api.UHM_REAL, spec.n_rhs)
+    assert m.get_n_dof() == spec.n_dof()                 # the orphan node's 5 dofs are gone
+    m.copy_in_leaves(api.UHM_LHS, spec.mats, spec.elem_node.astype(np.int32))
+    assert m.status() == 0
+    s2, idx = _as_spec(spec, m)
+    eid, _, fs, ss = m.fronts()
+    got = np.zeros((s2.n_elements, 2), np.int64)
+    for e, a, b in zip(eid.tolist(), fs.tolist(), ss.tolist()):
+        got[idx[e]] = (a, b)
+    assert np.array_equal(got, uo.symbolic(s2).fs_ss())
+    x = uo.solve_mesh(s2, uo.LU_PIV).x
+    ref = uo.solve_mesh(spec, uo.LU_PIV).x
+    assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("bad", ["header", "node"])
+def test_import_rejects_bad_files(native_lib, tmp_path, bad):
+    spec = hpfem.poisson2d(2, 2, seed=11)
+    f = tmp_path / "bad.uhm"
+    _write_uhm(spec, f)
+    text = f.read_text()
+    if bad == "header":
+        text = text.replace("UHM", "XYZ", 1)
+    else:
+        text = text.rstrip("\n") + "\n1\n999999 0\n"
+        text = text.replace(f"\n{spec.n_leaves}\n", f"\n{spec.n_leaves + 1}\n", 1)
+    f.write_text(text)
+    m = api.Mesh()
+    with pytest.raises(api.UHMError):
+        m.import_file(str(f))
+    assert m.status() != 0
