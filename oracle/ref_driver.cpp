@@ -10,7 +10,16 @@
 // copy_in of every leaf matrix and right-hand side, set_rhs, factor, solve,
 // copy_out of the solution.
 //
-// usage: uhm_ref_driver IN OUT [n_threads]
+// usage: uhm_ref_driver IN OUT [n_threads] [sparse]
+//
+// With "sparse" the driver stops after copy_in and instead writes the
+// reference's own sparse export of the leaves (DSparse_(fort 0, cs 0,
+// n_rhs): import_element of every leaf in input order, then triplet with
+// is_sym = 0; UHM/src/interf/sparse.cxx:196-330):
+//     "UHMP" int32 version=1, int32 n_nodes; per node (input order) int32
+//     its first global dof (Node_::get_offset); int32 n_dof (triplet's),
+//     n_rhs, n_nz; int32 ia[n_nz], ja[n_nz]; float64 a[n_nz];
+//     int32 n_b; float64 b[n_b]
 //
 // IN  (little-endian): "UHMS" int32 version=1
 //     int32 n_nodes; per node int32 id, n_dof, p, kind
@@ -117,6 +126,37 @@ int main(int argc, char** argv) {
   }
   std::fclose(fin);
   m->set_rhs();
+
+  if (argc > 4 && !std::strcmp(argv[4], "sparse")) {
+    uhm::DSparse_ sp(0, 0, n_rhs);
+    for (int e = 0; e < n_leaves; ++e)
+      if (elem_m[e]) sp.import_element(elt[e]);
+    int sd = 0, sr = 0, snz = 0;
+    std::vector<int> ia, ja;
+    std::vector<double> a, b;
+    sp.triplet(0, sd, sr, snz, ia, ja, a, b);
+    FILE* fo = std::fopen(argv[2], "wb");
+    if (!fo) fail("cannot open output");
+    int hdr[2] = {1, n_nodes};
+    std::fwrite("UHMP", 1, 4, fo);
+    std::fwrite(hdr, 4, 2, fo);
+    for (int i = 0; i < n_nodes; ++i) {
+      int o = m->find_node(std::pair<int, int>(nid[i], 0))->get_offset();
+      std::fwrite(&o, 4, 1, fo);
+    }
+    int t[3] = {sd, sr, snz};
+    std::fwrite(t, 4, 3, fo);
+    std::fwrite(ia.data(), 4, ia.size(), fo);
+    std::fwrite(ja.data(), 4, ja.size(), fo);
+    std::fwrite(a.data(), 8, a.size(), fo);
+    int nb = (int)b.size();
+    std::fwrite(&nb, 4, 1, fo);
+    std::fwrite(b.data(), 8, b.size(), fo);
+    std::fclose(fo);
+    delete m;
+    FLA_Finalize();
+    return 0;
+  }
 
   double fd = 0, fs = 0, buf = 0;
   unsigned int nnz = 0;

@@ -87,3 +87,38 @@ def run(spec, method: int, threads: int = 1) -> RefResult:
         subprocess.run([DRIVER, fin, fout, str(threads)], check=True, env=env,
                        stdout=subprocess.DEVNULL)
         return read_result(fout, spec)
+
+
+def run_sparse(spec) -> dict:
+    """The reference's own sparse export of the spec's leaves (DSparse_ with
+    C numbering, row keys: import_element of every leaf in order, then
+    triplet without symmetry), with each node's first global dof in the
+    reference's numbering."""
+    if not available():
+        raise RuntimeError("reference solver not built (make -C oracle)")
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        write_spec(spec, 1, fin)
+        env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+        subprocess.run([DRIVER, fin, fout, "1", "sparse"], check=True, env=env, stdout=subprocess.DEVNULL)
+        buf = open(fout, "rb").read()
+    if buf[:4] != b"UHMP":
+        raise ValueError("bad reference sparse output")
+    p = 4
+    ver, n_nodes = np.frombuffer(buf, "<i4", 2, p)
+    p += 8
+    assert ver == 1 and n_nodes == spec.n_nodes
+    offsets = np.frombuffer(buf, "<i4", n_nodes, p).copy()
+    p += 4 * n_nodes
+    n_dof, n_rhs, nnz = (int(v) for v in np.frombuffer(buf, "<i4", 3, p))
+    p += 12
+    ia = np.frombuffer(buf, "<i4", nnz, p).copy()
+    p += 4 * nnz
+    ja = np.frombuffer(buf, "<i4", nnz, p).copy()
+    p += 4 * nnz
+    a = np.frombuffer(buf, "<f8", nnz, p).copy()
+    p += 8 * nnz
+    nb = int(np.frombuffer(buf, "<i4", 1, p)[0])
+    p += 4
+    b = np.frombuffer(buf, "<f8", nb, p).copy()
+    return dict(offsets=offsets, n_dof=n_dof, n_rhs=n_rhs, ia=ia, ja=ja, a=a, b=b)

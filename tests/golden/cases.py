@@ -35,6 +35,15 @@ CASES = [
                                      seed=10), CHOL),
 ]
 
+# meshes whose assembled operator the reference exports (DSparse_::triplet);
+# stored as sparse_<name>.npz
+SPARSE_CASES = [
+    ("2d_4x4_p2_rhs2", "poisson2d", dict(n=4, p=2, seed=21, n_rhs=2)),
+    ("cd_3_p2", "convdiff3d", dict(n=3, p=2, seed=22)),
+    ("varp_3_3d", "build_mesh", dict(dim=3, n=3, p=[int(v) for v in np.random.default_rng(23).integers(1, 5, 27)],
+                                     seed=23)),
+]
+
 
 def make_spec(gen, kwargs):
     kw = dict(kwargs)

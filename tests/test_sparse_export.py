@@ -122,3 +122,55 @@ def test_export_needs_element_matrices(native_lib):
     m = api.load_spec(spec, lhs=False)
     with pytest.raises(api.UHMError):
         m.export_sparse()
+
+
+# ---- pinned to the reference's own DSparse_ (tests/golden/sparse_*.npz) ----
+import importlib.util  # noqa: E402
+import os  # noqa: E402
+
+from oracle import ref_runner  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+_gs = importlib.util.spec_from_file_location("golden_cases_sparse", os.path.join(GOLDEN, "cases.py"))
+golden_cases = importlib.util.module_from_spec(_gs)
+_gs.loader.exec_module(golden_cases)
+SPARSE_CASES = golden_cases.SPARSE_CASES
+
+
+def _by_node_dof(offsets, spec, ia, ja, a):
+    """triplets keyed by ((node index, dof k), (node index, dof k)), whatever
+    the numbering that produced them"""
+    owner = {}
+    for i, (o, d) in enumerate(zip(offsets.tolist(), spec.node_ndof.tolist())):
+        for k in range(d):
+            owner[o + k] = (i, k)
+    return {(owner[int(r)], owner[int(c)]): v for r, c, v in zip(ia, ja, a)}, owner
+
+
+def _compare_with_reference(m, spec, ref):
+    s = m.export_sparse()
+    ours, our_owner = _by_node_dof(m.node_offsets(spec.node_id), spec, s["ia"], s["ja"], s["a"])
+    theirs, ref_owner = _by_node_dof(ref["offsets"], spec, ref["ia"], ref["ja"], ref["a"])
+    assert ours.keys() == theirs.keys()
+    assert all(ours[k] == theirs[k] for k in theirs)                 # bit for bit
+    n, nr = spec.n_dof(), spec.n_rhs
+    assert ref["n_dof"] == n - 1                                     # the reference's triplet: its last row index
+    rb = np.asarray(ref["b"]).reshape(nr, n).T                       # column-major over the reference's rows
+    ob = s["b"]
+    for g_ref, key in ref_owner.items():
+        g_our = [g for g, kk in our_owner.items() if kk == key][0]
+        assert np.array_equal(ob[g_our], rb[g_ref])
+
+
+@pytest.mark.parametrize("name,gen,kw", SPARSE_CASES, ids=[c[0] for c in SPARSE_CASES])
+def test_export_equals_reference_fixture(native_lib, name, gen, kw):
+    g = dict(np.load(os.path.join(GOLDEN, "sparse_" + name + ".npz")))
+    spec = golden_cases.make_spec(gen, kw)
+    assert golden_cases.spec_digest(spec) == str(g["digest"]), "mesh generator changed: regenerate fixtures"
+    _compare_with_reference(api.load_spec(spec), spec, g)
+
+
+@pytest.mark.skipif(not ref_runner.available(), reason="reference solver not built here (make -C oracle)")
+def test_export_equals_live_reference(native_lib):
+    spec = hpfem.diffusion3d(3, 3, seed=24, contrast=1e3, n_rhs=2)
+    _compare_with_reference(api.load_spec(spec), spec, ref_runner.run_sparse(spec))
