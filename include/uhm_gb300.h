@@ -149,7 +149,7 @@ int uhm_gpu_get_children(long* mesh, int elt_id, int cap, int* child_id, int* n)
  * ja columns) or columns (cs = 1: ja pointers, ia rows) (DSparse_::compress).
  * is_sym keeps the entries whose key has second >= first; fort adds 1 to
  * every index and pointer.  b is the assembled right-hand sides, column-major
- * (n_dof x n_rhs).  Call once with ia, ja, a, b NULL for the lengths
+ * (n_dof x n_rhs); n_rhs = 0 and no b when some leaf has none copied in.  Call once with ia, ja, a, b NULL for the lengths
  * (len_ia, len_ja, n_nz), then with arrays of those lengths.  n_dof is the
  * number of dofs (the reference's triplet reports its last index instead). */
 int uhm_gpu_export_sparse(long* mesh, int is_sym, int fort, int cs, int compress, int axpy, int* n_dof,

@@ -124,6 +124,28 @@ def test_export_needs_element_matrices(native_lib):
         m.export_sparse()
 
 
+def test_export_without_right_hand_sides(native_lib):
+    spec = hpfem.poisson2d(3, 2, seed=87)
+    m = api.Mesh()
+    nods = {nid: m.add_node(nid, nd, p)
+            for nid, nd, p in zip(spec.node_id.tolist(), spec.node_ndof.tolist(), spec.node_p.tolist())}
+    elts = [m.add_element(int(g)) for g in spec.generation.tolist()]
+    for e in range(spec.n_leaves):
+        for nid in spec.element_nodes(e).tolist():
+            m.element_add_node(elts[e], nods[nid])
+    for e in range(spec.n_elements):
+        for c in spec.children(e).tolist():
+            m.set_parent(elts[c], elts[e])
+            m.add_child(elts[e], elts[c])
+    m.lock()
+    m.create_matrix_without_buffer(api.UHM_REAL, 1)
+    m.copy_in_leaves(api.UHM_LHS, spec.mats, spec.elem_node.astype(np.int32))
+    s = m.export_sparse()
+    full = api.load_spec(spec).export_sparse()
+    assert s["n_rhs"] == 0 and s["b"].size == 0
+    assert np.array_equal(s["ia"], full["ia"]) and np.array_equal(s["a"], full["a"])
+
+
 # ---- pinned to the reference's own DSparse_ (tests/golden/sparse_*.npz) ----
 import importlib.util  # noqa: E402
 import os  # noqa: E402

@@ -24,15 +24,20 @@ static void ck(cudaError_t e, const char* what) {
 
 void Engine::export_sparse(int is_sym, int fort, int cs, int compress, int axpy, SparseOut& out) {
   ensure_plan();
-  for (auto& es : esrc)
-    if (!es.has_lhs || !es.has_rhs) fail("export_sparse: element matrices and right-hand sides must be copied in", 7);
+  // the operator needs every element matrix; the right-hand sides are
+  // exported when every leaf has one (the reference takes what is there)
+  bool with_rhs = true;
+  for (auto& es : esrc) {
+    if (!es.has_lhs) fail("export_sparse: an element matrix has not been copied in", 7);
+    with_rhs = with_rhs && es.has_rhs;
+  }
   if (dev_ok && emat_device_only) {
     ck(cudaStreamSynchronize(stream), "export_sparse: sync");
     ck(cudaMemcpy(h_pinned, ctx.emat, sizeof(double) * (size_t)emat_total, cudaMemcpyDeviceToHost),
        "export_sparse: element matrices");
     emat_device_only = false;
   }
-  if (dev_ok && erhs_device_only) {
+  if (with_rhs && dev_ok && erhs_device_only) {
     ck(cudaStreamSynchronize(stream), "export_sparse: sync");
     ck(cudaMemcpy(h_pinned + emat_total, d_erhs, sizeof(double) * (size_t)erhs_total, cudaMemcpyDeviceToHost),
        "export_sparse: right-hand sides");
@@ -80,14 +85,14 @@ void Engine::export_sparse(int is_sym, int fort, int cs, int compress, int axpy,
         ea.push_back(cs ? Entry{c, r, A[i + (int64_t)j * es.m]} : Entry{r, c, A[i + (int64_t)j * es.m]});
       }
     // right-hand sides keyed (rhs column, row): a column-major vector
-    for (int q = 0; q < nr; ++q)
+    for (int q = 0; q < (with_rhs ? nr : 0); ++q)
       for (int i = 0; i < es.m; ++i) eb.push_back(Entry{q + shift, es.gdof[i] + shift, B[i + (int64_t)q * es.m]});
   }
   std::vector<Entry> a = reduce(ea), b = reduce(eb);
   ea.clear();
   ea.shrink_to_fit();
   out = SparseOut{};
-  out.n_rhs = nr;
+  out.n_rhs = with_rhs ? nr : 0;
   // sparse.cxx:269-330 (triplet) and 332-460 (compress)
   int prev = a.empty() ? 0 : a.front().k0;
   int cnt = shift;
