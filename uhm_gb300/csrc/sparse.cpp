@@ -116,8 +116,8 @@ void Engine::export_sparse(int is_sym, int fort, int cs, int compress, int axpy,
     out.a.push_back(e.v);
   }
   if (compress) {
-    out.n_dof = (int)ptr.size();
-    ptr.push_back(cnt);
+    out.n_dof = out.a.empty() ? 0 : (int)ptr.size();
+    if (!out.a.empty()) ptr.push_back(cnt);
   } else {
     out.n_dof = (int)n_global;
   }
