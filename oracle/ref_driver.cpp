@@ -32,7 +32,7 @@
 //     int32 n_nodes, n_rhs; per node (input order) float64 x[n_dof*n_rhs]
 //     (node-major, rhs-minor); int32 n_elements; per element (input order)
 //     int32 n_factor, n_schur; float64 t_factor, t_solve (seconds),
-//     flop_decompose, flop_solve
+//     flop_decompose, flop_solve, t_lock (seconds, the symbolic phase)
 #include "uhm.hxx"
 
 #include <cstdio>
@@ -109,7 +109,9 @@ int main(int argc, char** argv) {
       elt[cidx[k]]->set_parent(elt[e]);
     }
 
+  const double tl0 = now();
   m->lock();
+  const double t_lock = now() - tl0;
   m->create_matrix_without_buffer(UHM_REAL, n_rhs);
 
   std::vector<int> elem_m(n_leaves);
@@ -208,8 +210,8 @@ int main(int argc, char** argv) {
     int v[2] = {nd.first, nd.second};
     std::fwrite(v, 4, 2, fo);
   }
-  double tail[4] = {t1 - t0, t2 - t1, fd, fs};
-  std::fwrite(tail, 8, 4, fo);
+  double tail[5] = {t1 - t0, t2 - t1, fd, fs, t_lock};
+  std::fwrite(tail, 8, 5, fo);
   std::fclose(fo);
   delete m;
   FLA_Finalize();

@@ -27,6 +27,7 @@ class RefResult:
     t_solve: float
     flop_decompose: float
     flop_solve: float
+    t_lock: float = float("nan")   # the symbolic phase (Mesh_::lock), seconds
 
 
 def available() -> bool:
@@ -74,7 +75,9 @@ def read_result(path: str, spec) -> RefResult:
     fronts = np.frombuffer(buf, "<i4", 2 * n_el, p).reshape(n_el, 2).astype(np.int64)
     p += 8 * n_el
     tf, ts, fd, fs = np.frombuffer(buf, "<f8", 4, p)
-    return RefResult(x, fronts, float(tf), float(ts), float(fd), float(fs))
+    p += 32
+    tl = float(np.frombuffer(buf, "<f8", 1, p)[0]) if len(buf) >= p + 8 else float("nan")
+    return RefResult(x, fronts, float(tf), float(ts), float(fd), float(fs), tl)
 
 
 def run(spec, method: int, threads: int = 1) -> RefResult:
