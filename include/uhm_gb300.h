@@ -49,62 +49,92 @@ extern "C" {
 #endif
 
 /* ---- Part 1: reference interface (fort.hxx) ---------------------------- */
-/* fort.hxx:51-52 */ void uhm_initialize_fla_(void);
+/* fort.hxx:51    */ void uhm_initialize_fla_(void);
 /* fort.hxx:52    */ void uhm_finalize_fla_(void);
-/* fort.hxx:54-55 */ void uhm_set_num_threads_(int* n_threads);
+/* fort.hxx:54    */ void uhm_set_num_threads_(int* n_threads);
 /* fort.hxx:55    */ void uhm_get_num_threads_(int* n_threads);
-/* fort.hxx:57-58 */ void uhm_set_hier_block_size_(int* size);
+/* fort.hxx:57    */ void uhm_set_hier_block_size_(int* size);
 /* fort.hxx:58    */ void uhm_get_hier_block_size_(int* size);
-/* fort.hxx:67-68 */ void uhm_reset_flop_(void);
+/* fort.hxx:60-65: thresholds of SVD fronts (the reference declares them
+ * without defining them); kept and returned, used by nothing here */
+/* fort.hxx:60    */ void set_svd_relative_threshold_(double* val);
+/* fort.hxx:61    */ void set_svd_absolute_threshold_(double* val);
+/* fort.hxx:62    */ void get_svd_relative_threshold_(double* val);
+/* fort.hxx:63    */ void get_svd_absolute_threshold_(double* val);
+/* fort.hxx:64    */ void set_svd_cutoff_small_(int* flag);
+/* fort.hxx:65    */ void get_svd_cutoff_small_(int* flag);
+/* fort.hxx:67    */ void uhm_reset_flop_(void);
 /* fort.hxx:68    */ void uhm_get_flop_(double* flop);
 /* fort.hxx:69    */ void uhm_get_buffer_used_(double* buffer);
 /* fort.hxx:70    */ void uhm_get_max_buffer_used_(double* buffer);
-/* fort.hxx:71    */ void uhm_is_multithreading_enable_(int* flag);
-/* fort.hxx:72    */ void uhm_is_hier_matrix_enable_(int* flag);
-/* fort.hxx:73    */ void uhm_timer_(double* t);
+/* fort.hxx:72    */ void uhm_is_multithreading_enable_(int* flag);
+/* fort.hxx:73    */ void uhm_is_hier_matrix_enable_(int* flag);
+/* fort.hxx:75    */ void uhm_timer_(double* t);
 
-/* fort.hxx:77-78 */ void uhm_mesh_create_(long* mesh);
-/* fort.hxx:78    */ void uhm_mesh_delete_(long* mesh);
-/* fort.hxx:79-80 */ void uhm_add_element_(long* mesh, long* elt);
-/* fort.hxx:81-86 */ void uhm_add_node_(long* mesh, int* id, int* phy, int* n_dof, int* p, long* nod);
-/* fort.hxx:87-88 */ void uhm_element_add_node_(long* elt, long* nod);
-/* fort.hxx:89-97 */ void uhm_copy_in_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
+/* fort.hxx:79    */ void uhm_mesh_create_(long* mesh);
+/* fort.hxx:80    */ void uhm_mesh_delete_(long* mesh);
+/* fort.hxx:82-83 */ void uhm_add_element_(long* mesh, long* elt);
+/* fort.hxx:85-90 */ void uhm_add_node_(long* mesh, int* id, int* phy, int* n_dof, int* p, long* nod);
+/* fort.hxx:92-93 */ void uhm_element_add_node_(long* elt, long* nod);
+/* fort.hxx:95-103*/ void uhm_copy_in_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
                                        int* node_disp, int* nods, int* side, double* buffer);
-/* fort.hxx:98-106*/ void uhm_copy_out_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
+/* fort.hxx:105-113*/ void uhm_copy_out_(long* mesh, long* elt, int* datatype, int* mm, int* nn,
                                         int* node_disp, int* nods, int* side, double* buffer);
-/* fort.hxx:107   */ void uhm_mesh_disp_(long* mesh);
-/* fort.hxx:108-109*/ void uhm_get_n_dof_(long* mesh, int* n_dof);
-/* fort.hxx:110-111*/ void uhm_get_n_nonzero_(long* mesh, int* n_nonzero);
-/* fort.hxx:112-119*/ void uhm_estimate_cost_(long* mesh, int* method, int* datatype, int* n_rhs,
+/* fort.hxx:115   */ void uhm_mesh_disp_(long* mesh);
+/* fort.hxx:117-118*/ void uhm_get_n_dof_(long* mesh, int* n_dof);
+/* fort.hxx:120-121*/ void uhm_get_n_nonzero_(long* mesh, int* n_nonzero);
+/* fort.hxx:124-131*/ void uhm_estimate_cost_(long* mesh, int* method, int* datatype, int* n_rhs,
                                              double* flop_decompose, double* flop_solve,
                                              unsigned* n_nonzero_factor, double* buffer);
-/* fort.hxx:120-121*/ void uhm_mesh_import_(long* mesh, char* filename);
-/* fort.hxx:122: the reference partitions with METIS (build_tree.cxx:52-54,
+/* fort.hxx:133-134*/ void uhm_mesh_import_(long* mesh, char* filename);
+/* fort.hxx:136: the reference partitions with METIS (build_tree.cxx:52-54,
  * build_tree_var4.cxx); here the heavy-edge matching of its
  * build_tree_var1.cxx:53-181 over the elements without a parent (ties by
  * element and node id; one tree per connected part; new elements that would
  * eliminate nothing are left out) */
-/* fort.hxx:122   */ void uhm_build_tree_(long* mesh);
-/* fort.hxx:123-125*/ void uhm_create_matrix_without_buffer_(long* mesh, int* datatype, int* n_rhs);
-/* fort.hxx:126   */ void uhm_create_leaf_matrix_buffer_(long* mesh);
-/* fort.hxx:127-128*/ void uhm_create_element_matrix_buffer_(long* mesh, int* is_schur);
-/* fort.hxx:129   */ void uhm_set_rhs_(long* mesh);
-/* fort.hxx:133   */ void uhm_lock_(long* mesh);
-/* fort.hxx:134   */ void uhm_unlock_(long* mesh);
+/* fort.hxx:136   */ void uhm_build_tree_(long* mesh);
+/* fort.hxx:138-140*/ void uhm_create_matrix_without_buffer_(long* mesh, int* datatype, int* n_rhs);
+/* fort.hxx:142   */ void uhm_create_leaf_matrix_buffer_(long* mesh);
+/* fort.hxx:143-144*/ void uhm_create_element_matrix_buffer_(long* mesh, int* is_schur);
+/* fort.hxx:146   */ void uhm_set_rhs_(long* mesh);
+/* fort.hxx:148-150: pseudo-random leaf matrices and right-hand sides for
+ * benchmarks (the reference uses libflame's generator, whose values are not
+ * reproduced: see uhm_gb300/csrc/fill.cpp); triangularize is a no-op, every
+ * Cholesky kernel here reading lower triangles only */
+/* fort.hxx:148   */ void uhm_random_spd_matrix_(long* mesh);
+/* fort.hxx:149   */ void uhm_random_matrix_(long* mesh);
+/* fort.hxx:150   */ void uhm_triangularize_(long* mesh);
+/* fort.hxx:152   */ void uhm_lock_(long* mesh);
+/* fort.hxx:153   */ void uhm_unlock_(long* mesh);
 
-/* fort.hxx:137-142 decomposition */
+/* fort.hxx:158-163 decomposition */
 void uhm_chol_with_free_(long* mesh);
 void uhm_lu_nopiv_with_free_(long* mesh);
 void uhm_lu_piv_with_free_(long* mesh);
-/* fort.hxx:145-150 solution */
+/* fort.hxx:168-173 solution */
 void uhm_solve_chol_(long* mesh);
 void uhm_solve_lu_nopiv_(long* mesh);
 void uhm_solve_lu_piv_(long* mesh);
-/* fort.hxx:153-158 checking (computes the residual on the element matrices) */
+/* fort.hxx:178-183 checking (computes the residual on the element matrices) */
 void uhm_check_chol_(long* mesh);
 void uhm_check_lu_nopiv_(long* mesh);
 void uhm_check_lu_piv_(long* mesh);
-/* fort.hxx:161-162 residual: ||b - A x||_1 on the unassembled operator */
+/* fort.hxx:161,171,181: lu_incpiv factors the fronts with partial pivoting
+ * over their eliminated rows, exactly as lu_piv (the reference pivots within
+ * each diagonal block; solutions agree to rounding) and is solved by
+ * uhm_solve_lu_piv_ or uhm_solve_lu_incpiv_ (the same call).
+ * fort.hxx:162-163,172-173,182-183: QR and SVD fronts are not provided:
+ * status 30. */
+void uhm_lu_incpiv_with_free_(long* mesh);
+void uhm_solve_lu_incpiv_(long* mesh);
+void uhm_check_lu_incpiv_(long* mesh);
+void uhm_qr_with_free_(long* mesh);
+void uhm_solve_qr_(long* mesh);
+void uhm_check_qr_(long* mesh);
+void uhm_svd_with_free_(long* mesh);
+void uhm_solve_svd_(long* mesh);
+void uhm_check_svd_(long* mesh);
+/* fort.hxx:188-189 residual: ||b - A x||_1 on the unassembled operator */
 void uhm_get_residual_(long* mesh, double* res);
 
 /* ---- Part 2: device-path additions (no counterpart in fort.hxx) ------- */

@@ -23,7 +23,9 @@
 //
 // IN  (little-endian): "UHMS" int32 version=1
 //     int32 n_nodes; per node int32 id, n_dof, p, kind
-//     int32 n_elements, n_leaves, n_rhs, method (1 chol, 2 lu_nopiv, 3 lu_piv)
+//     int32 n_elements, n_leaves, n_rhs, method (1 chol, 2 lu_nopiv, 3 lu_piv,
+//     4 lu_incpiv: factored by lu_incpiv_with_free, solved by solve_lu_piv as
+//     the reference's Fortran flow does)
 //     int32 generation[n_elements]; int32 child_ptr[n_elements+1];
 //     int32 child_idx[child_ptr[n_elements]] (children in add_child order)
 //     int32 elem_ptr[n_leaves+1]; int32 elem_node[elem_ptr[n_leaves]]
@@ -168,6 +170,7 @@ int main(int argc, char** argv) {
   if (method == 1) m->chol_with_free();
   else if (method == 2) m->lu_nopiv_with_free();
   else if (method == 3) m->lu_piv_with_free();
+  else if (method == 4) m->lu_incpiv_with_free();
   else fail("unknown method");
   const double t1 = now();
   if (method == 1) m->solve_chol();

@@ -5,8 +5,9 @@ function of ``uhm_gb300.hpfem``; ``make_golden.py`` runs the reference solver
 (built by ``oracle/Makefile``) on the mesh and stores its solution, its front
 sizes and its LAWN-41 flop estimates in ``<name>.npz`` beside a digest of the
 mesh's inputs, so a change of the generator is caught instead of compared.
-Methods: 1 Cholesky, 2 LU without pivoting, 3 LU with partial pivoting
-(UHM/include/uhm/const.hxx:76).
+Methods: 1 Cholesky, 2 LU without pivoting, 3 LU with partial pivoting, 4 LU
+with incremental pivoting (UHM/include/uhm/const.hxx:76; solved by
+solve_lu_piv, as the reference's Fortran flow does).
 """
 import hashlib
 
@@ -14,7 +15,7 @@ import numpy as np
 
 from uhm_gb300 import hpfem
 
-CHOL, LU_NOPIV, LU_PIV = 1, 2, 3
+CHOL, LU_NOPIV, LU_PIV, LU_INCPIV = 1, 2, 3, 4
 
 CASES = [
     ("2d_4x4_p2", "poisson2d", dict(n=4, p=2, seed=1), CHOL),
@@ -31,6 +32,7 @@ CASES = [
     ("cd_4_p3_lupiv", "convdiff3d", dict(n=4, p=3, seed=6), LU_PIV),
     ("cd_6_p3_lupiv_merge32", "convdiff3d", dict(n=6, p=3, seed=7, merges=[3, 2]), LU_PIV),
     ("cd_4_p2_lunopiv", "convdiff3d", dict(n=4, p=2, seed=8, pe=1.0), LU_NOPIV),
+    ("cd_4_p3_lu_incpiv", "convdiff3d", dict(n=4, p=3, seed=12), LU_INCPIV),
     ("varp_4_3d", "build_mesh", dict(dim=3, n=4, p=[int(v) for v in np.random.default_rng(3).integers(2, 6, 64)],
                                      seed=10), CHOL),
 ]

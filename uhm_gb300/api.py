@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libuhm_gb300.so")
 UHM_REAL, UHM_COMPLEX = 101, 103
 UHM_LHS, UHM_RHS = 1, 2
 UHM_PHYSICS_SINGLE, UHM_PHYSICS_MULTI = 1, 2
-UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV = 1, 2, 3
+UHM_CHOL, UHM_LU_NOPIV, UHM_LU_PIV, UHM_LU_INCPIV = 1, 2, 3, 4
 PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16X6, PREC_LEARNED = 0, 1, 2, 3, 4
 STATUS_RECOMPUTED_FP64 = 20     # refinement missed; the solution was recomputed in FP64
 
@@ -309,6 +309,21 @@ class Mesh:
     def lu_nopiv_with_free(self):
         self._call("lu_nopiv_with_free")
 
+    def lu_incpiv_with_free(self):
+        self._call("lu_incpiv_with_free")
+
+    def qr_with_free(self):
+        self._call("qr_with_free")
+
+    def random_spd_matrix(self):
+        self._call("random_spd_matrix")
+
+    def random_matrix(self):
+        self._call("random_matrix")
+
+    def triangularize(self):
+        self._call("triangularize")
+
     def solve_chol(self):
         self._call("solve_chol")
 
@@ -320,11 +335,12 @@ class Mesh:
 
     def factor(self, method):
         {UHM_CHOL: self.chol_with_free, UHM_LU_PIV: self.lu_piv_with_free,
-         UHM_LU_NOPIV: self.lu_nopiv_with_free}[method]()
+         UHM_LU_NOPIV: self.lu_nopiv_with_free, UHM_LU_INCPIV: self.lu_incpiv_with_free}[method]()
 
     def solve(self, method):
+        # an lu_incpiv factorisation is solved by solve_lu_piv, as in the reference
         {UHM_CHOL: self.solve_chol, UHM_LU_PIV: self.solve_lu_piv,
-         UHM_LU_NOPIV: self.solve_lu_nopiv}[method]()
+         UHM_LU_NOPIV: self.solve_lu_nopiv, UHM_LU_INCPIV: self.solve_lu_piv}[method]()
 
     def get_residual(self) -> float:
         r = _d(0)

@@ -21,6 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "mesh.cpp",
     "sparse.cpp",
+    "fill.cpp",
     "capi.cpp",
     "engine.cu",
     "k_factor.cu",

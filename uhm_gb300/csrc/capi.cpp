@@ -157,6 +157,43 @@ void uhm_solve_lu_piv_(long* mesh) {
 void uhm_check_chol_(long* mesh) { M(mesh)->check_chol(); }
 void uhm_check_lu_nopiv_(long* mesh) { M(mesh)->check_lu_nopiv(); }
 void uhm_check_lu_piv_(long* mesh) { M(mesh)->check_lu_piv(); }
+void uhm_lu_incpiv_with_free_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->lu_incpiv_with_free(); account_flops(M(mesh), uhm::UHM_LU_PIV, true); });
+}
+void uhm_solve_lu_incpiv_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->solve_lu_piv(); account_flops(M(mesh), uhm::UHM_LU_PIV, false); });
+}
+void uhm_check_lu_incpiv_(long* mesh) { M(mesh)->check_lu_piv(); }
+void uhm_random_spd_matrix_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->random_spd_matrix(); });
+}
+void uhm_random_matrix_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->random_matrix(); });
+}
+void uhm_triangularize_(long* mesh) { M(mesh)->triangularize(); }
+void uhm_svd_with_free_(long* mesh) {
+  set_err(M(mesh), "SVD fronts are not provided by this library", 30);
+}
+void uhm_solve_svd_(long* mesh) { set_err(M(mesh), "SVD fronts are not provided by this library", 30); }
+void uhm_check_svd_(long* mesh) { set_err(M(mesh), "SVD fronts are not provided by this library", 30); }
+// thresholds of the SVD fronts: kept and returned, used by nothing here
+static double g_svd_rel = 0.0, g_svd_abs = 0.0;
+static int g_svd_cutoff = 0;
+void set_svd_relative_threshold_(double* val) { g_svd_rel = *val; }
+void set_svd_absolute_threshold_(double* val) { g_svd_abs = *val; }
+void get_svd_relative_threshold_(double* val) { *val = g_svd_rel; }
+void get_svd_absolute_threshold_(double* val) { *val = g_svd_abs; }
+void set_svd_cutoff_small_(int* flag) { g_svd_cutoff = *flag; }
+void get_svd_cutoff_small_(int* flag) { *flag = g_svd_cutoff; }
+void uhm_qr_with_free_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->qr_with_free(); });
+}
+void uhm_solve_qr_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->solve_qr(); });
+}
+void uhm_check_qr_(long* mesh) {
+  guard(M(mesh), [&] { M(mesh)->check_qr(); });
+}
 void uhm_get_residual_(long* mesh, double* res) {
   guard(M(mesh), [&] { *res = M(mesh)->get_residual(); });
 }

@@ -132,6 +132,11 @@ class Engine {
     std::vector<double> a, b;
   };
   void export_sparse(int is_sym, int fort, int cs, int compress, int axpy, SparseOut& out);
+  // Mesh_::random_spd_matrix / random_matrix (UHM/src/mesh/matrix.cxx:
+  // 155-170,295-310): every leaf gets a pseudo-random element matrix and
+  // right-hand sides (fill.cpp)
+  void random_elements(int spd);
+  uint64_t random_calls = 0;
   void node_solution(int n_nodes, const int* ids, double* out, int64_t n_values);
 
   // --- numerics -----------------------------------------------------------

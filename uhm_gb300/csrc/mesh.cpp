@@ -552,6 +552,18 @@ void Mesh_::solve_lu_piv_1() { run_solve(UHM_LU_PIV, 1); }
 void Mesh_::solve_lu_piv_2() { run_solve(UHM_LU_PIV, 2); }
 void Mesh_::solve_lu_piv() { run_solve(UHM_LU_PIV, 3); }
 void Mesh_::check_lu_piv() {}
+void Mesh_::lu_incpiv_with_free() { run_factor(UHM_LU_PIV, 0); }
+void Mesh_::lu_incpiv_without_free() { run_factor(UHM_LU_PIV, 1); }
+void Mesh_::random_spd_matrix() { eng().random_elements(1); }
+void Mesh_::random_matrix() { eng().random_elements(0); }
+void Mesh_::triangularize() {}
+static void no_qr() { throw std::invalid_argument("QR fronts are not provided by this library"); }
+void Mesh_::qr_with_free() { no_qr(); }
+void Mesh_::qr_without_free() { no_qr(); }
+void Mesh_::solve_qr_1() { no_qr(); }
+void Mesh_::solve_qr_2() { no_qr(); }
+void Mesh_::solve_qr() { no_qr(); }
+void Mesh_::check_qr() { no_qr(); }
 
 // The reference returns sum over fronts of ||rt||_1 of its factor-based
 // check (UHM/src/matrix/uhm/fla/matrix.cxx:222-234); here: ||b - A x||_1 of

@@ -197,6 +197,27 @@ class Mesh_ {
   void solve_lu_piv_2();
   void solve_lu_piv();
   void check_lu_piv();
+  // mesh.hxx:257-259: the reference pivots within each diagonal block
+  // (LINAL/src/dense/lu_incpiv.cxx); here the fronts are factored with
+  // partial pivoting over their eliminated rows, as lu_piv does, and solved
+  // by solve_lu_piv (the reference's Fortran flow solves an lu_incpiv
+  // factorisation with solve_lu_piv too).  Solutions agree to rounding.
+  void lu_incpiv_with_free();
+  void lu_incpiv_without_free();
+  // matrix.cxx:155-170,295-310: pseudo-random leaf matrices and right-hand
+  // sides (values differ from the reference's libflame generator; see
+  // fill.cpp); triangularize is a no-op here, as every Cholesky kernel reads
+  // only lower triangles and the element matrices stay whole for the residual
+  void random_spd_matrix();
+  void random_matrix();
+  void triangularize();
+  // mesh.hxx:280-292: QR fronts are not provided; these record status 30
+  void qr_with_free();
+  void qr_without_free();
+  void solve_qr_1();
+  void solve_qr_2();
+  void solve_qr();
+  void check_qr();
 
   double get_residual();
   unsigned get_n_dof();
