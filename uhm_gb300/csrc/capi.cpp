@@ -3,7 +3,6 @@
 #include "../../include/uhm_gb300.h"
 
 #include <omp.h>
-#include <sys/time.h>
 
 #include <cstdio>
 #include <cstring>
@@ -21,7 +20,6 @@ using uhm::Mesh;
 using uhm::Node;
 
 namespace {
-int g_hier_block = 256;          // UHM/src/matrix/uhm/matrix.cxx:39-42 default
 double g_flop = 0.0;
 double g_buffer = 0.0, g_buffer_max = 0.0;
 thread_local std::string g_err;  // errors raised before a mesh exists
@@ -64,21 +62,17 @@ extern "C" {
 
 void uhm_initialize_fla_(void) {}
 void uhm_finalize_fla_(void) {}
-void uhm_set_num_threads_(int* n) { if (n && *n > 0) omp_set_num_threads(*n); }
-void uhm_get_num_threads_(int* n) { *n = omp_get_max_threads(); }
-void uhm_set_hier_block_size_(int* s) { if (s && *s > 0) g_hier_block = *s; }
-void uhm_get_hier_block_size_(int* s) { *s = g_hier_block; }
+void uhm_set_num_threads_(int* n) { if (n) uhm::set_num_threads(*n); }
+void uhm_get_num_threads_(int* n) { *n = uhm::get_num_threads(); }
+void uhm_set_hier_block_size_(int* s) { if (s) uhm::set_hier_block_size(*s); }
+void uhm_get_hier_block_size_(int* s) { *s = uhm::get_hier_block_size(); }
 void uhm_reset_flop_(void) { g_flop = 0.0; }
 void uhm_get_flop_(double* f) { *f = g_flop; }
 void uhm_get_buffer_used_(double* b) { *b = g_buffer; }
 void uhm_get_max_buffer_used_(double* b) { *b = g_buffer_max; }
 void uhm_is_multithreading_enable_(int* f) { *f = 1; }
 void uhm_is_hier_matrix_enable_(int* f) { *f = 1; }
-void uhm_timer_(double* t) {
-  timeval tv;
-  gettimeofday(&tv, nullptr);
-  *t = tv.tv_sec + tv.tv_usec * 1e-6;
-}
+void uhm_timer_(double* t) { *t = uhm::timer(); }
 
 void uhm_mesh_create_(long* mesh) { *mesh = reinterpret_cast<long>(new uhm::Mesh_()); }
 void uhm_mesh_delete_(long* mesh) {

@@ -5,7 +5,10 @@
 // The numerical methods delegate to the device engine (engine.hpp).
 #include "mesh.hpp"
 
+#include <omp.h>
+
 #include <algorithm>
+#include <chrono>
 #include <cassert>
 #include <cstdio>
 #include <cstdlib>
@@ -408,6 +411,30 @@ int Mesh_::build_tree() {
   return roots;
 }
 
+// ---------------------------------------------------------------------------
+// free functions (util.hxx:44-60, matrix.hxx:40-41, operation/mesh.hxx:48)
+// ---------------------------------------------------------------------------
+static int g_hier_block_size = 256;   // the reference's default (UHM/src/matrix/uhm/matrix.cxx:39-42)
+
+double timer() {
+  return std::chrono::duration<double>(std::chrono::system_clock::now().time_since_epoch()).count();
+}
+bool is_hier_matrix_enable() { return true; }
+bool is_multithreading_enable() { return true; }
+void set_num_threads(int nt) {
+  if (nt > 0) omp_set_num_threads(nt);
+}
+int get_num_threads() { return omp_get_max_threads(); }
+void set_hier_block_size(int size) {
+  if (size > 0) g_hier_block_size = size;
+}
+int get_hier_block_size() { return g_hier_block_size; }
+bool build_tree(Mesh m) {
+  if (!m) return false;
+  m->build_tree();
+  return true;
+}
+
 // .uhm text format of Mesh_::import_file (UHM/src/mesh/mesh.cxx:511-579)
 bool Mesh_::import_file(const char* path) {
   reset();
@@ -564,6 +591,36 @@ void Mesh_::solve_qr_1() { no_qr(); }
 void Mesh_::solve_qr_2() { no_qr(); }
 void Mesh_::solve_qr() { no_qr(); }
 void Mesh_::check_qr() { no_qr(); }
+void Mesh_::qr_with_ooc() { no_qr(); }
+void Mesh_::check_qr_1() { no_qr(); }
+void Mesh_::check_qr_2() { no_qr(); }
+void Mesh_::improve_qr() {}
+void Mesh_::chol_with_ooc() { run_factor(UHM_CHOL, 0); }
+void Mesh_::solve_chol_1_ooc() { run_solve(UHM_CHOL, 1); }
+void Mesh_::solve_chol_2_ooc() { run_solve(UHM_CHOL, 2); }
+void Mesh_::solve_chol_ooc() { run_solve(UHM_CHOL, 3); }
+void Mesh_::check_chol_1() {}
+void Mesh_::check_chol_2() {}
+void Mesh_::improve_chol() {}
+void Mesh_::lu_nopiv_with_ooc() { run_factor(UHM_LU_NOPIV, 0); }
+void Mesh_::solve_lu_nopiv_1_ooc() { run_solve(UHM_LU_NOPIV, 1); }
+void Mesh_::solve_lu_nopiv_2_ooc() { run_solve(UHM_LU_NOPIV, 2); }
+void Mesh_::solve_lu_nopiv_ooc() { run_solve(UHM_LU_NOPIV, 3); }
+void Mesh_::check_lu_nopiv_1() {}
+void Mesh_::check_lu_nopiv_2() {}
+void Mesh_::improve_lu_nopiv() {}
+void Mesh_::lu_piv_with_ooc() { run_factor(UHM_LU_PIV, 0); }
+void Mesh_::lu_incpiv_with_ooc() { run_factor(UHM_LU_PIV, 0); }
+void Mesh_::solve_lu_piv_1_ooc() { run_solve(UHM_LU_PIV, 1); }
+void Mesh_::solve_lu_piv_2_ooc() { run_solve(UHM_LU_PIV, 2); }
+void Mesh_::solve_lu_piv_ooc() { run_solve(UHM_LU_PIV, 3); }
+void Mesh_::check_lu_piv_1() {}
+void Mesh_::check_lu_piv_2() {}
+void Mesh_::check_lu_piv_1_ooc() {}
+void Mesh_::check_lu_piv_2_ooc() {}
+void Mesh_::check_lu_piv_ooc() {}
+void Mesh_::improve_lu_piv() {}
+void Mesh_::improve_lu_piv_ooc() {}
 
 // The reference returns sum over fronts of ||rt||_1 of its factor-based
 // check (UHM/src/matrix/uhm/fla/matrix.cxx:222-234); here: ||b - A x||_1 of

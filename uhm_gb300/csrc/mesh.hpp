@@ -211,6 +211,37 @@ class Mesh_ {
   void random_spd_matrix();
   void random_matrix();
   void triangularize();
+  // Out-of-core variants (mesh.hxx:208-275): every front lives in device
+  // memory, so these run the in-core factorisation and solves.  check_*_1/2
+  // do nothing, as check_* (the residual is get_residual).  improve_* do
+  // nothing, as in the reference's multithreaded build, whose bodies are
+  // empty (UHM/src/mesh/chol.cxx:136-150, lu_piv.cxx:232-246).
+  void chol_with_ooc();
+  void solve_chol_1_ooc();
+  void solve_chol_2_ooc();
+  void solve_chol_ooc();
+  void check_chol_1();
+  void check_chol_2();
+  void improve_chol();
+  void lu_nopiv_with_ooc();
+  void solve_lu_nopiv_1_ooc();
+  void solve_lu_nopiv_2_ooc();
+  void solve_lu_nopiv_ooc();
+  void check_lu_nopiv_1();
+  void check_lu_nopiv_2();
+  void improve_lu_nopiv();
+  void lu_piv_with_ooc();
+  void lu_incpiv_with_ooc();
+  void solve_lu_piv_1_ooc();
+  void solve_lu_piv_2_ooc();
+  void solve_lu_piv_ooc();
+  void check_lu_piv_1();
+  void check_lu_piv_2();
+  void check_lu_piv_1_ooc();
+  void check_lu_piv_2_ooc();
+  void check_lu_piv_ooc();
+  void improve_lu_piv();
+  void improve_lu_piv_ooc();
   // mesh.hxx:280-292: QR fronts are not provided; these record status 30
   void qr_with_free();
   void qr_without_free();
@@ -218,6 +249,10 @@ class Mesh_ {
   void solve_qr_2();
   void solve_qr();
   void check_qr();
+  void qr_with_ooc();
+  void check_qr_1();
+  void check_qr_2();
+  void improve_qr();
 
   double get_residual();
   unsigned get_n_dof();
@@ -242,5 +277,20 @@ class Mesh_ {
   void run_factor(int method, int keep_schur);
   void run_solve(int method, int phase);
 };
+
+// Process-wide settings and the tree builder as free functions, as the
+// reference declares them (UHM/include/uhm/util.hxx:44-60,
+// UHM/include/uhm/matrix/uhm/matrix.hxx:40-41,
+// UHM/include/uhm/operation/mesh.hxx:48).  The thread count sets OpenMP's
+// for the host work; the hierarchical block size is kept and reported (the
+// device kernels use their own tiles); both "enable" queries answer true.
+double timer();
+bool is_hier_matrix_enable();
+bool is_multithreading_enable();
+void set_num_threads(int nt);
+int get_num_threads();
+void set_hier_block_size(int size);
+int get_hier_block_size();
+bool build_tree(Mesh m);
 
 }  // namespace uhm
