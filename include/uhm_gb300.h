@@ -315,17 +315,33 @@ int uhm_gpu_mlp_train(const float* X, const int* Y, const float* class_weight, i
  * its own pool, a real-time loop that cannot take an allocation's implicit
  * synchronisation).  It has no counterpart in the reference.
  *   - n <= 262144; larger n returns 30, bad arguments return 7, a device
- *     wait that gave up returns 14.
+ *     wait that gave up returns 14.  After a return of 14 the contents of x
+ *     are undefined (blocks that gave up still write their part): keep a
+ *     copy of b if it is needed again.
  *   - Scratch: a fixed 32 KB device array inside this library (ticket, error
  *     word, per-block completion flags), present on every GPU that loads the
- *     library; each call clears the part it uses on `stream` first.
- *   - The first call on a device looks up that array's device address (once
- *     per device); make that first call before any stream capture.
+ *     library; each call clears the part it uses on `stream` first.  The
+ *     first call on a device looks up that array's device address (once per
+ *     device).
  *   - Calls share the array: calls that overlap on the GPU (other streams,
  *     other host threads) race and must be serialised by the caller.
- *   - The call waits for `stream` (it reads the error word back) and runs the
- *     work on `stream` (NULL = the legacy default stream). */
+ *   - The call reads the error word back into host memory and waits for
+ *     `stream`, so it cannot be made while `stream` (or any stream) is being
+ *     captured into a CUDA graph.  The work runs on `stream` (NULL = the
+ *     legacy default stream). */
 int uhm_gpu_dense_chol_solve_noalloc(const double* L, int n, int ld, double* x, void* stream);
+
+/* Iteration limit of every bounded wait inside the device kernels (flag
+ * hand-offs of the tree solves, the grid barrier of the cooperative LU panel,
+ * the mbarrier waits of the tensor-core update, the allocation-free solve).
+ * The default keeps each wait under about a second; a wait that runs out
+ * records an error, the call returns status 14 and the device stays usable.
+ * iters >= 0 sets the limit (0: a wait not satisfied at its first look gives
+ * up, which lets a test make a wait run out); iters < 0 restores the
+ * defaults.  Copies in flight are still waited for with a fixed limit before
+ * a kernel frees its memory.  It has no counterpart in the reference, which
+ * has no device waits.  Returns 0, or 7 when no device is present. */
+int uhm_gpu_set_wait_limit(long long iters);
 
 /* pinned host memory for the bulk transfers */
 void* uhm_gpu_host_alloc(long bytes);

@@ -10,7 +10,14 @@
 // copy_in of every leaf matrix and right-hand side, set_rhs, factor, solve,
 // copy_out of the solution.
 //
-// usage: uhm_ref_driver IN OUT [n_threads] [sparse]
+// usage: uhm_ref_driver IN OUT [n_threads] [sparse | reps]
+//
+// With a number reps > 1 the factorisation and solve are repeated: before
+// each repetition after the first the front matrices are freed and created
+// again (free_matrix, create_matrix_without_buffer) and every leaf matrix and
+// right-hand side is copied in again, so each repetition does the whole
+// numeric work of the first.  The solution written is the last one's; the
+// time of every repetition follows the tail (see OUT).
 //
 // With "sparse" the driver stops after copy_in and instead writes the
 // reference's own sparse export of the leaves (DSparse_(fort 0, cs 0,
@@ -34,7 +41,8 @@
 //     int32 n_nodes, n_rhs; per node (input order) float64 x[n_dof*n_rhs]
 //     (node-major, rhs-minor); int32 n_elements; per element (input order)
 //     int32 n_factor, n_schur; float64 t_factor, t_solve (seconds),
-//     flop_decompose, flop_solve, t_lock (seconds, the symbolic phase)
+//     flop_decompose, flop_solve, t_lock (seconds, the symbolic phase);
+//     int32 reps; per repetition float64 t_factor, t_solve
 #include "uhm.hxx"
 
 #include <cstdio>
@@ -116,7 +124,10 @@ int main(int argc, char** argv) {
   const double t_lock = now() - tl0;
   m->create_matrix_without_buffer(UHM_REAL, n_rhs);
 
+  const bool sparse_mode = argc > 4 && !std::strcmp(argv[4], "sparse");
+  const int reps = (argc > 4 && !sparse_mode && std::atoi(argv[4]) > 1) ? std::atoi(argv[4]) : 1;
   std::vector<int> elem_m(n_leaves);
+  std::vector<std::vector<double> > As(n_leaves), Bs(n_leaves);
   for (int e = 0; e < n_leaves; ++e) {
     int msz = 0;
     for (int k = eptr[e]; k < eptr[e + 1]; ++k) msz += ndof[node_index[enode[k]]];
@@ -127,11 +138,15 @@ int main(int argc, char** argv) {
     if (msz == 0) continue;
     m->copy_in(elt[e], UHM_REAL, msz, msz, &enode[eptr[e]], UHM_LHS, (void*)A.data());
     m->copy_in(elt[e], UHM_REAL, msz, n_rhs, &enode[eptr[e]], UHM_RHS, (void*)B.data());
+    if (reps > 1) {
+      As[e].swap(A);
+      Bs[e].swap(B);
+    }
   }
   std::fclose(fin);
   m->set_rhs();
 
-  if (argc > 4 && !std::strcmp(argv[4], "sparse")) {
+  if (sparse_mode) {
     uhm::DSparse_ sp(0, 0, n_rhs);
     for (int e = 0; e < n_leaves; ++e)
       if (elem_m[e]) sp.import_element(elt[e]);
@@ -166,17 +181,34 @@ int main(int argc, char** argv) {
   unsigned int nnz = 0;
   m->estimate_cost(method, UHM_REAL, n_rhs, fd, fs, nnz, buf);
 
-  const double t0 = now();
-  if (method == 1) m->chol_with_free();
-  else if (method == 2) m->lu_nopiv_with_free();
-  else if (method == 3) m->lu_piv_with_free();
-  else if (method == 4) m->lu_incpiv_with_free();
-  else fail("unknown method");
-  const double t1 = now();
-  if (method == 1) m->solve_chol();
-  else if (method == 2) m->solve_lu_nopiv();
-  else m->solve_lu_piv();
-  const double t2 = now();
+  std::vector<double> rep_times;
+  double t0 = 0, t1 = 0, t2 = 0;
+  for (int rep = 0; rep < reps; ++rep) {
+    if (rep > 0) {
+      m->free_matrix();
+      m->create_matrix_without_buffer(UHM_REAL, n_rhs);
+      for (int e = 0; e < n_leaves; ++e) {
+        const int msz = elem_m[e];
+        if (msz == 0) continue;
+        m->copy_in(elt[e], UHM_REAL, msz, msz, &enode[eptr[e]], UHM_LHS, (void*)As[e].data());
+        m->copy_in(elt[e], UHM_REAL, msz, n_rhs, &enode[eptr[e]], UHM_RHS, (void*)Bs[e].data());
+      }
+      m->set_rhs();
+    }
+    t0 = now();
+    if (method == 1) m->chol_with_free();
+    else if (method == 2) m->lu_nopiv_with_free();
+    else if (method == 3) m->lu_piv_with_free();
+    else if (method == 4) m->lu_incpiv_with_free();
+    else fail("unknown method");
+    t1 = now();
+    if (method == 1) m->solve_chol();
+    else if (method == 2) m->solve_lu_nopiv();
+    else m->solve_lu_piv();
+    t2 = now();
+    rep_times.push_back(t1 - t0);
+    rep_times.push_back(t2 - t1);
+  }
 
   // solution per node, taken from the first leaf element that holds the node
   std::vector<std::vector<double> > x(n_nodes);
@@ -215,6 +247,8 @@ int main(int argc, char** argv) {
   }
   double tail[5] = {t1 - t0, t2 - t1, fd, fs, t_lock};
   std::fwrite(tail, 8, 5, fo);
+  std::fwrite(&reps, 4, 1, fo);
+  std::fwrite(rep_times.data(), 8, rep_times.size(), fo);
   std::fclose(fo);
   delete m;
   FLA_Finalize();

@@ -1,7 +1,7 @@
 """Runs the reference solver built by ``oracle/Makefile`` (TEST INFRASTRUCTURE).
 
 Writes a :class:`uhm_gb300.hpfem.MeshSpec` in the binary layout that
-``oracle/ref_driver.cpp`` reads, runs ``oracle/_ref/uhm_ref_driver`` and
+``oracle/ref_driver.cpp`` reads, runs ``oracle/_ref/<machine>/uhm_ref_driver`` and
 parses its output.  Only the fixture generator (``tests/golden/make_golden.py``)
 and tests that skip when the binary is absent use this module; the reference
 checkout is needed only to build the binary.
@@ -9,6 +9,7 @@ checkout is needed only to build the binary.
 from __future__ import annotations
 
 import os
+import platform
 import subprocess
 import tempfile
 from dataclasses import dataclass
@@ -16,7 +17,15 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DRIVER = os.path.join(HERE, "_ref", "uhm_ref_driver")
+MACHINE = platform.machine()
+DRIVER = os.path.join(HERE, "_ref", MACHINE, "uhm_ref_driver")
+STAGED = os.path.join(HERE, "_ref", "src")          # git-ignored copy of the sources the recipe needs
+
+
+def reference_root() -> str:
+    """Where the reference checkout is read from: $UHM_REFERENCE, else the
+    checkout's usual place in the build container."""
+    return os.environ.get("UHM_REFERENCE", "/root/reference")
 
 
 @dataclass
@@ -28,17 +37,28 @@ class RefResult:
     flop_decompose: float
     flop_solve: float
     t_lock: float = float("nan")   # the symbolic phase (Mesh_::lock), seconds
+    rep_times: np.ndarray | None = None   # (reps, 2): factor and solve seconds of each repetition
 
 
 def available() -> bool:
     return os.path.exists(DRIVER)
 
 
-def build(ref_root: str = "/root/reference", jobs: int = 16) -> bool:
-    """Compile the reference solver when its sources are present."""
-    if not os.path.isdir(os.path.join(ref_root, "UHM", "src")):
+def build(ref_root: str | None = None, jobs: int = 16) -> bool:
+    """Compile the reference solver for this machine.  With the checkout
+    present, its sources are also staged into oracle/_ref/src (git-ignored),
+    which travels with the working tree, so that a machine without the
+    checkout (the GPU host, another architecture) can build the same solver
+    from the staged copy.  Returns whether the driver binary exists."""
+    ref_root = ref_root or reference_root()
+    if os.path.isdir(os.path.join(ref_root, "UHM", "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF={ref_root}"], check=True)
+        src = ref_root
+    elif os.path.isdir(os.path.join(STAGED, "UHM", "src")):
+        src = os.path.join("_ref", "src")
+    else:
         return available()
-    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", f"REF={ref_root}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", f"REF={src}"], check=True)
     return available()
 
 
@@ -77,17 +97,27 @@ def read_result(path: str, spec) -> RefResult:
     tf, ts, fd, fs = np.frombuffer(buf, "<f8", 4, p)
     p += 32
     tl = float(np.frombuffer(buf, "<f8", 1, p)[0]) if len(buf) >= p + 8 else float("nan")
-    return RefResult(x, fronts, float(tf), float(ts), float(fd), float(fs), tl)
+    p += 8
+    reps = None
+    if len(buf) >= p + 4:
+        nrep = int(np.frombuffer(buf, "<i4", 1, p)[0])
+        p += 4
+        reps = np.frombuffer(buf, "<f8", 2 * nrep, p).reshape(nrep, 2).copy()
+    return RefResult(x, fronts, float(tf), float(ts), float(fd), float(fs), tl, reps)
 
 
-def run(spec, method: int, threads: int = 1) -> RefResult:
+def run(spec, method: int, threads: int = 1, reps: int = 1) -> RefResult:
+    """Factor and solve the spec with the reference solver on `threads` OpenMP
+    threads (sequential OpenBLAS inside each task, as the reference's own
+    builds use); with reps > 1 the numeric work is repeated and every
+    repetition's factor and solve times are returned in rep_times."""
     if not available():
         raise RuntimeError("reference solver not built (make -C oracle)")
     with tempfile.TemporaryDirectory() as d:
         fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
         write_spec(spec, method, fin)
         env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
-        subprocess.run([DRIVER, fin, fout, str(threads)], check=True, env=env,
+        subprocess.run([DRIVER, fin, fout, str(threads), str(max(1, int(reps)))], check=True, env=env,
                        stdout=subprocess.DEVNULL)
         return read_result(fout, spec)
 

@@ -1,6 +1,6 @@
 """Regenerates the golden fixtures in this folder from the reference solver.
 
-    make -C oracle REF=<reference checkout>    # builds oracle/_ref/uhm_ref_driver
+    make -C oracle REF=<reference checkout>    # builds oracle/_ref/<machine>/uhm_ref_driver
     python tests/golden/make_golden.py
 
 For every case in ``cases.py`` the mesh is generated, solved by the

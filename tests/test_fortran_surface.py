@@ -14,7 +14,13 @@ import pytest
 
 from uhm_gb300 import api, hpfem
 
-FORT = "/root/reference/UHM/include/uhm/wrapper/fort.hxx"
+# the reference header, read from the checkout ($UHM_REFERENCE) or from the
+# staged copy of its sources (oracle/_ref/src) when either is present
+_REL = os.path.join("UHM", "include", "uhm", "wrapper", "fort.hxx")
+_ROOTS = [os.environ.get("UHM_REFERENCE", ""),
+          os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "src")]
+FORT = next((os.path.join(r, _REL) for r in _ROOTS if r and os.path.exists(os.path.join(r, _REL))),
+            os.path.join("/root/reference", _REL))
 
 
 @pytest.mark.skipif(not os.path.exists(FORT), reason="reference checkout absent")

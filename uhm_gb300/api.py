@@ -47,6 +47,7 @@ def _declare(L):
         f.argtypes = args
         f.restype = res
     sig("uhm_mesh_create_", [_P(_l)])
+    sig("uhm_gpu_set_wait_limit", [C.c_longlong], _i)
     sig("uhm_mesh_delete_", [_P(_l)])
     sig("uhm_add_element_", [_P(_l), _P(_l)])
     sig("uhm_add_node_", [_P(_l), _P(_i), _P(_i), _P(_i), _P(_i), _P(_l)])
@@ -517,6 +518,14 @@ class Mesh:
         self._check(self.L.uhm_gpu_copy_out_leaves(C.byref(self.h), out.ctypes.data_as(_P(_d)),
                                                    n_values))
         return out
+
+
+def set_wait_limit(iters: int) -> None:
+    """Iteration limit of every bounded wait inside the device kernels
+    (uhm_gpu_set_wait_limit); iters < 0 restores the defaults."""
+    rc = lib().uhm_gpu_set_wait_limit(int(iters))
+    if rc:
+        raise UHMError(rc, "uhm_gpu_set_wait_limit failed")
 
 
 def pinned_empty(n: int, dtype=np.float64):

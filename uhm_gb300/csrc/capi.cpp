@@ -19,6 +19,14 @@ using uhm::Element;
 using uhm::Mesh;
 using uhm::Node;
 
+namespace uhm_gpu {
+// iteration limits of the bounded device waits, one per kernel unit
+int set_wait_limit_factor(long long v);
+int set_wait_limit_solve(long long v);
+int set_wait_limit_tc(long long v);
+int set_wait_limit_noalloc(long long v);
+}  // namespace uhm_gpu
+
 namespace {
 double g_flop = 0.0;
 double g_buffer = 0.0, g_buffer_max = 0.0;
@@ -474,6 +482,15 @@ void* uhm_gpu_host_alloc(long bytes) {
 }
 void uhm_gpu_host_free(void* p) {
   if (p) cudaFreeHost(p);
+}
+
+int uhm_gpu_set_wait_limit(long long iters) {
+  int rc = 0;
+  rc |= uhm_gpu::set_wait_limit_factor(iters);
+  rc |= uhm_gpu::set_wait_limit_solve(iters);
+  rc |= uhm_gpu::set_wait_limit_tc(iters);
+  rc |= uhm_gpu::set_wait_limit_noalloc(iters);
+  return rc ? 7 : 0;
 }
 
 }  // extern "C"

@@ -1254,7 +1254,7 @@ void Engine::alloc_device(int method) {
   d_d = (double*)dmalloc(gv);
   d_erhs = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, erhs_total));
   d_y = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, y_total));
-  d_red = (double*)dmalloc(sizeof(double) * 2048);
+  d_red = (double*)dmalloc(sizeof(double) * 2560);
   {
     // tree of every global dof (roots numbered in slot order)
     std::vector<int> root_of(fronts.size(), -1);
@@ -1531,6 +1531,9 @@ void Engine::factor(int method) {
       }
   if (n_keep > 0 && act != part_mask) build_partial(method, act);
   n_refactored = (int)fronts.size() - n_keep;
+  // until this factorisation succeeds, no front holds a trustworthy factor
+  factored = false;
+  front_kept.clear();
   CK(cudaEventRecord(ev0, stream));
   if (!anorm_valid) enqueue_anorm();
   if (n_keep > 0) launch_ops(fac_ops_part, nullptr, nullptr, d_items_part);
@@ -1540,11 +1543,7 @@ void Engine::factor(int method) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.factor_ms = ms;
   check_status("factor");
-  {
-    int derr = 0;
-    CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (derr) fail("a kernel gave up waiting (bounded wait expired)", 14);
-  }
+  check_device_error("factor");
   if (status && mode == 1) {
     // a low-precision front broke down: escalate the failed fronts to FP64
     std::vector<int> st(fronts.size());
@@ -1615,17 +1614,24 @@ void Engine::solve_into(int method, double* rhs, double* out, int phase) {
   if (phase & 2) run_ops(bwd_ops, rhs, out);
 }
 
+// The error word of the bounded device waits: read, and cleared when set so
+// that the next call starts clean (the device itself stays usable).
 void Engine::check_device_error(const char* where) {
   int derr = 0;
   CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (derr) fail(std::string(where) + ": a device wait gave up (bounded wait expired)", 14);
+  if (derr) {
+    CK(cudaMemset(d_err, 0, sizeof(int)));
+    fail(std::string(where) + ": a device wait gave up (bounded wait expired)", 14);
+  }
 }
 
 void Engine::solve(int method, int phase) {
   if (!factored) fail("solve: the mesh has not been factorised", 9);
   if (method != factored_method) fail("solve: method differs from the factorisation", 9);
   float ms = 0;
-  if (status == 20) { status = 0; last_error.clear(); }
+  // a status left by an earlier solve (refinement redone in FP64, a bad
+  // right-hand side, a wait that gave up) does not carry over to this one
+  if (status == 20 || status == 13 || status == 14) { status = 0; last_error.clear(); }
   CK(cudaEventRecord(ev0, stream));
   if (phase & 1) assemble_rhs();
   solve_into(method, d_b, d_x, phase);
@@ -1635,7 +1641,17 @@ void Engine::solve(int method, int phase) {
   timing.solve_ms = ms;
   h_x_valid = false;
   check_device_error("solve");
-  if (mode == 1 && phase == 3) refine(method);
+  if (mode == 1 && phase == 3) {
+    refine(method);
+    return;
+  }
+  // plain path: a NaN or infinity in the right-hand sides (or factors)
+  // reaches the solution; report it rather than return it silently
+  if (phase & 2) {
+    launch_absmax(d_x, n_global * mesh->n_rhs, d_red + 2048, stream);
+    const double xn = read_scalar(d_red + 2048);
+    if (!std::isfinite(xn)) fail("solve: the solution is not finite (NaN or infinity in the right-hand side or the factors)", 13);
+  }
 }
 
 // FP64 iterative refinement on the unassembled element matrices:
@@ -1650,6 +1666,12 @@ void Engine::refine(int method) {
   const double an = operator_norm_inf();
   launch_absmax(d_b, nv, d_red + 1024, stream);
   const double bn = read_scalar(d_red + 1024);
+  if (!std::isfinite(bn) || !std::isfinite(an)) {
+    // refinement cannot repair a bad input, and an FP64 redo would not either
+    timing.berr = timing.berr_first = NAN;
+    fail(std::string("refine: the ") + (std::isfinite(bn) ? "operator" : "right-hand side") +
+             " is not finite (NaN or infinity)", 13);
+  }
   double berr = 1.0;
   int it = 0;
   const bool forest = n_trees > 1;
@@ -1690,8 +1712,14 @@ void Engine::refine(int method) {
     const int saved = mode;
     mode = 0;
     prec_dirty = true;
-    factor(method);
-    solve(method, 3);
+    try {
+      factor(method);
+      solve(method, 3);
+    } catch (...) {
+      mode = saved;
+      prec_dirty = true;
+      throw;
+    }
     mode = saved;
     prec_dirty = true;
     Timing t2 = timing;

@@ -31,4 +31,24 @@ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 #define UHM_CUDA_LAUNCH_CHECK() do { cudaError_t e__ = cudaGetLastError(); (void)e__; } while (0)
 
+// Iteration limit of the bounded spin-waits in one translation unit's kernels
+// (flag hand-offs, grid barriers, mbarrier waits).  Each unit that waits
+// defines its own copy with UHM_DEFINE_WAIT_LIMIT(setter, default) and reads
+// g_wait_limit once per wait.  The default keeps every wait under about a
+// second; uhm_gpu_set_wait_limit lowers it (0: a wait that is not satisfied
+// on its first look gives up) so that tests can make a wait run out on the
+// GPU and check the status it returns.  setter(v): v < 0 restores the default.
+#define UHM_DEFINE_WAIT_LIMIT(setter, dflt)                                        \
+  static __device__ uint32_t g_wait_limit = (dflt);                                \
+  int setter(long long v) {                                                        \
+    const uint32_t u = v < 0 ? (uint32_t)(dflt) : v > 0xFFFFFFFFll ? 0xFFFFFFFFu : (uint32_t)v; \
+    return cudaMemcpyToSymbol(g_wait_limit, &u, sizeof(u)) == cudaSuccess ? 0 : 7; \
+  }
+
+// setters of the units that wait (k_factor.cu, k_solve.cu, k_tc_gemm.cu, k_noalloc.cu)
+int set_wait_limit_factor(long long v);
+int set_wait_limit_solve(long long v);
+int set_wait_limit_tc(long long v);
+int set_wait_limit_noalloc(long long v);
+
 }  // namespace uhm_gpu

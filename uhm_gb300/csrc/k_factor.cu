@@ -926,6 +926,8 @@ void launch_getrf_panel(const DevCtx& c, const Item* items, int n_items, int dty
 // the error flag, and every CTA then skips the remaining barriers.
 constexpr int GC_THREADS = 256;
 
+UHM_DEFINE_WAIT_LIMIT(set_wait_limit_factor, 1u << 22)
+
 __device__ __forceinline__ unsigned int gc_ld_acquire(const unsigned int* p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -944,7 +946,8 @@ __device__ __forceinline__ bool gc_grid_barrier(unsigned int* ctr, unsigned int 
       atomicAdd(ctr, 1u);
       const unsigned int target = round * total;
       ok = false;
-      for (uint32_t i = 0; i < (1u << 22); ++i) {
+      const uint32_t lim = g_wait_limit;
+      for (uint32_t i = 0; i < lim; ++i) {
         if (gc_ld_acquire(ctr) >= target) { ok = true; break; }
         if (gc_ld_acquire(ctr + 1)) break;          // another CTA gave up
         __nanosleep(20);

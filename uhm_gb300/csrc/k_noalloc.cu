@@ -20,14 +20,20 @@
 #include <cstdint>
 #include <mutex>
 
+#include "k_common.cuh"
+
+namespace uhm_gpu {
+UHM_DEFINE_WAIT_LIMIT(set_wait_limit_noalloc, 1u << 22)   // bounded waits (~0.5 s)
+}  // namespace uhm_gpu
+
 namespace {
+using uhm_gpu::g_wait_limit;
 
 constexpr int NA_FB = 64;                          // rows per block
 constexpr int NA_MAX_BLOCKS = 4096;                // largest system: 262144 rows
 constexpr int NA_MAX_N = NA_FB * NA_MAX_BLOCKS;
 constexpr int STATIC_WORDS = 2 + 2 * NA_MAX_BLOCKS;
 constexpr int NA_THREADS = 256;
-constexpr uint32_t NA_SPIN_LIMIT = 1u << 22;       // bounded waits (~0.5 s)
 
 // [0] ticket, [1] error word, then flags: 2b = forward block b done,
 // 2b + 1 = backward block b done.  The first 2 + 2 nb words must be zero
@@ -43,13 +49,18 @@ __device__ __forceinline__ void na_st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// thread 0 waits for *flag (bounded); the block learns whether to go on
+// thread 0 waits for *flag (bounded); the block learns whether to go on.
+// The leading barrier keeps thread 0 from overwriting *s_ok while a slower
+// warp has not yet read the previous wait's answer, so every thread of the
+// block takes the same branch after each wait.
 __device__ bool na_wait(const int* flag, int* err, int* s_ok) {
+  __syncthreads();
   if (threadIdx.x == 0) {
     bool ok = na_ld_acquire(err) == 0;
     if (ok) {
       ok = false;
-      for (uint32_t it = 0; it < NA_SPIN_LIMIT; ++it) {
+      const uint32_t lim = g_wait_limit;
+      for (uint32_t it = 0; it < lim; ++it) {
         if (na_ld_acquire(flag) == 1) { ok = true; break; }
         if ((it & 255) == 255 && na_ld_acquire(err) != 0) break;
         __nanosleep(64);

@@ -592,16 +592,20 @@ void launch_dof_gather(const int64_t* ptr, const int64_t* idx, const double* y, 
 }
 
 // out[0] = max |v| (single-pass, deterministic: per-block max then a final block)
+// max(a, b) of non-negative values that keeps a NaN (fmax drops it), so that
+// a NaN anywhere in the vector reaches the result
+__device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
+
 __global__ void k_absmax_partial(const double* __restrict__ v, int64_t n, double* __restrict__ part) {
   __shared__ double s[256];
   double m = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    m = fmax(m, fabs(v[i]));
+    m = nanmax(m, fabs(v[i]));
   s[threadIdx.x] = m;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + o]);
+    if (threadIdx.x < o) s[threadIdx.x] = nanmax(s[threadIdx.x], s[threadIdx.x + o]);
     __syncthreads();
   }
   if (threadIdx.x == 0) part[blockIdx.x] = s[0];
@@ -610,11 +614,11 @@ __global__ void k_absmax_partial(const double* __restrict__ v, int64_t n, double
 __global__ void k_absmax_final(const double* __restrict__ part, int np, double* __restrict__ out) {
   __shared__ double s[256];
   double m = 0.0;
-  for (int i = threadIdx.x; i < np; i += blockDim.x) m = fmax(m, part[i]);
+  for (int i = threadIdx.x; i < np; i += blockDim.x) m = nanmax(m, part[i]);
   s[threadIdx.x] = m;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + o]);
+    if (threadIdx.x < o) s[threadIdx.x] = nanmax(s[threadIdx.x], s[threadIdx.x + o]);
     __syncthreads();
   }
   if (threadIdx.x == 0) out[0] = s[0];
@@ -776,11 +780,14 @@ __device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
 // Thread 0 waits (bounded) until flag[first] is set, extends the ready range
 // while further flags are set (step +1 or -1), issues one acquire fence for
 // all of them and returns the end of the range (exclusive) in *s_ready.
+UHM_DEFINE_WAIT_LIMIT(set_wait_limit_solve, 1u << 22)
+
 __device__ __forceinline__ void ready_range(const int* flg, int first, int last, int step, int* s_ready,
                                             int* err) {
   if (threadIdx.x == 0) {
     bool ok = false;
-    for (uint32_t i = 0; i < (1u << 22); ++i) {
+    const uint32_t lim = g_wait_limit;
+    for (uint32_t i = 0; i < lim; ++i) {
       if (ld_relaxed_gpu(flg + first) == 1) { ok = true; break; }
       __nanosleep(32);
     }
@@ -799,7 +806,8 @@ __device__ __forceinline__ void ready_range(const int* flg, int first, int last,
 }
 
 __device__ __forceinline__ bool wait_flag(const int* p, int* err) {
-  for (uint32_t i = 0; i < (1u << 22); ++i) {
+  const uint32_t lim = g_wait_limit;
+  for (uint32_t i = 0; i < lim; ++i) {
     if (ld_acquire_gpu(p) == 1) return true;
     __nanosleep(32);
   }

@@ -38,7 +38,9 @@ constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 2;   // 16 KB (A and B tiles 
 constexpr uint32_t TC_CPAD = TC_BN + 1;                 // padded row of the staged C tile
 constexpr uint32_t TC_CTILE_BYTES = TC_BM * TC_CPAD * 4;
 constexpr uint32_t TC_SMEM = 1024 + TC_STAGES * 2 * TC_TILE_BYTES + 256 + TC_CTILE_BYTES;
-constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+constexpr uint32_t TC_DRAIN_LIMIT = 1u << 22;   // waits for the CTA's own copies in flight
+
+UHM_DEFINE_WAIT_LIMIT(set_wait_limit_tc, 1u << 24)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -66,7 +68,8 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 // bounded wait: false (and error flag) when the barrier never completes
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                           int* err) {
-  for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i) {
+  const uint32_t lim = g_wait_limit;
+  for (uint32_t i = 0; i < lim; ++i) {
     if (mbar_try(bar, parity)) return true;
     if (*abort_flag) return false;
     if (i > 64) __nanosleep(64);
@@ -74,6 +77,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   *abort_flag = 1;
   if (err) atomicExch(err, 1);
   return false;
+}
+
+// wait with a fixed limit that the settable one does not shorten: used only
+// to let the CTA's own TMA copies and MMAs land before it frees its memory
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < TC_DRAIN_LIMIT; ++i) {
+    if (mbar_try(bar, parity)) return;
+    __nanosleep(64);
+  }
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
@@ -153,6 +165,7 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
   uint64_t* acc_empty = bars + 2 * TC_STAGES + 2;
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 2 * TC_STAGES + 4);
   uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 5);
+  uint64_t* drain_bar = bars + 2 * TC_STAGES + 6;
   float* s_c = reinterpret_cast<float*>(smem + 2 * TC_STAGES * TC_TILE_BYTES + 256);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -165,6 +178,7 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       mbar_init(smem_u32(&acc_full[b]), 1);
       mbar_init(smem_u32(&acc_empty[b]), TC_EPI_THREADS);
     }
+    mbar_init(smem_u32(drain_bar), 1);
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -226,6 +240,10 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
                       T.row0 + pb * T.prow + (T.C0 - T.base), fb);
         }
       }
+      // the last loads issued (one per stage at most) have landed before the
+      // CTA exits, whether or not the MMA thread consumed them
+      for (uint32_t g2 = g > TC_STAGES ? g - TC_STAGES : 0; g2 < g; ++g2)
+        mbar_drain(smem_u32(&bars[g2 % TC_STAGES]), (g2 / TC_STAGES) & 1);
     }
   } else if (warp == 9) {
     if (lane == 0) {
@@ -256,6 +274,9 @@ k_tc_syrk(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         }
         if (live) umma_commit(smem_u32(&acc_full[b]));
       }
+      // every MMA this thread issued has completed before TMEM is freed
+      umma_commit(smem_u32(drain_bar));
+      mbar_drain(smem_u32(drain_bar), 0);
     }
   } else {
     // epilogue warps 0-7: warp w reads TMEM lanes [32 (w % 4), +32) (its
