@@ -268,6 +268,7 @@ void Engine::node_solution(int n_nodes, const int* ids, double* out, int64_t n_v
 void Engine::copy_in(Element e, int m, int n, int nod_disp, const int* nods, int side,
                      const double* buf) {
   ensure_plan();
+  if (side != UHM_LHS) clear_solve_status();
   if (m <= 0 || n <= 0) fail("copy_in: dimension is null", 7);
   std::vector<std::pair<int, int>> order;
   std::vector<int> pos;
@@ -350,6 +351,7 @@ void Engine::copy_in_leaves(int side, const double* buf, int64_t n_values) {
     factored = false;
     anorm_inf = -1.0;
   } else {
+    clear_solve_status();
     if (n_values != erhs_total) fail("copy_in_leaves: size mismatch", 7);
     if (!dev_ok) {
       std::memcpy(h_pinned + emat_total, buf, sizeof(double) * (size_t)erhs_total);
@@ -1629,9 +1631,7 @@ void Engine::solve(int method, int phase) {
   if (!factored) fail("solve: the mesh has not been factorised", 9);
   if (method != factored_method) fail("solve: method differs from the factorisation", 9);
   float ms = 0;
-  // a status left by an earlier solve (refinement redone in FP64, a bad
-  // right-hand side, a wait that gave up) does not carry over to this one
-  if (status == 20 || status == 13 || status == 14) { status = 0; last_error.clear(); }
+  clear_solve_status();
   CK(cudaEventRecord(ev0, stream));
   if (phase & 1) assemble_rhs();
   solve_into(method, d_b, d_x, phase);

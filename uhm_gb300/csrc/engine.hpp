@@ -316,6 +316,15 @@ class Engine {
   void* dmalloc(size_t bytes);
   int64_t add_items(const std::vector<uhm_gpu::Item>& it);
   void fail(const std::string& msg, int code);
+  // A status left by an earlier solve (refinement redone in FP64, a bad
+  // right-hand side, a device wait that gave up) does not carry over to the
+  // next solve or to new right-hand sides.
+  void clear_solve_status() {
+    if (status == 20 || status == 13 || status == 14) {
+      status = 0;
+      last_error.clear();
+    }
+  }
   void element_map(Element e, int nod_disp, const int* nods, std::vector<std::pair<int, int>>& order,
                    std::vector<int>& pos, std::vector<int32_t>& gd);
   void fetch_x();
