@@ -273,7 +273,10 @@ int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh
  * values[3] LU panels on many CTAs from this many rows below the diagonal,
  * values[4] k: diagonal block and panel TRSM of a Cholesky step in one launch
  * when that launch has at most k CTAs per SM (0: never), values[5] outer
- * panel width of tensor-core fronts (128, 256 or 512).
+ * panel width of tensor-core fronts factored step by step (128, 256 or 512:
+ * LU fronts, and Cholesky fronts when values[6] is 0), values[6] outer panel
+ * width of BF16X3 Cholesky fronts factored by the cooperative panel kernel
+ * (256 or 512; 0 puts them on the step-by-step path).
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

@@ -377,7 +377,8 @@ class Mesh:
                 "getrf_panel", "lu_row_update", "gemm_update", "fwd_gather", "fwd_small",
                 "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
                 "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
-                "laswp", "potrf_trsm", "assemble_scatter", "tc_gemm_bf16"] + [f"op{k}" for k in range(26, 32)]
+                "laswp", "potrf_trsm", "assemble_scatter", "tc_gemm_bf16", "chol_panel", "tc_chol_trail",
+                "tc_chol_schur", "clear_flags"] + [f"op{k}" for k in range(30, 32)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
@@ -454,7 +455,8 @@ class Mesh:
             ptr(r["beta"], np.float64, _d), ptr(r["sel_ptr"], np.int64, _l), ptr(r["sel"], np.int32, _i)))
 
     # -- kernel-selection thresholds --------------------------------------------
-    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo")
+    TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo",
+                "tc_panel")
 
     def tunables(self) -> dict:
         v = np.zeros(len(self.TUNABLES), np.int32)

@@ -27,6 +27,7 @@ SOURCES = [
     "k_factor.cu",
     "k_solve.cu",
     "k_tc_gemm.cu",
+    "k_chol_tc.cu",
     "k_noalloc.cu",
     "k_selector.cu",
     "k_elements.cu",

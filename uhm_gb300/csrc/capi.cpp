@@ -25,6 +25,7 @@ int set_wait_limit_factor(long long v);
 int set_wait_limit_solve(long long v);
 int set_wait_limit_tc(long long v);
 int set_wait_limit_noalloc(long long v);
+int set_wait_limit_chol_tc(long long v);
 }  // namespace uhm_gpu
 
 namespace {
@@ -490,6 +491,7 @@ int uhm_gpu_set_wait_limit(long long iters) {
   rc |= uhm_gpu::set_wait_limit_solve(iters);
   rc |= uhm_gpu::set_wait_limit_tc(iters);
   rc |= uhm_gpu::set_wait_limit_noalloc(iters);
+  rc |= uhm_gpu::set_wait_limit_chol_tc(iters);
   return rc ? 7 : 0;
 }
 

@@ -76,6 +76,9 @@ void Engine::free_device() {
   d_b = d_x = d_r = d_d = d_erhs = d_y = d_red = d_scratch = nullptr;
   d_ws = nullptr;
   d_ws_off = d_ws_stride = nullptr;
+  d_ws2 = nullptr;
+  d_ws2_row0 = nullptr;
+  d_pflags = nullptr;
   d_err = nullptr;
   d_dof_tree = nullptr;
   d_tree_red = nullptr;
@@ -525,11 +528,21 @@ void Engine::build_plan(int method) {
     // (its two operands take four packed parts)
     f.tc = f.n >= tune.tc_min_n &&
            (method == UHM_CHOL ? (p == PREC_BF16X3 || p == PREC_BF16X6) : p == PREC_BF16X3);
+    // BF16X3 Cholesky fronts: cooperative panels + one deep tensor-core pass over ABR
+    f.tcc = f.tc && method == UHM_CHOL && p == PREC_BF16X3 && tune.tc_panel > 0;
   }
   arena64_n = arena32_n = vec_n = piv_n = 0;
   ws_total = 0;
+  ws2_rows = 0;
   for (auto& f : fronts) {
-    if (!f.tc) continue;
+    if (!f.tcc) continue;
+    // two parts (hi, lo) of every 64-column chunk of the factor block, all n rows
+    f.ws2_row0 = ws2_rows;
+    ws2_rows += 2 * (int64_t)((f.fs + 63) / 64) * f.n;
+  }
+  if (ws2_rows + 512 > ((int64_t)1 << 31) - 1) fail("operand workspace beyond the tensor map's row range", 4);
+  for (auto& f : fronts) {
+    if (!f.tc || f.tcc) continue;
     const int64_t mmax = f.n - std::min(tune.tc_nbo, f.fs);
     f.ws_off = ws_total;
     f.ws_stride = mmax * tune.tc_nbo;
@@ -685,6 +698,7 @@ void Engine::build_programs(int method) {
   fac_ops.clear();
   fwd_ops.clear();
   bwd_ops.clear();
+  int64_t pf = 0;   // tickets and flags of the cooperative panel launches
   auto push = [&](std::vector<Op>& ops, int kind, int dtype, int nb, int param, const std::vector<Item>& it,
                   double flops = 0, double bytes = 0) {
     if (it.empty()) return;
@@ -789,9 +803,11 @@ void Engine::build_programs(int method) {
       for (int s : lv)
         if (h_fronts[s].dtype == dt && (!fac_mask || (*fac_mask)[s])) fl.push_back(s);
       if (fl.empty()) continue;
-      std::vector<int> tcf;
-      for (int s : fl)
-        if (fronts[s].tc) tcf.push_back(s);
+      std::vector<int> tcf, tccf;
+      for (int s : fl) {
+        if (fronts[s].tcc) tccf.push_back(s);
+        else if (fronts[s].tc) tcf.push_back(s);
+      }
       std::vector<Item> asm_items, small_items;
       std::vector<int> large;
       int max_small = 1;
@@ -1034,8 +1050,88 @@ void Engine::build_programs(int method) {
         push(fac_ops, OP_TC_PACK, dt, NBO, parts, pk);
         push(fac_ops, OP_TC_SYRK, dt, NBO, parts, tt, ftc, btc);
       }
+      // BF16X3 Cholesky fronts (k_chol_tc.cu): per outer panel of W1 columns
+      // one cooperative panel launch (factor, TRSM, in-panel updates, BF16
+      // parts) and one tensor-core launch over the factor block's trailing
+      // columns; ABR once at the end with K = fs
+      if (!tccf.empty()) {
+        const int W1 = tune.tc_panel;
+        const int TM = TCC_TILE_M, TN = TCC_TILE_N;
+        int maxfs_c = 0;
+        for (int s : tccf) maxfs_c = std::max(maxfs_c, fronts[s].fs);
+        for (int K0 = 0; K0 < maxfs_c; K0 += W1) {
+          std::vector<int> act;
+          for (int s : tccf)
+            if (fronts[s].fs > K0) act.push_back(s);
+          const int64_t tick = pf++;
+          std::vector<int64_t> foff(act.size());
+          std::vector<int> nrel(act.size());
+          int max_rel = 0;
+          double fp = 0, fbytes = 0;
+          for (size_t a = 0; a < act.size(); ++a) {
+            const HostFront& f = fronts[act[a]];
+            const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
+            foff[a] = pf;
+            pf += CP_FLAGS_PER_FRONT;
+            nrel[a] = nd + (f.n - K0 - W + 63) / 64;
+            max_rel = std::max(max_rel, nrel[a]);
+            fp += get_flop_chol(0, W) + get_flop_trsm_lower(0, W, f.n - K0 - W);
+            fbytes += 8.0 * (double)(f.n - K0) * W;
+          }
+          // tickets by distance from the diagonal, then front: every CTA waits
+          // only on CTAs with smaller tickets
+          std::vector<Item> pit;
+          for (int rel = 0; rel < max_rel; ++rel)
+            for (size_t a = 0; a < act.size(); ++a)
+              if (rel < nrel[a]) pit.push_back(Item{act[a], K0, rel, (int)foff[a]});
+          {
+            Op op{OP_CHOL_PANEL, F32, W1, (int)tick, add_items(pit), (int)pit.size()};
+            op.flops = fp;
+            op.bytes = fbytes;
+            fac_ops.push_back(op);
+          }
+          std::vector<Item> tt;
+          double ft = 0, bt = 0;
+          for (int sl : act) {
+            const HostFront& f = fronts[sl];
+            const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
+            const int base = K0 + W;
+            if (base >= f.fs) continue;
+            const int kc0 = K0 / 64, kc1 = kc0 + nd;
+            for (int r0 = base; r0 < f.n; r0 += TM)
+              for (int c0 = base; c0 < f.fs && c0 <= r0 + TM - 1; c0 += TN)
+                tt.push_back(Item{sl, r0, c0, kc0 | (kc1 << 16)});
+            const double w = f.fs - base, m = f.n - base;
+            const double area = w * m - 0.5 * w * (w - 1);
+            ft += 2.0 * W * area;
+            bt += 8.0 * area + 2.0 * 2.0 * m * 64.0 * nd;
+          }
+          push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tt, ft, bt);
+        }
+        std::vector<Item> tt;
+        double ft = 0, bt = 0;
+        for (int sl : tccf) {
+          const HostFront& f = fronts[sl];
+          if (f.ss <= 0) continue;
+          const int nch = (f.fs + 63) / 64;
+          for (int r0 = f.fs; r0 < f.n; r0 += TM)
+            for (int c0 = f.fs; c0 <= r0 + TM - 1 && c0 < f.n; c0 += TN)
+              tt.push_back(Item{sl, r0, c0, 0 | (nch << 16)});
+          ft += get_flop_syrk(0, f.fs, f.ss);
+          bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
+        }
+        push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
+      }
     }
   }
+  if (pf > 0) {
+    // the panel launches' tickets and flags start at zero in every factorisation
+    Op op{OP_CLEAR_FLAGS, 0, 0, 0, 0, 0};
+    op.q0 = (int)pf;
+    fac_ops.insert(fac_ops.begin(), op);
+  }
+  if (!fac_mask) pflags_n = pf;
+  else if (pf > pflags_n) fail("partial factor program needs more panel flags than allocated", 6);
   if (fac_mask) return;   // a partial factor program (build_partial) needs no solves
   // solve programs
   const int gm = chol ? M_CHOL : (method == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV);
@@ -1218,6 +1314,20 @@ void Engine::alloc_device(int method) {
     d_gc_xbuf = (double*)dmalloc(sizeof(double) * (size_t)std::max(1, n_sm) * (2 * 66 + 2 * 64));
     d_gc_ctr = (unsigned int*)dmalloc(2 * sizeof(unsigned int));
   }
+  if (ws2_rows > 0) {
+    // 512 spare rows: tiles that run past the last front's rows stay inside the tensor
+    const size_t bytes = 128 * (size_t)(ws2_rows + 512);
+    d_ws2 = dmalloc(bytes);
+    CK(cudaMemsetAsync(d_ws2, 0, bytes, stream));
+    if (!tcc_encode(&ws2_map, d_ws2, ws2_rows + 512)) fail("tensor map encoding failed", 4);
+    std::vector<int64_t> r0(fronts.size(), 0);
+    for (auto& f : fronts)
+      if (f.tcc) r0[f.slot] = f.ws2_row0;
+    d_ws2_row0 = (int64_t*)dmalloc(sizeof(int64_t) * r0.size());
+    CK(cudaMemcpyAsync(d_ws2_row0, r0.data(), sizeof(int64_t) * r0.size(), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+  if (pflags_n > 0) d_pflags = (int*)dmalloc(sizeof(int) * (size_t)pflags_n);
   if (ws_total > 0) {
     // one extra row block so tiles that run past the last part stay inside the tensor
     d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * tune.tc_nbo));
@@ -1446,6 +1556,13 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
         launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, 3, TC_TERMS_LU_BF16X3, 0, d_err,
                        stream);
         break;
+      case OP_CLEAR_FLAGS: CK(cudaMemsetAsync(d_pflags, 0, sizeof(int) * (size_t)op.q0, stream)); break;
+      case OP_CHOL_PANEL:
+        launch_chol_panel(ctx, it, op.n_items, op.nb, d_pflags + op.param, d_pflags, d_err, d_ws2, d_ws2_row0,
+                          stream);
+        break;
+      case OP_TC_CHOL_TRAIL:
+      case OP_TC_CHOL_SCHUR: launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, stream); break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
       case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream); break;
       case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;
@@ -1460,7 +1577,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
     }
     if (profiling) CK(cudaEventRecord(evs[2 * k + 1], stream));
     ++k;
-    timing.kernel_launches++;
+    if (op.kind != OP_CLEAR_FLAGS) timing.kernel_launches++;
   }
   CK(cudaGetLastError());
   if (profiling) {
@@ -1985,9 +2102,11 @@ void Engine::set_tunables(const int* v) {
   t.gc_min_rows = v[3];
   t.fuse_potrf_trsm = v[4] < 0 ? 0 : v[4];
   t.tc_nbo = v[5];
+  t.tc_panel = v[6];
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
       t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64 ||
-      (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512))
+      (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512) ||
+      (t.tc_panel != 0 && t.tc_panel != 256 && t.tc_panel != 512))
     fail("set_tunables: value outside the kernels' limits", 7);
   tune = t;
   prec_dirty = true;
@@ -2002,6 +2121,7 @@ void Engine::get_tunables(int* v) const {
   v[3] = tune.gc_min_rows;
   v[4] = tune.fuse_potrf_trsm;
   v[5] = tune.tc_nbo;
+  v[6] = tune.tc_panel;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -2041,6 +2161,7 @@ int Engine::autotune(int method, int reps) {
       {&tune.small_max_f64, {64, 96, 128, 160}},
   };
   if (!lu) knobs.push_back({&tune.fuse_potrf_trsm, {0, 1, 2, 4}});
+  if (!lu) knobs.push_back({&tune.tc_panel, {0, 256, 512}});
   if (!lu) knobs.push_back({&tune.tc_nbo, {128, 256, 512}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;

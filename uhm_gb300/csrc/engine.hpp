@@ -14,6 +14,7 @@
 
 #include "kernels.cuh"
 #include "k_tc.cuh"
+#include "k_chol_tc.cuh"
 #include "mesh.hpp"
 
 namespace uhm {
@@ -30,7 +31,9 @@ struct HostFront {
   std::vector<int> children;       // slots, in child order
   int prec = PREC_FP64;
   bool tc = false;                 // trailing updates on tensor cores (BF16-split)
+  bool tcc = false;                // ... through the cooperative panel kernel (BF16X3 Cholesky, k_chol_tc.cu)
   int64_t ws_off = 0, ws_stride = 0;
+  int64_t ws2_row0 = 0;            // first 128-byte row of its parts in the chunk-major workspace
   bool blocked = false;            // large front: blocked kernels, 64-col diagonal blocks
   int flag_off = 0;
   int64_t dinv_off = 0;
@@ -73,7 +76,8 @@ enum OpKind : int {
   OP_ASSEMBLE, OP_SMALL_FACTOR, OP_POTRF, OP_TRSM, OP_SYRK, OP_GETRF, OP_LUROW, OP_GEMM,
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
-  OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_KIND_END
+  OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_CHOL_PANEL, OP_TC_CHOL_TRAIL,
+  OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_KIND_END
 };
 static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
 
@@ -94,8 +98,10 @@ struct Tunables {
   int fuse_potrf_trsm = 2;   // Cholesky step: diagonal block + panel TRSM in one launch when it
                              // has at most this many CTAs per SM (0: never)
   int tc_nbo = 256;          // outer panel width of tensor-core fronts (128, 256 or 512)
+  int tc_panel = 512;        // BF16X3 Cholesky fronts: width of the cooperative panel (256 or 512;
+                             // 0: the step-by-step path of the other tensor-core fronts)
 };
-constexpr int N_TUNABLES = 6;
+constexpr int N_TUNABLES = 7;
 
 class Engine {
  public:
@@ -249,6 +255,12 @@ class Engine {
   double* d_scratch = nullptr;  // backward-solve partial sums
   int64_t* d_scr_off = nullptr;
   int* d_counters = nullptr;
+  void* d_ws2 = nullptr;             // chunk-major BF16 parts of the cooperative-panel fronts
+  int64_t ws2_rows = 0;              // its size in rows of 64 BF16
+  int64_t* d_ws2_row0 = nullptr;     // per front: first row of its parts
+  CUtensorMap ws2_map;
+  int* d_pflags = nullptr;           // tickets and flags of the panel launches (cleared per factorisation)
+  int64_t pflags_n = 0;
   void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
   int64_t* d_ws_off = nullptr;
   int64_t* d_ws_stride = nullptr;

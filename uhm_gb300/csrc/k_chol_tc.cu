@@ -1,0 +1,502 @@
+// Cholesky fronts factored with BF16-split tensor-core updates.
+//
+// Restates, for one front, the reference's partial factorisation
+// chol(ATL); ABL <- ABL L^{-T}; ABR <- ABR - ABL ABL^T
+// (UHM/src/matrix/uhm/fla/chol/decompose.cxx:50-98, with the blocked
+// right-looking Cholesky of LINAL/src/dense/chol.cxx:46-92 inside ATL) in
+// three kinds of launch per level of the tree:
+//
+//  1. k_chol_panel, once per outer panel of W1 columns [K0, K0 + W1) of the
+//     factor block: the whole panel, all rows K0..n-1 of every front of the
+//     level, is factored in one launch.  One CTA per 64-row block holds its
+//     rows of the panel in shared memory.  The CTAs of the panel's first
+//     rows own its 64 x 64 diagonal blocks; the owner of block j factors it
+//     (and forms its inverse) once the updates of the steps before have
+//     reached it, publishes the inverse and raises a flag; every CTA below
+//     multiplies its block column j by the inverse (TRSM), the owners of
+//     later diagonal blocks publish that product, and every CTA applies the
+//     rank-64 updates of step j to its rows of the panel's later columns.
+//     CTAs wait only on CTAs with smaller tickets (tickets are handed out in
+//     order of the diagonal distance, then front), so the launch needs no
+//     co-residency.  The CTAs below the panel then write their rows back and
+//     split them into BF16 parts (hi + lo) for the tensor cores.
+//  2. k_tc_chol over the trailing columns of the factor block, after every
+//     panel: C[rows >= K0+W, K0+W <= cols < fs] -= P P^T (lower part), with
+//     P the panel's rows below it and K = W.
+//  3. k_tc_chol over ABR once per level, after the last panel:
+//     ABR -= ABL ABL^T with K = fs in one pass, so every 128 x 256 tile of
+//     the Schur complement accumulates the whole contraction in tensor
+//     memory and is read and written once.
+//
+// BF16-split products (the "bf16x3" of k_tc_gemm.cu): a = hi + lo with hi,
+// lo BF16 (round to nearest), a b ~ hi_a hi_b + hi_a lo_b + lo_a hi_b,
+// accumulated in FP32 in tensor memory.
+//
+// Operand workspace, chunk-major: per front and part p, per 64-column chunk
+// kc of the factor block, the n rows of that chunk as rows of 64 BF16
+// (128 bytes): row index row0[front] + (p * nch + kc) * n + r.  One 2D
+// tensor map of 128-byte rows covers all of it.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "k_common.cuh"
+#include "k_potrf.cuh"
+#include "k_tc_ptx.cuh"
+#include "k_chol_tc.cuh"
+
+namespace uhm_gpu {
+
+UHM_DEFINE_WAIT_LIMIT(set_wait_limit_chol_tc, 1u << 22)
+
+// ---------------------------------------------------------------------------
+// 1. the cooperative panel kernel
+// ---------------------------------------------------------------------------
+constexpr int CP_THREADS = 256;
+constexpr int CP_LT = 68;          // row of a transposed 64 x 64 operand in shared memory (16-byte rows)
+constexpr int CP_ERR = 5;          // error word value of a panel wait that gave up
+
+template <int W1>
+struct CpSmem {
+  float P[64 * W1];                // the CTA's 64 rows of the panel, column-major (leading dimension 64)
+  union {
+    PotrfShared<float> sh;         // diagonal owner: the block's factorisation
+    struct {
+      float Lt[64 * CP_LT];        // inverse of the step's diagonal block, transposed
+      float Bt[64 * CP_LT];        // the update operand L[block jp, block j], transposed
+    } t;
+  } u;
+  int s_t, s_ok;
+};
+
+__device__ __forceinline__ int cp_ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cp_st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// thread 0 waits (bounded) for *flag; every thread learns whether it came.
+// The leading barrier keeps thread 0 from overwriting *s_ok before a slower
+// warp has read the previous answer.  A wait gives up at once when another
+// CTA has already given up (the error word is set).
+__device__ bool cp_wait(const int* flag, int* err, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = cp_ld_acquire(err) == 0;
+    if (ok) {
+      ok = false;
+      const uint32_t lim = g_wait_limit;
+      for (uint32_t i = 0; i < lim; ++i) {
+        if (cp_ld_acquire(flag) != 0) {
+          ok = true;
+          break;
+        }
+        if ((i & 255) == 255 && cp_ld_acquire(err) != 0) break;
+        __nanosleep(32);
+      }
+      if (!ok) atomicExch(err, CP_ERR);
+    }
+    __threadfence();
+    *s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// every thread's stores to global memory are visible before thread 0 raises *flag
+__device__ __forceinline__ void cp_publish(int* flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) cp_st_release(flag, 1);
+}
+
+// P[:, dst .. dst+63] (the CTA's 64 rows) = or -= P[:, src .. src+kb-1] * T^T,
+// T given transposed in Tt (Tt[t * CP_LT + jj] = T[jj][t], zero where unused).
+// Thread (row i, 16-column group jg); the destination is written only after
+// every thread has read its source row (src may equal dst).
+__device__ __forceinline__ void cp_gemm64(float* __restrict__ P, int src, int dst, const float* __restrict__ Tt,
+                                          int kb, bool sub) {
+  const int i = threadIdx.x & 63, jg = threadIdx.x >> 6;
+  float acc[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) acc[u] = 0.f;
+#pragma unroll 4
+  for (int t = 0; t < kb; ++t) {
+    const float x = P[i + (src + t) * 64];
+#pragma unroll
+    for (int u4 = 0; u4 < 16; u4 += 4) {
+      const float4 l4 = *reinterpret_cast<const float4*>(&Tt[t * CP_LT + jg * 16 + u4]);
+      acc[u4 + 0] += x * l4.x;
+      acc[u4 + 1] += x * l4.y;
+      acc[u4 + 2] += x * l4.z;
+      acc[u4 + 3] += x * l4.w;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    float* d = &P[i + (dst + jg * 16 + u) * 64];
+    *d = sub ? *d - acc[u] : acc[u];
+  }
+  __syncthreads();
+}
+
+// item: front, a = K0 (first column of the panel), b = rel, the CTA's
+// block of rows: rel < nd is the panel's diagonal block rel (rows
+// K0 + 64 rel .., as many as the block has columns), rel >= nd the 64 rows
+// from K0 + W + 64 (rel - nd) (W = the panel's width, nd = its diagonal
+// blocks); c = offset of the front's flags in this launch (D[j] at c + j,
+// R[jp][j] at c + 8 + 8 jp + j).  Tickets are taken in item order.
+template <int W1>
+__global__ void __launch_bounds__(CP_THREADS, W1 <= 256 ? 2 : 1)
+k_chol_panel(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, int* err,
+             __nv_bfloat16* __restrict__ ws, const int64_t* __restrict__ ws_row0) {
+  extern __shared__ __align__(16) unsigned char cp_raw[];
+  CpSmem<W1>& S = *reinterpret_cast<CpSmem<W1>*>(cp_raw);
+  const int tid = threadIdx.x;
+  if (tid == 0) S.s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[S.s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, K0 = it.a, rel = it.b;
+  const int W = min(W1, fs - K0), nd = (W + 63) / 64;
+  const int r0 = rel < nd ? K0 + 64 * rel : K0 + W + 64 * (rel - nd);
+  const int rows = rel < nd ? min(64, W - 64 * rel) : min(64, n - r0);
+  int* D = flags + it.c;
+  int* R = D + 8;
+  float* __restrict__ G = c.a32 + f.off;
+  // the CTA's rows of the panel (a diagonal owner needs only its columns up to
+  // and including its diagonal block)
+  const int ncol = rel < nd ? min(W, 64 * (rel + 1)) : W;
+  for (int idx = tid; idx < 64 * ncol; idx += CP_THREADS) {
+    const int i = idx & 63, col = idx >> 6;
+    S.P[idx] = i < rows ? G[(r0 + i) + (int64_t)(K0 + col) * n] : 0.f;
+  }
+  __syncthreads();
+  auto write_back = [&](int ncols) {
+    for (int idx = tid; idx < 64 * ncols; idx += CP_THREADS) {
+      const int i = idx & 63, col = idx >> 6;
+      if (i < rows) G[(r0 + i) + (int64_t)(K0 + col) * n] = S.P[idx];
+    }
+  };
+  for (int j = 0; j < nd; ++j) {
+    const int cj = 64 * j, kbj = min(64, W - cj);
+    if (rel == j) {
+      // diagonal owner: every update of steps < j has been applied to this
+      // block; factor it in place and publish its inverse
+      float x[4][4];
+      bool bad;
+      potrf_block<float>(S.P + cj * 64, 64, kbj, S.u.sh, x, bad, S.P + cj * 64);
+      if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+      potrf_store_inverse<float>(kbj, x, c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + j) * 4096);
+      write_back(cj + kbj);
+      cp_publish(D + j);
+      return;
+    }
+    // rel > j: X_j = A[rows, block j] L_jj^{-T}
+    cp_wait(D + j, err, &S.s_ok);
+    {
+      const float* Di = c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + j) * 4096;
+      for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+        const int t = idx >> 6, jj = idx & 63;   // Di[t * 64 + jj] = Linv[jj][t]
+        S.u.t.Lt[t * CP_LT + jj] = (t < kbj && jj < kbj) ? __ldcg(Di + idx) : 0.f;
+      }
+    }
+    __syncthreads();
+    cp_gemm64(S.P, cj, cj, S.u.t.Lt, kbj, false);
+    if (rel < nd) {
+      // a later diagonal owner: its block of L in column block j is an
+      // operand of every CTA below it
+      for (int idx = tid; idx < 64 * kbj; idx += CP_THREADS) {
+        const int i = idx & 63, col = idx >> 6;
+        if (i < rows) G[(r0 + i) + (int64_t)(K0 + cj + col) * n] = S.P[i + (cj + col) * 64];
+      }
+      cp_publish(R + rel * 8 + j);
+    }
+    // rank-kbj updates of this CTA's later column blocks (a diagonal owner
+    // stops at its own block: columns right of it are above the diagonal)
+    const int jlast = rel < nd ? rel : nd - 1;
+    for (int jp = j + 1; jp <= jlast; ++jp) {
+      const int cjp = 64 * jp, kbp = min(64, W - cjp);
+      if (jp == rel) {
+        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+          const int t = idx >> 6, jj = idx & 63;
+          S.u.t.Bt[t * CP_LT + jj] = (t < kbj && jj < kbp) ? S.P[jj + (cj + t) * 64] : 0.f;
+        }
+      } else {
+        cp_wait(R + jp * 8 + j, err, &S.s_ok);
+        const int rjp = K0 + cjp;
+        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+          const int t = idx >> 6, jj = idx & 63;
+          S.u.t.Bt[t * CP_LT + jj] =
+              (t < kbj && jj < kbp) ? __ldcg(G + (rjp + jj) + (int64_t)(K0 + cj + t) * n) : 0.f;
+        }
+      }
+      __syncthreads();
+      cp_gemm64(S.P, cj, cjp, S.u.t.Bt, kbj, true);
+    }
+  }
+  // below the panel's diagonal blocks: the finished rows back to the front,
+  // and their BF16 parts into the operand workspace (chunks K0/64 ..)
+  write_back(W);
+  const int nch = (fs + 63) / 64;
+  const int64_t row0 = ws_row0[it.front];
+  for (int cc = 0; cc < nd; ++cc) {
+    const int kc = K0 / 64 + cc;
+    __nv_bfloat16* w0 = ws + (row0 + (int64_t)kc * n + r0) * 64;
+    __nv_bfloat16* w1 = ws + (row0 + (int64_t)(nch + kc) * n + r0) * 64;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int idx = tid + CP_THREADS * h, i = idx & 63, g8 = idx >> 6;
+      if (i >= rows) continue;
+      __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int col = 64 * cc + 8 * g8 + q;
+        const float xv = col < W ? S.P[i + col * 64] : 0.f;
+        hi[q] = __float2bfloat16_rn(xv);
+        lo[q] = __float2bfloat16_rn(xv - __bfloat162float(hi[q]));
+      }
+      *reinterpret_cast<uint4*>(w0 + (int64_t)i * 64 + 8 * g8) = *reinterpret_cast<const uint4*>(hi);
+      *reinterpret_cast<uint4*>(w1 + (int64_t)i * 64 + 8 * g8) = *reinterpret_cast<const uint4*>(lo);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2./3. tensor-core update over 128 x 256 tiles
+// ---------------------------------------------------------------------------
+constexpr int TCC_BM = 128, TCC_BN = 256, TCC_STAGES = 2;
+constexpr int TCC_THREADS = 320;             // warps 0-7 epilogue, 8 TMA producer, 9 MMA issuer
+constexpr int TCC_EPI_THREADS = 256;
+constexpr uint32_t TCC_BOX = 128 * 128;      // one TMA box: 128 rows of 64 BF16 = 16 KB
+constexpr uint32_t TCC_STAGE = 6 * TCC_BOX;  // A hi, A lo (128 rows), B hi, B lo (256 rows each): 96 KB
+constexpr uint32_t TCC_SMEM = 1024 + TCC_STAGES * TCC_STAGE + 256;
+constexpr int TCC_ERR = 6;
+
+// item: front, a = first row r0, b = first column c0, c = kc0 | kc1 << 16
+// (chunks [kc0, kc1) of the factor block).  Columns stop at fs for tiles of
+// the factor block (c0 < fs) and at n for tiles of ABR (c0 >= fs); only
+// entries with col <= row are stored (Cholesky keeps the lower triangle).
+__global__ void __launch_bounds__(TCC_THREADS, 1)
+k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_row0,
+          const Item* __restrict__ items, int n_items, int* err) {
+  extern __shared__ __align__(1024) uint8_t tcc_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tcc_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TCC_STAGES * TCC_STAGE);
+  // bars: [0, S) full, [S, 2S) empty, then acc_full[2], acc_empty[2], drain
+  uint64_t* acc_full = bars + 2 * TCC_STAGES;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* drain_bar = acc_full + 4;
+  volatile int* s_abort = reinterpret_cast<volatile int*>(acc_full + 5);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(acc_full + 6);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TCC_STAGES; ++s) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[TCC_STAGES + s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), TCC_EPI_THREADS);
+    }
+    mbar_init(smem_u32(drain_bar), 1);
+    *s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                 "r"(2 * TCC_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *s_tmem;
+  const uint32_t lim = g_wait_limit;
+
+  if (warp == 8) {
+    if (lane == 0) {
+      // TMA producer: per chunk one stage holding both parts of A and of B
+      uint32_t g = 0;
+      bool live = true;
+      for (int t = blockIdx.x; t < n_items && live; t += gridDim.x) {
+        const Item it = items[t];
+        const FrontDev f = c.fronts[it.front];
+        const int n = f.n, nch = (f.fs + 63) / 64;
+        const int kc0 = it.c & 0xFFFF, kc1 = it.c >> 16;
+        const int64_t row0 = ws_row0[it.front];
+        for (int kc = kc0; kc < kc1; ++kc, ++g) {
+          const uint32_t s = g % TCC_STAGES;
+          if (g >= TCC_STAGES &&
+              !mbar_wait_lim(smem_u32(&bars[TCC_STAGES + s]), ((g / TCC_STAGES) + 1) & 1, s_abort, err, TCC_ERR,
+                             lim)) {
+            live = false;
+            break;
+          }
+          const uint32_t fb = smem_u32(&bars[s]);
+          const uint32_t st = smem_u32(smem + s * TCC_STAGE);
+          mbar_expect_tx(fb, TCC_STAGE);
+          const int yh = (int)(row0 + (int64_t)kc * n), yl = (int)(row0 + (int64_t)(nch + kc) * n);
+          tma_load_2d(st + 0 * TCC_BOX, &wsmap, 0, yh + it.a, fb);
+          tma_load_2d(st + 1 * TCC_BOX, &wsmap, 0, yl + it.a, fb);
+          tma_load_2d(st + 2 * TCC_BOX, &wsmap, 0, yh + it.b, fb);
+          tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, yh + it.b + 128, fb);
+          tma_load_2d(st + 4 * TCC_BOX, &wsmap, 0, yl + it.b, fb);
+          tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, yl + it.b + 128, fb);
+        }
+      }
+      // the last loads issued (one per stage at most) land before the CTA exits
+      for (uint32_t g2 = g > TCC_STAGES ? g - TCC_STAGES : 0; g2 < g; ++g2)
+        mbar_drain(smem_u32(&bars[g2 % TCC_STAGES]), (g2 / TCC_STAGES) & 1);
+    }
+  } else if (warp == 9) {
+    if (lane == 0) {
+      // MMA issuer: per chunk hi*hi, hi*lo, lo*hi, 4 K=16 steps each
+      const uint32_t idesc = idesc_bf16_f32(TCC_BM, TCC_BN);
+      uint32_t g = 0;
+      int i = 0;
+      bool live = true;
+      for (int t = blockIdx.x; t < n_items && live; t += gridDim.x, ++i) {
+        const Item it = items[t];
+        const int kc0 = it.c & 0xFFFF, kc1 = it.c >> 16;
+        const int b = i & 1, u = i >> 1;
+        if (u >= 1 && !mbar_wait_lim(smem_u32(&acc_empty[b]), (u - 1) & 1, s_abort, err, TCC_ERR, lim)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + b * TCC_BN;
+        for (int kc = kc0; kc < kc1; ++kc, ++g) {
+          const uint32_t s = g % TCC_STAGES;
+          if (!mbar_wait_lim(smem_u32(&bars[s]), (g / TCC_STAGES) & 1, s_abort, err, TCC_ERR, lim)) {
+            live = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(smem + s * TCC_STAGE);
+          const uint32_t ah = st, al = st + TCC_BOX, bh = st + 2 * TCC_BOX, bl = st + 4 * TCC_BOX;
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            umma_bf16(acc, sdesc_sw128(ah + k * 32), sdesc_sw128(bh + k * 32), idesc, (kc > kc0 || k > 0) ? 1u : 0u);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) umma_bf16(acc, sdesc_sw128(ah + k * 32), sdesc_sw128(bl + k * 32), idesc, 1u);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) umma_bf16(acc, sdesc_sw128(al + k * 32), sdesc_sw128(bh + k * 32), idesc, 1u);
+          umma_commit(smem_u32(&bars[TCC_STAGES + s]));
+        }
+        if (live) umma_commit(smem_u32(&acc_full[b]));
+      }
+      // every MMA issued has completed before tensor memory is freed
+      umma_commit(smem_u32(drain_bar));
+      mbar_drain(smem_u32(drain_bar), 0);
+    }
+  } else {
+    // epilogue warps 0-7: warp w reads tensor-memory lanes 32 (w % 4) .. +31
+    // (tile rows) and columns 128 (w / 4) .. +127; C -= acc column by
+    // column, 32 columns at a time (a warp's loads and stores of one column
+    // are 32 consecutive rows: 128 contiguous bytes)
+    const int quarter = warp & 3, half = warp >> 2;
+    int i = 0;
+    for (int t = blockIdx.x; t < n_items; t += gridDim.x, ++i) {
+      const Item it = items[t];
+      const FrontDev f = c.fronts[it.front];
+      float* __restrict__ G = c.a32 + f.off;
+      const int n = f.n;
+      const int cmax = it.b >= f.fs ? n : f.fs;
+      const int row = it.a + quarter * 32 + lane;
+      const int b = i & 1, u = i >> 1;
+      if (!mbar_wait_lim(smem_u32(&acc_full[b]), u & 1, s_abort, err, TCC_ERR, lim)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t v[32];
+        TC_LD32(tmem + ((uint32_t)(quarter * 32) << 16) + b * TCC_BN + half * 128 + cc * 32, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int cb = it.b + half * 128 + cc * 32;
+        const bool rok = row < n && !*s_abort;
+        float cv[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = cb + j;
+          cv[j] = (rok && col < cmax && col <= row) ? __ldcg(G + row + (int64_t)col * n) : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = cb + j;
+          if (rok && col < cmax && col <= row) G[row + (int64_t)col * n] = cv[j] - __uint_as_float(v[j]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(smem_u32(&acc_empty[b]));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCC_BN));
+  }
+}
+
+// ---- host side ---------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode_cc = nullptr;
+
+bool tcc_encode(CUtensorMap* map, void* base, int64_t rows) {
+  if (!g_encode_cc) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      return false;
+    }
+    g_encode_cc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  cuuint64_t dims[2] = {64, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {128};
+  cuuint32_t box[2] = {64, 128};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode_cc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <int W1>
+static void launch_panel_w(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,
+                           void* ws, const int64_t* ws_row0, cudaStream_t s) {
+  const int sm = (int)sizeof(CpSmem<W1>);
+  cudaFuncSetAttribute(k_chol_panel<W1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  k_chol_panel<W1><<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, flags, err, (__nv_bfloat16*)ws, ws_row0);
+}
+
+void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, int* ticket, int* flags, int* err,
+                       void* ws, const int64_t* ws_row0, cudaStream_t s) {
+  if (!n_items) return;
+  if (w1 == 256) launch_panel_w<256>(c, items, n_items, ticket, flags, err, ws, ws_row0, s);
+  else if (w1 == 512) launch_panel_w<512>(c, items, n_items, ticket, flags, err, ws, ws_row0, s);
+  else throw std::invalid_argument("chol_panel: panel width must be 256 or 512, got " + std::to_string(w1));
+}
+
+void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
+                    int* err, cudaStream_t s) {
+  if (!n_items) return;
+  static int n_sm = 0;
+  if (!n_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm <= 0) n_sm = 1;
+  }
+  cudaFuncSetAttribute(k_tc_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TCC_SMEM);
+  const int grid = n_items < n_sm ? n_items : n_sm;
+  k_tc_chol<<<grid, TCC_THREADS, TCC_SMEM, s>>>(c, map, ws_row0, items, n_items, err);
+}
+
+int chol_panel_max_w1() { return 512; }
+
+}  // namespace uhm_gpu

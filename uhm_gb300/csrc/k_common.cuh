@@ -45,10 +45,11 @@ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
     return cudaMemcpyToSymbol(g_wait_limit, &u, sizeof(u)) == cudaSuccess ? 0 : 7; \
   }
 
-// setters of the units that wait (k_factor.cu, k_solve.cu, k_tc_gemm.cu, k_noalloc.cu)
+// setters of the units that wait (k_factor.cu, k_solve.cu, k_tc_gemm.cu, k_noalloc.cu, k_chol_tc.cu)
 int set_wait_limit_factor(long long v);
 int set_wait_limit_solve(long long v);
 int set_wait_limit_tc(long long v);
 int set_wait_limit_noalloc(long long v);
+int set_wait_limit_chol_tc(long long v);
 
 }  // namespace uhm_gpu
