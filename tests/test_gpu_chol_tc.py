@@ -79,4 +79,5 @@ def test_panel_path_launches_its_kernels(native_lib):
     prof = m.profile()
     for k in ("chol_panel", "tc_chol_trail", "tc_chol_schur"):
         assert prof[k]["launches"] > 0, k
-    assert prof["potrf_trsm"]["launches"] == 0 or prof["tc_syrk_bf16"]["launches"] == 0
+    # no front of this mesh went through the step-by-step tensor-core path
+    assert "tc_syrk_bf16" not in prof and "tc_pack" not in prof
