@@ -195,8 +195,10 @@ k_chol_panel(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, 
       potrf_block<float>(S.P + cj * 64, 64, kbj, S.u.sh, x, bad, S.P + cj * 64);
       if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
       potrf_store_inverse<float>(kbj, x, c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + j) * 4096);
-      write_back(cj + kbj);
+      // the CTAs below need only the inverse: raise the flag before the
+      // write-back of this CTA's rows, which nothing in this launch reads
       cp_publish(D + j);
+      write_back(cj + kbj);
       return;
     }
     // rel > j: X_j = A[rows, block j] L_jj^{-T}
