@@ -228,8 +228,10 @@ int uhm_gpu_get_timing(long* mesh, double* out);
  * is bracketed by CUDA events (use outside timed regions).  Per op kind
  * (0 assemble, 1 small-front factor, 2 diagonal POTRF, 3 panel TRSM,
  * 4 trailing SYRK, 5 LU panel, 6 LU row solve, 7 LU trailing GEMM,
- * 8..16 solve kernels): total ms, algorithmic flops, algorithmic bytes,
- * launches since profiling was switched on. */
+ * 8..16 solve kernels, 17..25 the step-by-step tensor-core and LU
+ * kernels, 26..32 the cooperative-panel Cholesky kernels; n_kinds up to
+ * 40): total ms, algorithmic flops, algorithmic bytes, launches since
+ * profiling was switched on. */
 int uhm_gpu_set_profiling(long* mesh, int on);
 int uhm_gpu_get_profile(long* mesh, int n_kinds, double* ms, double* flops, double* bytes,
                         long* launches);
@@ -275,8 +277,11 @@ int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh
  * when that launch has at most k CTAs per SM (0: never), values[5] outer
  * panel width of tensor-core fronts factored step by step (128, 256 or 512:
  * LU fronts, and Cholesky fronts when values[6] is 0), values[6] outer panel
- * width of BF16X3 Cholesky fronts factored by the cooperative panel kernel
- * (256 or 512; 0 puts them on the step-by-step path).
+ * width of BF16X3 Cholesky fronts on the cooperative-panel path: 256 (the
+ * default) factors each panel's diagonal block and its inverse with a
+ * cooperative kernel and solves the rows below on the tensor cores, 512
+ * factors whole panels with the cooperative kernel, 0 puts these fronts on
+ * the step-by-step path.
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

@@ -378,13 +378,14 @@ class Mesh:
                 "trsv_fwd_step", "gemv_fwd", "bwd_prepare", "bwd_small", "gemv_bwd", "trsv_bwd_step",
                 "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
                 "laswp", "potrf_trsm", "assemble_scatter", "tc_gemm_bf16", "chol_panel", "tc_chol_trail",
-                "tc_chol_schur", "clear_flags"] + [f"op{k}" for k in range(30, 32)]
+                "tc_chol_schur", "clear_flags", "chol_diag", "chol_pack", "tc_chol_trsm"] + \
+               [f"op{k}" for k in range(33, 40)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
 
     def profile(self) -> dict:
-        n = 32
+        n = len(self.OP_NAMES)
         ms, fl, by = (_d * n)(), (_d * n)(), (_d * n)()
         la = (_l * n)()
         self._check(self.L.uhm_gpu_get_profile(C.byref(self.h), n, ms, fl, by, la))

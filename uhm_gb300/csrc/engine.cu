@@ -78,6 +78,8 @@ void Engine::free_device() {
   d_ws_off = d_ws_stride = nullptr;
   d_ws2 = nullptr;
   d_ws2_row0 = nullptr;
+  d_ws2b_row0 = d_linv_row0 = d_linv32_off = nullptr;
+  d_linv32 = nullptr;
   d_pflags = nullptr;
   d_err = nullptr;
   d_dof_tree = nullptr;
@@ -534,11 +536,29 @@ void Engine::build_plan(int method) {
   arena64_n = arena32_n = vec_n = piv_n = 0;
   ws_total = 0;
   ws2_rows = 0;
+  linv32_n = 0;
   for (auto& f : fronts) {
     if (!f.tcc) continue;
     // two parts (hi, lo) of every 64-column chunk of the factor block, all n rows
     f.ws2_row0 = ws2_rows;
     ws2_rows += 2 * (int64_t)((f.fs + 63) / 64) * f.n;
+  }
+  if (tune.tc_panel == CD_PANEL) {
+    // the panel rows before their TRSM (same layout), then per front the
+    // current panel's Linv parts and its FP32 exchange area
+    const int64_t r2 = ws2_rows;
+    for (auto& f : fronts) {
+      if (!f.tcc) continue;
+      f.ws2b_row0 = f.ws2_row0 + r2;
+    }
+    ws2_rows += r2;
+    for (auto& f : fronts) {
+      if (!f.tcc) continue;
+      f.linv_row0 = ws2_rows;
+      ws2_rows += CD_LINV_ROWS;
+      f.linv32_off = linv32_n;
+      linv32_n += (int64_t)CD_PANEL * CD_PANEL;
+    }
   }
   if (ws2_rows + 512 > ((int64_t)1 << 31) - 1) fail("operand workspace beyond the tensor map's row range", 4);
   for (auto& f : fronts) {
@@ -1054,7 +1074,79 @@ void Engine::build_programs(int method) {
       // one cooperative panel launch (factor, TRSM, in-panel updates, BF16
       // parts) and one tensor-core launch over the factor block's trailing
       // columns; ABR once at the end with K = fs
-      if (!tccf.empty()) {
+      if (!tccf.empty() && tune.tc_panel == CD_PANEL) {
+        // panels of 256 columns: diagonal block + its inverse (cooperative,
+        // nd CTAs per front), BF16 parts of the rows below, X = A Linv^T on
+        // the tensor cores (X and its parts written), trailing update
+        const int W1 = CD_PANEL;
+        const int TM = TCC_TILE_M, TN = TCC_TILE_N;
+        int maxfs_c = 0;
+        for (int s : tccf) maxfs_c = std::max(maxfs_c, fronts[s].fs);
+        for (int K0 = 0; K0 < maxfs_c; K0 += W1) {
+          std::vector<int> act;
+          for (int s : tccf)
+            if (fronts[s].fs > K0) act.push_back(s);
+          const int64_t tick = pf++;
+          std::vector<Item> dit, pit, xit, tt;
+          double fp = 0, fx = 0, bx = 0, ft = 0, bt = 0, bp = 0;
+          for (int rel = 0; rel < 4; ++rel)
+            for (int sl : act) {
+              const HostFront& f = fronts[sl];
+              const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
+              (void)nd;
+              if (rel < (W + 63) / 64) dit.push_back(Item{sl, K0, rel, 0});
+            }
+          std::vector<int64_t> foff(fronts.size(), 0);
+          for (int sl : act) {
+            foff[sl] = pf;
+            pf += CP_FLAGS_PER_FRONT;
+          }
+          for (Item& d : dit) d.c = (int)foff[d.front];
+          for (int sl : act) {
+            const HostFront& f = fronts[sl];
+            const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
+            const int base = K0 + W;
+            fp += get_flop_chol(0, W);
+            for (int r0 = base; r0 < f.n; r0 += 64)
+              for (int cc = 0; cc < nd; ++cc) pit.push_back(Item{sl, K0, r0, cc});
+            bp += (double)(f.n - base) * W * (4.0 + 4.0);
+            for (int r0 = base; r0 < f.n; r0 += TM) xit.push_back(Item{sl, r0, 0, K0});
+            fx += get_flop_trsm_lower(0, W, f.n - base);
+            bx += (double)(f.n - base) * 64.0 * nd * (4.0 + 4.0 + 4.0);
+            if (base < f.fs) {
+              const int kc0 = K0 / 64, kc1 = kc0 + nd;
+              for (int r0 = base; r0 < f.n; r0 += TM)
+                for (int c0 = base; c0 < f.fs && c0 <= r0 + TM - 1; c0 += TN)
+                  tt.push_back(Item{sl, r0, c0, kc0 | (kc1 << 16)});
+              const double w = f.fs - base, m = f.n - base;
+              const double area = w * m - 0.5 * w * (w - 1);
+              ft += 2.0 * W * area;
+              bt += 8.0 * area + 2.0 * 2.0 * m * 64.0 * nd;
+            }
+          }
+          {
+            Op op{OP_CHOL_DIAG, F32, W1, (int)tick, add_items(dit), (int)dit.size()};
+            op.flops = fp;
+            fac_ops.push_back(op);
+          }
+          push(fac_ops, OP_CHOL_PACK, F32, 0, 0, pit, 0, bp);
+          push(fac_ops, OP_TC_CHOL_TRSM, F32, 0, 0, xit, fx, bx);
+          push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tt, ft, bt);
+        }
+        std::vector<Item> tt;
+        double ft = 0, bt = 0;
+        for (int sl : tccf) {
+          const HostFront& f = fronts[sl];
+          if (f.ss <= 0) continue;
+          const int nch = (f.fs + 63) / 64;
+          for (int r0 = f.fs; r0 < f.n; r0 += TM)
+            for (int c0 = f.fs; c0 <= r0 + TM - 1 && c0 < f.n; c0 += TN)
+              tt.push_back(Item{sl, r0, c0, 0 | (nch << 16)});
+          ft += get_flop_syrk(0, f.fs, f.ss);
+          bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
+        }
+        push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
+      } else if (!tccf.empty()) {
         const int W1 = tune.tc_panel;
         const int TM = TCC_TILE_M, TN = TCC_TILE_N;
         int maxfs_c = 0;
@@ -1320,11 +1412,23 @@ void Engine::alloc_device(int method) {
     d_ws2 = dmalloc(bytes);
     CK(cudaMemsetAsync(d_ws2, 0, bytes, stream));
     if (!tcc_encode(&ws2_map, d_ws2, ws2_rows + 512)) fail("tensor map encoding failed", 4);
-    std::vector<int64_t> r0(fronts.size(), 0);
+    std::vector<int64_t> r0(fronts.size(), 0), rb(fronts.size(), 0), rl(fronts.size(), 0), lo(fronts.size(), 0);
     for (auto& f : fronts)
-      if (f.tcc) r0[f.slot] = f.ws2_row0;
-    d_ws2_row0 = (int64_t*)dmalloc(sizeof(int64_t) * r0.size());
-    CK(cudaMemcpyAsync(d_ws2_row0, r0.data(), sizeof(int64_t) * r0.size(), cudaMemcpyHostToDevice, stream));
+      if (f.tcc) {
+        r0[f.slot] = f.ws2_row0;
+        rb[f.slot] = f.ws2b_row0;
+        rl[f.slot] = f.linv_row0;
+        lo[f.slot] = f.linv32_off;
+      }
+    auto up64 = [&](int64_t*& d, const std::vector<int64_t>& h) {
+      d = (int64_t*)dmalloc(sizeof(int64_t) * h.size());
+      CK(cudaMemcpyAsync(d, h.data(), sizeof(int64_t) * h.size(), cudaMemcpyHostToDevice, stream));
+    };
+    up64(d_ws2_row0, r0);
+    up64(d_ws2b_row0, rb);
+    up64(d_linv_row0, rl);
+    up64(d_linv32_off, lo);
+    if (linv32_n > 0) d_linv32 = (float*)dmalloc(sizeof(float) * (size_t)linv32_n);
     CK(cudaStreamSynchronize(stream));
   }
   if (pflags_n > 0) d_pflags = (int*)dmalloc(sizeof(int) * (size_t)pflags_n);
@@ -1563,6 +1667,14 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
         break;
       case OP_TC_CHOL_TRAIL:
       case OP_TC_CHOL_SCHUR: launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, stream); break;
+      case OP_CHOL_DIAG:
+        launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_linv32, d_ws2, d_linv_row0,
+                         d_linv32_off, stream);
+        break;
+      case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, stream); break;
+      case OP_TC_CHOL_TRSM:
+        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, stream, 1, d_ws2b_row0, d_linv_row0, d_ws2);
+        break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
       case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream); break;
       case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;

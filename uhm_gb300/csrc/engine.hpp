@@ -34,6 +34,9 @@ struct HostFront {
   bool tcc = false;                // ... through the cooperative panel kernel (BF16X3 Cholesky, k_chol_tc.cu)
   int64_t ws_off = 0, ws_stride = 0;
   int64_t ws2_row0 = 0;            // first 128-byte row of its parts in the chunk-major workspace
+  int64_t ws2b_row0 = 0;           // ... of the panel rows before their TRSM (tc_panel 256)
+  int64_t linv_row0 = 0;           // ... of the current panel's Linv parts (tc_panel 256)
+  int64_t linv32_off = 0;          // its FP32 Linv exchange area (floats)
   bool blocked = false;            // large front: blocked kernels, 64-col diagonal blocks
   int flag_off = 0;
   int64_t dinv_off = 0;
@@ -66,7 +69,7 @@ struct Op {
   int aux = 0;        // rows per CTA (cooperative LU panel)
 };
 
-constexpr int N_OP_KINDS = 32;
+constexpr int N_OP_KINDS = 40;
 struct OpProfile {
   double ms[N_OP_KINDS] = {0}, flops[N_OP_KINDS] = {0}, bytes[N_OP_KINDS] = {0};
   int64_t launches[N_OP_KINDS] = {0};
@@ -77,9 +80,9 @@ enum OpKind : int {
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
   OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_CHOL_PANEL, OP_TC_CHOL_TRAIL,
-  OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_KIND_END
+  OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_CHOL_DIAG, OP_CHOL_PACK, OP_TC_CHOL_TRSM, OP_KIND_END
 };
-static_assert(OP_KIND_END <= 32, "profile arrays hold 32 op kinds");
+static_assert(OP_KIND_END <= N_OP_KINDS, "profile arrays hold N_OP_KINDS op kinds");
 
 struct Timing {
   double upload_ms = 0, factor_ms = 0, solve_ms = 0, refine_ms = 0, total_ms = 0;
@@ -98,8 +101,11 @@ struct Tunables {
   int fuse_potrf_trsm = 2;   // Cholesky step: diagonal block + panel TRSM in one launch when it
                              // has at most this many CTAs per SM (0: never)
   int tc_nbo = 256;          // outer panel width of tensor-core fronts (128, 256 or 512)
-  int tc_panel = 512;        // BF16X3 Cholesky fronts: width of the cooperative panel (256 or 512;
-                             // 0: the step-by-step path of the other tensor-core fronts)
+  int tc_panel = 256;        // BF16X3 Cholesky fronts: 256 = panels of 256 columns, diagonal block
+                             // and its inverse by a cooperative kernel, the rows below solved on
+                             // the tensor cores; 512 = panels of 512 columns factored whole by the
+                             // cooperative kernel (SIMT in-panel work); 0 = the step-by-step path
+                             // of the other tensor-core fronts
 };
 constexpr int N_TUNABLES = 7;
 
@@ -260,6 +266,11 @@ class Engine {
   int64_t* d_ws2_row0 = nullptr;     // per front: first row of its parts
   CUtensorMap ws2_map;
   int* d_pflags = nullptr;           // tickets and flags of the panel launches (cleared per factorisation)
+  int64_t* d_ws2b_row0 = nullptr;
+  int64_t* d_linv_row0 = nullptr;
+  int64_t* d_linv32_off = nullptr;
+  float* d_linv32 = nullptr;
+  int64_t linv32_n = 0;
   int64_t pflags_n = 0;
   void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
   int64_t* d_ws_off = nullptr;

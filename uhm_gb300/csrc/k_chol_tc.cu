@@ -116,33 +116,49 @@ __device__ __forceinline__ void cp_publish(int* flag) {
   if (threadIdx.x == 0) cp_st_release(flag, 1);
 }
 
-// P[:, dst .. dst+63] (the CTA's 64 rows) = or -= P[:, src .. src+kb-1] * T^T,
-// T given transposed in Tt (Tt[t * CP_LT + jj] = T[jj][t], zero where unused).
-// Thread (row i, 16-column group jg); the destination is written only after
-// every thread has read its source row (src may equal dst).
-__device__ __forceinline__ void cp_gemm64(float* __restrict__ P, int src, int dst, const float* __restrict__ Tt,
-                                          int kb, bool sub) {
-  const int i = threadIdx.x & 63, jg = threadIdx.x >> 6;
-  float acc[16];
-#pragma unroll
-  for (int u = 0; u < 16; ++u) acc[u] = 0.f;
+// acc (this thread's 4 x 4 tile: rows 4 ti .., columns 4 tj .., ti = tid % 16,
+// tj = tid / 16) += X * B, X = 64 x kb column-major (leading dimension 64),
+// B = kb x 64 row-major with rows of CP_LT (zero where unused): two 128-bit
+// shared loads per 16 FMAs.
+__device__ __forceinline__ void cp_mma_tile(const float* __restrict__ X, const float* __restrict__ B, int kb,
+                                            float (&acc)[4][4]) {
+  const int ti = threadIdx.x & 15, tj = threadIdx.x >> 4;
 #pragma unroll 4
   for (int t = 0; t < kb; ++t) {
-    const float x = P[i + (src + t) * 64];
+    const float4 x4 = *reinterpret_cast<const float4*>(&X[4 * ti + t * 64]);
+    const float4 b4 = *reinterpret_cast<const float4*>(&B[t * CP_LT + 4 * tj]);
+    const float xv[4] = {x4.x, x4.y, x4.z, x4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-    for (int u4 = 0; u4 < 16; u4 += 4) {
-      const float4 l4 = *reinterpret_cast<const float4*>(&Tt[t * CP_LT + jg * 16 + u4]);
-      acc[u4 + 0] += x * l4.x;
-      acc[u4 + 1] += x * l4.y;
-      acc[u4 + 2] += x * l4.z;
-      acc[u4 + 3] += x * l4.w;
-    }
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] += xv[u] * bv[v];
   }
+}
+
+// P[:, dst .. dst+63] (the CTA's 64 rows) = or -= P[:, src .. src+kb-1] * T^T,
+// T given transposed in Tt (Tt[t * CP_LT + jj] = T[jj][t], zero where unused).
+// The destination is written only after every thread has read its source
+// (src may equal dst).
+__device__ __forceinline__ void cp_gemm64(float* __restrict__ P, int src, int dst, const float* __restrict__ Tt,
+                                          int kb, bool sub) {
+  const int ti = threadIdx.x & 15, tj = threadIdx.x >> 4;
+  float acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+  cp_mma_tile(P + src * 64, Tt, kb, acc);
   __syncthreads();
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    float* d = &P[i + (dst + jg * 16 + u) * 64];
-    *d = sub ? *d - acc[u] : acc[u];
+  for (int v = 0; v < 4; ++v) {
+    float4* d = reinterpret_cast<float4*>(&P[4 * ti + (dst + 4 * tj + v) * 64]);
+    float4 o = *d;
+    if (sub) {
+      o.x -= acc[0][v]; o.y -= acc[1][v]; o.z -= acc[2][v]; o.w -= acc[3][v];
+    } else {
+      o = make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+    }
+    *d = o;
   }
   __syncthreads();
 }
@@ -272,6 +288,243 @@ k_chol_panel(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, 
 }
 
 // ---------------------------------------------------------------------------
+// 1b. the panel's diagonal block and its inverse (panels of 256 columns whose
+//     rows below are solved on the tensor cores)
+// ---------------------------------------------------------------------------
+// The panel's W x W diagonal block (W <= 256, nd <= 4 blocks of 64) is
+// factored by nd CTAs exactly as in k_chol_panel (CTA j owns block row j).
+// Each then forms block row j of the inverse Linv of the factored block:
+//   Linv[j][j] = L_jj^{-1},
+//   Linv[j][i] = -L_jj^{-1} sum_{k=i}^{j-1} L[j][k] Linv[k][i]      (i < j),
+// taking the rows k < j from the CTAs that own them (flag Q[k], FP32
+// exchange area linv32, row-major W1 x W1 per front).  It writes its rows of
+// Linv, split into BF16 hi / lo, as the B operand of the TRSM on the
+// tensor cores (X = A Linv^T for the rows below the block): row c of Linv
+// = row c of B, chunk i = columns 64 i .. 64 i + 63.
+constexpr int CD_W = 256;
+
+struct CdSmem {
+  float P[64 * CD_W];              // the CTA's rows of the diagonal block (columns 0 .. 64 j + 63 used)
+  union {
+    PotrfShared<float> sh;
+    struct {
+      float Lt[64 * CP_LT];
+      float Bt[64 * CP_LT];
+    } t;
+  } u;
+  float Dm[64 * 64];               // L_jj^{-1}, column-major
+  int s_t, s_ok;
+};
+
+// item: front, a = K0, b = j (diagonal block), c = flag offset (D at +0, R at
+// +8, Q at +72); linv_row0: first B-operand row of the front's Linv parts
+__global__ void __launch_bounds__(CP_THREADS, 1)
+k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, int* err,
+            float* __restrict__ linv32, __nv_bfloat16* __restrict__ ws, const int64_t* __restrict__ linv_row0,
+            const int64_t* __restrict__ linv32_off) {
+  extern __shared__ __align__(16) unsigned char cd_raw[];
+  CdSmem& S = *reinterpret_cast<CdSmem*>(cd_raw);
+  const int tid = threadIdx.x;
+  const int ti = tid & 15, tj = tid >> 4;
+  if (tid == 0) S.s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[S.s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, K0 = it.a, rel = it.b;
+  const int W = min(CD_W, fs - K0);
+  const int r0 = K0 + 64 * rel, rows = min(64, W - 64 * rel);
+  int* D = flags + it.c;
+  int* R = D + 8;
+  int* Q = D + 72;
+  float* __restrict__ G = c.a32 + f.off;
+  float* __restrict__ LI = linv32 + linv32_off[it.front];   // Linv, row-major CD_W x CD_W
+  const int ncol = min(W, 64 * (rel + 1));
+  for (int idx = tid; idx < 64 * ncol; idx += CP_THREADS) {
+    const int i = idx & 63, col = idx >> 6;
+    S.P[idx] = i < rows ? G[(r0 + i) + (int64_t)(K0 + col) * n] : 0.f;
+  }
+  __syncthreads();
+  // steps j < rel: as the diagonal owners of k_chol_panel
+  for (int j = 0; j < rel; ++j) {
+    const int cj = 64 * j, kbj = min(64, W - cj);
+    cp_wait(D + j, err, &S.s_ok);
+    {
+      const float* Di = c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + j) * 4096;
+      for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+        const int t = idx >> 6, jj = idx & 63;
+        S.u.t.Lt[t * CP_LT + jj] = (t < kbj && jj < kbj) ? __ldcg(Di + idx) : 0.f;
+      }
+    }
+    __syncthreads();
+    cp_gemm64(S.P, cj, cj, S.u.t.Lt, kbj, false);
+    for (int idx = tid; idx < 64 * kbj; idx += CP_THREADS) {
+      const int i = idx & 63, col = idx >> 6;
+      if (i < rows) G[(r0 + i) + (int64_t)(K0 + cj + col) * n] = S.P[i + (cj + col) * 64];
+    }
+    cp_publish(R + rel * 8 + j);
+    for (int jp = j + 1; jp <= rel; ++jp) {
+      const int cjp = 64 * jp, kbp = min(64, W - cjp);
+      if (jp == rel) {
+        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+          const int t = idx >> 6, jj = idx & 63;
+          S.u.t.Bt[t * CP_LT + jj] = (t < kbj && jj < kbp) ? S.P[jj + (cj + t) * 64] : 0.f;
+        }
+      } else {
+        cp_wait(R + jp * 8 + j, err, &S.s_ok);
+        const int rjp = K0 + cjp;
+        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+          const int t = idx >> 6, jj = idx & 63;
+          S.u.t.Bt[t * CP_LT + jj] =
+              (t < kbj && jj < kbp) ? __ldcg(G + (rjp + jj) + (int64_t)(K0 + cj + t) * n) : 0.f;
+        }
+      }
+      __syncthreads();
+      cp_gemm64(S.P, cj, cjp, S.u.t.Bt, kbj, true);
+    }
+  }
+  // the diagonal block itself
+  const int cr = 64 * rel, kbr = rows;
+  float x[4][4];
+  {
+    bool bad;
+    potrf_block<float>(S.P + cr * 64, 64, kbr, S.u.sh, x, bad, S.P + cr * 64);
+    if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
+    potrf_store_inverse<float>(kbr, x, c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + rel) * 4096);
+  }
+  cp_publish(D + rel);
+  for (int idx = tid; idx < 64 * (cr + kbr); idx += CP_THREADS) {
+    const int i = idx & 63, col = idx >> 6;
+    if (i < rows) G[(r0 + i) + (int64_t)(K0 + col) * n] = S.P[idx];
+  }
+  // L_jj^{-1} (zero outside the block's kbr rows and columns), column-major
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int r = 4 * ti + u, cc = 4 * tj + v;
+      x[u][v] = (r < kbr && cc < kbr) ? x[u][v] : 0.f;
+      S.Dm[r + cc * 64] = x[u][v];
+    }
+  __syncthreads();
+  // block row rel of Linv: columns i = 0 .. rel (the diagonal block last)
+  const int64_t lrow0 = linv_row0[it.front];
+  for (int i = 0; i <= rel; ++i) {
+    float out[4][4];
+    if (i == rel) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) out[u][v] = x[u][v];
+    } else {
+      // T = sum_{k=i}^{rel-1} L[rel][k] Linv[k][i]
+      float acc[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+      for (int k = i; k < rel; ++k) {
+        cp_wait(Q + k, err, &S.s_ok);
+        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+          const int t = idx >> 6, cc = idx & 63;     // Bt row t = row t of Linv[k][i]
+          S.u.t.Bt[t * CP_LT + cc] = __ldcg(LI + (int64_t)(64 * k + t) * CD_W + 64 * i + cc);
+        }
+        __syncthreads();
+        cp_mma_tile(S.P + 64 * k * 64, S.u.t.Bt, 64, acc);
+      }
+      __syncthreads();
+      // out = -L_jj^{-1} T: T as the row-major right operand
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) S.u.t.Bt[(4 * ti + u) * CP_LT + 4 * tj + v] = acc[u][v];
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) out[u][v] = 0.f;
+      cp_mma_tile(S.Dm, S.u.t.Bt, 64, out);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) out[u][v] = -out[u][v];
+      __syncthreads();
+    }
+    // FP32 row block for the later rows, BF16 parts as the B operand
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = 4 * ti + u;
+      *reinterpret_cast<float4*>(LI + (int64_t)(64 * rel + r) * CD_W + 64 * i + 4 * tj) =
+          make_float4(out[u][0], out[u][1], out[u][2], out[u][3]);
+      __align__(8) __nv_bfloat16 hi[4], lo[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        hi[v] = __float2bfloat16_rn(out[u][v]);
+        lo[v] = __float2bfloat16_rn(out[u][v] - __bfloat162float(hi[v]));
+      }
+      const int64_t rh = lrow0 + (int64_t)(0 * 4 + i) * CD_W + 64 * rel + r;
+      const int64_t rl = lrow0 + (int64_t)(1 * 4 + i) * CD_W + 64 * rel + r;
+      *reinterpret_cast<uint2*>(ws + rh * 64 + 4 * tj) = *reinterpret_cast<const uint2*>(hi);
+      *reinterpret_cast<uint2*>(ws + rl * 64 + 4 * tj) = *reinterpret_cast<const uint2*>(lo);
+    }
+  }
+  // chunks right of the diagonal block are zero (Linv is lower triangular)
+  for (int i = rel + 1; i < 4; ++i)
+    for (int idx = tid; idx < 64 * 8; idx += CP_THREADS) {
+      const int r = idx >> 3, q = idx & 7;
+      const int64_t rh = lrow0 + (int64_t)(0 * 4 + i) * CD_W + 64 * rel + r;
+      const int64_t rl = lrow0 + (int64_t)(1 * 4 + i) * CD_W + 64 * rel + r;
+      *reinterpret_cast<uint4*>(ws + rh * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(ws + rl * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
+    }
+  cp_publish(Q + rel);
+}
+
+// BF16 parts (hi, lo) of the panel's rows below its diagonal block, the A
+// operand of the TRSM on the tensor cores: item front, a = K0, b = first row
+// (64 rows), c = chunk of the panel (0 .. nd-1); written chunk-major at
+// row0b[front] + (p * nch + K0 / 64 + c) * n + r.
+__global__ void __launch_bounds__(256) k_chol_pack(DevCtx c, const Item* __restrict__ items,
+                                                   __nv_bfloat16* __restrict__ ws,
+                                                   const int64_t* __restrict__ row0b) {
+  __shared__ float tile[64][65];
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, K0 = it.a, r0 = it.b, cc = it.c;
+  const int W = min(CD_W, f.fs - K0);
+  const int col0 = K0 + 64 * cc, kb = min(64, W - 64 * cc);
+  const float* __restrict__ G = c.a32 + f.off;
+  float v[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int idx = threadIdx.x + 256 * u, i = idx & 63, k = idx >> 6;
+    v[u] = (r0 + i < n && k < kb) ? G[(r0 + i) + (int64_t)(col0 + k) * n] : 0.f;
+  }
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int idx = threadIdx.x + 256 * u;
+    tile[idx & 63][idx >> 6] = v[u];
+  }
+  __syncthreads();
+  const int nch = (f.fs + 63) / 64, kc = K0 / 64 + cc;
+  const int64_t b0 = row0b[it.front];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int idx = threadIdx.x + 256 * h, i = idx >> 3, k8 = (idx & 7) * 8;
+    if (r0 + i >= n) continue;
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float xv = tile[i][k8 + q];
+      hi[q] = __float2bfloat16_rn(xv);
+      lo[q] = __float2bfloat16_rn(xv - __bfloat162float(hi[q]));
+    }
+    *reinterpret_cast<uint4*>(ws + (b0 + (int64_t)kc * n + r0 + i) * 64 + k8) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(ws + (b0 + (int64_t)(nch + kc) * n + r0 + i) * 64 + k8) =
+        *reinterpret_cast<const uint4*>(lo);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // 2./3. tensor-core update over 128 x 256 tiles
 // ---------------------------------------------------------------------------
 constexpr int TCC_BM = 128, TCC_BN = 256, TCC_STAGES = 2;
@@ -282,13 +535,22 @@ constexpr uint32_t TCC_STAGE = 6 * TCC_BOX;  // A hi, A lo (128 rows), B hi, B l
 constexpr uint32_t TCC_SMEM = 1024 + TCC_STAGES * TCC_STAGE + 256;
 constexpr int TCC_ERR = 6;
 
-// item: front, a = first row r0, b = first column c0, c = kc0 | kc1 << 16
-// (chunks [kc0, kc1) of the factor block).  Columns stop at fs for tiles of
-// the factor block (c0 < fs) and at n for tiles of ABR (c0 >= fs); only
-// entries with col <= row are stored (Cholesky keeps the lower triangle).
+// Two modes.
+// mode 0 (update): item front, a = first row r0, b = first column c0,
+// c = kc0 | kc1 << 16 (chunks [kc0, kc1) of the factor block); C -= A B^T
+// with A rows r0.. and B rows c0.. of the packed factor (ws_row0).  Columns
+// stop at fs for tiles of the factor block (c0 < fs) and at n for tiles of
+// ABR (c0 >= fs); only entries with col <= row are stored (Cholesky keeps
+// the lower triangle).
+// mode 1 (TRSM below a panel's diagonal block): item front, a = r0, b = c0
+// (column within the panel), c = K0; X = A Linv^T with A the panel's rows
+// r0.. packed at row0b and B the packed rows c0.. of Linv (linv_row0), K =
+// the panel's width; X is stored over the panel's columns K0 + c0 .. and its
+// BF16 parts into the packed factor (ws_row0) for the updates that follow.
 __global__ void __launch_bounds__(TCC_THREADS, 1)
 k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_row0,
-          const Item* __restrict__ items, int n_items, int* err) {
+          const Item* __restrict__ items, int n_items, int* err, int mode, const int64_t* __restrict__ row0b,
+          const int64_t* __restrict__ linv_row0, __nv_bfloat16* __restrict__ ws) {
   extern __shared__ __align__(1024) uint8_t tcc_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tcc_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TCC_STAGES * TCC_STAGE);
@@ -332,8 +594,29 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         const Item it = items[t];
         const FrontDev f = c.fronts[it.front];
         const int n = f.n, nch = (f.fs + 63) / 64;
-        const int kc0 = it.c & 0xFFFF, kc1 = it.c >> 16;
-        const int64_t row0 = ws_row0[it.front];
+        int kc0, kc1;
+        int64_t ya_h, ya_l, yb_h, yb_l, ya_step, yb_step;   // rows of chunk kc0 and the step per chunk
+        if (mode == 0) {
+          kc0 = it.c & 0xFFFF;
+          kc1 = it.c >> 16;
+          const int64_t row0 = ws_row0[it.front];
+          ya_h = row0 + (int64_t)kc0 * n + it.a;
+          ya_l = row0 + (int64_t)(nch + kc0) * n + it.a;
+          yb_h = row0 + (int64_t)kc0 * n + it.b;
+          yb_l = row0 + (int64_t)(nch + kc0) * n + it.b;
+          ya_step = yb_step = n;
+        } else {
+          const int K0 = it.c;
+          kc0 = 0;
+          kc1 = (min(CD_W, f.fs - K0) + 63) / 64;
+          const int64_t rb = row0b[it.front], rl = linv_row0[it.front];
+          ya_h = rb + (int64_t)(K0 / 64) * n + it.a;
+          ya_l = rb + (int64_t)(nch + K0 / 64) * n + it.a;
+          yb_h = rl + it.b;
+          yb_l = rl + 4 * CD_W + it.b;
+          ya_step = n;
+          yb_step = CD_W;
+        }
         for (int kc = kc0; kc < kc1; ++kc, ++g) {
           const uint32_t s = g % TCC_STAGES;
           if (g >= TCC_STAGES &&
@@ -345,13 +628,13 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
           const uint32_t fb = smem_u32(&bars[s]);
           const uint32_t st = smem_u32(smem + s * TCC_STAGE);
           mbar_expect_tx(fb, TCC_STAGE);
-          const int yh = (int)(row0 + (int64_t)kc * n), yl = (int)(row0 + (int64_t)(nch + kc) * n);
-          tma_load_2d(st + 0 * TCC_BOX, &wsmap, 0, yh + it.a, fb);
-          tma_load_2d(st + 1 * TCC_BOX, &wsmap, 0, yl + it.a, fb);
-          tma_load_2d(st + 2 * TCC_BOX, &wsmap, 0, yh + it.b, fb);
-          tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, yh + it.b + 128, fb);
-          tma_load_2d(st + 4 * TCC_BOX, &wsmap, 0, yl + it.b, fb);
-          tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, yl + it.b + 128, fb);
+          const int64_t da = (int64_t)(kc - kc0) * ya_step, db = (int64_t)(kc - kc0) * yb_step;
+          tma_load_2d(st + 0 * TCC_BOX, &wsmap, 0, (int)(ya_h + da), fb);
+          tma_load_2d(st + 1 * TCC_BOX, &wsmap, 0, (int)(ya_l + da), fb);
+          tma_load_2d(st + 2 * TCC_BOX, &wsmap, 0, (int)(yb_h + db), fb);
+          tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, (int)(yb_h + db + 128), fb);
+          tma_load_2d(st + 4 * TCC_BOX, &wsmap, 0, (int)(yb_l + db), fb);
+          tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, (int)(yb_l + db + 128), fb);
         }
       }
       // the last loads issued (one per stage at most) land before the CTA exits
@@ -367,7 +650,14 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       bool live = true;
       for (int t = blockIdx.x; t < n_items && live; t += gridDim.x, ++i) {
         const Item it = items[t];
-        const int kc0 = it.c & 0xFFFF, kc1 = it.c >> 16;
+        int kc0, kc1;
+        if (mode == 0) {
+          kc0 = it.c & 0xFFFF;
+          kc1 = it.c >> 16;
+        } else {
+          kc0 = 0;
+          kc1 = (min(CD_W, c.fronts[it.front].fs - it.c) + 63) / 64;
+        }
         const int b = i & 1, u = i >> 1;
         if (u >= 1 && !mbar_wait_lim(smem_u32(&acc_empty[b]), (u - 1) & 1, s_abort, err, TCC_ERR, lim)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -413,6 +703,42 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
       const int b = i & 1, u = i >> 1;
       if (!mbar_wait_lim(smem_u32(&acc_full[b]), u & 1, s_abort, err, TCC_ERR, lim)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (mode == 1) {
+        // X = acc over the panel's columns, and its BF16 parts (zero beyond
+        // the panel's width W) for the updates that follow
+        const int K0 = it.c, W = min(CD_W, f.fs - K0), nch = (f.fs + 63) / 64;
+        const int64_t row0 = ws_row0[it.front];
+        const bool rok = row < n && !*s_abort;
+#pragma unroll 1
+        for (int cc = 0; cc < 4; ++cc) {
+          uint32_t v[32];
+          TC_LD32(tmem + ((uint32_t)(quarter * 32) << 16) + b * TCC_BN + half * 128 + cc * 32, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          const int cb = it.b + half * 128 + cc * 32;     // panel column of v[0]
+          if (!rok || cb >= 64 * ((W + 63) / 64)) continue;
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (cb + j < W) G[row + (int64_t)(K0 + cb + j) * n] = __uint_as_float(v[j]);
+          const int kc = K0 / 64 + cb / 64, e0 = cb & 63;
+          __nv_bfloat16* wh = ws + (row0 + (int64_t)kc * n + row) * 64 + e0;
+          __nv_bfloat16* wl = ws + (row0 + (int64_t)(nch + kc) * n + row) * 64 + e0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              const float xv = cb + 8 * q + e < W ? __uint_as_float(v[8 * q + e]) : 0.f;
+              hi[e] = __float2bfloat16_rn(xv);
+              lo[e] = __float2bfloat16_rn(xv - __bfloat162float(hi[e]));
+            }
+            *reinterpret_cast<uint4*>(wh + 8 * q) = *reinterpret_cast<const uint4*>(hi);
+            *reinterpret_cast<uint4*>(wl + 8 * q) = *reinterpret_cast<const uint4*>(lo);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(smem_u32(&acc_empty[b]));
+        continue;
+      }
 #pragma unroll 1
       for (int cc = 0; cc < 4; ++cc) {
         uint32_t v[32];
@@ -484,8 +810,23 @@ void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, 
   else throw std::invalid_argument("chol_panel: panel width must be 256 or 512, got " + std::to_string(w1));
 }
 
+void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,
+                      float* linv32, void* ws, const int64_t* linv_row0, const int64_t* linv32_off, cudaStream_t s) {
+  if (!n_items) return;
+  const int sm = (int)sizeof(CdSmem);
+  cudaFuncSetAttribute(k_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  k_chol_diag<<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, flags, err, linv32, (__nv_bfloat16*)ws, linv_row0,
+                                              linv32_off);
+}
+
+void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws, const int64_t* row0b,
+                      cudaStream_t s) {
+  if (!n_items) return;
+  k_chol_pack<<<n_items, 256, 0, s>>>(c, items, (__nv_bfloat16*)ws, row0b);
+}
+
 void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
-                    int* err, cudaStream_t s) {
+                    int* err, cudaStream_t s, int mode, const int64_t* row0b, const int64_t* linv_row0, void* ws) {
   if (!n_items) return;
   static int n_sm = 0;
   if (!n_sm) {
@@ -496,7 +837,8 @@ void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_r
   }
   cudaFuncSetAttribute(k_tc_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TCC_SMEM);
   const int grid = n_items < n_sm ? n_items : n_sm;
-  k_tc_chol<<<grid, TCC_THREADS, TCC_SMEM, s>>>(c, map, ws_row0, items, n_items, err);
+  k_tc_chol<<<grid, TCC_THREADS, TCC_SMEM, s>>>(c, map, ws_row0, items, n_items, err, mode, row0b, linv_row0,
+                                                (__nv_bfloat16*)ws);
 }
 
 int chol_panel_max_w1() { return 512; }
