@@ -281,7 +281,9 @@ int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh
  * default) factors each panel's diagonal block and its inverse with a
  * cooperative kernel and solves the rows below on the tensor cores, 512
  * factors whole panels with the cooperative kernel, 0 puts these fronts on
- * the step-by-step path.
+ * the step-by-step path; values[7] rows (columns) per CTA of the
+ * flag-driven forward (backward) solves of large Cholesky fronts (64 or
+ * 256).
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

@@ -457,7 +457,7 @@ class Mesh:
 
     # -- kernel-selection thresholds --------------------------------------------
     TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo",
-                "tc_panel")
+                "tc_panel", "solve_rows")
 
     def tunables(self) -> dict:
         v = np.zeros(len(self.TUNABLES), np.int32)

@@ -1268,15 +1268,17 @@ void Engine::build_programs(int method) {
         // one flag-driven launch for every large front of this level (per
         // group of FLAG_NR right-hand sides)
         std::vector<Item> fi, ai;
+        const int RB = tune.solve_rows;     // rows per CTA: 64 (k_fwd_flags) or 256 (k_fwd_flags4)
+        const int per = RB / NB;
         int maxb = 0;
-        for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        for (int s : large) maxb = std::max(maxb, ((fronts[s].fs + NB - 1) / NB + per - 1) / per);
         for (int b = 0; b < maxb; ++b)
           for (int s : large)
-            if (b < (fronts[s].fs + NB - 1) / NB) fi.push_back(Item{s, b, 0, 0});
+            if (b < ((fronts[s].fs + NB - 1) / NB + per - 1) / per) fi.push_back(Item{s, b, 0, 0});
         for (int s : large) {
           const HostFront& f = fronts[s];
-          const int nfb = (f.fs + NB - 1) / NB;
-          for (int k = 0; k * NB < f.ss; ++k) ai.push_back(Item{s, nfb + k, 0, 0});
+          const int nfbr = ((f.fs + NB - 1) / NB + per - 1) / per;
+          for (int k = 0; k * RB < f.ss; ++k) ai.push_back(Item{s, nfbr + k, 0, 0});
         }
         fi.insert(fi.end(), ai.begin(), ai.end());
         int f0 = 1 << 30, f1 = 0;
@@ -1288,6 +1290,7 @@ void Engine::build_programs(int method) {
         for (int q0 = 0; q0 < nr; q0 += FLAG_NR) {
           Op op{OP_FWD_FLAGS, dt, f1 - f0, f0, io, (int)fi.size()};
           op.q0 = q0;
+          op.aux = RB;
           fwd_ops.push_back(op);
         }
         large.clear();
@@ -1323,20 +1326,23 @@ void Engine::build_programs(int method) {
       push(bwd_ops, OP_BWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
       if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
         std::vector<Item> bi;
+        const int per = tune.solve_rows / NB;    // 64-column blocks per CTA (k_bwd_flags4 at 4)
         int maxb = 0;
-        for (int s : large) maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        for (int s : large) maxb = std::max(maxb, ((fronts[s].fs + NB - 1) / NB + per - 1) / per);
         for (int b = maxb - 1; b >= 0; --b)
           for (int s : large)
-            if (b < (fronts[s].fs + NB - 1) / NB) bi.push_back(Item{s, b, 0, 0});
+            if (b < ((fronts[s].fs + NB - 1) / NB + per - 1) / per) bi.push_back(Item{s, b, 0, 0});
         int f0 = 1 << 30, f1 = 0;
         for (int s : large) {
           f0 = std::min(f0, fronts[s].flag_off);
           f1 = std::max(f1, fronts[s].flag_off + (fronts[s].fs + NB - 1) / NB);
         }
         const int64_t io = add_items(bi);
-        for (int q0 = 0; q0 < nr; q0 += (dt == F64 ? FLAG_NR_BWD_F64 : FLAG_NR)) {
+        const int qstep = per > 1 ? FLAG_NR : (dt == F64 ? FLAG_NR_BWD_F64 : FLAG_NR);
+        for (int q0 = 0; q0 < nr; q0 += qstep) {
           Op op{OP_BWD_FLAGS, dt, f1 - f0, f0, io, (int)bi.size()};
           op.q0 = q0;
+          op.aux = tune.solve_rows;
           bwd_ops.push_back(op);
         }
         large.clear();
@@ -1634,12 +1640,20 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
       case OP_POTRF_TRSM: launch_potrf_trsm(ctx, it, op.n_items, op.dtype, stream); break;
       case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
       case OP_FWD_FLAGS:
-        launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                         stream);
+        if (op.aux == 256)
+          launch_fwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                            stream);
+        else
+          launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                           stream);
         break;
       case OP_BWD_FLAGS:
-        launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                         stream);
+        if (op.aux == 256)
+          launch_bwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                            stream);
+        else
+          launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+                           stream);
         break;
       case OP_TC_PACK:
         launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, op.q0, op.aux, stream);
@@ -2215,10 +2229,11 @@ void Engine::set_tunables(const int* v) {
   t.fuse_potrf_trsm = v[4] < 0 ? 0 : v[4];
   t.tc_nbo = v[5];
   t.tc_panel = v[6];
+  t.solve_rows = v[7];
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
       t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64 ||
       (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512) ||
-      (t.tc_panel != 0 && t.tc_panel != 256 && t.tc_panel != 512))
+      (t.tc_panel != 0 && t.tc_panel != 256 && t.tc_panel != 512) || (t.solve_rows != 64 && t.solve_rows != 256))
     fail("set_tunables: value outside the kernels' limits", 7);
   tune = t;
   prec_dirty = true;
@@ -2234,6 +2249,7 @@ void Engine::get_tunables(int* v) const {
   v[4] = tune.fuse_potrf_trsm;
   v[5] = tune.tc_nbo;
   v[6] = tune.tc_panel;
+  v[7] = tune.solve_rows;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -2274,6 +2290,7 @@ int Engine::autotune(int method, int reps) {
   };
   if (!lu) knobs.push_back({&tune.fuse_potrf_trsm, {0, 1, 2, 4}});
   if (!lu) knobs.push_back({&tune.tc_panel, {0, 256, 512}});
+  if (!lu) knobs.push_back({&tune.solve_rows, {64, 256}});
   if (!lu) knobs.push_back({&tune.tc_nbo, {128, 256, 512}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;

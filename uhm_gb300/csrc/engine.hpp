@@ -106,8 +106,10 @@ struct Tunables {
                              // the tensor cores; 512 = panels of 512 columns factored whole by the
                              // cooperative kernel (SIMT in-panel work); 0 = the step-by-step path
                              // of the other tensor-core fronts
+  int solve_rows = 256;      // rows per CTA of the flag-driven forward solve of large Cholesky fronts
+                             // (64 or 256)
 };
-constexpr int N_TUNABLES = 7;
+constexpr int N_TUNABLES = 8;
 
 class Engine {
  public:

@@ -946,6 +946,170 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   }
 }
 
+// Forward solve of large Cholesky fronts with 256-row CTAs.  Item: front,
+// a = B: B < nfb4 (= ceil(nfb / 4)) the factor rows 256 B .. (64-row blocks
+// 4 B .. 4 B + 3, solved here in turn), otherwise the ABL rows
+// fs + 256 (B - nfb4) ...  One thread per row; the row's 64 factor entries of
+// the next column block are loaded into registers before that block's
+// values are waited for.  Column blocks left of the CTA come from other CTAs
+// (their completion flags, one per 64-row block); the CTA's own blocks are
+// solved in order: the block's rows form v = z - (sum so far), y = Dinv v,
+// y is published (its warps fence and raise the flag while the rest of the
+// CTA goes on with the rows below), and every later row of the CTA adds
+// its product with y.  Tickets in item order: every CTA waits only on
+// smaller tickets.
+constexpr int F4_ROWS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_flags4(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
+                                                    int q0) {
+  using CT = T;
+  extern __shared__ __align__(16) unsigned char f4_dyn[];
+  T* dsh = reinterpret_cast<T*>(f4_dyn);          // 4 inverse diagonal blocks, dsh[s][t * 65 + i] = Dinv_s[i][t]
+  __shared__ int s_t, s_ready;
+  __shared__ CT ysh[SF_NR][FB];
+  __shared__ CT vsh[SF_NR][FB];
+  const int tid = threadIdx.x;
+  if (tid == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs;
+  const int nfb = (fs + FB - 1) / FB, nfb4 = (nfb + 3) / 4;
+  const bool factor_cta = it.a < nfb4;
+  const int b0 = factor_cta ? 4 * it.a : nfb;                 // first own 64-row block (factor CTAs)
+  const int ns = factor_cta ? min(4, nfb - b0) : 0;           // own blocks
+  const int r0 = factor_cta ? F4_ROWS * it.a : fs + F4_ROWS * (it.a - nfb4);
+  const int r1 = factor_cta ? min(r0 + F4_ROWS, fs) : min(r0 + F4_ROWS, n);
+  const int row = r0 + tid;
+  const bool rv = row < r1;
+  const int sub = tid >> 6;                                   // own block of this row (factor CTAs)
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = z + (int64_t)n * nr;
+  int* flg = c.flags + f.flag_off;
+  if (factor_cta) {
+    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b0 * FB * FB;
+    for (int idx = tid; idx < ns * FB * FB; idx += 256) {
+      const int s2 = idx / (FB * FB), e = idx % (FB * FB);
+      dsh[s2 * FB * (FB + 1) + (e / FB) * (FB + 1) + e % FB] = Dg[idx];
+    }
+  }
+  CT acc[SF_NR], zr[SF_NR];
+#pragma unroll
+  for (int q = 0; q < SF_NR; ++q) {
+    acc[q] = CT(0);
+    zr[q] = (rv && q0 + q < nr) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);
+  }
+  const int jext = b0;                    // column blocks solved by other CTAs
+  const int jend = factor_cta ? b0 + ns : nfb;
+  // the row's entries of column block j, where this row needs them
+  CT tile[FB];
+  auto load_tile = [&](int j) {
+    const bool need = rv && (j < jext || sub > j - b0);
+    const int kbj = min(FB, fs - j * FB);
+#pragma unroll
+    for (int u = 0; u < FB; ++u) tile[u] = (need && u < kbj) ? (CT)G[row + (int64_t)(j * FB + u) * n] : CT(0);
+  };
+  if (jend > 0) load_tile(0);
+  int ready = 0;                          // external blocks known to be complete: [0, ready)
+  for (int j = 0; j < jend; ++j) {
+    const int kbj = min(FB, fs - j * FB);
+    if (j < jext) {
+      if (j >= ready) {
+        // every thread reaches this together (ready is the same in all of
+        // them); s_ready is read only after ready_range's closing barrier
+        ready_range(flg, j, jext, 1, &s_ready, err);
+        ready = s_ready;
+      }
+      if (tid < 32) {
+        for (int q = 0; q < SF_NR && q0 + q < nr; ++q) {
+          const double* yj = y + j * FB + (int64_t)(q0 + q) * n;
+          for (int cc = tid; cc < FB; cc += 32) ysh[q][cc] = cc < kbj ? (CT)__ldcg(yj + cc) : CT(0);
+        }
+      }
+      __syncthreads();
+    } else {
+      // own block s: v = z - acc on its rows, y = Dinv_s v
+      const int s2 = j - b0;
+      if (sub == s2) {
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q) vsh[q][tid & 63] = (rv && q0 + q < nr) ? zr[q] - acc[q] : CT(0);
+      }
+      __syncthreads();
+      if (sub == s2) {
+        const int i = tid & 63;
+        const T* Ds = dsh + s2 * FB * (FB + 1);
+        CT yv[SF_NR];
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q) yv[q] = CT(0);
+        for (int t = 0; t <= i && t < kbj; ++t) {
+          const CT d = (CT)Ds[t * (FB + 1) + i];
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) yv[q] += d * vsh[q][t];
+        }
+#pragma unroll
+        for (int q = 0; q < SF_NR; ++q) {
+          ysh[q][i] = (i < kbj) ? yv[q] : CT(0);
+          if (rv && q0 + q < nr) y[row + (int64_t)(q0 + q) * n] = (double)yv[q];
+        }
+      }
+      __syncthreads();
+      if (sub == s2) {
+        // this block's warps publish it; the rest of the CTA goes on
+        __threadfence();
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + s2), "r"(64) : "memory");
+        if ((tid & 63) == 0) st_release_gpu(flg + j, 1);
+      }
+    }
+    const bool use = j < jext || sub > j - b0;
+    if constexpr (sizeof(T) == 4) {
+      // FP32: the next block's loads are issued before this block's products
+      CT cur[FB];
+#pragma unroll
+      for (int u = 0; u < FB; ++u) cur[u] = tile[u];
+      if (j + 1 < jend) load_tile(j + 1);
+      if (use) {
+#pragma unroll
+        for (int u = 0; u < FB; ++u)
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) acc[q] += cur[u] * ysh[q][u];
+      }
+    } else {
+      // FP64 (register budget): products first, then the next block's loads
+      if (use) {
+#pragma unroll
+        for (int u = 0; u < FB; ++u)
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) acc[q] += tile[u] * ysh[q][u];
+      }
+      if (j + 1 < jend) load_tile(j + 1);
+    }
+    __syncthreads();
+  }
+  if (!factor_cta && rv) {
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q)
+      if (q0 + q < nr) z[row + (int64_t)(q0 + q) * n] = (double)(zr[q] - acc[q]);
+  }
+}
+
+void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
+                       int n_flags, int* err, int q0, cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
+  if (dtype == F64) {
+    const int sm = (int)(sizeof(double) * 4 * FB * (FB + 1));
+    cudaFuncSetAttribute(k_fwd_flags4<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    k_fwd_flags4<double><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
+  } else {
+    const int sm = (int)(sizeof(float) * 4 * FB * (FB + 1));
+    cudaFuncSetAttribute(k_fwd_flags4<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    k_fwd_flags4<float><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
+  }
+}
+
 // item: front, a = factor block index, tickets in descending block order;
 // right-hand sides q0 .. q0+NQ-1, accumulated in the same pass over the
 // factor tiles (a pass per right-hand side would put NQ-1 un-overlapped
@@ -1083,6 +1247,183 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) st_release_gpu(c.flags + f.flag_off + b, 1);
+}
+
+// Backward solve of large Cholesky fronts with 256-column CTAs.  Item:
+// front, a = B, the factor columns 256 B .. (64-column blocks 4 B .. 4 B + 3);
+// tickets in descending B.  One thread per column accumulates
+// sum_r L[r][col] x_r over the rows below the CTA's blocks: 32-row chunks of
+// L are loaded coalesced (a warp reads 32 consecutive rows of a column)
+// into registers one chunk ahead, staged in shared memory and read along
+// the row.  Order: the ABL rows (x known from the parent), the factor rows
+// of later CTAs as their flags arrive (last block first), then the CTA's own
+// blocks from the last one down: x_s = Dinv_s^T (y_s - sum), published (its
+// warps fence and raise the flag while the rest go on), and its rows are
+// added into the columns left of it.
+constexpr int B4_CH = 32;          // rows per chunk
+
+template <typename T, int NQ>
+__global__ void __launch_bounds__(256) k_bwd_flags4(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
+                                                    int q0) {
+  using CT = T;
+  extern __shared__ __align__(16) unsigned char b4_dyn[];
+  T* dsh = reinterpret_cast<T*>(b4_dyn);                          // 4 x 64 x 65: dsh[s][t * 65 + i] = Dinv_s[i][t]
+  T* tile = dsh + 4 * FB * (FB + 1);                              // B4_CH x 257
+  __shared__ CT xs[NQ][B4_CH];
+  __shared__ CT vsh[NQ][FB];
+  __shared__ int s_t, s_ready;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs;
+  const int nfb = (fs + FB - 1) / FB;
+  const int b0 = 4 * it.a, ns = min(4, nfb - b0);
+  const int c0 = FB * b0, c1 = min(c0 + 4 * FB, fs);
+  const int col = c0 + tid;
+  const bool cv = col < c1;
+  const int sub = tid >> 6;
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
+  int* flg = c.flags + f.flag_off;
+  {
+    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b0 * FB * FB;
+    for (int idx = tid; idx < ns * FB * FB; idx += 256) {
+      const int s2 = idx / (FB * FB), e = idx % (FB * FB);
+      dsh[s2 * FB * (FB + 1) + (e / FB) * (FB + 1) + e % FB] = Dg[idx];
+    }
+  }
+  CT acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) acc[q] = CT(0);
+  // chunk list: ABL rows, then later factor blocks (last first), then own blocks (last first)
+  const int n_abl = (n - fs + B4_CH - 1) / B4_CH;
+  const int n_ext_blk = nfb - (b0 + ns);
+  const int n_chunks = n_abl + 2 * n_ext_blk + 2 * ns;
+  auto chunk_row = [&](int k) -> int {       // first row of chunk k
+    if (k < n_abl) return fs + B4_CH * k;
+    k -= n_abl;
+    if (k < 2 * n_ext_blk) return FB * (nfb - 1 - k / 2) + B4_CH * (k & 1);
+    k -= 2 * n_ext_blk;
+    return FB * (b0 + ns - 1 - k / 2) + B4_CH * (k & 1);
+  };
+  auto chunk_end = [&](int k) -> int {       // end of the rows that chunk k may hold
+    if (k < n_abl) return n;
+    k -= n_abl;
+    const int blk = k < 2 * n_ext_blk ? nfb - 1 - k / 2 : b0 + ns - 1 - (k - 2 * n_ext_blk) / 2;
+    return min(FB * (blk + 1), fs);
+  };
+  // this thread's 32 values of a chunk: warp w takes columns 32 w .. 32 w + 31, lane = row
+  CT reg[B4_CH];
+  auto load_chunk = [&](int k) {
+    const int r = chunk_row(k) + lane, re = chunk_end(k);
+#pragma unroll
+    for (int u = 0; u < B4_CH; ++u) {
+      const int cc = c0 + 32 * warp + u;
+      reg[u] = (r < re && cc < c1) ? (CT)G[r + (int64_t)cc * n] : CT(0);
+    }
+  };
+  if (n_chunks > 0) load_chunk(0);
+  int ready = nfb;                              // factor blocks >= ready are known complete
+  for (int k = 0; k < n_chunks; ++k) {
+    const int rk = chunk_row(k), re = chunk_end(k);
+    __syncthreads();                            // the previous chunk's tile has been read
+#pragma unroll
+    for (int u = 0; u < B4_CH; ++u) tile[lane * (4 * FB + 1) + 32 * warp + u] = reg[u];
+    if (k + 1 < n_chunks) load_chunk(k + 1);
+    const bool ext = k >= n_abl && k < n_abl + 2 * n_ext_blk;
+    const bool own = k >= n_abl + 2 * n_ext_blk;
+    const int blk = rk / FB;
+    if (ext && blk < ready) {
+      // every thread reaches this together; s_ready is read after ready_range's barrier
+      ready_range(flg, blk, b0 + ns - 1, -1, &s_ready, err);
+      ready = s_ready + 1;
+    }
+    if (own && (rk % FB) == 0) {
+      // own block s: its columns are complete once the rows below have been added
+      const int s2 = blk - b0, kbs = min(FB, fs - FB * blk);
+      if (sub == s2) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+          vsh[q][tid & 63] = (cv && q0 + q < nr) ? (CT)y[col + (int64_t)(q0 + q) * n] - acc[q] : CT(0);
+      }
+      __syncthreads();
+      CT xv[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) xv[q] = CT(0);
+      if (sub == s2) {
+        const int i = tid & 63;
+        const T* Ds = dsh + s2 * FB * (FB + 1);
+        for (int t = i; t < kbs; ++t) {
+          const CT d = (CT)Ds[i * (FB + 1) + t];     // Dinv_s[t][i]
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) xv[q] += d * vsh[q][t];
+        }
+      }
+      __syncthreads();                            // every v read before x replaces it
+      if (sub == s2) {
+        const int i = tid & 63;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          vsh[q][i] = i < kbs ? xv[q] : CT(0);
+          if (cv && q0 + q < nr) y[col + (int64_t)(q0 + q) * n] = (double)xv[q];
+        }
+      }
+      __syncthreads();
+      if (sub == s2) {
+        __threadfence();
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + s2), "r"(64) : "memory");
+        if ((tid & 63) == 0) st_release_gpu(flg + blk, 1);
+      }
+    }
+    // x of the chunk's rows
+    if (own) {
+      if (tid < B4_CH) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) xs[q][tid] = rk + tid < re ? vsh[q][(rk % FB) + tid] : CT(0);
+      }
+    } else if (tid < B4_CH) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+        xs[q][tid] = (rk + tid < re && q0 + q < nr) ? (CT)__ldcg(y + rk + tid + (int64_t)(q0 + q) * n) : CT(0);
+    }
+    __syncthreads();
+    // own rows add only into the columns left of their block
+    if (!own || tid < (blk - b0) * FB) {
+#pragma unroll 8
+      for (int r = 0; r < B4_CH; ++r) {
+        const CT lv = tile[r * (4 * FB + 1) + tid];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] += lv * xs[q][r];
+      }
+    }
+  }
+}
+
+template <typename T, int NQ>
+static void bwd_flags4_nq(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                          cudaStream_t s) {
+  const size_t dyn = sizeof(T) * (4 * FB * (FB + 1) + B4_CH * (4 * FB + 1));
+  cudaFuncSetAttribute(k_bwd_flags4<T, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  k_bwd_flags4<T, NQ><<<n_items, 256, dyn, s>>>(c, items, ticket, err, q0);
+}
+
+void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
+                       int n_flags, int* err, int q0, cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
+  const int nq = c.n_rhs - q0 < FLAG_NR ? c.n_rhs - q0 : FLAG_NR;
+  if (dtype == F64) {
+    if (nq >= 4) bwd_flags4_nq<double, 4>(c, items, n_items, ticket, err, q0, s);
+    else if (nq >= 2) bwd_flags4_nq<double, 2>(c, items, n_items, ticket, err, q0, s);
+    else bwd_flags4_nq<double, 1>(c, items, n_items, ticket, err, q0, s);
+  } else {
+    if (nq >= 4) bwd_flags4_nq<float, 4>(c, items, n_items, ticket, err, q0, s);
+    else if (nq >= 2) bwd_flags4_nq<float, 2>(c, items, n_items, ticket, err, q0, s);
+    else bwd_flags4_nq<float, 1>(c, items, n_items, ticket, err, q0, s);
+  }
 }
 
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
