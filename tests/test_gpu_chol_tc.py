@@ -49,6 +49,8 @@ CASES = [
     ("diff_8_p3_w512", lambda: hpfem.diffusion3d(8, 3, seed=33, contrast=1e3), 512),
     # two right-hand sides and a 3-way top merge (one large root front)
     ("3d_6_p4_merge32_rhs2", lambda: hpfem.poisson3d(6, 4, seed=34, merges=[3, 2], n_rhs=2), 256),
+    # seven right-hand sides: the solves' second group holds three
+    ("3d_6_p3_rhs7", lambda: hpfem.poisson3d(6, 3, seed=38, n_rhs=7), 256),
 ]
 
 

@@ -1415,13 +1415,14 @@ void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtyp
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
   cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
   const int nq = c.n_rhs - q0 < FLAG_NR ? c.n_rhs - q0 : FLAG_NR;
+  // NQ covers every right-hand side of the group (3 of them take the 4-wide kernel)
   if (dtype == F64) {
-    if (nq >= 4) bwd_flags4_nq<double, 4>(c, items, n_items, ticket, err, q0, s);
-    else if (nq >= 2) bwd_flags4_nq<double, 2>(c, items, n_items, ticket, err, q0, s);
+    if (nq >= 3) bwd_flags4_nq<double, 4>(c, items, n_items, ticket, err, q0, s);
+    else if (nq == 2) bwd_flags4_nq<double, 2>(c, items, n_items, ticket, err, q0, s);
     else bwd_flags4_nq<double, 1>(c, items, n_items, ticket, err, q0, s);
   } else {
-    if (nq >= 4) bwd_flags4_nq<float, 4>(c, items, n_items, ticket, err, q0, s);
-    else if (nq >= 2) bwd_flags4_nq<float, 2>(c, items, n_items, ticket, err, q0, s);
+    if (nq >= 3) bwd_flags4_nq<float, 4>(c, items, n_items, ticket, err, q0, s);
+    else if (nq == 2) bwd_flags4_nq<float, 2>(c, items, n_items, ticket, err, q0, s);
     else bwd_flags4_nq<float, 1>(c, items, n_items, ticket, err, q0, s);
   }
 }
@@ -1446,8 +1447,8 @@ static void bwd_flags_nq(const DevCtx& c, const Item* items, int n_items, int* t
 template <typename T>
 static void bwd_flags_t(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
                         int nq, cudaStream_t s) {
-  if (nq >= 4) bwd_flags_nq<T, 4>(c, items, n_items, ticket, err, q0, s);
-  else if (nq >= 2) bwd_flags_nq<T, 2>(c, items, n_items, ticket, err, q0, s);
+  if (nq >= 3) bwd_flags_nq<T, 4>(c, items, n_items, ticket, err, q0, s);
+  else if (nq == 2) bwd_flags_nq<T, 2>(c, items, n_items, ticket, err, q0, s);
   else bwd_flags_nq<T, 1>(c, items, n_items, ticket, err, q0, s);
 }
 
