@@ -46,10 +46,12 @@ METRIC = "factor+solve s at 16³ p=4: plain FP64 vs mixed+IR+learned, bwd err≤
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of its first
 # root-level launch on the 12^3 p=4 profiling case (trailing block above the
 # L2 size); scaled to the bench's launches by their algorithmic bytes
-TC_TRAFFIC_PER_ALG_BYTE = 0.916
-TC_TRAFFIC_SOURCE = ("ncu --set full, k_tc_syrk first root-level launch of 3D Poisson 12^3 p=4 "
-                     "(578.8 MB DRAM read+write for 632.0 MB algorithmic), scaled by algorithmic bytes; "
-                     "profiles/tc_syrk_bf16_poisson3d_12_p4_root.md")
+# DRAM traffic of the Schur-update launch per algorithmic byte, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of k_tc_chol's ABR
+# launch on a smaller mesh, scaled to the bench's launch by its algorithmic
+# bytes (None until captured)
+SCHUR_TRAFFIC_PER_ALG_BYTE = None
+SCHUR_TRAFFIC_SOURCE = "not captured"
 WORKLOAD = "3D Poisson 16^3 hex p=4 Legendre-hierarchic, Dirichlet, octree ND, Cholesky fronts, 1 RHS"
 
 
@@ -292,33 +294,37 @@ def run_gpu(args):
     one_step(m)
     prof = m.profile()
     m.set_profiling(False)
-    # Roofline of the dominant contraction, the BF16-split Schur update
-    # (tcgen05).  With 256-wide outer panels every 128 x 128 tile does
-    # 2 * 256 algorithmic flops per 8 bytes of FP32 C read-modify-write (64
-    # flop/B, below the GPU's ~300 flop/B balance), so its bound is HBM:
-    # achieved = algorithmic bytes per launch (C lower triangle read + write,
-    # packed panel parts read once) / average launch time.  The tensor-pipe
-    # view is kept beside it: algorithmic flops / time against the BF16 peak,
-    # times the number of split products per algorithmic one.
-    tc_name = "tc_syrk_bf16"
-    if tc_name in prof and prof[tc_name]["ms"] > 0:
-        p = prof[tc_name]
-        terms = 6 if args.prec == api.PREC_BF16X6 else 3
+    # Roofline of the Schur update ABR -= ABL ABL^T (the contraction the
+    # metric names), k_tc_chol over the ABR tiles of every tensor-core front
+    # with K = fs in one pass.  Each algorithmic flop is three BF16 products
+    # (hi*hi + hi*lo + lo*hi) on the tensor cores, so the peak it is held
+    # against is a third of the measured dense BF16 rate (the BF16X3
+    # emulated-FP32 peak); mma_frac is the tensor pipe's own share.
+    # achieved = LAWN-41 SYRK flops of the launch / its CUDA-event time.
+    bf16_peak = float(peaks.get("bf16_tflops"))
+    terms = 3
+    if "tc_chol_schur" in prof and prof["tc_chol_schur"]["ms"] > 0:
+        p = prof["tc_chol_schur"]
         nl = max(1, p["launches"])
-        t_launch = p["ms"] * 1e-3 / nl
-        achieved = p["bytes"] / nl / t_launch / 1e9
         tflops = p["flops"] / (p["ms"] * 1e-3) / 1e12
-        bf16_peak = float(peaks.get("bf16_tflops"))
-        traffic = None
-        if TC_TRAFFIC_PER_ALG_BYTE is not None:
-            traffic = TC_TRAFFIC_PER_ALG_BYTE * p["bytes"] / nl
-        roof = {"bound": "hbm", "kernel": tc_name, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                "algorithmic_bytes_per_launch": p["bytes"] / nl, "us_per_launch": 1e6 * t_launch,
-                "launches": p["launches"], "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_src})",
-                "traffic_source": TC_TRAFFIC_SOURCE,
-                "tensor": {"achieved_tflops": tflops, "peak_tflops": bf16_peak, "frac": tflops / bf16_peak,
-                           "mma_frac": terms * tflops / bf16_peak, "split_terms": terms}}
+        eff_peak = bf16_peak / terms
+        traffic = SCHUR_TRAFFIC_PER_ALG_BYTE * p["bytes"] / nl if SCHUR_TRAFFIC_PER_ALG_BYTE else None
+        roof = {"bound": "tensor", "kernel": "tc_chol_schur", "achieved": tflops, "peak": eff_peak,
+                "unit": "TFLOP/s", "frac": tflops / eff_peak, "traffic": traffic,
+                "traffic_unit": "bytes per launch (dram read+write)",
+                "algorithmic_flops_per_launch": p["flops"] / nl, "us_per_launch": 1e3 * p["ms"] / nl,
+                "launches": p["launches"],
+                "peak_source": f"bf16_tflops of MEASURED_PEAKS.json ({peak_src}) / 3 BF16 products per algorithmic flop",
+                "traffic_source": SCHUR_TRAFFIC_SOURCE,
+                "tensor": {"achieved_tflops": tflops, "peak_tflops": bf16_peak, "mma_frac": terms * tflops / bf16_peak,
+                           "split_terms": terms}}
+        if "tc_chol_trail" in prof and prof["tc_chol_trail"]["ms"] > 0:
+            q = prof["tc_chol_trail"]
+            ttf = q["flops"] / (q["ms"] * 1e-3) / 1e12
+            roof["trailing_update"] = {"kernel": "tc_chol_trail", "achieved_tflops": ttf,
+                                       "mma_frac": terms * ttf / bf16_peak,
+                                       "gbs": q["bytes"] / (q["ms"] * 1e-3) / 1e9,
+                                       "hbm_frac": q["bytes"] / (q["ms"] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
     else:
         name, p = max(prof.items(), key=lambda kv: kv[1]["ms"])
         achieved = p["bytes"] / (p["ms"] * 1e-3) / 1e9

@@ -283,7 +283,8 @@ int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh
  * factors whole panels with the cooperative kernel, 0 puts these fronts on
  * the step-by-step path; values[7] rows (columns) per CTA of the
  * flag-driven forward (backward) solves of large Cholesky fronts (64 or
- * 256).
+ * 256), values[8] 1: with panels of 256, the next panel's diagonal kernel
+ * runs on a second stream beside the current panel's trailing update.
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

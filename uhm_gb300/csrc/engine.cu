@@ -42,6 +42,8 @@ Engine::~Engine() {
   } catch (...) {
   }
   release_staging();
+  for (cudaEvent_t e : evpool) cudaEventDestroy(e);
+  if (stream2) cudaStreamDestroy(stream2);
   if (stream) cudaStreamDestroy(stream);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
@@ -1077,36 +1079,60 @@ void Engine::build_programs(int method) {
       if (!tccf.empty() && tune.tc_panel == CD_PANEL) {
         // panels of 256 columns: diagonal block + its inverse (cooperative,
         // nd CTAs per front), BF16 parts of the rows below, X = A Linv^T on
-        // the tensor cores (X and its parts written), trailing update
+        // the tensor cores (X and its parts written), trailing update.
+        // Lookahead: the trailing update first covers the next panel's
+        // diagonal block, then the next panel's diagonal kernel runs on the
+        // side stream while the rest of the trailing update (on SMs left
+        // free for it) and the next panel's packing run on the main stream.
         const int W1 = CD_PANEL;
         const int TM = TCC_TILE_M, TN = TCC_TILE_N;
         int maxfs_c = 0;
         for (int s : tccf) maxfs_c = std::max(maxfs_c, fronts[s].fs);
-        for (int K0 = 0; K0 < maxfs_c; K0 += W1) {
+        const int n_panels = (maxfs_c + W1 - 1) / W1;
+        // the diagonal launch of panel p (items and flags)
+        auto diag_op = [&](int K0) {
           std::vector<int> act;
           for (int s : tccf)
             if (fronts[s].fs > K0) act.push_back(s);
           const int64_t tick = pf++;
-          std::vector<Item> dit, pit, xit, tt;
-          double fp = 0, fx = 0, bx = 0, ft = 0, bt = 0, bp = 0;
-          for (int rel = 0; rel < 4; ++rel)
-            for (int sl : act) {
-              const HostFront& f = fronts[sl];
-              const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
-              (void)nd;
-              if (rel < (W + 63) / 64) dit.push_back(Item{sl, K0, rel, 0});
-            }
           std::vector<int64_t> foff(fronts.size(), 0);
           for (int sl : act) {
             foff[sl] = pf;
             pf += CP_FLAGS_PER_FRONT;
           }
-          for (Item& d : dit) d.c = (int)foff[d.front];
+          std::vector<Item> dit;
+          double fp = 0;
+          for (int rel = 0; rel < 4; ++rel)
+            for (int sl : act) {
+              const int W = std::min(W1, fronts[sl].fs - K0);
+              if (rel < (W + 63) / 64) dit.push_back(Item{sl, K0, rel, (int)foff[sl]});
+            }
+          for (int sl : act) fp += get_flop_chol(0, std::min(W1, fronts[sl].fs - K0));
+          Op op{OP_CHOL_DIAG, F32, W1, (int)tick, add_items(dit), (int)dit.size()};
+          op.flops = fp;
+          op.aux = (int)dit.size();          // CTAs: the SMs a concurrent update leaves free
+          return op;
+        };
+        auto ev_op = [&](int kind, int id, int strm) {
+          Op op{kind, 0, 0, id, 0, 0};
+          op.strm = strm;
+          return op;
+        };
+        const bool la = tune.lookahead != 0;
+        Op d0 = diag_op(0);
+        fac_ops.push_back(d0);
+        for (int p = 0; p < n_panels; ++p) {
+          const int K0 = p * W1;
+          std::vector<int> act;
+          for (int s : tccf)
+            if (fronts[s].fs > K0) act.push_back(s);
+          std::vector<Item> pit, xit, tdiag, trest;
+          double fx = 0, bx = 0, fd = 0, bd = 0, fr = 0, br = 0, bp = 0;
+          bool next = false;
           for (int sl : act) {
             const HostFront& f = fronts[sl];
             const int W = std::min(W1, f.fs - K0), nd = (W + 63) / 64;
             const int base = K0 + W;
-            fp += get_flop_chol(0, W);
             for (int r0 = base; r0 < f.n; r0 += 64)
               for (int cc = 0; cc < nd; ++cc) pit.push_back(Item{sl, K0, r0, cc});
             bp += (double)(f.n - base) * W * (4.0 + 4.0);
@@ -1114,24 +1140,43 @@ void Engine::build_programs(int method) {
             fx += get_flop_trsm_lower(0, W, f.n - base);
             bx += (double)(f.n - base) * 64.0 * nd * (4.0 + 4.0 + 4.0);
             if (base < f.fs) {
+              next = true;
               const int kc0 = K0 / 64, kc1 = kc0 + nd;
+              const int dnext = base + std::min(W1, f.fs - base);   // end of the next diagonal block
               for (int r0 = base; r0 < f.n; r0 += TM)
-                for (int c0 = base; c0 < f.fs && c0 <= r0 + TM - 1; c0 += TN)
-                  tt.push_back(Item{sl, r0, c0, kc0 | (kc1 << 16)});
-              const double w = f.fs - base, m = f.n - base;
-              const double area = w * m - 0.5 * w * (w - 1);
-              ft += 2.0 * W * area;
-              bt += 8.0 * area + 2.0 * 2.0 * m * 64.0 * nd;
+                for (int c0 = base; c0 < f.fs && c0 <= r0 + TM - 1; c0 += TN) {
+                  const Item t{sl, r0, c0, kc0 | (kc1 << 16)};
+                  const bool in_next_diag = la && c0 == base && r0 < dnext;
+                  const double rows = std::min(TM, f.n - r0), cols = std::min(TN, f.fs - c0);
+                  const double fl = 2.0 * W * rows * cols, by = 8.0 * rows * cols + 2.0 * 2.0 * (rows + cols) * 64.0 * nd;
+                  if (in_next_diag) { tdiag.push_back(t); fd += fl; bd += by; }
+                  else { trest.push_back(t); fr += fl; br += by; }
+                }
             }
           }
-          {
-            Op op{OP_CHOL_DIAG, F32, W1, (int)tick, add_items(dit), (int)dit.size()};
-            op.flops = fp;
-            fac_ops.push_back(op);
-          }
           push(fac_ops, OP_CHOL_PACK, F32, 0, 0, pit, 0, bp);
+          if (p > 0 && la) fac_ops.push_back(ev_op(OP_EV_WAIT, 2 * p, 0));   // diagonal kernel of panel p done
           push(fac_ops, OP_TC_CHOL_TRSM, F32, 0, 0, xit, fx, bx);
-          push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tt, ft, bt);
+          if (next && la) {
+            push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tdiag, fd, bd);
+            fac_ops.push_back(ev_op(OP_EV_RECORD, 2 * p + 1, 0));
+            fac_ops.push_back(ev_op(OP_EV_WAIT, 2 * p + 1, 1));
+            Op dn = diag_op(K0 + W1);
+            dn.strm = 1;
+            const int reserve = std::min(dn.aux, 16);
+            fac_ops.push_back(dn);
+            fac_ops.push_back(ev_op(OP_EV_RECORD, 2 * (p + 1), 1));
+            Op tr{OP_TC_CHOL_TRAIL, F32, 0, 0, add_items(trest), (int)trest.size()};
+            tr.flops = fr;
+            tr.bytes = br;
+            tr.q0 = reserve;
+            if (!trest.empty()) fac_ops.push_back(tr);
+          } else {
+            std::vector<Item> tt = tdiag;
+            tt.insert(tt.end(), trest.begin(), trest.end());
+            push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tt, fd + fr, bd + br);
+            if (next) fac_ops.push_back(diag_op(K0 + W1));
+          }
         }
         std::vector<Item> tt;
         double ft = 0, bt = 0;
@@ -1382,6 +1427,7 @@ void Engine::alloc_device(int method) {
   free_device();
   if (!stream) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
   }
@@ -1612,7 +1658,7 @@ void Engine::run_ops(const std::vector<Op>& ops, double* g_in, double* g_out) {
     cudaGraphDestroy(g);
   }
   CK(cudaGraphLaunch(ge->exec, stream));
-  timing.kernel_launches += (int64_t)ops.size();
+  for (const Op& op : ops) timing.kernel_launches += is_kernel_op(op.kind) ? 1 : 0;
 }
 
 void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out, const uhm_gpu::Item* base) {
@@ -1625,85 +1671,104 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
   for (const Op& op : ops) {
     const Item* it = (base ? base : d_items) + op.item_off;
     if (profiling) CK(cudaEventRecord(evs[2 * k], stream));
+    // the side stream only when not profiling (profiled launches are serial)
+    const cudaStream_t st = (op.strm && !profiling) ? stream2 : stream;
+    if (op.kind == OP_EV_RECORD || op.kind == OP_EV_WAIT) {
+      if (!profiling) {
+        while ((int)evpool.size() <= op.param) {
+          cudaEvent_t e;
+          CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+          evpool.push_back(e);
+        }
+        if (op.kind == OP_EV_RECORD) CK(cudaEventRecord(evpool[op.param], st));
+        else CK(cudaStreamWaitEvent(st, evpool[op.param], 0));
+      }
+      if (profiling) CK(cudaEventRecord(evs[2 * k + 1], stream));
+      ++k;
+      continue;
+    }
     switch (op.kind) {
-      case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, stream); break;
+      case OP_ASSEMBLE: launch_assemble(ctx, it, op.n_items, op.dtype, op.param, st); break;
       case OP_ASSEMBLE_SCATTER:
-        launch_assemble_scatter(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream);
+        launch_assemble_scatter(ctx, it, op.n_items, op.dtype, op.param, op.nb, st);
         break;
       case OP_SMALL_FACTOR:
         launch_small_factor(ctx, it, op.n_items, op.dtype,
                             ctx.symmetric ? M_CHOL : (method_built == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV),
-                            op.param, stream);
+                            op.param, st);
         break;
-      case OP_POTRF: launch_potrf_diag(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
-      case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
-      case OP_POTRF_TRSM: launch_potrf_trsm(ctx, it, op.n_items, op.dtype, stream); break;
-      case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
+      case OP_POTRF: launch_potrf_diag(ctx, it, op.n_items, op.dtype, op.nb, st); break;
+      case OP_TRSM: launch_trsm_panel(ctx, it, op.n_items, op.dtype, op.nb, st); break;
+      case OP_POTRF_TRSM: launch_potrf_trsm(ctx, it, op.n_items, op.dtype, st); break;
+      case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, st); break;
       case OP_FWD_FLAGS:
         if (op.aux == 256)
           launch_fwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                            stream);
+                            st);
         else
           launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                           stream);
+                           st);
         break;
       case OP_BWD_FLAGS:
         if (op.aux == 256)
           launch_bwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                            stream);
+                            st);
         else
           launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                           stream);
+                           st);
         break;
       case OP_TC_PACK:
-        launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, op.q0, op.aux, stream);
+        launch_tc_pack(ctx, it, op.n_items, op.nb, op.param, d_ws, d_ws_off, d_ws_stride, op.q0, op.aux, st);
         break;
       case OP_TC_SYRK:
         launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, op.param == 3 ? 6 : 3,
-                       op.param == 3 ? TC_TERMS_BF16X6 : TC_TERMS_BF16X3, 1, d_err, stream);
+                       op.param == 3 ? TC_TERMS_BF16X6 : TC_TERMS_BF16X3, 1, d_err, st);
         break;
-      case OP_GETRF: launch_getrf_panel(ctx, it, op.n_items, op.dtype, op.nb, op.param, stream); break;
+      case OP_GETRF: launch_getrf_panel(ctx, it, op.n_items, op.dtype, op.nb, op.param, st); break;
       case OP_GETRF_COOP:
         launch_getrf_coop(ctx, it, op.n_items, op.q0, op.dtype, op.nb, op.param, op.aux, d_gc_xbuf, d_gc_ctr, d_err,
-                          stream);
+                          st);
         break;
-      case OP_LASWP: launch_laswp(ctx, it, op.n_items, op.dtype, op.nb, stream); break;
-      case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, stream); break;
-      case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, op.q0, op.aux, stream); break;
+      case OP_LASWP: launch_laswp(ctx, it, op.n_items, op.dtype, op.nb, st); break;
+      case OP_LUROW: launch_lu_row_update(ctx, it, op.n_items, op.dtype, op.nb, 0, st); break;
+      case OP_GEMM: launch_gemm_update(ctx, it, op.n_items, op.dtype, op.nb, op.q0, op.aux, st); break;
       case OP_TC_GEMM:
         launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, 3, TC_TERMS_LU_BF16X3, 0, d_err,
-                       stream);
+                       st);
         break;
-      case OP_CLEAR_FLAGS: CK(cudaMemsetAsync(d_pflags, 0, sizeof(int) * (size_t)op.q0, stream)); break;
+      case OP_CLEAR_FLAGS: CK(cudaMemsetAsync(d_pflags, 0, sizeof(int) * (size_t)op.q0, st)); break;
       case OP_CHOL_PANEL:
         launch_chol_panel(ctx, it, op.n_items, op.nb, d_pflags + op.param, d_pflags, d_err, d_ws2, d_ws2_row0,
-                          stream);
+                          st);
         break;
       case OP_TC_CHOL_TRAIL:
-      case OP_TC_CHOL_SCHUR: launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, stream); break;
+      case OP_TC_CHOL_SCHUR:
+        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, st, 0, nullptr, nullptr, nullptr,
+                       profiling ? 0 : op.q0);
+        break;
       case OP_CHOL_DIAG:
         launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_linv32, d_ws2, d_linv_row0,
-                         d_linv32_off, stream);
+                         d_linv32_off, st);
         break;
-      case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, stream); break;
+      case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, st); break;
       case OP_TC_CHOL_TRSM:
-        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, stream, 1, d_ws2b_row0, d_linv_row0, d_ws2);
+        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, st, 1, d_ws2b_row0, d_linv_row0, d_ws2);
         break;
-      case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, stream); break;
-      case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, stream); break;
-      case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, stream); break;
-      case OP_BWD_PREP: launch_bwd_prepare(ctx, it, op.n_items, 0, op.param, g_out, n_global, stream); break;
+      case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, st); break;
+      case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, st); break;
+      case OP_TRSV_F: launch_fwd_step(ctx, it, op.n_items, op.dtype, op.param, st); break;
+      case OP_BWD_PREP: launch_bwd_prepare(ctx, it, op.n_items, 0, op.param, g_out, n_global, st); break;
       case OP_BWD_SMALL:
-        launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, op.nb, stream);
+        launch_bwd_small(ctx, it, op.n_items, op.dtype, op.param, g_out, n_global, op.nb, st);
         break;
       case OP_TRSV_B:
-        launch_bwd_step(ctx, it, op.n_items, op.dtype, op.param, d_scratch, d_scr_off, d_counters, stream);
+        launch_bwd_step(ctx, it, op.n_items, op.dtype, op.param, d_scratch, d_scr_off, d_counters, st);
         break;
-      case OP_BWD_STORE: launch_bwd_store(ctx, it, op.n_items, g_out, n_global, stream); break;
+      case OP_BWD_STORE: launch_bwd_store(ctx, it, op.n_items, g_out, n_global, st); break;
     }
     if (profiling) CK(cudaEventRecord(evs[2 * k + 1], stream));
     ++k;
-    if (op.kind != OP_CLEAR_FLAGS) timing.kernel_launches++;
+    if (is_kernel_op(op.kind)) timing.kernel_launches++;
   }
   CK(cudaGetLastError());
   if (profiling) {
@@ -2230,6 +2295,7 @@ void Engine::set_tunables(const int* v) {
   t.tc_nbo = v[5];
   t.tc_panel = v[6];
   t.solve_rows = v[7];
+  t.lookahead = v[8] ? 1 : 0;
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
       t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64 ||
       (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512) ||
@@ -2250,6 +2316,7 @@ void Engine::get_tunables(int* v) const {
   v[5] = tune.tc_nbo;
   v[6] = tune.tc_panel;
   v[7] = tune.solve_rows;
+  v[8] = tune.lookahead;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -2291,6 +2358,7 @@ int Engine::autotune(int method, int reps) {
   if (!lu) knobs.push_back({&tune.fuse_potrf_trsm, {0, 1, 2, 4}});
   if (!lu) knobs.push_back({&tune.tc_panel, {0, 256, 512}});
   if (!lu) knobs.push_back({&tune.solve_rows, {64, 256}});
+  if (!lu) knobs.push_back({&tune.lookahead, {0, 1}});
   if (!lu) knobs.push_back({&tune.tc_nbo, {128, 256, 512}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;

@@ -65,8 +65,10 @@ struct Op {
   int n_items;
   double flops = 0;   // algorithmic flops of this launch (LAWN-41 terms)
   double bytes = 0;   // algorithmic HBM bytes of this launch
-  int q0 = 0;         // first right-hand side (flag-driven solves) / CTAs (cooperative LU panel)
-  int aux = 0;        // rows per CTA (cooperative LU panel)
+  int q0 = 0;         // first right-hand side (flag-driven solves) / CTAs (cooperative LU panel) /
+                      // SMs left free for a concurrent launch (tensor-core Cholesky update)
+  int aux = 0;        // rows per CTA (cooperative LU panel, flag-driven solves)
+  int strm = 0;       // 0: the engine's stream, 1: its side stream (panel lookahead)
 };
 
 constexpr int N_OP_KINDS = 40;
@@ -80,7 +82,8 @@ enum OpKind : int {
   OP_FWD_GATHER, OP_FWD_SMALL, OP_TRSV_F, OP_GEMV_F, OP_BWD_PREP, OP_BWD_SMALL, OP_GEMV_B,
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
   OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_CHOL_PANEL, OP_TC_CHOL_TRAIL,
-  OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_CHOL_DIAG, OP_CHOL_PACK, OP_TC_CHOL_TRSM, OP_KIND_END
+  OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_CHOL_DIAG, OP_CHOL_PACK, OP_TC_CHOL_TRSM, OP_EV_RECORD, OP_EV_WAIT,
+  OP_KIND_END
 };
 static_assert(OP_KIND_END <= N_OP_KINDS, "profile arrays hold N_OP_KINDS op kinds");
 
@@ -106,10 +109,11 @@ struct Tunables {
                              // the tensor cores; 512 = panels of 512 columns factored whole by the
                              // cooperative kernel (SIMT in-panel work); 0 = the step-by-step path
                              // of the other tensor-core fronts
-  int solve_rows = 256;      // rows per CTA of the flag-driven forward solve of large Cholesky fronts
-                             // (64 or 256)
+  int solve_rows = 64;       // rows (columns) per CTA of the flag-driven forward (backward) solves of
+                             // large Cholesky fronts (64 or 256)
+  int lookahead = 1;         // panels of 256: the next panel's diagonal kernel overlaps the update
 };
-constexpr int N_TUNABLES = 8;
+constexpr int N_TUNABLES = 9;
 
 class Engine {
  public:
@@ -215,6 +219,11 @@ class Engine {
   bool factored = false;
   int factored_method = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;    // side stream of the panel lookahead
+  std::vector<cudaEvent_t> evpool;   // events ordering the two streams (by id)
+  static bool is_kernel_op(int kind) {
+    return kind != OP_CLEAR_FLAGS && kind != OP_EV_RECORD && kind != OP_EV_WAIT;
+  }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   // element sources

@@ -826,7 +826,8 @@ void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws,
 }
 
 void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
-                    int* err, cudaStream_t s, int mode, const int64_t* row0b, const int64_t* linv_row0, void* ws) {
+                    int* err, cudaStream_t s, int mode, const int64_t* row0b, const int64_t* linv_row0, void* ws,
+                    int reserve) {
   if (!n_items) return;
   static int n_sm = 0;
   if (!n_sm) {
@@ -836,7 +837,8 @@ void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_r
     if (n_sm <= 0) n_sm = 1;
   }
   cudaFuncSetAttribute(k_tc_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TCC_SMEM);
-  const int grid = n_items < n_sm ? n_items : n_sm;
+  const int slots = n_sm - reserve > 1 ? n_sm - reserve : 1;
+  const int grid = n_items < slots ? n_items : slots;
   k_tc_chol<<<grid, TCC_THREADS, TCC_SMEM, s>>>(c, map, ws_row0, items, n_items, err, mode, row0b, linv_row0,
                                                 (__nv_bfloat16*)ws);
 }
