@@ -44,8 +44,6 @@ template <typename T>
 struct PotrfShared {
   T V[64][64];      // V[p][i]: column p of the reduced block (zero above p)
   T XR[8][4][8];    // per warp: rows P..P+3 of its block of X, finished
-  T aux[512];       // potrf_block2: inverse pivot tiles, then one tile row of X
-  int bad_flag;
 };
 
 // Factor the 64 x 64 block at G (leading dimension n, kb <= 64 valid rows and
@@ -54,9 +52,8 @@ struct PotrfShared {
 // (leading dimension n); bad is set when a pivot was not positive.  Ends
 // with a block barrier.
 template <typename T>
-__device__ __forceinline__ void potrf_block_interleaved(const T* __restrict__ G, int n, int kb,
-                                                        PotrfShared<T>& sh, T (&x)[4][4], bool& bad,
-                                                        T* __restrict__ Lout) {
+__device__ __forceinline__ void potrf_block(const T* __restrict__ G, int n, int kb, PotrfShared<T>& sh,
+                                            T (&x)[4][4], bool& bad, T* __restrict__ Lout) {
   const int tid = threadIdx.x, w = tid >> 5;
   const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
   const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
@@ -187,211 +184,6 @@ __device__ __forceinline__ void potrf_block_interleaved(const T* __restrict__ G,
     }
     __syncthreads();
   }
-}
-
-// The factorisation the kernels use, same contract as
-// potrf_block_interleaved (which forms X in the same phases as L and is about
-// twice as slow):
-// x = this thread's tile of L^{-1}, L into Lout, bad on a non-positive pivot,
-// ends with a block barrier.  Two passes instead of one interleaved pass:
-//  1. L: 16 phases of 4 columns; the 4 x 4 tiles are thread-owned (thread
-//     (ti, tj) = rows 4 ti .., columns 4 tj .., lower tiles only).  In phase q
-//     the owners of tile column q factor the pivot tile (each redundantly,
-//     read from shared memory), form their tile of L and publish it; after a
-//     barrier every tile right of the column subtracts its rank-4 product,
-//     the owners of the next tile column publishing their updated tiles.
-//  2. L^{-1}: right-looking block substitution on L X = I: in step k the
-//     tiles (k, j) become X[k][j] = L_kk^{-1} B[k][j] and are published, then
-//     every tile (i > k, j <= k) subtracts L[i][k] X[k][j] from its B.
-// Two barriers per phase or step, no sequential work beyond a 4 x 4 tile.
-template <typename T>
-__device__ __forceinline__ void potrf_block(const T* __restrict__ G, int n, int kb, PotrfShared<T>& sh,
-                                            T (&x)[4][4], bool& bad, T* __restrict__ Lout) {
-  const int tid = threadIdx.x;
-  const int ti = tid & 15, tj = tid >> 4;
-  const int r0 = 4 * ti, c0 = 4 * tj;
-  const bool low = ti >= tj;
-  {
-    T g[16];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-      g[u] = (i >= j && i < kb && j < kb) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
-    }
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
-      if (i >= j) sh.V[j][i] = g[u];
-    }
-  }
-  __syncthreads();
-  T a[4][4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int i = r0 + u, j = c0 + v;
-      a[u][v] = low ? (i >= j ? sh.V[j][i] : sh.V[i][j]) : T(0);
-    }
-  T* DI = sh.aux;                       // 16 inverse pivot tiles, DI[q * 16 + u * 4 + v]
-  bool my_bad = false;
-  if (tid == 0) sh.bad_flag = 0;
-  __syncthreads();
-#pragma unroll 1
-  for (int q = 0; q < 16; ++q) {
-    const int P = 4 * q;
-    if (tj == q && low) {
-      // the pivot tile (columns P..P+3 of V hold the current tile column)
-      T bk[4][4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        T t4[4];
-        Vec4<T>::ld(&sh.V[P + v][P], t4);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) bk[u][v] = t4[u];
-      }
-      T lb[4][4], rd[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        T s = bk[v][v];
-#pragma unroll
-        for (int m = 0; m < v; ++m) s -= lb[v][m] * lb[v][m];
-        if (!(s > T(0))) { my_bad = true; s = T(1); }
-        T d;
-        pivot_root<T>(s, d, rd[v]);
-        lb[v][v] = d;
-#pragma unroll
-        for (int u = v + 1; u < 4; ++u) {
-          T t = bk[u][v];
-#pragma unroll
-          for (int m = 0; m < v; ++m) t -= lb[u][m] * lb[v][m];
-          lb[u][v] = t * rd[v];
-        }
-#pragma unroll
-        for (int u = 0; u < v; ++u) lb[u][v] = T(0);
-      }
-      T l[4][4];
-      if (ti == q) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) l[u][v] = lb[u][v];
-        // the pivot tile's inverse, for the second pass
-        T w[4][4];
-#pragma unroll
-        for (int cc = 0; cc < 4; ++cc)
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            T t = (u == cc) ? T(1) : T(0);
-#pragma unroll
-            for (int m = 0; m < u; ++m) t -= lb[u][m] * w[m][cc];
-            w[u][cc] = (u >= cc) ? t * rd[u] : T(0);
-          }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) DI[q * 16 + u * 4 + v] = w[u][v];
-      } else {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            T t = a[u][v];
-#pragma unroll
-            for (int m = 0; m < v; ++m) t -= l[u][m] * lb[v][m];
-            l[u][v] = t * rd[v];
-          }
-      }
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        T wv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) wv[u] = l[u][v];
-        Vec4<T>::st(&sh.V[P + v][r0], wv);
-      }
-      if (Lout) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            const int i = r0 + u, k = P + v;
-            if (i >= k && i < kb && k < kb) Lout[i + (int64_t)k * n] = l[u][v];
-          }
-      }
-    }
-    __syncthreads();
-    if (low && tj > q) {
-      T li[4][4], lj[4][4];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        Vec4<T>::ld(&sh.V[P + m][r0], li[m]);
-        Vec4<T>::ld(&sh.V[P + m][c0], lj[m]);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-#pragma unroll
-          for (int m = 0; m < 4; ++m) a[u][v] -= li[m][u] * lj[m][v];
-      if (tj == q + 1) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          T wv[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) wv[u] = a[u][v];
-          Vec4<T>::st(&sh.V[c0 + v][r0], wv);
-        }
-      }
-    }
-    __syncthreads();
-  }
-  // pass 2: X = L^{-1}; B starts as the identity, x holds B then X
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) x[u][v] = (ti == tj && u == v) ? T(1) : T(0);
-  if (my_bad) sh.bad_flag = 1;
-  T* XB = sh.aux + 256;                 // row k of X: tile j at XB[j * 16 + u * 4 + v]
-#pragma unroll 1
-  for (int k = 0; k < 16; ++k) {
-    if (ti == k && tj <= k) {
-      T y[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          T t = T(0);
-#pragma unroll
-          for (int m = 0; m < 4; ++m) t += DI[k * 16 + u * 4 + m] * x[m][v];
-          y[u][v] = t;
-        }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          x[u][v] = y[u][v];
-          XB[tj * 16 + u * 4 + v] = y[u][v];
-        }
-    }
-    __syncthreads();
-    if (ti > k && tj <= k) {
-      T lk[4][4], xk[4][4];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) Vec4<T>::ld(&sh.V[4 * k + m][r0], lk[m]);   // lk[m][u] = L[r0+u][4k+m]
-#pragma unroll
-      for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) xk[m][v] = XB[tj * 16 + m * 4 + v];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-#pragma unroll
-          for (int m = 0; m < 4; ++m) x[u][v] -= lk[m][u] * xk[m][v];
-    }
-    __syncthreads();
-  }
-  bad = sh.bad_flag != 0;
 }
 
 // the inverse, column-major with 128-bit stores (Dinv[j * 64 + i] = X[i][j]), into D
