@@ -300,6 +300,14 @@ int uhm_gpu_autotune(long* mesh, int method, int reps, int* n_timed);
  * refinement tolerance is redone in FP64 (status 20).  Parameters: 5187
  * floats, layout W1[64][12] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]. */
 int uhm_gpu_set_selector(long* mesh, const float* params, int n);
+/* One block of a front, read back from the device (the C form of
+ * uhm::Matrix_::copy_out, UHM/include/uhm/matrix/uhm/matrix.hxx:86-87):
+ * mat 1 ATL (fs x fs), 2 ATR (fs x ss), 3 ABL (ss x fs), 4 ABR (ss x ss)
+ * after a factorisation; 5 P (fs int pivots, LU) ; 7 XT (fs x n_rhs), 8 XB
+ * (ss x n_rhs) after a solve.  out is column-major with leading dimension m;
+ * (m, n) must be the block's size.  Cholesky blocks hold L (ATL, lower
+ * triangle) and the Schur complement (ABR, lower triangle), zero above. */
+int uhm_gpu_get_front_block(long* mesh, int elt_id, int mat, int m, int n, void* out);
 /* per-front features (front order of uhm_gpu_get_fronts, 12 floats each),
  * after the element matrices are copied in; method as for the factorisation */
 int uhm_gpu_get_front_features(long* mesh, int method, int n_fronts, float* out);

@@ -416,6 +416,21 @@ class Mesh:
                                   ss.ctypes.data_as(_P(_i)))
         return eid, gen, fs, ss
 
+    FRONT_BLOCKS = {"ATL": 1, "ATR": 2, "ABL": 3, "ABR": 4, "P": 5, "XT": 7, "XB": 8}
+
+    def front_block(self, elt_id, name):
+        """One block of a front (uhm_gpu_get_front_block), column-major as a
+        numpy array; P as int32 pivots."""
+        eid, _, fs, ss = self.fronts()
+        k = int(np.nonzero(eid == elt_id)[0][0])
+        f, s_ = int(fs[k]), int(ss[k])
+        dims = {"ATL": (f, f), "ATR": (f, s_), "ABL": (s_, f), "ABR": (s_, s_), "P": (f, 1),
+                "XT": (f, self.n_rhs), "XB": (s_, self.n_rhs)}[name]
+        out = np.zeros(dims[0] * dims[1], np.int32 if name == "P" else np.float64)
+        self._check(self.L.uhm_gpu_get_front_block(C.byref(self.h), int(elt_id), self.FRONT_BLOCKS[name],
+                                                   dims[0], dims[1], out.ctypes.data_as(C.c_void_p)))
+        return out if name == "P" else out.reshape(dims[1], dims[0]).T
+
     def front_nodes(self, elt_id, cap=1 << 20):
         ids = np.zeros(cap, np.int32)
         nf, ns = _i(0), _i(0)

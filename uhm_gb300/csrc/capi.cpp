@@ -473,6 +473,27 @@ int uhm_gpu_get_front_nodes(long* mesh, int elt_id, int cap, int* ids, int* nf, 
     *ns = (int)e->schur.size();
   });
 }
+int uhm_gpu_get_front_block(long* mesh, int elt_id, int mat, int m, int n, void* out) {
+  return guard(M(mesh), [&] {
+    Element e = M(mesh)->find_element(elt_id);
+    if (!e || !e->get_matrix()) throw std::invalid_argument("get_front_block: no such element or no matrix");
+    const int fs = e->hm.fs, ss = e->hm.ss, nr = e->hm.n_rhs;
+    int em = 0, en = 0;
+    switch (mat) {
+      case uhm::UHM_ATL: em = fs; en = fs; break;
+      case uhm::UHM_ATR: em = fs; en = ss; break;
+      case uhm::UHM_ABL: em = ss; en = fs; break;
+      case uhm::UHM_ABR: em = ss; en = ss; break;
+      case uhm::UHM_P: em = fs; en = 1; break;
+      case uhm::UHM_XT: em = fs; en = nr; break;
+      case uhm::UHM_XB: em = ss; en = nr; break;
+      default: throw std::invalid_argument("get_front_block: block not held by this engine");
+    }
+    if (m != em || n != en) throw std::invalid_argument("get_front_block: buffer dimensions do not match the block");
+    e->get_matrix()->copy_out(mat, out);
+  });
+}
+
 void* uhm_gpu_host_alloc(long bytes) {
   void* p = nullptr;
   if (cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) {

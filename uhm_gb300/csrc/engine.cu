@@ -469,6 +469,80 @@ void Engine::generate_lobatto_elements(int method, int dim, double hh, double cm
   anorm_inf = -1.0;
 }
 
+bool Engine::front_block_ready(Element e, int mat) const {
+  if (!e || e->slot < 0 || e->slot >= (int)fronts.size() || fronts[e->slot].e != e) return false;
+  if (mat == UHM_XT || mat == UHM_XB) return solved;
+  if (mat == UHM_P) return factored && factored_method != UHM_CHOL;
+  return factored && (mat == UHM_ATL || mat == UHM_ATR || mat == UHM_ABL || mat == UHM_ABR);
+}
+
+void Engine::front_block(Element e, int mat, void* out) {
+  if (!front_block_ready(e, mat)) fail("front_block: block not available", 9);
+  const HostFront& f = fronts[e->slot];
+  const int n = f.n, fs = f.fs, nr = mesh->n_rhs;
+  CK(cudaStreamSynchronize(stream));
+  if (mat == UHM_P) {
+    if (fs) CK(cudaMemcpy(out, ctx.piv + f.piv_off, sizeof(int32_t) * fs, cudaMemcpyDeviceToHost));
+    return;
+  }
+  double* o = static_cast<double*>(out);
+  if (mat == UHM_XT || mat == UHM_XB) {
+    const int r0 = mat == UHM_XT ? 0 : fs, m = mat == UHM_XT ? fs : f.ss;
+    std::vector<double> y((size_t)n * nr);
+    CK(cudaMemcpy(y.data(), ctx.vec + f.voff + (int64_t)n * nr, sizeof(double) * y.size(), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < nr; ++q)
+      for (int i = 0; i < m; ++i) o[(size_t)q * m + i] = y[(size_t)q * n + r0 + i];
+    return;
+  }
+  const int r0 = (mat == UHM_ATL || mat == UHM_ATR) ? 0 : fs, c0 = (mat == UHM_ATL || mat == UHM_ABL) ? 0 : fs;
+  const int m = r0 == 0 ? fs : f.ss, nc = c0 == 0 ? fs : f.ss;
+  if (!m || !nc) return;
+  const bool f64 = h_fronts[f.slot].dtype == F64;
+  if (f64) {
+    CK(cudaMemcpy2D(o, sizeof(double) * m, ctx.a64 + f.off + r0 + (int64_t)c0 * n, sizeof(double) * n,
+                    sizeof(double) * m, nc, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> t((size_t)m * nc);
+    CK(cudaMemcpy2D(t.data(), sizeof(float) * m, ctx.a32 + f.off + r0 + (int64_t)c0 * n, sizeof(float) * n,
+                    sizeof(float) * m, nc, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < t.size(); ++k) o[k] = t[k];
+  }
+  if (factored_method != UHM_CHOL) return;
+  // Cholesky keeps the lower triangles; the 64 x 64 diagonal blocks of a
+  // blocked front are held by their inverses (the solves use those), so L
+  // there is the inverse of the inverse, by forward substitution
+  if (mat == UHM_ATL || mat == UHM_ABR)
+    for (int j = 0; j < nc; ++j)
+      for (int i = 0; i < std::min(j, m); ++i) o[(size_t)j * m + i] = 0.0;
+  if (mat == UHM_ATL && f.blocked) {
+    const int nfb = (fs + NB - 1) / NB;
+    std::vector<double> di((size_t)NB * NB);
+    for (int b = 0; b < nfb; ++b) {
+      const int kb = std::min(NB, fs - NB * b);
+      if (f64) {
+        CK(cudaMemcpy(di.data(), ctx.dinv64 + f.dinv_off + (int64_t)b * NB * NB, sizeof(double) * NB * NB,
+                      cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<float> t((size_t)NB * NB);
+        CK(cudaMemcpy(t.data(), ctx.dinv32 + f.dinv_off + (int64_t)b * NB * NB, sizeof(float) * NB * NB,
+                      cudaMemcpyDeviceToHost));
+        for (int k = 0; k < NB * NB; ++k) di[k] = t[k];
+      }
+      // X = dinv (lower, column-major); L = X^{-1}: solve X L = I column by column
+      for (int c = 0; c < kb; ++c)
+        for (int i = 0; i < kb; ++i) {
+          double v = 0.0;
+          if (i >= c) {
+            double t = i == c ? 1.0 : 0.0;
+            for (int k = c; k < i; ++k) t -= di[(size_t)k * NB + i] * o[(size_t)(NB * b + c) * m + NB * b + k];
+            v = t / di[(size_t)i * NB + i];
+          }
+          o[(size_t)(NB * b + c) * m + NB * b + i] = v;
+        }
+    }
+  }
+}
+
 void Engine::copy_out(Element e, int m, int n, int nod_disp, const int* nods, int side, double* buf) {
   ensure_plan();
   if (side != UHM_RHS) fail("copy_out: only the solution (UHM_RHS) is supported", 7);
@@ -1843,6 +1917,7 @@ void Engine::factor(int method) {
   n_refactored = (int)fronts.size() - n_keep;
   // until this factorisation succeeds, no front holds a trustworthy factor
   factored = false;
+  solved = false;
   front_kept.clear();
   CK(cudaEventRecord(ev0, stream));
   if (!anorm_valid) enqueue_anorm();
@@ -1948,7 +2023,9 @@ void Engine::solve(int method, int phase) {
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.solve_ms = ms;
   h_x_valid = false;
+  solved = false;
   check_device_error("solve");
+  solved = phase == 3;
   if (mode == 1 && phase == 3) {
     refine(method);
     return;

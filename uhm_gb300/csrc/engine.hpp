@@ -156,6 +156,11 @@ class Engine {
   void random_elements(int spd);
   uint64_t random_calls = 0;
   void node_solution(int n_nodes, const int* ids, double* out, int64_t n_values);
+  // one block of a front (uhm::Matrix_::copy_out): UHM_ATL / ATR / ABL / ABR
+  // after a factorisation, UHM_P (int pivots, LU), UHM_XT / XB after a solve;
+  // column-major, leading dimension = the block's rows
+  bool front_block_ready(Element e, int mat) const;
+  void front_block(Element e, int mat, void* out);
 
   // --- numerics -----------------------------------------------------------
   void factor(int method);
@@ -217,6 +222,7 @@ class Engine {
   bool anorm_valid = false;
   bool dev_ok = false;
   bool factored = false;
+  bool solved = false;          // the solution slabs hold the last solve's rows
   int factored_method = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;    // side stream of the panel lookahead

@@ -525,7 +525,14 @@ void Mesh_::create_matrix_without_buffer(int dt, int nrhs) {
   n_rhs = nrhs;
   for (auto& kv : elements) {
     std::pair<int, int> d = kv.second.get_n_dof();
-    kv.second.hm = FrontHandle{d.first, d.second, nrhs, dt, true};
+    Matrix_& h = kv.second.hm;
+    h.fs = d.first;
+    h.ss = d.second;
+    h.n_rhs = nrhs;
+    h.datatype = dt;
+    h.created = true;
+    h.mesh = this;
+    h.elt = &kv.second;
   }
   if (engine) engine->invalidate_plan();
 }
@@ -553,6 +560,86 @@ void Mesh_::copy_out(Element elt, int dt, int m, int n, int* nods, int side, voi
 void Mesh_::copy_out(Element elt, int dt, int m, int n, int nod_disp, int* nods, int side, void* buffer) {
   if (dt != UHM_REAL) throw std::invalid_argument("copy_out: only UHM_REAL is supported");
   eng().copy_out(elt, m, n, nod_disp, nods, side, (double*)buffer);
+}
+
+// ---- Matrix_: the front handle ----------------------------------------------
+static bool block_dims(const Matrix_& h, int mat, int& m, int& n) {
+  switch (mat) {
+    case UHM_ATL: m = h.fs; n = h.fs; return true;
+    case UHM_ATR: m = h.fs; n = h.ss; return true;
+    case UHM_ABL: m = h.ss; n = h.fs; return true;
+    case UHM_ABR: m = h.ss; n = h.ss; return true;
+    case UHM_P: m = h.fs; n = 1; return true;
+    case UHM_XT: m = h.fs; n = h.n_rhs; return true;
+    case UHM_XB: m = h.ss; n = h.n_rhs; return true;
+    default: m = n = 0; return false;
+  }
+}
+int Matrix_::is_created(int mat) const {
+  int m, n;
+  return created && block_dims(*this, mat, m, n) ? 1 : 0;
+}
+int Matrix_::is_buffer(int mat) const {
+  int m, n;
+  if (!created || !block_dims(*this, mat, m, n) || !mesh || !mesh->engine) return 0;
+  return mesh->engine->front_block_ready(elt, mat) ? 1 : 0;
+}
+void Matrix_::copy_out(int mat, void* buffer) {
+  int m, n;
+  if (!created || !mesh || !elt) throw std::invalid_argument("Matrix_::copy_out: the front has no matrix");
+  if (!block_dims(*this, mat, m, n)) throw std::invalid_argument("Matrix_::copy_out: block not held by this engine");
+  if (!mesh->engine || !mesh->engine->front_block_ready(elt, mat))
+    throw std::invalid_argument("Matrix_::copy_out: block not computed yet (factor / solve first)");
+  mesh->engine->front_block(elt, mat, buffer);
+}
+void Matrix_::copy_out(int mat, linal::Flat_ B) {
+  int m, n;
+  if (!block_dims(*this, mat, m, n)) throw std::invalid_argument("Matrix_::copy_out: block not held by this engine");
+  if (mat == UHM_P) throw std::invalid_argument("Matrix_::copy_out: pivots go to an int buffer");
+  if (B.get_m() != m || B.get_n() != n) throw std::invalid_argument("Matrix_::copy_out: view of the wrong size");
+  std::vector<double> buf((size_t)m * n);
+  copy_out(mat, buf.data());
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) B(i, j) = buf[(size_t)j * m + i];
+}
+bool Matrix_::disp(FILE* stream) {
+  std::fprintf(stream, "- uhm::Matrix_ (element %d): fs %d, ss %d, n_rhs %d, %s -\n", elt ? elt->get_id() : -1, fs, ss,
+               n_rhs, created ? "created" : "not created");
+  return true;
+}
+
+// The LINAL-view forms: the (id, physics) pairs as a UHM_PHYSICS_MULTI node
+// list, the view copied through a contiguous buffer when its leading
+// dimension is not its row count.
+static std::vector<int> pair_list(const std::vector<std::pair<int, int>>& nods) {
+  std::vector<int> v;
+  v.reserve(2 * nods.size());
+  for (const auto& p : nods) {
+    v.push_back(p.first);
+    v.push_back(p.second);
+  }
+  return v;
+}
+
+void Mesh_::copy_in(Element elt, std::vector<std::pair<int, int>>& nods, int side, linal::Flat_ A) {
+  if (A.get_data_type() != UHM_REAL) throw std::invalid_argument("copy_in: only UHM_REAL views are supported");
+  const int m = A.get_m(), n = side == UHM_LHS ? A.get_m() : A.get_n();
+  if (side == UHM_LHS && A.get_n() != m) throw std::invalid_argument("copy_in: element matrix view is not square");
+  std::vector<int> ids = pair_list(nods);
+  std::vector<double> buf((size_t)m * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) buf[(size_t)j * m + i] = A(i, j);
+  copy_in(elt, UHM_REAL, m, n, UHM_PHYSICS_MULTI, ids.data(), side, buf.data());
+}
+
+void Mesh_::copy_out(Element elt, std::vector<std::pair<int, int>>& nods, int side, linal::Flat_ B) {
+  if (B.get_data_type() != UHM_REAL) throw std::invalid_argument("copy_out: only UHM_REAL views are supported");
+  const int m = B.get_m(), n = B.get_n();
+  std::vector<int> ids = pair_list(nods);
+  std::vector<double> buf((size_t)m * n);
+  copy_out(elt, UHM_REAL, m, n, UHM_PHYSICS_MULTI, ids.data(), side, buf.data());
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) B(i, j) = buf[(size_t)j * m + i];
 }
 
 // matrix.cxx:54-62: the right-hand side is taken from the element rhs at solve time

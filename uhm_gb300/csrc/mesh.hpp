@@ -16,6 +16,8 @@
 #include <utility>
 #include <vector>
 
+#include "linal.hpp"
+
 namespace uhm {
 
 // UHM/include/uhm/const.hxx:58-88
@@ -67,11 +69,51 @@ class Node_ {
   void clean_connectivity();   // drop non-leaf owners (UHM/src/mesh/node.cxx:110-118)
 };
 
-// Per-element matrix handle: sizes and its slots in the device engine.
-struct FrontHandle {
+// The blocks of a front (UHM/include/uhm/const.hxx:74-75)
+enum { UHM_ATL = 1, UHM_ATR, UHM_ABL, UHM_ABR, UHM_P, UHM_T, UHM_XT, UHM_XB, UHM_BT, UHM_BB, UHM_RT, UHM_RB,
+       UHM_END };
+
+// A front's matrix: the reference's plugin object uhm::Matrix_
+// (UHM/include/uhm/matrix/uhm/matrix.hxx:53-156) as a handle into the device
+// engine's arena.  The per-front numerical methods of the reference (chol,
+// lu_piv, merge, solve_*_1_x ...) are not members: the engine runs every
+// front of a tree level in one batched launch behind Mesh_::*_with_free and
+// solve_*, which is the batching point of this library.  What a caller can do
+// per front is read it:
+//   get_dimension()          (fs, ss)
+//   get_n_rhs()              right-hand sides
+//   is_created(mat)          the front exists (after create_matrix_without_buffer)
+//   is_buffer(mat)           the block is held on the device (after a factorisation
+//                            for ATL, ATR, ABL, ABR, P; after a solve for XT, XB)
+//   copy_out(mat, buffer)    the block into column-major host memory (ld = rows):
+//                            ATL fs x fs (Cholesky: L in the lower triangle, zero
+//                            above; LU: L below the unit diagonal and U on and
+//                            above it), ATR fs x ss (LU: U12), ABL ss x fs (L21),
+//                            ABR ss x ss (the Schur complement; Cholesky: lower
+//                            triangle, zero above), P fs pivots (int, relative to
+//                            the front's first row; LU with pivoting), XT fs x
+//                            n_rhs and XB ss x n_rhs (the front's solution rows)
+//   copy_out(mat, Flat_ B)   the same into a LINAL view of those sizes
+//   disp(), disp(stream)     sizes and state
+class Matrix_ {
+ public:
   int fs = 0, ss = 0, n_rhs = 0, datatype = UHM_REAL;
   bool created = false;
+  Mesh_* mesh = nullptr;
+  Element_* elt = nullptr;
+
+  std::pair<int, int> get_dimension() const { return std::make_pair(fs, ss); }
+  int get_n_rhs() const { return n_rhs; }
+  int is_created(int mat) const;
+  int is_buffer(int mat) const;
+  int is_complex_datatype() const { return datatype == UHM_COMPLEX; }
+  void copy_out(int mat, void* buffer);
+  void copy_out(int mat, linal::Flat_ B);
+  bool disp() { return disp(stdout); }
+  bool disp(FILE* stream);
 };
+typedef Matrix_* Matrix;
+typedef Matrix_ FrontHandle;
 
 class Element_ {
  public:
@@ -98,6 +140,7 @@ class Element_ {
   bool is_orphan() const { return parent == nullptr; }
   bool is_leaf() const { return children.empty(); }
   bool is_matrix_created() const { return hm.created; }
+  Matrix get_matrix() { return hm.created ? &hm : nullptr; }   // element.hxx:104
   void set_reuse(int flag) { reuse = flag; }   // element.cxx:75
   bool is_matrix_reusable() const { return reuse != 0; }
   std::pair<int, int> get_n_dof() const;       // (fs, ss), element.cxx:112-126
@@ -174,6 +217,12 @@ class Mesh_ {
   void copy_in(Element elt, int datatype, int m, int n, int* nods, int side, void* buffer);
   void copy_in(Element elt, int datatype, int m, int n, int nod_disp, int* nods, int side,
                void* buffer);
+  // the element matrix / right-hand sides as a LINAL view (UHM/include/uhm/
+  // mesh/mesh.hxx:181-184, 194-197; UHM/src/mesh/interf.cxx:205-292): nods
+  // holds (node id, physics) per element node in the view's row order; the
+  // view may have any leading dimension
+  void copy_in(Element elt, std::vector<std::pair<int, int>>& nods, int side, linal::Flat_ A);
+  void copy_out(Element elt, std::vector<std::pair<int, int>>& nods, int side, linal::Flat_ B);
   void copy_out(Element elt, int datatype, int m, int n, int* nods, int side, void* buffer);
   void copy_out(Element elt, int datatype, int m, int n, int nod_disp, int* nods, int side,
                 void* buffer);
