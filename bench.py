@@ -42,16 +42,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "factor+solve s at 16³ p=4: plain FP64 vs mixed+IR+learned, bwd err≤1e-12"
-# DRAM traffic of the tensor-core Schur update per algorithmic byte, from one
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of its first
-# root-level launch on the 12^3 p=4 profiling case (trailing block above the
-# L2 size); scaled to the bench's launches by their algorithmic bytes
-# DRAM traffic of the Schur-update launch per algorithmic byte, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of k_tc_chol's ABR
-# launch on a smaller mesh, scaled to the bench's launch by its algorithmic
-# bytes (None until captured)
-SCHUR_TRAFFIC_PER_ALG_BYTE = None
-SCHUR_TRAFFIC_SOURCE = "not captured"
+# DRAM traffic of the tensor-core Schur pass per algorithmic byte, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of its launch on tree
+# level -2 of the 12^3 p=4 mesh (27 fronts, fs 631, 142.2 MB against 177.4 MB
+# algorithmic); scaled to the benchmark's launches by their algorithmic bytes
+SCHUR_TRAFFIC_PER_ALG_BYTE = 142.22 / 177.36
+SCHUR_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the Schur launch of poisson3d_12_p4 "
+                        "(profiles/tc_chol_schur_poisson3d_12_p4.md), 0.80 x its algorithmic bytes, scaled")
 WORKLOAD = "3D Poisson 16^3 hex p=4 Legendre-hierarchic, Dirichlet, octree ND, Cholesky fronts, 1 RHS"
 
 

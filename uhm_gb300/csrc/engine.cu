@@ -1370,7 +1370,11 @@ void Engine::build_programs(int method) {
       if (gm == M_LU_PIV) {
         g_items.push_back(Item{s, 0, 0, 0});
       } else {
-        for (int r0 = 0; r0 < fronts[s].n; r0 += GATHER_ROWS) g_items.push_back(Item{s, r0, GATHER_ROWS, 0});
+        // c = 1: the front takes the 64-row flag-driven solves, whose
+        // forward hand-off words the gather empties
+        const int hand = chol && nr <= NR_FLAGS_MAX && tune.solve_rows == 64 &&
+                         !solve_small(fronts[s], h_fronts[s].dtype);
+        for (int r0 = 0; r0 < fronts[s].n; r0 += GATHER_ROWS) g_items.push_back(Item{s, r0, GATHER_ROWS, hand});
       }
     }
     push(fwd_ops, OP_FWD_GATHER, 0, 0, gm, g_items);

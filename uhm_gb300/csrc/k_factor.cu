@@ -30,35 +30,13 @@ constexpr int ASM_TJ = 16;
 constexpr int ASM_MAXSRC = 64;
 
 // Extend-add of a front below ASM_SCATTER_MIN rows: 16 parent columns per
-// CTA, column by column.  Each thread owns up to ASM_ROWS rows of the column
-// (stride 256) and keeps their sums in registers; the column's sources are
-// walked in summation order (element first, then the children in child
-// order) with each source decoded once, and for every source all the
-// thread's row look-ups and loads are issued together.  Each parent entry
-// is written once; a child's lower-stored Schur block is read transposed
-// where the parent row falls above its diagonal.
-constexpr int ASM_ROWS = 8;        // rows per thread and chunk: 8 * 256 = 2048 rows per pass
-
-template <typename T, typename S>
-__device__ __forceinline__ void asm_add_source(const S* __restrict__ base, int ld, int cc, bool sym,
-                                               const int32_t* __restrict__ invk, int istart, int n,
-                                               double (&acc)[ASM_ROWS]) {
-  int is[ASM_ROWS];
-#pragma unroll
-  for (int u = 0; u < ASM_ROWS; ++u) {
-    const int I = istart + threadIdx.x + 256 * u;
-    is[u] = I < n ? __ldg(invk + I) : -1;
-  }
-#pragma unroll
-  for (int u = 0; u < ASM_ROWS; ++u) {
-    if (is[u] >= 0) {
-      int r = is[u], col = cc;
-      if (sym && r < col) { const int t = r; r = col; col = t; }
-      acc[u] += (double)base[r + (int64_t)col * ld];
-    }
-  }
-}
-
+// CTA, one thread per parent row, the column's sources walked in summation
+// order (element first, then the children in child order) through their
+// inverse row maps.  Each parent entry is written once; a child's
+// lower-stored Schur block is read transposed where the parent row falls
+// above its diagonal.  (Forms with several rows per thread, or a warp per
+// column with the sources decoded once per pass, issued more instructions
+// per entry on these front sizes and measured slower.)
 template <typename T>
 __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restrict__ items,
                                                   int lower) {
@@ -74,29 +52,24 @@ __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restri
   const int32_t* __restrict__ inv = c.inv + f.inv_off;
   const int J0 = it.a;
   const int J1 = min(J0 + ASM_TJ, n);
-  for (int J = J0; J < J1; ++J)
-    // rows in chunks of ASM_ROWS * 256 (one chunk below 2048 rows; fronts
-    // above the scatter kernel's limit take several)
-    for (int istart = lower ? J : 0; istart < n; istart += ASM_ROWS * 256) {
+  for (int J = J0; J < J1; ++J) {
     const int64_t k0 = cp[J], k1 = cp[J + 1];
-    double acc[ASM_ROWS];
-#pragma unroll
-    for (int u = 0; u < ASM_ROWS; ++u) acc[u] = 0.0;
-    for (int64_t k = k0; k < k1; ++k) {
-      const int2 cs = c.colsrc[k];
-      const SrcDev sd = cs.x < ASM_MAXSRC ? s_src[cs.x] : c.srcs[f.src0 + cs.x];
-      const int32_t* invk = inv + (int64_t)cs.x * n;
-      const bool sym = sd.is_child && c.symmetric;
-      if (!sd.is_child) asm_add_source<T, double>(c.emat + sd.off, sd.ld, cs.y, false, invk, istart, n, acc);
-      else if (sd.dtype == F64) asm_add_source<T, double>(c.a64 + sd.off, sd.ld, cs.y, sym, invk, istart, n, acc);
-      else asm_add_source<T, float>(c.a32 + sd.off, sd.ld, cs.y, sym, invk, istart, n, acc);
+    const int istart = lower ? J : 0;
+    for (int I = istart + threadIdx.x; I < n; I += blockDim.x) {
+      double acc = 0.0;
+      for (int64_t k = k0; k < k1; ++k) {
+        const int2 cs = c.colsrc[k];
+        const int is = inv[(int64_t)cs.x * n + I];
+        if (is >= 0) {
+          const SrcDev sd = cs.x < ASM_MAXSRC ? s_src[cs.x] : c.srcs[f.src0 + cs.x];
+          int r = is, cc = cs.y;
+          if (sd.is_child && c.symmetric && r < cc) { int t = r; r = cc; cc = t; }
+          acc += load_src(c, sd, r + (int64_t)cc * sd.ld);
+        }
+      }
+      P[I + (int64_t)J * n] = (T)acc;
     }
-#pragma unroll
-    for (int u = 0; u < ASM_ROWS; ++u) {
-      const int I = istart + threadIdx.x + 256 * u;
-      if (I < n) P[I + (int64_t)J * n] = (T)acc[u];
-    }
-    }
+  }
 }
 
 // Extend-add of a large front, one parent column J per CTA.  The column is
@@ -129,16 +102,16 @@ __global__ void __launch_bounds__(256) k_assemble_scatter(DevCtx c, const Item* 
     // look-ups, then all its loads, then the shared-memory adds
     const double* __restrict__ b64 = !sd.is_child ? c.emat + sd.off : (sd.dtype == F64 ? c.a64 + sd.off : nullptr);
     const float* __restrict__ b32 = (sd.is_child && sd.dtype != F64) ? c.a32 + sd.off : nullptr;
-    for (int r0 = 0; r0 < sd.m; r0 += ASM_ROWS * 256) {
-      int I[ASM_ROWS];
-      double v[ASM_ROWS];
+    for (int r0 = 0; r0 < sd.m; r0 += 4 * 256) {
+      int I[4];
+      double v[4];
 #pragma unroll
-      for (int u = 0; u < ASM_ROWS; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const int r = r0 + threadIdx.x + 256 * u;
         I[u] = r < sd.m ? __ldg(fw + r) : -1;
       }
 #pragma unroll
-      for (int u = 0; u < ASM_ROWS; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const int r = r0 + threadIdx.x + 256 * u;
         v[u] = 0.0;
         if (I[u] >= istart) {
@@ -149,7 +122,7 @@ __global__ void __launch_bounds__(256) k_assemble_scatter(DevCtx c, const Item* 
         }
       }
 #pragma unroll
-      for (int u = 0; u < ASM_ROWS; ++u)
+      for (int u = 0; u < 4; ++u)
         if (I[u] >= istart) s_col[I[u]] += v[u];
     }
     __syncthreads();

@@ -18,7 +18,13 @@
 
 namespace uhm_gpu {
 
-// z = [g[g0 .. g0+fs); 0] + sum over children of their xb (extend-add)
+// the empty value of the flag-driven solves' hand-off words (a signalling
+// NaN: no arithmetic result or conversion produces it)
+constexpr unsigned long long HAND_EMPTY = 0x7FF4DEAD7FF4DEADull;
+
+// z = [g[g0 .. g0+fs); 0] + sum over children of their xb (extend-add);
+// item: front, a = first row, b = rows (0: all), c = 1 for a front of the
+// 64-row flag-driven solves
 __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __restrict__ items,
                                                     const double* __restrict__ g, int64_t ldg,
                                                     int method) {
@@ -26,6 +32,7 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
   const FrontDev f = c.fronts[it.front];
   const int n = f.n;
   double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = z + (int64_t)n * c.n_rhs;
   const int32_t* __restrict__ inv = c.inv + f.inv_off;
   // rows [it.a, it.a + it.b) of the front (it.b == 0: all rows; only then
   // are pivots applied, which needs the whole gathered vector)
@@ -43,6 +50,9 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
         }
       }
       z[I + (int64_t)q * n] = acc;
+      // fronts of the 64-row flag-driven solves: their y factor rows are the
+      // forward hand-off, emptied here (the forward launch comes after)
+      if (it.c && I < f.fs) y[I + (int64_t)q * n] = __longlong_as_double((long long)HAND_EMPTY);
     }
   }
   __syncthreads();
@@ -753,9 +763,11 @@ namespace uhm_gpu {
 // starting at fs.  A CTA takes a ticket (atomic counter) and processes the
 // item of that rank; items are ordered so that each CTA only waits for blocks
 // owned by CTAs with smaller tickets, which are already running -- progress
-// is guaranteed whatever the residency.  A finished block publishes its
-// solution (y slab), then a release-store of its flag; readers acquire the
-// flag before reading.  Every wait is bounded (error flag, no hang).
+// is guaranteed whatever the residency.  The 64-row kernels publish a
+// finished block's solution as self-validating hand-off words (below); the
+// 256-row kernels publish it, then a release-store of the block's flag, and
+// readers acquire the flag before reading.  Every wait is bounded (error
+// flag, no hang).
 // Forward:  x_b = L_bb^{-1} (z_b - sum_{j<b} L_bj x_j)
 // Backward: x_b = L_bb^{-T} (y_b - sum_{r > block b} L_rb^T x_r)
 // with L_bb^{-1} precomputed at factorisation (64 x 64, dinv arenas).
@@ -819,6 +831,60 @@ template <typename T> __device__ __forceinline__ const T* dinv_arena(const DevCt
 template <> __device__ __forceinline__ const double* dinv_arena<double>(const DevCtx& c) { return c.dinv64; }
 template <> __device__ __forceinline__ const float* dinv_arena<float>(const DevCtx& c) { return c.dinv32; }
 
+// Hand-off words of the 64-row flag-driven solves.  A block's solution is
+// published as plain FP64 words that carry their own completion: before the
+// launch every word of the hand-off holds HAND_EMPTY, a signalling NaN that
+// no arithmetic result or conversion can produce, and the solving CTA
+// overwrites it with the value (one relaxed 8-byte store per entry, single-
+// copy atomic).  A reader polls the words themselves: once none of them is
+// HAND_EMPTY it holds the values, with no flag, no fence on the writer's side
+// and no second round trip on the reader's.  The forward hand-off is the y
+// slab's factor rows (filled by the gather before the launch), the backward
+// one the z slab's factor rows (filled by the forward CTA of the block, after
+// its last read of them).
+__device__ __forceinline__ unsigned long long ld_hand(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_hand(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(v)) : "memory");
+}
+
+// Warp 0 of a CTA: the 64 hand-off words of one block and right-hand side
+// (entries lane and lane + 32; entries at or past kb read as 0).
+struct HandWords {
+  unsigned long long w0, w1;
+  __device__ __forceinline__ void load(const double* base, int kb) {
+    const int lane = threadIdx.x & 31;
+    w0 = lane < kb ? ld_hand(base + lane) : 0ull;
+    w1 = lane + 32 < kb ? ld_hand(base + lane + 32) : 0ull;
+  }
+  __device__ __forceinline__ bool full() const {
+    return __all_sync(0xffffffffu, w0 != HAND_EMPTY && w1 != HAND_EMPTY);
+  }
+  // bounded wait until every word is written; false (and *err = 2) when the
+  // limit runs out
+  __device__ __forceinline__ bool wait(const double* base, int kb, int* err) {
+    const uint32_t lim = g_wait_limit;
+    for (uint32_t i = 0; !full(); ++i) {
+      if (i >= lim) {
+        if ((threadIdx.x & 31) == 0) atomicExch(err, 2);
+        return false;
+      }
+      __nanosleep(32);
+      load(base, kb);
+    }
+    return true;
+  }
+  template <typename CT>
+  __device__ __forceinline__ void stage(CT* dst) const {
+    const int lane = threadIdx.x & 31;
+    dst[lane] = (CT)__longlong_as_double(w0);
+    dst[lane + 32] = (CT)__longlong_as_double(w1);
+  }
+};
+
 // item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
 // right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
 template <typename T>
@@ -829,11 +895,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   __shared__ CT red[4][FB][SF_NR];
   __shared__ CT v[FB][SF_NR];
   __shared__ T dsh[FB * (FB + 1)];     // inverse diagonal block, staged before any wait
+  // y_j staged by warp 0, two buffers alternating by block: one barrier per block
+  __shared__ CT ysh[2][SF_NR][FB];
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
+  const int nq = min(SF_NR, nr - q0);
   const int nfb = (fs + FB - 1) / FB;
   const bool factor_block = b < nfb;
   if (factor_block) {
@@ -845,7 +914,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ z = c.vec + f.voff;
   double* __restrict__ y = z + (int64_t)n * nr;
-  const int* __restrict__ flg = c.flags + f.flag_off;
   const int i = threadIdx.x % FB, g = threadIdx.x / FB;
   const int row = r0 + i;
   const bool rv = row < r1;
@@ -853,12 +921,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) {
     acc[q] = CT(0);
-    zr[q] = (rv && q0 + q < nr && g == 0) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);   // before any wait
+    zr[q] = (rv && q < nq && g == 0) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);   // before any wait
+  }
+  // the factor rows of z are not read again: they become the backward
+  // solve's hand-off words for this block
+  if (factor_block && rv && g == 0) {
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q)
+      if (q < nq) z[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
   }
   const int jend = factor_block ? b : nfb;
-  __shared__ int s_ready;
-  // The factor tile of block column j does not depend on any flag: it is
-  // loaded one block ahead, so that only the loads of y_j follow the wait.
+  // The factor tile of block column j does not depend on y: it is loaded one
+  // block ahead, so that only the loads of y_j follow the wait.
   CT tile[16];
   auto load_tile = [&](int j) {
     const int kbj = min(FB, fs - j * FB);
@@ -868,37 +942,41 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
       tile[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
     }
   };
-  if (jend > 0) load_tile(0);
-  // y_j is read by every later block of the front at once: one warp per CTA
-  // stages it in shared memory (hundreds of CTAs hitting the same few lines
-  // with per-thread loads serialise in L2)
-  __shared__ CT ysh[SF_NR][FB];
-  int done = 0;
-  while (done < jend) {
-    ready_range(flg, done, jend, 1, &s_ready, err);
-    const int upto = s_ready;
-    for (int j = done; j < upto; ++j) {
+  const bool w0 = threadIdx.x < 32;
+  HandWords hw;
+  bool live = true;      // warp 0: false once a wait has run out (no more waiting)
+  if (jend > 0) {
+    load_tile(0);
+    if (w0) hw.load(y + (int64_t)q0 * n, min(FB, fs));
+  }
+  for (int j = 0; j < jend; ++j) {
+    const int buf = j & 1;
+    if (w0) {
+      // y_j is read by every later block of the front at once: one warp
+      // per CTA polls and stages it (the next block's words already in flight)
       const int kbj = min(FB, fs - j * FB);
-      if (threadIdx.x < 32) {
-        for (int q = 0; q < SF_NR && q0 + q < nr; ++q) {
-          const double* yj = y + j * FB + (int64_t)(q0 + q) * n;
-          for (int cc = threadIdx.x; cc < FB; cc += 32) ysh[q][cc] = cc < kbj ? (CT)__ldcg(yj + cc) : CT(0);
-        }
+      const double* yj = y + j * FB;
+      if (live) live = hw.wait(yj + (int64_t)q0 * n, kbj, err);
+      hw.stage(ysh[buf][0]);
+      for (int q = 1; q < nq; ++q) {
+        HandWords hq;
+        hq.load(yj + (int64_t)(q0 + q) * n, kbj);
+        if (live) live = hq.wait(yj + (int64_t)(q0 + q) * n, kbj, err);
+        hq.stage(ysh[buf][q]);
       }
-      CT cur[16];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) cur[u] = tile[u];
-      if (j + 1 < jend) load_tile(j + 1);
-      __syncthreads();
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-#pragma unroll
-        for (int q = 0; q < SF_NR; ++q)
-          if (q0 + q < nr) acc[q] += cur[u] * ysh[q][g * 16 + u];
-      }
-      __syncthreads();
+      if (j + 1 < jend) hw.load(y + (j + 1) * FB + (int64_t)q0 * n, min(FB, fs - (j + 1) * FB));
     }
-    done = upto;
+    CT cur[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+    if (j + 1 < jend) load_tile(j + 1);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q)
+        if (q < nq) acc[q] += cur[u] * ysh[buf][q][g * 16 + u];
+    }
   }
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
@@ -906,7 +984,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   if (threadIdx.x < FB) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      v[i][q] = (rv && q0 + q < nr) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
+      v[i][q] = (rv && q < nq) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
   }
   __syncthreads();
   if (factor_block) {
@@ -933,16 +1011,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
     if (threadIdx.x < FB && rv) {
 #pragma unroll
       for (int q = 0; q < SF_NR; ++q)
-        if (q0 + q < nr)
-          y[row + (int64_t)(q0 + q) * n] = (double)(red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]);
+        if (q < nq)
+          st_hand(y + row + (int64_t)(q0 + q) * n,
+                  (double)(red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]));
     }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) st_release_gpu(c.flags + f.flag_off + b, 1);
   } else if (threadIdx.x < FB && rv) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      if (q0 + q < nr) z[row + (int64_t)(q0 + q) * n] = (double)v[i][q];
+      if (q < nq) z[row + (int64_t)(q0 + q) * n] = (double)v[i][q];
   }
 }
 
@@ -1122,13 +1198,15 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   extern __shared__ __align__(16) unsigned char bwd_dyn[];
   CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(bwd_dyn);   // [row lane][column]
   __shared__ CT v[FB][NQ];
-  __shared__ int s_ready;
   __shared__ T dsh[FB * (FB + 1)];
+  // x_j staged by warp 0, two buffers alternating by block: one barrier per block
+  __shared__ CT xsh[2][NQ][FB];
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
+  const int nq = min(NQ, nr - q0);
   const int nfb = (fs + FB - 1) / FB;
   const int c0 = b * FB, kb = min(FB, fs - c0);
   {
@@ -1136,8 +1214,8 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[(idx / FB) * (FB + 1) + idx % FB] = Dg[idx];
   }
   const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
-  const int* __restrict__ flg = c.flags + f.flag_off;
+  double* __restrict__ hx = c.vec + f.voff;                  // hand-off: the z slab's factor rows
+  double* __restrict__ y = hx + (int64_t)n * nr;
   const int rl = threadIdx.x % FB, g = threadIdx.x / FB;   // row lane, column group
   CT acc[NQ][16];
 #pragma unroll
@@ -1153,7 +1231,7 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     for (int h = 0; h < 2; ++h) {
       const int r = rs + h * FB + rl;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) xr[h][q] = (r < n && q0 + q < nr) ? (CT)y[r + (int64_t)(q0 + q) * n] : CT(0);
+      for (int q = 0; q < NQ; ++q) xr[h][q] = (r < n && q < nq) ? (CT)y[r + (int64_t)(q0 + q) * n] : CT(0);
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int cc = g * 16 + u;
@@ -1167,8 +1245,8 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
 #pragma unroll
         for (int q = 0; q < NQ; ++q) acc[q][u] += gv[h][u] * xr[h][q];
   }
-  // the factor tile of row block j does not depend on any flag: loaded one
-  // block ahead, so that only the loads of x_j follow the wait
+  // the factor tile of row block j does not depend on x: loaded one block
+  // ahead, so that only the loads of x_j follow the wait
   CT tile[16];
   auto load_tile = [&](int j) {
     const int r = j * FB + rl;
@@ -1179,30 +1257,40 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
       tile[u] = (in && cc < kb) ? (CT)G[r + (int64_t)(c0 + cc) * n] : CT(0);
     }
   };
-  int next = nfb - 1;
-  if (next > b) load_tile(next);
-  while (next > b) {
-    ready_range(flg, next, b, -1, &s_ready, err);
-    const int stop = s_ready;
-    for (int j = next; j > stop; --j) {
-      CT cur[16];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) cur[u] = tile[u];
-      if (j - 1 > b) load_tile(j - 1);
-      const int r = j * FB + rl;
-      const bool in = r < min(j * FB + FB, fs);
-      if (in) {
-        CT xr[NQ];   // one distinct value per lane and right-hand side
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) xr[q] = q0 + q < nr ? (CT)__ldcg(y + r + (int64_t)(q0 + q) * n) : CT(0);
-#pragma unroll
-        for (int u = 0; u < 16; ++u)
-#pragma unroll
-          for (int q = 0; q < NQ; ++q) acc[q][u] += cur[u] * xr[q];
+  const bool w0 = threadIdx.x < 32;
+  HandWords hw;
+  bool live = true;      // warp 0: false once a wait has run out (no more waiting)
+  if (nfb - 1 > b) {
+    load_tile(nfb - 1);
+    if (w0) hw.load(hx + (nfb - 1) * FB + (int64_t)q0 * n, min(FB, fs - (nfb - 1) * FB));
+  }
+  for (int j = nfb - 1, k = 0; j > b; --j, ++k) {
+    const int buf = k & 1;
+    if (w0) {
+      const int kbj = min(FB, fs - j * FB);
+      const double* xj = hx + j * FB;
+      if (live) live = hw.wait(xj + (int64_t)q0 * n, kbj, err);
+      hw.stage(xsh[buf][0]);
+      for (int q = 1; q < nq; ++q) {
+        HandWords hq;
+        hq.load(xj + (int64_t)(q0 + q) * n, kbj);
+        if (live) live = hq.wait(xj + (int64_t)(q0 + q) * n, kbj, err);
+        hq.stage(xsh[buf][q]);
       }
+      if (j - 1 > b) hw.load(hx + (j - 1) * FB + (int64_t)q0 * n, min(FB, fs - (j - 1) * FB));
     }
-    next = stop;
+    CT cur[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+    if (j - 1 > b) load_tile(j - 1);
     __syncthreads();
+    const int r = j * FB + rl;
+    if (r < min(j * FB + FB, fs)) {
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q][u] += cur[u] * xsh[buf][q][rl];
+    }
   }
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
@@ -1213,7 +1301,7 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     if (threadIdx.x < FB) {
       CT s = CT(0);
       for (int r = 0; r < FB; ++r) s += red[r][threadIdx.x];
-      v[threadIdx.x][q] = (threadIdx.x < kb && q0 + q < nr)
+      v[threadIdx.x][q] = (threadIdx.x < kb && q < nq)
                               ? (CT)y[c0 + threadIdx.x + (int64_t)(q0 + q) * n] - s : CT(0);
     }
   }
@@ -1239,14 +1327,12 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
     const int ii = threadIdx.x;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      if (q0 + q >= nr) break;
-      y[c0 + ii + (int64_t)(q0 + q) * n] =
-          (double)(red[q][ii] + red[NQ + q][ii] + red[2 * NQ + q][ii] + red[3 * NQ + q][ii]);
+      if (q >= nq) break;
+      const double x = (double)(red[q][ii] + red[NQ + q][ii] + red[2 * NQ + q][ii] + red[3 * NQ + q][ii]);
+      y[c0 + ii + (int64_t)(q0 + q) * n] = x;
+      st_hand(hx + c0 + ii + (int64_t)(q0 + q) * n, x);
     }
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) st_release_gpu(c.flags + f.flag_off + b, 1);
 }
 
 // Backward solve of large Cholesky fronts with 256-column CTAs.  Item:
@@ -1430,8 +1516,8 @@ void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtyp
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
                       int* flag_base, int n_flags, int* err, int q0, cudaStream_t s) {
   if (!n_items) return;
+  (void)flag_base; (void)n_flags;     // hand-off words, no flags
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
-  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
   if (dtype == F64) k_fwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
   else k_fwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
 }
@@ -1455,8 +1541,8 @@ static void bwd_flags_t(const DevCtx& c, const Item* items, int n_items, int* ti
 void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
                       int* flag_base, int n_flags, int* err, int q0, cudaStream_t s) {
   if (!n_items) return;
+  (void)flag_base; (void)n_flags;     // hand-off words, no flags
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
-  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
   // right-hand sides of this launch: FLAG_NR, or FLAG_NR_BWD_F64 in FP64
   // (register budget of the NQ x 16 accumulators)
   const int grp = dtype == F64 ? FLAG_NR_BWD_F64 : FLAG_NR;
