@@ -284,7 +284,11 @@ int uhm_gpu_generate_lobatto_elements(long* mesh, int method, int dim, double hh
  * the step-by-step path; values[7] rows (columns) per CTA of the
  * flag-driven forward (backward) solves of large Cholesky fronts (64 or
  * 256), values[8] 1: with panels of 256, the next panel's diagonal kernel
- * runs on a second stream beside the current panel's trailing update.
+ * runs on a second stream beside the current panel's trailing update,
+ * values[9] 1: the 64-row solves of FP32 fronts run as chains (one CTA per
+ * front solves the diagonal blocks from shared memory, helper CTAs sum the
+ * blocks further from the diagonal), 0 (the default): as flag-driven 64-row
+ * blocks.
  * uhm_gpu_autotune times candidate values on this mesh (element matrices and
  * right-hand sides copied in; reps factor+solve runs per candidate, the
  * fastest kept) and leaves the mesh factored and solved with the choice;

@@ -80,7 +80,7 @@ def test_tunables_round_trip_and_limits(native_lib):
     m = api.Mesh()
     assert m.tunables() == dict(small_max_f64=160, small_max_f32=224, tc_min_n=512, gc_min_rows=512,
                                 fuse_potrf_trsm=2, tc_nbo=256, tc_panel=256,
-                                solve_rows=64, lookahead=1)
+                                solve_rows=64, lookahead=1, solve_chain=0)
     m.set_tunables(tc_min_n=768, small_max_f32=128)
     assert m.tunables()["tc_min_n"] == 768 and m.tunables()["small_max_f32"] == 128
     # whole-front shared-memory kernels hold at most 160 (FP64) / 224 (FP32) rows

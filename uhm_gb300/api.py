@@ -379,7 +379,7 @@ class Mesh:
                 "bwd_store", "tc_pack", "tc_syrk_bf16", "fwd_flags", "bwd_flags", "getrf_coop",
                 "laswp", "potrf_trsm", "assemble_scatter", "tc_gemm_bf16", "chol_panel", "tc_chol_trail",
                 "tc_chol_schur", "clear_flags", "chol_diag", "chol_pack", "tc_chol_trsm", "event_record",
-                "event_wait"] + [f"op{k}" for k in range(35, 40)]
+                "event_wait", "fwd_chain", "bwd_chain"] + [f"op{k}" for k in range(37, 40)]
 
     def set_profiling(self, on=True):
         self._check(self.L.uhm_gpu_set_profiling(C.byref(self.h), int(on)))
@@ -472,7 +472,7 @@ class Mesh:
 
     # -- kernel-selection thresholds --------------------------------------------
     TUNABLES = ("small_max_f64", "small_max_f32", "tc_min_n", "gc_min_rows", "fuse_potrf_trsm", "tc_nbo",
-                "tc_panel", "solve_rows", "lookahead")
+                "tc_panel", "solve_rows", "lookahead", "solve_chain")
 
     def tunables(self) -> dict:
         v = np.zeros(len(self.TUNABLES), np.int32)

@@ -44,6 +44,9 @@ Engine::~Engine() {
   release_staging();
   for (cudaEvent_t e : evpool) cudaEventDestroy(e);
   if (stream2) cudaStreamDestroy(stream2);
+  if (stream3) cudaStreamDestroy(stream3);
+  if (ev_up) cudaEventDestroy(ev_up);
+  if (ev_anorm) cudaEventDestroy(ev_anorm);
   if (stream) cudaStreamDestroy(stream);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
@@ -69,6 +72,8 @@ void* Engine::dmalloc(size_t bytes) {
 
 void Engine::free_device() {
   if (stream) cudaStreamSynchronize(stream);
+  if (stream3) cudaStreamSynchronize(stream3);
+  anorm_pending = false;
   clear_graphs();
   for (void* p : allocations) cudaFree(p);
   allocations.clear();
@@ -76,6 +81,7 @@ void Engine::free_device() {
   ctx = DevCtx{};
   d_items = nullptr;
   d_b = d_x = d_r = d_d = d_erhs = d_y = d_red = d_scratch = nullptr;
+  d_sel = nullptr;
   d_ws = nullptr;
   d_ws_off = d_ws_stride = nullptr;
   d_ws2 = nullptr;
@@ -661,7 +667,7 @@ void Engine::build_plan(int method) {
     f.off = an;
     an += ((int64_t)n * n + 63) / 64 * 64;
     f.voff = vec_n;
-    vec_n += 2 * (int64_t)n * nr;          // z slab (forward) and y slab (solution)
+    vec_n += 3 * (int64_t)n * nr;          // z slab (forward), y slab (solution), w slab (chain partial sums)
     f.piv_off = piv_n;
     piv_n += f.fs;
   }
@@ -1387,6 +1393,33 @@ void Engine::build_programs(int method) {
         else large.push_back(s);
       }
       push(fwd_ops, OP_FWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
+      if (chol && nr <= NR_FLAGS_MAX && !large.empty() && dt == F32 && tune.solve_rows == 64 &&
+          tune.solve_chain && (int)large.size() <= CH_MAX_CHAINS) {
+        // one chain launch for every large front of this level (per group of
+        // FLAG_NR right-hand sides): the chains, the helpers of row blocks
+        // b > CH_K in ascending b, then the ABL row blocks
+        std::vector<Item> ci;
+        int maxb = 0;
+        for (int s : large) {
+          ci.push_back(Item{s, 0, CH_CHAIN, 0});
+          maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        }
+        for (int b = CH_K + 1; b < maxb; ++b)
+          for (int s : large)
+            if (b < (fronts[s].fs + NB - 1) / NB) ci.push_back(Item{s, b, CH_HELPER, 0});
+        for (int s : large) {
+          const HostFront& f = fronts[s];
+          const int nfb = (f.fs + NB - 1) / NB;
+          for (int k = 0; k * NB < f.ss; ++k) ci.push_back(Item{s, nfb + k, CH_ABL, 0});
+        }
+        const int64_t io = add_items(ci);
+        for (int q0 = 0; q0 < nr; q0 += FLAG_NR) {
+          Op op{OP_FWD_CHAIN, dt, 0, 0, io, (int)ci.size()};
+          op.q0 = q0;
+          fwd_ops.push_back(op);
+        }
+        large.clear();
+      }
       if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
         // one flag-driven launch for every large front of this level (per
         // group of FLAG_NR right-hand sides)
@@ -1447,6 +1480,31 @@ void Engine::build_programs(int method) {
         else { large.push_back(s); st.push_back(Item{s, 0, 0, 0}); }
       }
       push(bwd_ops, OP_BWD_SMALL, dt, staged_bytes(sm, dt), gm, sm);
+      if (chol && nr <= NR_FLAGS_MAX && !large.empty() && dt == F32 && tune.solve_rows == 64 &&
+          tune.solve_chain && (int)large.size() <= CH_MAX_CHAINS) {
+        // the chains, then the helpers of the column blocks that have rows
+        // outside the chain's window (ABL rows, or factor blocks below
+        // b + CH_K) in descending b
+        std::vector<Item> ci;
+        int maxb = 0;
+        for (int s : large) {
+          ci.push_back(Item{s, 0, CH_CHAIN, 0});
+          maxb = std::max(maxb, (fronts[s].fs + NB - 1) / NB);
+        }
+        for (int b = maxb - 1; b >= 0; --b)
+          for (int s : large) {
+            const HostFront& f = fronts[s];
+            const int nfb = (f.fs + NB - 1) / NB;
+            if (b < nfb && (f.ss > 0 || b + CH_K + 1 <= nfb - 1)) ci.push_back(Item{s, b, CH_HELPER, 0});
+          }
+        const int64_t io = add_items(ci);
+        for (int q0 = 0; q0 < nr; q0 += FLAG_NR) {
+          Op op{OP_BWD_CHAIN, dt, 0, 0, io, (int)ci.size()};
+          op.q0 = q0;
+          bwd_ops.push_back(op);
+        }
+        large.clear();
+      }
       if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
         std::vector<Item> bi;
         const int per = tune.solve_rows / NB;    // 64-column blocks per CTA (k_bwd_flags4 at 4)
@@ -1506,6 +1564,9 @@ void Engine::alloc_device(int method) {
   if (!stream) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_up, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_anorm, cudaEventDisableTiming));
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
   }
@@ -1601,6 +1662,10 @@ void Engine::alloc_device(int method) {
   d_erhs = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, erhs_total));
   d_y = (double*)dmalloc(sizeof(double) * std::max<int64_t>(1, y_total));
   d_red = (double*)dmalloc(sizeof(double) * 2560);
+  // the selector's scratch, kept with the plan (a per-call cudaMalloc /
+  // cudaFree pair would synchronise the device on every new set of matrices)
+  d_sel = (float*)dmalloc(sizeof(float) * (4 * esrc.size() + fronts.size() * (uhm_gpu::SEL_F + uhm_gpu::SEL_C) +
+                                           uhm_gpu::SEL_NPARAMS + 4));
   {
     // tree of every global dof (roots numbered in slot order)
     std::vector<int> root_of(fronts.size(), -1);
@@ -1787,6 +1852,8 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
           launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
                            st);
         break;
+      case OP_FWD_CHAIN: launch_fwd_chain(ctx, it, op.n_items, d_ticket, d_err, op.q0, st); break;
+      case OP_BWD_CHAIN: launch_bwd_chain(ctx, it, op.n_items, d_ticket, d_err, op.q0, st); break;
       case OP_BWD_FLAGS:
         if (op.aux == 256)
           launch_bwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
@@ -2010,7 +2077,9 @@ void Engine::check_device_error(const char* where) {
   CK(cudaMemcpy(&derr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (derr) {
     CK(cudaMemset(d_err, 0, sizeof(int)));
-    fail(std::string(where) + ": a device wait gave up (bounded wait expired)", 14);
+    const int at = uhm_gpu::solve_wait_where();
+    fail(std::string(where) + ": a device wait gave up (bounded wait expired" +
+             (at > 0 ? ", solve hand-off " + std::to_string(at) : std::string()) + ")", 14);
   }
 }
 
@@ -2115,12 +2184,14 @@ void Engine::refine(int method) {
     timing = keep;
     timing.factor_ms += t2.factor_ms;
     timing.solve_ms += t2.solve_ms;
+    timing.berr = backward_error();    // of the FP64 solution now in x
     status = 20;
     last_error = "refinement missed its tolerance; solution recomputed in FP64";
   }
 }
 
 void Engine::compute_residual(const double* x, double* r) {
+  sync_anorm();
   launch_elem_gemv(ctx.emat, d_emat_off, d_elem_m, d_emap_off, d_emap, x, n_global, d_y, d_y_off,
                    (int)esrc.size(), mesh->n_rhs, stream);
   launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, d_b, n_global, r, n_global, mesh->n_rhs, 1, stream);
@@ -2144,14 +2215,28 @@ double Engine::residual_norm1() {
 // ||A||_inf of the assembled operator sum_e P_e^T A_e P_e, exact, on the device
 // (k_anorm_partial + deterministic per-dof gather); result in d_red[1536]
 void Engine::enqueue_anorm() {
+  // on its own stream, after the element matrices' upload on the main
+  // stream: it overlaps the factorisation, and the first use joins it
+  sync_anorm();
+  CK(cudaEventRecord(ev_up, stream));
+  CK(cudaStreamWaitEvent(stream3, ev_up, 0));
   launch_anorm_partial(ctx.emat, d_emat_off, d_elem_m, d_emap_off, d_emap, d_dof_ptr, d_dof_el, d_y,
-                       d_y_off, (int)esrc.size(), stream);
-  launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, nullptr, n_global, d_r, n_global, 1, 0, stream);
-  launch_absmax(d_r, n_global, d_red + 1536, stream);
-  if (n_trees > 1) tree_max_async(d_r, n_global, n_global, 3);
+                       d_y_off, (int)esrc.size(), stream3);
+  launch_dof_gather(d_dof_ptr, d_dof_idx, d_y, nullptr, n_global, d_r, n_global, 1, 0, stream3);
+  launch_absmax(d_r, n_global, d_red + 1536, stream3);
+  if (n_trees > 1)
+    launch_absmax_tree(d_r, n_global, n_global, d_dof_tree, n_trees, d_tree_red + (size_t)3 * n_trees, stream3);
+  CK(cudaEventRecord(ev_anorm, stream3));
+  anorm_pending = true;
   anorm_valid = true;
   anorm_inf = -1.0;
   tree_anorm.clear();
+}
+
+void Engine::sync_anorm() {
+  if (!anorm_pending) return;
+  CK(cudaStreamWaitEvent(stream, ev_anorm, 0));
+  anorm_pending = false;
 }
 
 double Engine::read_scalar(const double* d) {
@@ -2194,6 +2279,7 @@ double Engine::forest_berr(const std::vector<double>& rn, const std::vector<doub
 
 double Engine::operator_norm_inf() {
   if (!anorm_valid) enqueue_anorm();
+  sync_anorm();
   if (anorm_inf < 0) anorm_inf = read_scalar(d_red + 1536);
   return anorm_inf;
 }
@@ -2233,12 +2319,9 @@ void Engine::front_features(std::vector<float>& feat) {
   const int ne = (int)esrc.size();
   std::vector<float> st((size_t)ne * 4, 0.f);
   if (ne) {
-    float* d_st = nullptr;
-    CK(cudaMalloc(&d_st, sizeof(float) * 4 * (size_t)ne));
-    uhm_gpu::launch_elem_stats(ctx.emat, d_emat_off, d_elem_m, ne, d_st, stream);
-    CK(cudaMemcpyAsync(st.data(), d_st, sizeof(float) * st.size(), cudaMemcpyDeviceToHost, stream));
+    uhm_gpu::launch_elem_stats(ctx.emat, d_emat_off, d_elem_m, ne, d_sel, stream);
+    CK(cudaMemcpyAsync(st.data(), d_sel, sizeof(float) * st.size(), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    CK(cudaFree(d_st));
   }
   struct Agg {
     double cnt = 0, dmax = 0, dmin = 1e300, rsum = 0, rmin = 1e300, osum = 0, omin = 1e300;
@@ -2324,11 +2407,9 @@ void Engine::apply_selector(int method) {
   std::vector<float> feat;
   front_features(feat);
   const int nf = (int)fronts.size();
-  float *d_feat = nullptr, *d_par = nullptr;
-  float* d_prob = nullptr;
-  CK(cudaMalloc(&d_feat, sizeof(float) * std::max<size_t>(1, feat.size())));
-  CK(cudaMalloc(&d_par, sizeof(float) * selector_params.size()));
-  CK(cudaMalloc(&d_prob, sizeof(float) * uhm_gpu::SEL_C * (size_t)std::max(1, nf)));
+  float* d_feat = d_sel + 4 * esrc.size();
+  float* d_par = d_feat + (size_t)nf * uhm_gpu::SEL_F;
+  float* d_prob = d_par + uhm_gpu::SEL_NPARAMS;
   CK(cudaMemcpyAsync(d_feat, feat.data(), sizeof(float) * feat.size(), cudaMemcpyHostToDevice, stream));
   CK(cudaMemcpyAsync(d_par, selector_params.data(), sizeof(float) * selector_params.size(),
                      cudaMemcpyHostToDevice, stream));
@@ -2336,9 +2417,6 @@ void Engine::apply_selector(int method) {
   std::vector<float> prob((size_t)uhm_gpu::SEL_C * nf);
   CK(cudaMemcpyAsync(prob.data(), d_prob, sizeof(float) * prob.size(), cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
-  CK(cudaFree(d_feat));
-  CK(cudaFree(d_par));
-  CK(cudaFree(d_prob));
   std::vector<int> depth(nf, 0);
   int max_depth = 0;
   for (int s = nf - 1; s >= 0; --s) {
@@ -2377,6 +2455,7 @@ void Engine::set_tunables(const int* v) {
   t.tc_panel = v[6];
   t.solve_rows = v[7];
   t.lookahead = v[8] ? 1 : 0;
+  t.solve_chain = v[9] ? 1 : 0;
   if (t.small_max_f64 < 1 || t.small_max_f64 > SMALL_MAX_F64 || t.small_max_f32 < 1 ||
       t.small_max_f32 > SMALL_MAX_F32 || t.tc_min_n < 256 || t.gc_min_rows < 64 ||
       (t.tc_nbo != 128 && t.tc_nbo != 256 && t.tc_nbo != 512) ||
@@ -2398,6 +2477,7 @@ void Engine::get_tunables(int* v) const {
   v[6] = tune.tc_panel;
   v[7] = tune.solve_rows;
   v[8] = tune.lookahead;
+  v[9] = tune.solve_chain;
 }
 
 int Engine::autotune(int method, int reps) {
@@ -2440,6 +2520,7 @@ int Engine::autotune(int method, int reps) {
   if (!lu) knobs.push_back({&tune.tc_panel, {0, 256, 512}});
   if (!lu) knobs.push_back({&tune.solve_rows, {64, 256}});
   if (!lu) knobs.push_back({&tune.lookahead, {0, 1}});
+  if (!lu) knobs.push_back({&tune.solve_chain, {0, 1}});
   if (!lu) knobs.push_back({&tune.tc_nbo, {128, 256, 512}});
   if (lu) knobs.push_back({&tune.gc_min_rows, {256, 512, 1024, 2048, 1 << 30}});
   int timed = 0;

@@ -83,7 +83,7 @@ enum OpKind : int {
   OP_TRSV_B, OP_BWD_STORE, OP_TC_PACK, OP_TC_SYRK, OP_FWD_FLAGS, OP_BWD_FLAGS, OP_GETRF_COOP,
   OP_LASWP, OP_POTRF_TRSM, OP_ASSEMBLE_SCATTER, OP_TC_GEMM, OP_CHOL_PANEL, OP_TC_CHOL_TRAIL,
   OP_TC_CHOL_SCHUR, OP_CLEAR_FLAGS, OP_CHOL_DIAG, OP_CHOL_PACK, OP_TC_CHOL_TRSM, OP_EV_RECORD, OP_EV_WAIT,
-  OP_KIND_END
+  OP_FWD_CHAIN, OP_BWD_CHAIN, OP_KIND_END
 };
 static_assert(OP_KIND_END <= N_OP_KINDS, "profile arrays hold N_OP_KINDS op kinds");
 
@@ -112,8 +112,12 @@ struct Tunables {
   int solve_rows = 64;       // rows (columns) per CTA of the flag-driven forward (backward) solves of
                              // large Cholesky fronts (64 or 256)
   int lookahead = 1;         // panels of 256: the next panel's diagonal kernel overlaps the update
+  int solve_chain = 0;       // 1: 64-row solves of FP32 fronts as chains (one CTA per front solves
+                             // the diagonal blocks, helper CTAs the rest); 0: the flag-driven
+                             // kernels, faster on the meshes measured (the chain CTA's per-step
+                             // block loads from one SM bound it)
 };
-constexpr int N_TUNABLES = 9;
+constexpr int N_TUNABLES = 10;
 
 class Engine {
  public:
@@ -226,6 +230,10 @@ class Engine {
   int factored_method = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;    // side stream of the panel lookahead
+  cudaStream_t stream3 = nullptr;    // side stream of ||A||_inf, beside the factorisation
+  cudaEvent_t ev_up = nullptr, ev_anorm = nullptr;
+  bool anorm_pending = false;        // ||A||_inf enqueued on stream3, not yet joined into stream
+  void sync_anorm();                 // stream waits for it (it writes d_y, d_r and d_red[1536..])
   std::vector<cudaEvent_t> evpool;   // events ordering the two streams (by id)
   static bool is_kernel_op(int kind) {
     return kind != OP_CLEAR_FLAGS && kind != OP_EV_RECORD && kind != OP_EV_WAIT;
@@ -276,6 +284,7 @@ class Engine {
   double* d_y = nullptr;        // per-element A_e x_e
   double* d_red = nullptr;      // reduction scratch
   double* d_scratch = nullptr;  // backward-solve partial sums
+  float* d_sel = nullptr;       // selector scratch: element statistics, features, parameters, probabilities
   int64_t* d_scr_off = nullptr;
   int* d_counters = nullptr;
   void* d_ws2 = nullptr;             // chunk-major BF16 parts of the cooperative-panel fronts

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
   const int n = f.n;
   double* __restrict__ z = c.vec + f.voff;
   double* __restrict__ y = z + (int64_t)n * c.n_rhs;
+  double* __restrict__ w = y + (int64_t)n * c.n_rhs;
   const int32_t* __restrict__ inv = c.inv + f.inv_off;
   // rows [it.a, it.a + it.b) of the front (it.b == 0: all rows; only then
   // are pivots applied, which needs the whole gathered vector)
@@ -50,9 +51,13 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
         }
       }
       z[I + (int64_t)q * n] = acc;
-      // fronts of the 64-row flag-driven solves: their y factor rows are the
-      // forward hand-off, emptied here (the forward launch comes after)
-      if (it.c && I < f.fs) y[I + (int64_t)q * n] = __longlong_as_double((long long)HAND_EMPTY);
+      // fronts of the 64-row flag-driven and chain solves: their y factor
+      // rows (solutions) and w factor rows (partial sums) are forward
+      // hand-offs, emptied here (the forward launch comes after)
+      if (it.c && I < f.fs) {
+        y[I + (int64_t)q * n] = __longlong_as_double((long long)HAND_EMPTY);
+        w[I + (int64_t)q * n] = __longlong_as_double((long long)HAND_EMPTY);
+      }
     }
   }
   __syncthreads();
@@ -851,6 +856,22 @@ __device__ __forceinline__ void st_hand(double* p, double v) {
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(v)) : "memory");
 }
 
+// Where the first hand-off wait of a solve gave up (0: none): kind * 10^8 +
+// awaited block * 10^4 + the waiting block (kind 1 forward rows, 2 backward
+// columns, 3 forward chain, 4 backward chain), read and cleared by the host
+// with the error word.
+__device__ int g_solve_where = 0;
+__device__ __forceinline__ int wait_code(int kind, int awaited, int own) {
+  return kind * 100000000 + min(awaited, 9999) * 10000 + min(own, 9999);
+}
+int solve_wait_where() {
+  int v = 0;
+  const int zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_solve_where, sizeof(int)) != cudaSuccess) return -1;
+  if (v) cudaMemcpyToSymbol(g_solve_where, &zero, sizeof(int));
+  return v;
+}
+
 // Warp 0 of a CTA: the 64 hand-off words of one block and right-hand side
 // (entries lane and lane + 32; entries at or past kb read as 0).
 struct HandWords {
@@ -863,13 +884,16 @@ struct HandWords {
   __device__ __forceinline__ bool full() const {
     return __all_sync(0xffffffffu, w0 != HAND_EMPTY && w1 != HAND_EMPTY);
   }
-  // bounded wait until every word is written; false (and *err = 2) when the
-  // limit runs out
-  __device__ __forceinline__ bool wait(const double* base, int kb, int* err) {
+  // bounded wait until every word is written; false (and *err = 2, where
+  // recorded) when the limit runs out
+  __device__ __forceinline__ bool wait(const double* base, int kb, int* err, int where) {
     const uint32_t lim = g_wait_limit;
     for (uint32_t i = 0; !full(); ++i) {
       if (i >= lim) {
-        if ((threadIdx.x & 31) == 0) atomicExch(err, 2);
+        if ((threadIdx.x & 31) == 0) {
+          atomicExch(err, 2);
+          atomicCAS(&g_solve_where, 0, where);
+        }
         return false;
       }
       __nanosleep(32);
@@ -884,6 +908,67 @@ struct HandWords {
     dst[lane + 32] = (CT)__longlong_as_double(w1);
   }
 };
+
+// acc[q] += sum over the column blocks j < jend of L[row, block j] y_j for
+// the CTA's rows (thread: row lane tid % 64, column group tid / 64), y_j read
+// from its hand-off words: warp 0 polls and stages them (the next block's
+// words already in flight), the other warps wait at the block barrier.
+template <typename T>
+__device__ __forceinline__ void fwd_gather_blocks(const DevCtx& c, const FrontDev& f, int row, bool rv, int jend,
+                                                  int q0, int nq, int* err, T (&acc)[SF_NR],
+                                                  T (*ysh)[SF_NR][FB]) {
+  using CT = T;
+  const int n = f.n, fs = f.fs, g = threadIdx.x / FB;
+  const T* __restrict__ G = arena<T>(c) + f.off;
+  const double* __restrict__ y = c.vec + f.voff + (int64_t)n * c.n_rhs;
+  // The factor tile of block column j does not depend on y: it is loaded one
+  // block ahead, so that only the loads of y_j follow the wait.
+  CT tile[16];
+  auto load_tile = [&](int j) {
+    const int kbj = min(FB, fs - j * FB);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int cc = g * 16 + u;
+      tile[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
+    }
+  };
+  const bool w0 = threadIdx.x < 32;
+  HandWords hw;
+  bool live = true;      // warp 0: false once a wait has run out (no more waiting)
+  if (jend > 0) {
+    load_tile(0);
+    if (w0) hw.load(y + (int64_t)q0 * n, min(FB, fs));
+  }
+  for (int j = 0; j < jend; ++j) {
+    const int buf = j & 1;
+    if (w0) {
+      // y_j is read by every later block of the front at once: one warp
+      // per CTA polls and stages it (the next block's words already in flight)
+      const int kbj = min(FB, fs - j * FB);
+      const double* yj = y + j * FB;
+      if (live) live = hw.wait(yj + (int64_t)q0 * n, kbj, err, wait_code(1, j, row / FB));
+      hw.stage(ysh[buf][0]);
+      for (int q = 1; q < nq; ++q) {
+        HandWords hq;
+        hq.load(yj + (int64_t)(q0 + q) * n, kbj);
+        if (live) live = hq.wait(yj + (int64_t)(q0 + q) * n, kbj, err, wait_code(1, j, row / FB));
+        hq.stage(ysh[buf][q]);
+      }
+      if (j + 1 < jend) hw.load(y + (j + 1) * FB + (int64_t)q0 * n, min(FB, fs - (j + 1) * FB));
+    }
+    CT cur[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) cur[u] = tile[u];
+    if (j + 1 < jend) load_tile(j + 1);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q)
+        if (q < nq) acc[q] += cur[u] * ysh[buf][q][g * 16 + u];
+    }
+  }
+}
 
 // item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
 // right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
@@ -911,7 +996,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   }
   const int r0 = factor_block ? b * FB : fs + (b - nfb) * FB;
   const int r1 = factor_block ? min(r0 + FB, fs) : min(r0 + FB, n);
-  const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ z = c.vec + f.voff;
   double* __restrict__ y = z + (int64_t)n * nr;
   const int i = threadIdx.x % FB, g = threadIdx.x / FB;
@@ -930,54 +1014,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
     for (int q = 0; q < SF_NR; ++q)
       if (q < nq) z[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
   }
-  const int jend = factor_block ? b : nfb;
-  // The factor tile of block column j does not depend on y: it is loaded one
-  // block ahead, so that only the loads of y_j follow the wait.
-  CT tile[16];
-  auto load_tile = [&](int j) {
-    const int kbj = min(FB, fs - j * FB);
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int cc = g * 16 + u;
-      tile[u] = (rv && cc < kbj) ? (CT)G[row + (int64_t)(j * FB + cc) * n] : CT(0);
-    }
-  };
-  const bool w0 = threadIdx.x < 32;
-  HandWords hw;
-  bool live = true;      // warp 0: false once a wait has run out (no more waiting)
-  if (jend > 0) {
-    load_tile(0);
-    if (w0) hw.load(y + (int64_t)q0 * n, min(FB, fs));
-  }
-  for (int j = 0; j < jend; ++j) {
-    const int buf = j & 1;
-    if (w0) {
-      // y_j is read by every later block of the front at once: one warp
-      // per CTA polls and stages it (the next block's words already in flight)
-      const int kbj = min(FB, fs - j * FB);
-      const double* yj = y + j * FB;
-      if (live) live = hw.wait(yj + (int64_t)q0 * n, kbj, err);
-      hw.stage(ysh[buf][0]);
-      for (int q = 1; q < nq; ++q) {
-        HandWords hq;
-        hq.load(yj + (int64_t)(q0 + q) * n, kbj);
-        if (live) live = hq.wait(yj + (int64_t)(q0 + q) * n, kbj, err);
-        hq.stage(ysh[buf][q]);
-      }
-      if (j + 1 < jend) hw.load(y + (j + 1) * FB + (int64_t)q0 * n, min(FB, fs - (j + 1) * FB));
-    }
-    CT cur[16];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) cur[u] = tile[u];
-    if (j + 1 < jend) load_tile(j + 1);
-    __syncthreads();
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-#pragma unroll
-      for (int q = 0; q < SF_NR; ++q)
-        if (q < nq) acc[q] += cur[u] * ysh[buf][q][g * 16 + u];
-    }
-  }
+  fwd_gather_blocks<T>(c, f, row, rv, factor_block ? b : nfb, q0, nq, err, acc, ysh);
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
   __syncthreads();
@@ -1186,42 +1223,22 @@ void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtyp
   }
 }
 
-// item: front, a = factor block index, tickets in descending block order;
-// right-hand sides q0 .. q0+NQ-1, accumulated in the same pass over the
-// factor tiles (a pass per right-hand side would put NQ-1 un-overlapped
-// re-reads of the whole block column on the chain of hand-offs)
+// acc[q][u] += sum over the rows r below the factor block (the ABL rows, x
+// known from the parent, then the factor blocks j = nfb - 1 down to stop + 1
+// as their hand-off words arrive) of L[r, 64 b + 16 g + u] x_r, for column
+// block b (thread: row lane tid % 64, column group tid / 64).  Warp 0 polls
+// and stages x_j (the next block's words already in flight).
 template <typename T, int NQ>
-__global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restrict__ items,
-                                                   int* ticket, int* err, int q0) {
+__device__ __forceinline__ void bwd_gather_rows(const DevCtx& c, const FrontDev& f, int b, int stop, int q0, int nq,
+                                                int* err, T (&acc)[NQ][16], T (*xsh)[NQ][FB]) {
   using CT = T;
-  __shared__ int s_t;
-  extern __shared__ __align__(16) unsigned char bwd_dyn[];
-  CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(bwd_dyn);   // [row lane][column]
-  __shared__ CT v[FB][NQ];
-  __shared__ T dsh[FB * (FB + 1)];
-  // x_j staged by warp 0, two buffers alternating by block: one barrier per block
-  __shared__ CT xsh[2][NQ][FB];
-  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
-  __syncthreads();
-  const Item it = items[s_t];
-  const FrontDev f = c.fronts[it.front];
-  const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
-  const int nq = min(NQ, nr - q0);
+  const int n = f.n, fs = f.fs, nr = c.n_rhs;
   const int nfb = (fs + FB - 1) / FB;
   const int c0 = b * FB, kb = min(FB, fs - c0);
-  {
-    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
-    for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[(idx / FB) * (FB + 1) + idx % FB] = Dg[idx];
-  }
   const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ hx = c.vec + f.voff;                  // hand-off: the z slab's factor rows
-  double* __restrict__ y = hx + (int64_t)n * nr;
-  const int rl = threadIdx.x % FB, g = threadIdx.x / FB;   // row lane, column group
-  CT acc[NQ][16];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q)
-#pragma unroll
-    for (int u = 0; u < 16; ++u) acc[q][u] = CT(0);
+  const double* __restrict__ hx = c.vec + f.voff;                  // hand-off: the z slab's factor rows
+  const double* __restrict__ y = hx + (int64_t)n * nr;
+  const int rl = threadIdx.x % FB, g = threadIdx.x / FB;
   // rows below block b: the ABL part (known) first, two row blocks per
   // round with all loads issued before the arithmetic, then factor blocks
   // from the last one down (they complete in that order)
@@ -1260,29 +1277,29 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   const bool w0 = threadIdx.x < 32;
   HandWords hw;
   bool live = true;      // warp 0: false once a wait has run out (no more waiting)
-  if (nfb - 1 > b) {
+  if (nfb - 1 > stop) {
     load_tile(nfb - 1);
     if (w0) hw.load(hx + (nfb - 1) * FB + (int64_t)q0 * n, min(FB, fs - (nfb - 1) * FB));
   }
-  for (int j = nfb - 1, k = 0; j > b; --j, ++k) {
+  for (int j = nfb - 1, k = 0; j > stop; --j, ++k) {
     const int buf = k & 1;
     if (w0) {
       const int kbj = min(FB, fs - j * FB);
       const double* xj = hx + j * FB;
-      if (live) live = hw.wait(xj + (int64_t)q0 * n, kbj, err);
+      if (live) live = hw.wait(xj + (int64_t)q0 * n, kbj, err, wait_code(2, j, b));
       hw.stage(xsh[buf][0]);
       for (int q = 1; q < nq; ++q) {
         HandWords hq;
         hq.load(xj + (int64_t)(q0 + q) * n, kbj);
-        if (live) live = hq.wait(xj + (int64_t)(q0 + q) * n, kbj, err);
+        if (live) live = hq.wait(xj + (int64_t)(q0 + q) * n, kbj, err, wait_code(2, j, b));
         hq.stage(xsh[buf][q]);
       }
-      if (j - 1 > b) hw.load(hx + (j - 1) * FB + (int64_t)q0 * n, min(FB, fs - (j - 1) * FB));
+      if (j - 1 > stop) hw.load(hx + (j - 1) * FB + (int64_t)q0 * n, min(FB, fs - (j - 1) * FB));
     }
     CT cur[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) cur[u] = tile[u];
-    if (j - 1 > b) load_tile(j - 1);
+    if (j - 1 > stop) load_tile(j - 1);
     __syncthreads();
     const int r = j * FB + rl;
     if (r < min(j * FB + FB, fs)) {
@@ -1292,6 +1309,43 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
         for (int q = 0; q < NQ; ++q) acc[q][u] += cur[u] * xsh[buf][q][rl];
     }
   }
+}
+
+// item: front, a = factor block index, tickets in descending block order;
+// right-hand sides q0 .. q0+NQ-1, accumulated in the same pass over the
+// factor tiles (a pass per right-hand side would put NQ-1 un-overlapped
+// re-reads of the whole block column on the chain of hand-offs)
+template <typename T, int NQ>
+__global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restrict__ items,
+                                                   int* ticket, int* err, int q0) {
+  using CT = T;
+  __shared__ int s_t;
+  extern __shared__ __align__(16) unsigned char bwd_dyn[];
+  CT (*red)[FB + 1] = reinterpret_cast<CT (*)[FB + 1]>(bwd_dyn);   // [row lane][column]
+  __shared__ CT v[FB][NQ];
+  __shared__ T dsh[FB * (FB + 1)];
+  // x_j staged by warp 0, two buffers alternating by block: one barrier per block
+  __shared__ CT xsh[2][NQ][FB];
+  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
+  const int nq = min(NQ, nr - q0);
+  const int c0 = b * FB, kb = min(FB, fs - c0);
+  {
+    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b * FB * FB;
+    for (int idx = threadIdx.x; idx < FB * FB; idx += 256) dsh[(idx / FB) * (FB + 1) + idx % FB] = Dg[idx];
+  }
+  double* __restrict__ hx = c.vec + f.voff;                  // hand-off: the z slab's factor rows
+  double* __restrict__ y = hx + (int64_t)n * nr;
+  const int rl = threadIdx.x % FB, g = threadIdx.x / FB;   // row lane, column group
+  CT acc[NQ][16];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[q][u] = CT(0);
+  bwd_gather_rows<T, NQ>(c, f, b, b, q0, nq, err, acc, xsh);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     __syncthreads();
@@ -1549,6 +1603,679 @@ void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype
   const int nq = c.n_rhs - q0 < grp ? c.n_rhs - q0 : grp;
   if (dtype == F64) bwd_flags_t<double>(c, items, n_items, ticket, err, q0, nq, s);
   else bwd_flags_t<float>(c, items, n_items, ticket, err, q0, nq, s);
+}
+
+// ===========================================================================
+// Chain solves of large FP32 Cholesky fronts.
+//
+// In the flag-driven solves every 64-row block waits for its neighbour's
+// solution to cross from one SM to another (a store, the reader's poll, its
+// load): that latency is paid once per block along the whole diagonal.  Here
+// one CTA per front (the chain) solves all diagonal blocks in turn from its
+// own shared memory, and other CTAs (helpers) feed it:
+//
+//   forward   x_b = Dinv_b (z_b - P_b - sum_{j = b-K}^{b-1} L_bj x_j)
+//             P_b = sum_{j < b-K} L_bj x_j            (helper of row block b)
+//   backward  x_b = Dinv_b^T (y_b - P_b - sum_{r = b+1}^{b+K} L_rb^T x_r)
+//             P_b = sum_{r > b+K} L_rb^T x_r + (ABL rows) (helper of column block b)
+//
+// The chain applies the K = CH_K blocks next to the diagonal itself, so a
+// helper's partial sum for block b needs solutions at least K + 1 blocks
+// back: it has K chain steps to arrive.  Solutions and partial sums travel
+// as hand-off words (HAND_EMPTY until written): x in y's factor rows
+// (forward) and z's (backward), P in the third slab w.  The chain stages its
+// window of blocks and the diagonal inverse with cp.async, CH_STAGES - 1
+// steps ahead (asking L2 for them CH_L2_AHEAD steps ahead), and loads each
+// step's right-hand side and partial sum a step ahead; the helpers stream their blocks through shared memory CH_HS - 1
+// ahead.  Rows of ABL (forward) are finished by their own CTAs once every
+// x_j is out.
+//
+// Items: front, a = block, b = role.  Tickets: the chains first, then the
+// helpers in the order their sums are needed, then the ABL rows.  A chain
+// waits on helpers with larger tickets, but a helper needs only chain steps
+// that in turn need only helpers with smaller tickets: as long as the
+// chains and one more CTA fit on the GPU together (at most CH_MAX_CHAINS
+// chains per launch, one CTA per SM), the lowest unfinished helper can
+// always run and finish, and every wait ends.
+// ===========================================================================
+constexpr int CH_STAGES = 3;
+constexpr int CH_LD = 68;           // floats per staged block column: 64 + room for the 16-byte alignment shift
+constexpr int CH_TILE = 64 * CH_LD;
+constexpr int CH_HS = 8;            // shared-memory stages of a helper's blocks
+constexpr int CH_HW = 4;            // blocks of hand-off words warp 0 of a helper keeps in flight
+constexpr int CH_L2_AHEAD = 12;     // steps ahead whose blocks the chain asks L2 for
+
+struct ChainSmem {
+  float L[CH_STAGES][CH_K + 1][CH_TILE];   // per stage: the window's blocks, the diagonal inverse (slot CH_K)
+  float xs[CH_K][SF_NR][FB];               // the window's solutions (block j at j % CH_K)
+  float ts[SF_NR][FB];
+};
+struct ChainRowSmem {
+  float L[CH_HS][CH_TILE];
+  float vsh[2][SF_NR][FB];          // the staged solution values of the current block
+  float red[4][FB][SF_NR];
+  float redb[FB][FB + 1];
+};
+constexpr size_t CH_SMEM = sizeof(ChainSmem) > sizeof(ChainRowSmem) ? sizeof(ChainSmem) : sizeof(ChainRowSmem);
+
+__device__ __forceinline__ void ch_cp16(float* dst, const float* src) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void ch_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ch_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void ch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// The 64 x 64 block of the panel G (ld n) at rows r0.., columns c0.. (c0 a
+// multiple of 64), its first ncols columns staged as columns of CH_LD
+// floats: column cc starts at the 16-byte boundary at or before entry
+// (r0, c0 + cc), so entry (i, cc) is at dst[cc * CH_LD + ch_sh(r0, cc, n) + i].
+// Two columns per warp and pass, 17 chunks of 16 bytes each.  Callers stage
+// only columns left of column n - 1 with r0 < n, n > 66: the up to 3 extra
+// entries either side lie in the neighbouring columns of the same panel.
+__device__ __forceinline__ void ch_stage_block(float* dst, const float* G, int64_t r0, int64_t c0, int64_t n,
+                                               int ncols = 64) {
+  const int lane = threadIdx.x & 31, p = lane & 15;
+  for (int k = threadIdx.x >> 5; 2 * k < ncols; k += blockDim.x >> 5) {
+    const int cc = 2 * k + (lane >> 4);
+    if (cc < ncols) {
+      const int64_t s0 = r0 + (c0 + cc) * n;
+      const float* src = G + (s0 & ~(int64_t)3);
+      float* d = dst + cc * CH_LD;
+      ch_cp16(d + 4 * p, src + 4 * p);
+      if (p == 0) ch_cp16(d + 64, src + 64);
+    }
+  }
+}
+// the alignment shift of staged column cc (c0 a multiple of 4)
+__device__ __forceinline__ int ch_sh(int64_t r0, int cc, int64_t n) {
+  return (int)(((r0 & 3) + (int64_t)(cc & 3) * (n & 3)) & 3);
+}
+// the lower triangle of the 64 x 64 diagonal inverse (column-major, 16-byte
+// aligned): entry (i, t), i >= t, at dst[t * CH_LD + i]; the 16-byte chunks
+// wholly above the diagonal are not copied
+__device__ __forceinline__ void ch_stage_dinv(float* dst, const float* D) {
+  for (int e = threadIdx.x; e < 64 * 16; e += blockDim.x) {
+    const int t = e >> 4, p = e & 15;
+    if (4 * p + 3 >= t) ch_cp16(dst + t * CH_LD + 4 * p, D + 4 * e);
+  }
+}
+__device__ __forceinline__ void ch_l2_dinv(const float* D) {
+  for (int e = threadIdx.x; e < 128; e += blockDim.x) ch_l2(D + 32 * e);
+}
+__device__ __forceinline__ void ch_l2_block(const float* G, int64_t r0, int64_t c0, int64_t n) {
+  for (int e = threadIdx.x; e < 64 * 3; e += blockDim.x) {
+    const int cc = e / 3, p = e - 3 * cc;
+    ch_l2(G + r0 + (c0 + cc) * n + (p == 2 ? 63 : 32 * p));
+  }
+}
+__device__ __forceinline__ float ch_sum4(float v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v + __shfl_xor_sync(0xffffffffu, v, 2);
+}
+
+// Bounded wait of a warp until the lanes' hand-off words (w[q], q < cnt,
+// where need) are written; reloads the missing ones.  Returns false (and
+// sets *err) when the limit runs out.
+template <int NQ>
+__device__ __forceinline__ bool ch_wait_words(unsigned long long (&w)[NQ], const double* const (&p)[NQ], int cnt,
+                                              bool need, int* err, int where) {
+  const uint32_t lim = g_wait_limit;
+  for (uint32_t it = 0;; ++it) {
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      if (need && q < cnt && w[q] == HAND_EMPTY) ok = false;
+    if (__all_sync(0xffffffffu, ok)) return true;
+    if (it >= lim) {
+      if ((threadIdx.x & 31) == 0) {
+        atomicExch(err, 2);
+        atomicCAS(&g_solve_where, 0, where);
+      }
+      return false;
+    }
+    __nanosleep(32);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      if (need && q < cnt && w[q] == HAND_EMPTY) w[q] = ld_hand(p[q]);
+  }
+}
+
+// forward chain of one front (thread: row i = tid / 4, column phase g = tid % 4);
+// right-hand sides q0 .. q0 + nq - 1, nq <= NQ
+template <int NQ>
+__device__ void fwd_chain(const DevCtx& c, const FrontDev& f, int q0, int nq, int* err, ChainSmem& S) {
+  const int tid = threadIdx.x, i = tid >> 2, g = tid & 3;
+  const int64_t n = f.n;
+  const int fs = f.fs, nr = c.n_rhs, nfb = (fs + FB - 1) / FB;
+  const float* __restrict__ G = c.a32 + f.off;
+  const float* __restrict__ Dg = c.dinv32 + f.dinv_off;
+  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ y = z + n * nr;
+  double* __restrict__ w = y + n * nr;
+  // every column this thread reads in a staged block (cc = 4 u + g) has the same shift
+  const int sh = ch_sh(0, g, n);
+  auto stage = [&](int b) {
+    if (b >= nfb) return;
+    float* St = &S.L[b % CH_STAGES][0][0];
+    for (int k = 0; k < CH_K && b - 1 - k >= 0; ++k)
+      ch_stage_block(St + k * CH_TILE, G, (int64_t)b * FB, (int64_t)(b - 1 - k) * FB, n);
+    ch_stage_dinv(St + CH_K * CH_TILE, Dg + (int64_t)b * FB * FB);
+  };
+  auto l2_ahead = [&](int b) {
+    if (b >= nfb) return;
+    for (int k = 0; k < CH_K && b - 1 - k >= 0; ++k) ch_l2_block(G, (int64_t)b * FB, (int64_t)(b - 1 - k) * FB, n);
+    ch_l2_dinv(Dg + (int64_t)b * FB * FB);
+  };
+  for (int b = CH_STAGES - 1; b < CH_L2_AHEAD; ++b) l2_ahead(b);
+  for (int b = 0; b < CH_STAGES - 1; ++b) {
+    stage(b);
+    ch_commit();
+  }
+  // the right-hand side and the helper's words of a step are loaded a step
+  // ahead, so that their round trip is off the chain
+  double zn[NQ];
+  unsigned long long pn[NQ];
+  auto load_rhs = [&](int b) {
+    const int row = b * FB + i;
+    const bool on = b < nfb && g == 0 && i < min(FB, fs - b * FB);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      zn[q] = (on && q < nq) ? z[row + (int64_t)(q0 + q) * n] : 0.0;
+      pn[q] = (on && q < nq && b > CH_K) ? ld_hand(w + row + (int64_t)(q0 + q) * n) : 0ull;
+    }
+  };
+  load_rhs(0);
+  bool live = true;
+  for (int b = 0; b < nfb; ++b) {
+    const int kb = min(FB, fs - b * FB), row = b * FB + i;
+    const bool rv = i < kb, lead = g == 0, helped = b > CH_K;
+    double zq[NQ];
+    unsigned long long pw[NQ];
+    const double* pp[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      pp[q] = w + row + (int64_t)(q0 + q) * n;
+      zq[q] = zn[q];
+      pw[q] = pn[q];
+    }
+    load_rhs(b + 1);
+    ch_wait<CH_STAGES - 2>();
+    __syncthreads();                      // step b's blocks staged, x of step b - 1 visible, stage (b - 1) free
+    stage(b + CH_STAGES - 1);
+    ch_commit();
+    l2_ahead(b + CH_L2_AHEAD);
+    const float* St = &S.L[b % CH_STAGES][0][0];
+    float acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.f;
+    for (int k = 0; k < CH_K; ++k) {
+      const int j = b - 1 - k;
+      if (j < 0) break;
+      const float* T = St + k * CH_TILE + sh + i;
+      const float* xj = &S.xs[j % CH_K][0][0];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int cc = 4 * u + g;
+        const float l = T[cc * CH_LD];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] += l * xj[q * FB + cc];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = ch_sum4(acc[q]);
+    if (helped && live) live = ch_wait_words<NQ>(pw, pp, nq, lead && rv, err, wait_code(3, b, b));
+    if (lead) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const bool on = rv && q < nq;
+        const float p = helped ? (float)__longlong_as_double((long long)pw[q]) : 0.f;
+        S.ts[q][i] = on ? (float)zq[q] - p - acc[q] : 0.f;
+        if (on) {
+          // the right-hand side and the partial sum are consumed: their words
+          // become the backward solve's hand-offs
+          z[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
+          w[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
+        }
+      }
+    }
+    __syncthreads();
+    // x_b = Dinv_b t (Dinv lower triangular)
+    const float* Dm = St + CH_K * CH_TILE + i;
+    float xp[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) xp[q] = 0.f;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int t = 4 * u + g;
+      if (t <= i) {
+        const float d = Dm[t * CH_LD];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) xp[q] += d * S.ts[q][t];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) xp[q] = ch_sum4(xp[q]);
+    if (lead) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const bool on = rv && q < nq;
+        S.xs[b % CH_K][q][i] = on ? xp[q] : 0.f;
+        if (on) st_hand(y + row + (int64_t)(q0 + q) * n, (double)xp[q]);
+      }
+    }
+  }
+  ch_wait<0>();
+}
+
+// backward chain of one front (thread: column cc = tid / 4 of the block, row phase g = tid % 4)
+template <int NQ>
+__device__ void bwd_chain(const DevCtx& c, const FrontDev& f, int q0, int nq, int* err, ChainSmem& S) {
+  const int tid = threadIdx.x, cc = tid >> 2, g = tid & 3;
+  const int64_t n = f.n;
+  const int fs = f.fs, nr = c.n_rhs, nfb = (fs + FB - 1) / FB;
+  const float* __restrict__ G = c.a32 + f.off;
+  const float* __restrict__ Dg = c.dinv32 + f.dinv_off;
+  double* __restrict__ hx = c.vec + f.voff;       // backward hand-off: the z slab's factor rows
+  double* __restrict__ y = hx + n * nr;
+  double* __restrict__ w = y + n * nr;
+  const bool has_abl = fs < f.n;
+  const int sh = ch_sh(0, cc, n);                 // this thread's column in every staged block
+  // step s solves block b = nfb - 1 - s; its window: row blocks b + 1 .. b + CH_K
+  auto stage = [&](int s) {
+    const int b = nfb - 1 - s;
+    if (b < 0) return;
+    float* St = &S.L[s % CH_STAGES][0][0];
+    for (int k = 0; k < CH_K && b + 1 + k < nfb; ++k)
+      ch_stage_block(St + k * CH_TILE, G, (int64_t)(b + 1 + k) * FB, (int64_t)b * FB, n);
+    ch_stage_dinv(St + CH_K * CH_TILE, Dg + (int64_t)b * FB * FB);
+  };
+  auto l2_ahead = [&](int s) {
+    const int b = nfb - 1 - s;
+    if (b < 0) return;
+    for (int k = 0; k < CH_K && b + 1 + k < nfb; ++k) ch_l2_block(G, (int64_t)(b + 1 + k) * FB, (int64_t)b * FB, n);
+    ch_l2_dinv(Dg + (int64_t)b * FB * FB);
+  };
+  for (int s = CH_STAGES - 1; s < CH_L2_AHEAD; ++s) l2_ahead(s);
+  for (int s = 0; s < CH_STAGES - 1; ++s) {
+    stage(s);
+    ch_commit();
+  }
+  // the forward solution and the helper's words of a step, a step ahead
+  double yn[NQ];
+  unsigned long long pn[NQ];
+  auto load_rhs = [&](int s) {
+    const int b = nfb - 1 - s, col = b * FB + cc;
+    const bool on = b >= 0 && g == 0 && cc < min(FB, fs - b * FB);
+    const bool helped = has_abl || b + CH_K + 1 <= nfb - 1;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      yn[q] = (on && q < nq) ? y[col + (int64_t)(q0 + q) * n] : 0.0;
+      pn[q] = (on && q < nq && helped) ? ld_hand(w + col + (int64_t)(q0 + q) * n) : 0ull;
+    }
+  };
+  load_rhs(0);
+  bool live = true;
+  for (int s = 0; s < nfb; ++s) {
+    const int b = nfb - 1 - s;
+    const int kb = min(FB, fs - b * FB), col = b * FB + cc;
+    const bool cv = cc < kb, lead = g == 0;
+    const bool helped = has_abl || b + CH_K + 1 <= nfb - 1;
+    double yq[NQ];
+    unsigned long long pw[NQ];
+    const double* pp[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      pp[q] = w + col + (int64_t)(q0 + q) * n;
+      yq[q] = yn[q];
+      pw[q] = pn[q];
+    }
+    load_rhs(s + 1);
+    ch_wait<CH_STAGES - 2>();
+    __syncthreads();
+    stage(s + CH_STAGES - 1);
+    ch_commit();
+    l2_ahead(s + CH_L2_AHEAD);
+    const float* St = &S.L[s % CH_STAGES][0][0];
+    float acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.f;
+    for (int k = 0; k < CH_K; ++k) {
+      const int r = b + 1 + k;
+      if (r >= nfb) break;
+      const int kbr = min(FB, fs - r * FB);
+      const float* T = St + k * CH_TILE + cc * CH_LD + sh;
+      const float* xr = &S.xs[r % CH_K][0][0];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int ii = 4 * u + g;
+        // rows past the factor block hold other data: skipped, not multiplied by 0
+        const float l = ii < kbr ? T[ii] : 0.f;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] += l * xr[q * FB + ii];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = ch_sum4(acc[q]);
+    if (helped && live) live = ch_wait_words<NQ>(pw, pp, nq, lead && cv, err, wait_code(4, b, b));
+    if (lead) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const bool on = cv && q < nq;
+        const float p = helped ? (float)__longlong_as_double((long long)pw[q]) : 0.f;
+        S.ts[q][cc] = on ? (float)yq[q] - p - acc[q] : 0.f;
+      }
+    }
+    __syncthreads();
+    // x_b = Dinv_b^T t: x[cc] = sum_{t >= cc} Dinv[t][cc] t[t]
+    const float* Dm = St + CH_K * CH_TILE + cc * CH_LD;
+    float xp[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) xp[q] = 0.f;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int t = 4 * u + g;
+      if (t >= cc) {
+        const float d = Dm[t];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) xp[q] += d * S.ts[q][t];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) xp[q] = ch_sum4(xp[q]);
+    if (lead) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const bool on = cv && q < nq;
+        S.xs[b % CH_K][q][cc] = on ? xp[q] : 0.f;
+        if (on) {
+          y[col + (int64_t)(q0 + q) * n] = (double)xp[q];
+          st_hand(hx + col + (int64_t)(q0 + q) * n, (double)xp[q]);
+        }
+      }
+    }
+  }
+  ch_wait<0>();
+}
+
+// Helper and ABL rows of the forward chain: acc[q] = sum over column blocks
+// j < jend of L[row, block j] x_j for the CTA's 64 rows r0.. (thread: row
+// lane tid % 64, column group tid / 64).  The blocks stream through
+// shared memory CH_HS - 1 ahead (cp.async); warp 0 keeps the hand-off words
+// of CH_HW blocks in flight, waits (bounded) for each block's words and
+// stages their values.
+template <int NQ>
+__device__ __forceinline__ void chain_fwd_rows(const DevCtx& c, const FrontDev& f, int r0, int jend, int q0, int nq,
+                                               int* err, float (&acc)[NQ], ChainRowSmem& S) {
+  const int64_t n = f.n;
+  const int fs = f.fs, i = threadIdx.x % FB, g = threadIdx.x / FB;
+  const float* __restrict__ G = c.a32 + f.off;
+  const double* __restrict__ y = c.vec + f.voff + n * c.n_rhs;
+  const bool w0 = threadIdx.x < 32;
+  int sh[4];                        // shift of the staged columns cc with cc % 4 = 0, 1, 2, 3
+#pragma unroll
+  for (int k = 0; k < 4; ++k) sh[k] = ch_sh(r0, k, n);
+  auto kbj = [&](int j) { return min(FB, fs - j * FB); };
+  auto stage = [&](int j) {
+    if (j < jend) ch_stage_block(S.L[j % CH_HS], G, r0, (int64_t)j * FB, n, kbj(j));
+  };
+  for (int j = 0; j < CH_HS - 1; ++j) {
+    stage(j);
+    ch_commit();
+  }
+  HandWords hw[CH_HW];
+  bool live = true;
+  if (w0) {
+#pragma unroll
+    for (int u = 0; u < CH_HW; ++u)
+      if (u < jend) hw[u].load(y + u * FB + (int64_t)q0 * n, kbj(u));
+  }
+  for (int J = 0; J < jend; J += CH_HW) {
+#pragma unroll
+    for (int u = 0; u < CH_HW; ++u) {
+      const int j = J + u;
+      if (j >= jend) break;
+      const int kb = kbj(j);
+      if (w0) {
+        const double* yj = y + j * FB;
+        if (live) live = hw[u].wait(yj + (int64_t)q0 * n, kb, err, wait_code(1, j, r0 / FB));
+        hw[u].stage(S.vsh[j & 1][0]);
+        for (int q = 1; q < nq; ++q) {
+          HandWords hq;
+          hq.load(yj + (int64_t)(q0 + q) * n, kb);
+          if (live) live = hq.wait(yj + (int64_t)(q0 + q) * n, kb, err, wait_code(1, j, r0 / FB));
+          hq.stage(S.vsh[j & 1][q]);
+        }
+        if (j + CH_HW < jend) hw[u].load(y + (j + CH_HW) * FB + (int64_t)q0 * n, kbj(j + CH_HW));
+      }
+      ch_wait<CH_HS - 2>();
+      __syncthreads();
+      stage(j + CH_HS - 1);
+      ch_commit();
+      const float* T = S.L[j % CH_HS] + i;
+      const float* v = &S.vsh[j & 1][0][0];
+#pragma unroll
+      for (int uu = 0; uu < 16; ++uu) {
+        const int cc = g * 16 + uu;
+        // columns past the factor block hold other data: skipped
+        const float l = cc < kb ? T[cc * CH_LD + sh[uu & 3]] : 0.f;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] += l * v[q * FB + cc];
+      }
+    }
+  }
+  ch_wait<0>();
+}
+
+// Helper rows of the backward chain for column block b: acc[q][u] = sum over
+// the row blocks below the chain's window (the ABL rows, x from the parent,
+// then the factor blocks nfb - 1 down to b + CH_K + 1, x from the hand-off
+// words) of L[r, 64 b + 16 g + u] x_r (thread: row lane tid % 64, column
+// group tid / 64); staged as in chain_fwd_rows.
+template <int NQ>
+__device__ __forceinline__ void chain_bwd_rows(const DevCtx& c, const FrontDev& f, int b, int q0, int nq, int* err,
+                                               float (&acc)[NQ][16], ChainRowSmem& S) {
+  const int64_t n = f.n;
+  const int fs = f.fs, nfb = (fs + FB - 1) / FB, rl = threadIdx.x % FB, g = threadIdx.x / FB;
+  const int kbc = min(FB, fs - b * FB);
+  const float* __restrict__ G = c.a32 + f.off;
+  const double* __restrict__ hx = c.vec + f.voff;
+  const double* __restrict__ y = hx + n * c.n_rhs;
+  const int nab = (int)((n - fs + FB - 1) / FB);
+  const int nfar = max(0, nfb - 1 - (b + CH_K));
+  const int tend = nab + nfar;
+  // row block t: the ABL blocks first, then factor blocks from the last one up
+  auto r0_of = [&](int t) { return t < nab ? fs + t * FB : (nfb - 1 - (t - nab)) * FB; };
+  auto rend_of = [&](int t) { return t < nab ? (int)n : min((nfb - 1 - (t - nab)) * FB + FB, fs); };
+  auto src_of = [&](int t) -> const double* { return t < nab ? y : hx; };
+  auto stage = [&](int t) {
+    if (t < tend) ch_stage_block(S.L[t % CH_HS], G, r0_of(t), (int64_t)b * FB, n, kbc);
+  };
+  for (int t = 0; t < CH_HS - 1; ++t) {
+    stage(t);
+    ch_commit();
+  }
+  const bool w0 = threadIdx.x < 32;
+  HandWords hw[CH_HW];
+  bool live = true;
+  if (w0) {
+#pragma unroll
+    for (int u = 0; u < CH_HW; ++u)
+      if (u < tend) hw[u].load(src_of(u) + r0_of(u) + (int64_t)q0 * n, rend_of(u) - r0_of(u));
+  }
+  for (int T0 = 0; T0 < tend; T0 += CH_HW) {
+#pragma unroll
+    for (int u = 0; u < CH_HW; ++u) {
+      const int t = T0 + u;
+      if (t >= tend) break;
+      const int r0 = r0_of(t), kr = rend_of(t) - r0;
+      if (w0) {
+        const double* xr = src_of(t) + r0;
+        if (live) live = hw[u].wait(xr + (int64_t)q0 * n, kr, err, wait_code(2, r0 / FB, b));
+        hw[u].stage(S.vsh[t & 1][0]);
+        for (int q = 1; q < nq; ++q) {
+          HandWords hq;
+          hq.load(xr + (int64_t)(q0 + q) * n, kr);
+          if (live) live = hq.wait(xr + (int64_t)(q0 + q) * n, kr, err, wait_code(2, r0 / FB, b));
+          hq.stage(S.vsh[t & 1][q]);
+        }
+        if (t + CH_HW < tend)
+          hw[u].load(src_of(t + CH_HW) + r0_of(t + CH_HW) + (int64_t)q0 * n, rend_of(t + CH_HW) - r0_of(t + CH_HW));
+      }
+      ch_wait<CH_HS - 2>();
+      __syncthreads();
+      stage(t + CH_HS - 1);
+      ch_commit();
+      if (rl < kr) {
+        // rows past the block (or the front) hold other data: skipped
+        const float* Tt = S.L[t % CH_HS] + rl;
+        int sh[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) sh[k] = ch_sh(r0, k, n);
+        float xv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) xv[q] = S.vsh[t & 1][q][rl];
+#pragma unroll
+        for (int uu = 0; uu < 16; ++uu) {
+          const int cc = g * 16 + uu;
+          const float l = cc < kbc ? Tt[cc * CH_LD + sh[uu & 3]] : 0.f;
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) acc[q][uu] += l * xv[q];
+        }
+      }
+    }
+  }
+  ch_wait<0>();
+}
+
+template <int NQ>
+__device__ __forceinline__ void fwd_chain_cta(const DevCtx& c, const Item& it, const FrontDev& f, int q0, int nq,
+                                              int* err, unsigned char* raw) {
+  if (it.b == CH_CHAIN) {
+    fwd_chain<NQ>(c, f, q0, nq, err, *reinterpret_cast<ChainSmem*>(raw));
+    return;
+  }
+  ChainRowSmem& H = *reinterpret_cast<ChainRowSmem*>(raw);
+  const int n = f.n, fs = f.fs, nfb = (fs + FB - 1) / FB, b = it.a;
+  const bool helper = it.b == CH_HELPER;      // else CH_ABL
+  const int r0 = helper ? b * FB : fs + (b - nfb) * FB;
+  const int r1 = helper ? min(r0 + FB, fs) : min(r0 + FB, n);
+  const int i = threadIdx.x % FB, gg = threadIdx.x / FB, row = r0 + i;
+  const bool rv = row < r1;
+  double* __restrict__ z = c.vec + f.voff;
+  double* __restrict__ w = z + 2 * (int64_t)n * c.n_rhs;
+  if (helper) {
+    // the chain reads this row block's CH_K blocks next to the diagonal and
+    // its inverse from one SM: start them towards L2 long before
+    for (int k = 1; k <= CH_K; ++k) ch_l2_block(c.a32 + f.off, (int64_t)b * FB, (int64_t)(b - k) * FB, n);
+    ch_l2_dinv(c.dinv32 + f.dinv_off + (int64_t)b * FB * FB);
+  }
+  float zr[NQ], acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    acc[q] = 0.f;
+    zr[q] = (!helper && rv && q < nq && gg == 0) ? (float)z[row + (int64_t)(q0 + q) * n] : 0.f;
+  }
+  chain_fwd_rows<NQ>(c, f, r0, helper ? b - CH_K : nfb, q0, nq, err, acc, H);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) H.red[gg][i][q] = acc[q];
+  __syncthreads();
+  if (threadIdx.x < FB && rv) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      if (q >= nq) break;
+      const float sum = H.red[0][i][q] + H.red[1][i][q] + H.red[2][i][q] + H.red[3][i][q];
+      if (helper) st_hand(w + row + (int64_t)(q0 + q) * n, (double)sum);
+      else z[row + (int64_t)(q0 + q) * n] = (double)(zr[q] - sum);
+    }
+  }
+}
+
+template <int NQ>
+__device__ __forceinline__ void bwd_chain_cta(const DevCtx& c, const Item& it, const FrontDev& f, int q0, int nq,
+                                              int* err, unsigned char* raw) {
+  if (it.b == CH_CHAIN) {
+    bwd_chain<NQ>(c, f, q0, nq, err, *reinterpret_cast<ChainSmem*>(raw));
+    return;
+  }
+  ChainRowSmem& H = *reinterpret_cast<ChainRowSmem*>(raw);
+  const int n = f.n, fs = f.fs, b = it.a;
+  const int c0 = b * FB, kb = min(FB, fs - c0);
+  double* __restrict__ w = c.vec + f.voff + 2 * (int64_t)n * c.n_rhs;
+  const int rl = threadIdx.x % FB, gg = threadIdx.x / FB;
+  {
+    // the chain's blocks below this column block's diagonal and its inverse, towards L2
+    const int nfb = (fs + FB - 1) / FB;
+    for (int k = 1; k <= CH_K && b + k < nfb; ++k) ch_l2_block(c.a32 + f.off, (int64_t)(b + k) * FB, (int64_t)b * FB, n);
+    ch_l2_dinv(c.dinv32 + f.dinv_off + (int64_t)b * FB * FB);
+  }
+  float acc[NQ][16];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc[q][u] = 0.f;
+  chain_bwd_rows<NQ>(c, f, b, q0, nq, err, acc, H);
+  // column sums over the 64 row lanes, one right-hand side at a time
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    if (q >= nq) break;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 16; ++u) H.redb[rl][gg * 16 + u] = acc[q][u];
+    __syncthreads();
+    if (threadIdx.x < kb) {
+      float s = 0.f;
+      for (int r = 0; r < FB; ++r) s += H.redb[r][threadIdx.x];
+      st_hand(w + c0 + threadIdx.x + (int64_t)(q0 + q) * n, (double)s);
+    }
+  }
+}
+
+// item: front, a = block, b = role; right-hand sides q0 .. q0 + SF_NR - 1
+__global__ void __launch_bounds__(256, 1) k_fwd_chain(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
+                                                      int q0) {
+  extern __shared__ __align__(16) unsigned char ch_raw[];
+  __shared__ int s_t;
+  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int nq = min(SF_NR, c.n_rhs - q0);
+  if (nq == 1) fwd_chain_cta<1>(c, it, f, q0, nq, err, ch_raw);
+  else if (nq == 2) fwd_chain_cta<2>(c, it, f, q0, nq, err, ch_raw);
+  else fwd_chain_cta<SF_NR>(c, it, f, q0, nq, err, ch_raw);
+}
+
+// item: front, a = column block, b = role (chain or helper); right-hand sides q0 .. q0 + SF_NR - 1
+__global__ void __launch_bounds__(256, 1) k_bwd_chain(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
+                                                      int q0) {
+  extern __shared__ __align__(16) unsigned char ch_raw[];
+  __shared__ int s_t;
+  if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
+  __syncthreads();
+  const Item it = items[s_t];
+  const FrontDev f = c.fronts[it.front];
+  const int nq = min(SF_NR, c.n_rhs - q0);
+  if (nq == 1) bwd_chain_cta<1>(c, it, f, q0, nq, err, ch_raw);
+  else if (nq == 2) bwd_chain_cta<2>(c, it, f, q0, nq, err, ch_raw);
+  else bwd_chain_cta<SF_NR>(c, it, f, q0, nq, err, ch_raw);
+}
+
+void launch_fwd_chain(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                      cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaFuncSetAttribute(k_fwd_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CH_SMEM);
+  k_fwd_chain<<<n_items, 256, CH_SMEM, s>>>(c, items, ticket, err, q0);
+}
+
+void launch_bwd_chain(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                      cudaStream_t s) {
+  if (!n_items) return;
+  cudaMemsetAsync(ticket, 0, sizeof(int), s);
+  cudaFuncSetAttribute(k_bwd_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CH_SMEM);
+  k_bwd_chain<<<n_items, 256, CH_SMEM, s>>>(c, items, ticket, err, q0);
 }
 
 }  // namespace uhm_gpu

@@ -7,7 +7,7 @@
 // as one contiguous panel in HBM.  Fronts live in one arena per storage type
 // (FP64 or FP32).  Right-hand sides travel in a global vector in elimination
 // order (dofs eliminated at front f are the contiguous range g0..g0+fs), plus
-// a per-front vector slab of n x n_rhs for the tree sweeps.
+// per-front vector slabs of n x n_rhs for the tree sweeps (z, y, w).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,7 +19,7 @@ enum Method : int { M_CHOL = 1, M_LU_NOPIV = 2, M_LU_PIV = 3 };
 
 struct FrontDev {
   int64_t off;        // element offset of the panel in its arena
-  int64_t voff;       // element offset of the n x n_rhs vector slab (FP64)
+  int64_t voff;       // element offset of the front's three n x n_rhs vector slabs z, y, w (FP64)
   int64_t inv_off;    // offset of this front's inverse maps (nsrc x n int32)
   int64_t colptr_off; // offset of this front's n+1 column-source pointers
   int64_t sgi_off;    // offset of the ss global dof indices of the schur rows
@@ -132,6 +132,25 @@ void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtyp
                        int n_flags, int* err, int q0, cudaStream_t s);
 void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
                       int* flag_base, int n_flags, int* err, int q0, cudaStream_t s);
+// chain solves of large FP32 Cholesky fronts (one launch per level and group
+// of FLAG_NR right-hand sides).  Items: front, a = block, b = role: CH_CHAIN
+// (one per front, first), CH_HELPER (forward: row blocks b > CH_K in
+// ascending b; backward: column blocks b with ABL rows or b + CH_K + 1 < nfb,
+// in descending b), CH_ABL (forward only: the ABL row blocks a >= nfb, last)
+constexpr int CH_K = 3;
+constexpr int CH_CHAIN = 0, CH_HELPER = 1, CH_ABL = 2;
+// A chain waits on helpers with larger tickets, so every chain of a launch
+// and at least one helper must be resident together (one CTA per SM: the
+// chain's shared memory): levels with more large fronts take the
+// flag-driven kernels.
+constexpr int CH_MAX_CHAINS = 64;
+void launch_fwd_chain(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                      cudaStream_t s);
+void launch_bwd_chain(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
+                      cudaStream_t s);
+// where the first hand-off wait of the solves gave up (0: none; kind * 10^8 +
+// awaited block * 10^4 + waiting block), cleared when read
+int solve_wait_where();
 // blocked solve steps of large fronts (64-column diagonal blocks)
 void launch_fwd_step(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                      cudaStream_t s);
