@@ -787,6 +787,26 @@ void Engine::build_plan(int method) {
   y_total = erhs_total;
 }
 
+// The tensor-core kernel hands its items round robin to one CTA per SM: the
+// last, partial round of a launch is spread over twice as many CTAs by
+// turning each of its tiles into two half tiles of 128 columns (bits 30-31
+// of the item's c, see k_tc_chol).
+static void split_last_round(std::vector<uhm_gpu::Item>& tt, int n_sm) {
+  const int n = (int)tt.size();
+  if (n_sm <= 0 || n < n_sm) return;
+  const int rem = n % n_sm;
+  if (rem == 0 || 2 * rem > n_sm) return;
+  std::vector<uhm_gpu::Item> out(tt.begin(), tt.end() - rem);
+  for (int k = n - rem; k < n; ++k) {
+    uhm_gpu::Item a = tt[k], b = tt[k];
+    a.c = (int)((unsigned)a.c | (1u << 30));
+    b.c = (int)((unsigned)b.c | (2u << 30));
+    out.push_back(a);
+    out.push_back(b);
+  }
+  tt.swap(out);
+}
+
 void Engine::build_programs(int method) {
   const bool chol = method == UHM_CHOL;
   const int nr = mesh->n_rhs;
@@ -1270,6 +1290,7 @@ void Engine::build_programs(int method) {
           ft += get_flop_syrk(0, f.fs, f.ss);
           bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
         }
+        split_last_round(tt, n_sm);
         push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
       } else if (!tccf.empty()) {
         const int W1 = tune.tc_panel;
@@ -1337,6 +1358,7 @@ void Engine::build_programs(int method) {
           ft += get_flop_syrk(0, f.fs, f.ss);
           bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
         }
+        split_last_round(tt, n_sm);
         push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
       }
     }

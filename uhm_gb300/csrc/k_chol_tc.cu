@@ -535,6 +535,11 @@ constexpr uint32_t TCC_STAGE = 6 * TCC_BOX;  // A hi, A lo (128 rows), B hi, B l
 constexpr uint32_t TCC_SMEM = 1024 + TCC_STAGES * TCC_STAGE + 256;
 constexpr int TCC_ERR = 6;
 
+// mode 0 items may stand for half a tile (bits 30-31 of c: 0 the whole
+// 128 x 256 tile, 1 / 2 its first / second 128 columns), so that the last
+// round of a launch can be spread over twice as many CTAs
+__device__ __forceinline__ int tcc_half(const Item& it) { return (int)(((unsigned)it.c >> 30) & 3u); }
+
 // Two modes.
 // mode 0 (update): item front, a = first row r0, b = first column c0,
 // c = kc0 | kc1 << 16 (chunks [kc0, kc1) of the factor block); C -= A B^T
@@ -596,14 +601,16 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         const int n = f.n, nch = (f.fs + 63) / 64;
         int kc0, kc1;
         int64_t ya_h, ya_l, yb_h, yb_l, ya_step, yb_step;   // rows of chunk kc0 and the step per chunk
+        const int hsel = mode == 0 ? tcc_half(it) : 0;
         if (mode == 0) {
           kc0 = it.c & 0xFFFF;
-          kc1 = it.c >> 16;
+          kc1 = (it.c >> 16) & 0x3FFF;
           const int64_t row0 = ws_row0[it.front];
+          const int cb = it.b + (hsel == 2 ? 128 : 0);
           ya_h = row0 + (int64_t)kc0 * n + it.a;
           ya_l = row0 + (int64_t)(nch + kc0) * n + it.a;
-          yb_h = row0 + (int64_t)kc0 * n + it.b;
-          yb_l = row0 + (int64_t)(nch + kc0) * n + it.b;
+          yb_h = row0 + (int64_t)kc0 * n + cb;
+          yb_l = row0 + (int64_t)(nch + kc0) * n + cb;
           ya_step = yb_step = n;
         } else {
           const int K0 = it.c;
@@ -627,14 +634,15 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
           }
           const uint32_t fb = smem_u32(&bars[s]);
           const uint32_t st = smem_u32(smem + s * TCC_STAGE);
-          mbar_expect_tx(fb, TCC_STAGE);
+          // a half tile (128 columns) takes one box of each B part
+          mbar_expect_tx(fb, hsel ? 4 * TCC_BOX : TCC_STAGE);
           const int64_t da = (int64_t)(kc - kc0) * ya_step, db = (int64_t)(kc - kc0) * yb_step;
           tma_load_2d(st + 0 * TCC_BOX, &wsmap, 0, (int)(ya_h + da), fb);
           tma_load_2d(st + 1 * TCC_BOX, &wsmap, 0, (int)(ya_l + da), fb);
           tma_load_2d(st + 2 * TCC_BOX, &wsmap, 0, (int)(yb_h + db), fb);
-          tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, (int)(yb_h + db + 128), fb);
+          if (!hsel) tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, (int)(yb_h + db + 128), fb);
           tma_load_2d(st + 4 * TCC_BOX, &wsmap, 0, (int)(yb_l + db), fb);
-          tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, (int)(yb_l + db + 128), fb);
+          if (!hsel) tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, (int)(yb_l + db + 128), fb);
         }
       }
       // the last loads issued (one per stage at most) land before the CTA exits
@@ -644,16 +652,17 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
   } else if (warp == 9) {
     if (lane == 0) {
       // MMA issuer: per chunk hi*hi, hi*lo, lo*hi, 4 K=16 steps each
-      const uint32_t idesc = idesc_bf16_f32(TCC_BM, TCC_BN);
+      const uint32_t idesc_full = idesc_bf16_f32(TCC_BM, TCC_BN), idesc_half = idesc_bf16_f32(TCC_BM, 128);
       uint32_t g = 0;
       int i = 0;
       bool live = true;
       for (int t = blockIdx.x; t < n_items && live; t += gridDim.x, ++i) {
         const Item it = items[t];
         int kc0, kc1;
+        const uint32_t idesc = (mode == 0 && tcc_half(it)) ? idesc_half : idesc_full;
         if (mode == 0) {
           kc0 = it.c & 0xFFFF;
-          kc1 = it.c >> 16;
+          kc1 = (it.c >> 16) & 0x3FFF;
         } else {
           kc0 = 0;
           kc1 = (min(CD_W, c.fronts[it.front].fs - it.c) + 63) / 64;
@@ -739,12 +748,15 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         mbar_arrive(smem_u32(&acc_empty[b]));
         continue;
       }
+      // a half tile's 128 columns sit in tensor-memory columns 0..127 (warps 0-3)
+      const int hsel = tcc_half(it);
+      const int cbase = it.b + (hsel == 2 ? 128 : 0);
 #pragma unroll 1
-      for (int cc = 0; cc < 4; ++cc) {
+      for (int cc = 0; cc < 4 && !(hsel && half); ++cc) {
         uint32_t v[32];
         TC_LD32(tmem + ((uint32_t)(quarter * 32) << 16) + b * TCC_BN + half * 128 + cc * 32, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int cb = it.b + half * 128 + cc * 32;
+        const int cb = cbase + half * 128 + cc * 32;
         const bool rok = row < n && !*s_abort;
         float cv[32];
 #pragma unroll
