@@ -86,8 +86,7 @@ void Engine::free_device() {
   d_ws_off = d_ws_stride = nullptr;
   d_ws2 = nullptr;
   d_ws2_row0 = nullptr;
-  d_ws2b_row0 = d_linv_row0 = d_linv32_off = nullptr;
-  d_linv32 = nullptr;
+  d_ws2b_row0 = d_linv_row0 = nullptr;
   d_pflags = nullptr;
   d_err = nullptr;
   d_dof_tree = nullptr;
@@ -618,7 +617,6 @@ void Engine::build_plan(int method) {
   arena64_n = arena32_n = vec_n = piv_n = 0;
   ws_total = 0;
   ws2_rows = 0;
-  linv32_n = 0;
   for (auto& f : fronts) {
     if (!f.tcc) continue;
     // two parts (hi, lo) of every 64-column chunk of the factor block, all n rows
@@ -627,7 +625,7 @@ void Engine::build_plan(int method) {
   }
   if (tune.tc_panel == CD_PANEL) {
     // the panel rows before their TRSM (same layout), then per front the
-    // current panel's Linv parts and its FP32 exchange area
+    // current panel's Linv parts
     const int64_t r2 = ws2_rows;
     for (auto& f : fronts) {
       if (!f.tcc) continue;
@@ -638,8 +636,6 @@ void Engine::build_plan(int method) {
       if (!f.tcc) continue;
       f.linv_row0 = ws2_rows;
       ws2_rows += CD_LINV_ROWS;
-      f.linv32_off = linv32_n;
-      linv32_n += (int64_t)CD_PANEL * CD_PANEL;
     }
   }
   if (ws2_rows + 512 > ((int64_t)1 << 31) - 1) fail("operand workspace beyond the tensor map's row range", 4);
@@ -1200,13 +1196,17 @@ void Engine::build_programs(int method) {
             foff[sl] = pf;
             pf += CP_FLAGS_PER_FRONT;
           }
+          // tickets front by front: a front's CTAs wait on one another in
+          // both directions (the factorisation on smaller, the inverse's
+          // column blocks on larger block rows), so the lowest unfinished
+          // front's CTAs are all running once four CTAs fit beside the
+          // concurrent update (at least min(items, 16) SMs are left to them)
           std::vector<Item> dit;
           double fp = 0;
-          for (int rel = 0; rel < 4; ++rel)
-            for (int sl : act) {
-              const int W = std::min(W1, fronts[sl].fs - K0);
-              if (rel < (W + 63) / 64) dit.push_back(Item{sl, K0, rel, (int)foff[sl]});
-            }
+          for (int sl : act) {
+            const int W = std::min(W1, fronts[sl].fs - K0);
+            for (int rel = 0; rel < (W + 63) / 64; ++rel) dit.push_back(Item{sl, K0, rel, (int)foff[sl]});
+          }
           for (int sl : act) fp += get_flop_chol(0, std::min(W1, fronts[sl].fs - K0));
           Op op{OP_CHOL_DIAG, F32, W1, (int)tick, add_items(dit), (int)dit.size()};
           op.flops = fp;
@@ -1625,13 +1625,12 @@ void Engine::alloc_device(int method) {
     d_ws2 = dmalloc(bytes);
     CK(cudaMemsetAsync(d_ws2, 0, bytes, stream));
     if (!tcc_encode(&ws2_map, d_ws2, ws2_rows + 512)) fail("tensor map encoding failed", 4);
-    std::vector<int64_t> r0(fronts.size(), 0), rb(fronts.size(), 0), rl(fronts.size(), 0), lo(fronts.size(), 0);
+    std::vector<int64_t> r0(fronts.size(), 0), rb(fronts.size(), 0), rl(fronts.size(), 0);
     for (auto& f : fronts)
       if (f.tcc) {
         r0[f.slot] = f.ws2_row0;
         rb[f.slot] = f.ws2b_row0;
         rl[f.slot] = f.linv_row0;
-        lo[f.slot] = f.linv32_off;
       }
     auto up64 = [&](int64_t*& d, const std::vector<int64_t>& h) {
       d = (int64_t*)dmalloc(sizeof(int64_t) * h.size());
@@ -1640,8 +1639,6 @@ void Engine::alloc_device(int method) {
     up64(d_ws2_row0, r0);
     up64(d_ws2b_row0, rb);
     up64(d_linv_row0, rl);
-    up64(d_linv32_off, lo);
-    if (linv32_n > 0) d_linv32 = (float*)dmalloc(sizeof(float) * (size_t)linv32_n);
     CK(cudaStreamSynchronize(stream));
   }
   if (pflags_n > 0) d_pflags = (int*)dmalloc(sizeof(int) * (size_t)pflags_n);
@@ -1914,8 +1911,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
                        profiling ? 0 : op.q0);
         break;
       case OP_CHOL_DIAG:
-        launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_linv32, d_ws2, d_linv_row0,
-                         d_linv32_off, st);
+        launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_ws2, d_linv_row0, st);
         break;
       case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, st); break;
       case OP_TC_CHOL_TRSM:

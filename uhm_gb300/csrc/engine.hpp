@@ -36,7 +36,6 @@ struct HostFront {
   int64_t ws2_row0 = 0;            // first 128-byte row of its parts in the chunk-major workspace
   int64_t ws2b_row0 = 0;           // ... of the panel rows before their TRSM (tc_panel 256)
   int64_t linv_row0 = 0;           // ... of the current panel's Linv parts (tc_panel 256)
-  int64_t linv32_off = 0;          // its FP32 Linv exchange area (floats)
   bool blocked = false;            // large front: blocked kernels, 64-col diagonal blocks
   int flag_off = 0;
   int64_t dinv_off = 0;
@@ -294,9 +293,6 @@ class Engine {
   int* d_pflags = nullptr;           // tickets and flags of the panel launches (cleared per factorisation)
   int64_t* d_ws2b_row0 = nullptr;
   int64_t* d_linv_row0 = nullptr;
-  int64_t* d_linv32_off = nullptr;
-  float* d_linv32 = nullptr;
-  int64_t linv32_n = 0;
   int64_t pflags_n = 0;
   void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
   int64_t* d_ws_off = nullptr;

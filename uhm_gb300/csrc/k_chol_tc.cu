@@ -293,14 +293,17 @@ k_chol_panel(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, 
 // ---------------------------------------------------------------------------
 // The panel's W x W diagonal block (W <= 256, nd <= 4 blocks of 64) is
 // factored by nd CTAs exactly as in k_chol_panel (CTA j owns block row j).
-// Each then forms block row j of the inverse Linv of the factored block:
+// Each then forms block COLUMN j of the inverse Linv of the factored block:
 //   Linv[j][j] = L_jj^{-1},
-//   Linv[j][i] = -L_jj^{-1} sum_{k=i}^{j-1} L[j][k] Linv[k][i]      (i < j),
-// taking the rows k < j from the CTAs that own them (flag Q[k], FP32
-// exchange area linv32, row-major W1 x W1 per front).  It writes its rows of
-// Linv, split into BF16 hi / lo, as the B operand of the TRSM on the
-// tensor cores (X = A Linv^T for the rows below the block): row c of Linv
-// = row c of B, chunk i = columns 64 i .. 64 i + 63.
+//   Linv[r][j] = -L_rr^{-1} sum_{k=j}^{r-1} L[r][k] Linv[k][j]      (r > j),
+// keeping its column in shared memory.  The sum for row r needs only the
+// rows of L that CTA r has solved (flags R[r][k]), so it is formed while
+// CTA r still factors; only the product with L_rr^{-1} waits for CTA r's
+// diagonal block (flag D[r]).  (By rows instead, row r needed every earlier
+// row of Linv in turn and the last row finished 40 us after the last
+// diagonal block.)  The blocks are written, split into BF16 hi / lo, as the
+// B operand of the TRSM on the tensor cores (X = A Linv^T for the rows below
+// the block): row c of Linv = row c of B, chunk i = columns 64 i .. 64 i + 63.
 constexpr int CD_W = 256;
 
 struct CdSmem {
@@ -312,16 +315,20 @@ struct CdSmem {
       float Bt[64 * CP_LT];
     } t;
   } u;
-  float Dm[64 * 64];               // L_jj^{-1}, column-major
+  float Dm[64 * 64];               // a 64 x 64 left operand, column-major (L_rk, then Dinv_r)
+  float Lc[4][64 * CP_LT];         // this CTA's column block of Linv, one 64 x 64 block per row block
   int s_t, s_ok;
 };
 
 // item: front, a = K0, b = j (diagonal block), c = flag offset (D at +0, R at
-// +8, Q at +72); linv_row0: first B-operand row of the front's Linv parts
+// +8); linv_row0: first B-operand row of the front's Linv parts.  Items come
+// front by front, and a CTA waits only on CTAs of its own front (the
+// factorisation on smaller block rows, the inverse's column on larger ones):
+// the lowest unfinished front's CTAs have all started, so every wait ends
+// once a front's CTAs fit on the GPU together.
 __global__ void __launch_bounds__(CP_THREADS, 1)
 k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, int* err,
-            float* __restrict__ linv32, __nv_bfloat16* __restrict__ ws, const int64_t* __restrict__ linv_row0,
-            const int64_t* __restrict__ linv32_off) {
+            __nv_bfloat16* __restrict__ ws, const int64_t* __restrict__ linv_row0) {
   extern __shared__ __align__(16) unsigned char cd_raw[];
   CdSmem& S = *reinterpret_cast<CdSmem*>(cd_raw);
   const int tid = threadIdx.x;
@@ -335,9 +342,7 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
   const int r0 = K0 + 64 * rel, rows = min(64, W - 64 * rel);
   int* D = flags + it.c;
   int* R = D + 8;
-  int* Q = D + 72;
   float* __restrict__ G = c.a32 + f.off;
-  float* __restrict__ LI = linv32 + linv32_off[it.front];   // Linv, row-major CD_W x CD_W
   const int ncol = min(W, 64 * (rel + 1));
   for (int idx = tid; idx < 64 * ncol; idx += CP_THREADS) {
     const int i = idx & 63, col = idx >> 6;
@@ -396,76 +401,83 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
     const int i = idx & 63, col = idx >> 6;
     if (i < rows) G[(r0 + i) + (int64_t)(K0 + col) * n] = S.P[idx];
   }
-  // L_jj^{-1} (zero outside the block's kbr rows and columns), column-major
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int r = 4 * ti + u, cc = 4 * tj + v;
-      x[u][v] = (r < kbr && cc < kbr) ? x[u][v] : 0.f;
-      S.Dm[r + cc * 64] = x[u][v];
-    }
-  __syncthreads();
-  // block row rel of Linv: columns i = 0 .. rel (the diagonal block last)
+  // this CTA's column block of Linv: the diagonal block first (zero outside
+  // the block's kbr rows and columns), row-major with rows of CP_LT
   const int64_t lrow0 = linv_row0[it.front];
-  for (int i = 0; i <= rel; ++i) {
-    float out[4][4];
-    if (i == rel) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) out[u][v] = x[u][v];
-    } else {
-      // T = sum_{k=i}^{rel-1} L[rel][k] Linv[k][i]
-      float acc[4][4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-      for (int k = i; k < rel; ++k) {
-        cp_wait(Q + k, err, &S.s_ok);
-        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
-          const int t = idx >> 6, cc = idx & 63;     // Bt row t = row t of Linv[k][i]
-          S.u.t.Bt[t * CP_LT + cc] = __ldcg(LI + (int64_t)(64 * k + t) * CD_W + 64 * i + cc);
-        }
-        __syncthreads();
-        cp_mma_tile(S.P + 64 * k * 64, S.u.t.Bt, 64, acc);
-      }
-      __syncthreads();
-      // out = -L_jj^{-1} T: T as the row-major right operand
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) S.u.t.Bt[(4 * ti + u) * CP_LT + 4 * tj + v] = acc[u][v];
-      __syncthreads();
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) out[u][v] = 0.f;
-      cp_mma_tile(S.Dm, S.u.t.Bt, 64, out);
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) out[u][v] = -out[u][v];
-      __syncthreads();
-    }
-    // FP32 row block for the later rows, BF16 parts as the B operand
+  const int nd = (W + 63) / 64;
+  auto store_b = [&](int r, const float (&out)[4][4]) {
+    // rows 64 r + 4 ti .. of Linv, chunk rel: BF16 parts as the B operand
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int r = 4 * ti + u;
-      *reinterpret_cast<float4*>(LI + (int64_t)(64 * rel + r) * CD_W + 64 * i + 4 * tj) =
-          make_float4(out[u][0], out[u][1], out[u][2], out[u][3]);
+      const int rr = 4 * ti + u;
       __align__(8) __nv_bfloat16 hi[4], lo[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         hi[v] = __float2bfloat16_rn(out[u][v]);
         lo[v] = __float2bfloat16_rn(out[u][v] - __bfloat162float(hi[v]));
       }
-      const int64_t rh = lrow0 + (int64_t)(0 * 4 + i) * CD_W + 64 * rel + r;
-      const int64_t rl = lrow0 + (int64_t)(1 * 4 + i) * CD_W + 64 * rel + r;
+      const int64_t rh = lrow0 + (int64_t)(0 * 4 + rel) * CD_W + 64 * r + rr;
+      const int64_t rl = lrow0 + (int64_t)(1 * 4 + rel) * CD_W + 64 * r + rr;
       *reinterpret_cast<uint2*>(ws + rh * 64 + 4 * tj) = *reinterpret_cast<const uint2*>(hi);
       *reinterpret_cast<uint2*>(ws + rl * 64 + 4 * tj) = *reinterpret_cast<const uint2*>(lo);
     }
+  };
+  {
+    float out[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = 4 * ti + u, cc = 4 * tj + v;
+        out[u][v] = (r < kbr && cc < kbr) ? x[u][v] : 0.f;
+        S.Lc[rel][r * CP_LT + cc] = out[u][v];
+      }
+    store_b(rel, out);
+  }
+  for (int r = rel + 1; r < nd; ++r) {
+    const int kbrr = min(64, W - 64 * r);
+    // T = sum_{k=rel}^{r-1} L[r][k] Linv[k][rel], each L[r][k] once CTA r has solved it
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    for (int k = rel; k < r; ++k) {
+      cp_wait(R + r * 8 + k, err, &S.s_ok);
+      for (int idx = tid; idx < 4096; idx += CP_THREADS) {
+        const int i = idx & 63, t = idx >> 6;      // Dm[t * 64 + i] = L[r][k](i, t)
+        S.Dm[idx] = i < kbrr ? __ldcg(G + (K0 + 64 * r + i) + (int64_t)(K0 + 64 * k + t) * n) : 0.f;
+      }
+      __syncthreads();
+      cp_mma_tile(S.Dm, S.Lc[k], 64, acc);
+      __syncthreads();
+    }
+    // T as the row-major right operand, then Linv[r][rel] = -Dinv_r T
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) S.u.t.Bt[(4 * ti + u) * CP_LT + 4 * tj + v] = acc[u][v];
+    cp_wait(D + r, err, &S.s_ok);
+    {
+      const float* Di = c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + r) * 4096;
+      for (int idx = tid; idx < 4096; idx += CP_THREADS) S.Dm[idx] = __ldcg(Di + idx);
+    }
+    __syncthreads();
+    float out[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) out[u][v] = 0.f;
+    cp_mma_tile(S.Dm, S.u.t.Bt, 64, out);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        out[u][v] = -out[u][v];
+        S.Lc[r][(4 * ti + u) * CP_LT + 4 * tj + v] = out[u][v];
+      }
+    store_b(r, out);
+    __syncthreads();
   }
   // chunks right of the diagonal block are zero (Linv is lower triangular)
   for (int i = rel + 1; i < 4; ++i)
@@ -476,7 +488,6 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
       *reinterpret_cast<uint4*>(ws + rh * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
       *reinterpret_cast<uint4*>(ws + rl * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
     }
-  cp_publish(Q + rel);
 }
 
 // BF16 parts (hi, lo) of the panel's rows below its diagonal block, the A
@@ -823,12 +834,11 @@ void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, 
 }
 
 void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,
-                      float* linv32, void* ws, const int64_t* linv_row0, const int64_t* linv32_off, cudaStream_t s) {
+                      void* ws, const int64_t* linv_row0, cudaStream_t s) {
   if (!n_items) return;
   const int sm = (int)sizeof(CdSmem);
   cudaFuncSetAttribute(k_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  k_chol_diag<<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, flags, err, linv32, (__nv_bfloat16*)ws, linv_row0,
-                                              linv32_off);
+  k_chol_diag<<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, flags, err, (__nv_bfloat16*)ws, linv_row0);
 }
 
 void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws, const int64_t* row0b,

@@ -20,16 +20,16 @@ void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, 
 void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
                     int* err, cudaStream_t s, int mode = 0, const int64_t* row0b = nullptr,
                     const int64_t* linv_row0 = nullptr, void* ws = nullptr, int reserve = 0);
-// a 256-column panel's diagonal block, its inverse in FP32 (linv32) and as
-// BF16 parts (item: front, a = K0, b = diagonal block, c = flag offset)
+// a 256-column panel's diagonal block and its inverse as BF16 parts (item:
+// front, a = K0, b = diagonal block, c = flag offset)
 void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,
-                      float* linv32, void* ws, const int64_t* linv_row0, const int64_t* linv32_off, cudaStream_t s);
+                      void* ws, const int64_t* linv_row0, cudaStream_t s);
 // BF16 parts of a 256-column panel's rows below its diagonal block (item:
 // front, a = K0, b = first row, c = chunk of the panel)
 void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws, const int64_t* row0b,
                       cudaStream_t s);
 constexpr int TCC_TILE_M = 128, TCC_TILE_N = 256;
-constexpr int CP_FLAGS_PER_FRONT = 80;   // D[8] + R[8][8] + Q[8] of one front in one panel launch
+constexpr int CP_FLAGS_PER_FRONT = 80;   // D[8] + R[8][8] (+ 8 spare) of one front in one panel launch
 constexpr int CD_PANEL = 256;            // panel width of the TRSM-on-tensor-cores path
 constexpr int CD_LINV_ROWS = 2 * 4 * 256;   // B-operand rows of one front's Linv parts
 
