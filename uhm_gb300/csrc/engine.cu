@@ -50,6 +50,9 @@ Engine::~Engine() {
   if (stream) cudaStreamDestroy(stream);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (ev_mid) cudaEventDestroy(ev_mid);
+  if (h_words) cudaFreeHost(h_words);
+  if (h_red) cudaFreeHost(h_red);
 }
 
 void Engine::fail(const std::string& msg, int code) {
@@ -783,23 +786,20 @@ void Engine::build_plan(int method) {
   y_total = erhs_total;
 }
 
-// The tensor-core kernel hands its items round robin to one CTA per SM: the
-// last, partial round of a launch is spread over twice as many CTAs by
-// turning each of its tiles into two half tiles of 128 columns (bits 30-31
-// of the item's c, see k_tc_chol).
-static void split_last_round(std::vector<uhm_gpu::Item>& tt, int n_sm) {
-  const int n = (int)tt.size();
-  if (n_sm <= 0 || n < n_sm) return;
-  const int rem = n % n_sm;
-  if (rem == 0 || 2 * rem > n_sm) return;
-  std::vector<uhm_gpu::Item> out(tt.begin(), tt.end() - rem);
-  for (int k = n - rem; k < n; ++k) {
-    uhm_gpu::Item a = tt[k], b = tt[k];
-    a.c = (int)((unsigned)a.c | (1u << 30));
-    b.c = (int)((unsigned)b.c | (2u << 30));
-    out.push_back(a);
-    out.push_back(b);
-  }
+// Every tile as two half tiles of 128 columns, halves wholly above the
+// diagonal left out: the next diagonal block's update is on the critical
+// path of the panel chain and has two tiles only, so half the operand
+// traffic per CTA (and three CTAs instead of two) shortens it.
+static void split_halves(std::vector<uhm_gpu::Item>& tt) {
+  std::vector<uhm_gpu::Item> out;
+  for (const uhm_gpu::Item& t : tt)
+    for (unsigned h = 1; h <= 2; ++h) {
+      const int cb = t.b + (h == 2 ? 128 : 0);
+      if (cb > t.a + 127) continue;
+      uhm_gpu::Item x = t;
+      x.c = (int)((unsigned)x.c | (h << 30));
+      out.push_back(x);
+    }
   tt.swap(out);
 }
 
@@ -823,6 +823,58 @@ void Engine::build_programs(int method) {
     Op op{kind, dtype, nb, param, add_items(it), (int)it.size()};
     op.flops = flops;
     op.bytes = bytes;
+    ops.push_back(op);
+  };
+  // The Schur pass of the tensor-core Cholesky fronts of a level, ABR -=
+  // ABL ABL^T with K = fs: 128 x 256 tiles of the lower triangle, launched in
+  // clusters of two whose CTAs take the two row tiles of one column pair (a
+  // filler where a column has an odd count) and share the column's B
+  // operand; the last partial round of pairs is spread over half tiles.
+  auto push_schur = [&](std::vector<Op>& ops, const std::vector<int>& tccf) {
+    const int TM = TCC_TILE_M, TN = TCC_TILE_N;
+    std::vector<Item> tt;
+    double ft = 0, bt = 0;
+    for (int sl : tccf) {
+      const HostFront& f = fronts[sl];
+      if (f.ss <= 0) continue;
+      const int nch = (f.fs + 63) / 64;
+      for (int c0 = f.fs; c0 < f.n; c0 += TN) {
+        std::vector<int> rows;
+        for (int r0 = f.fs; r0 < f.n; r0 += TM)
+          if (c0 <= r0 + TM - 1) rows.push_back(r0);
+        for (size_t k = 0; k < rows.size(); k += 2) {
+          const Item a{sl, rows[k], c0, 0 | (nch << 16)};
+          tt.push_back(a);
+          if (k + 1 < rows.size()) {
+            tt.push_back(Item{sl, rows[k + 1], c0, a.c});
+          } else {
+            Item d = a;
+            d.c = (int)((unsigned)d.c | (1u << 29));
+            tt.push_back(d);
+          }
+        }
+      }
+      ft += get_flop_syrk(0, f.fs, f.ss);
+      bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
+    }
+    if (tt.empty()) return;
+    // the last partial round of pairs (one pair per cluster of two SMs) as half-tile pairs
+    const int nclu = std::max(1, n_sm / 2), npair = (int)tt.size() / 2, rem = npair % nclu;
+    if (npair >= nclu && rem > 0 && 2 * rem <= nclu) {
+      std::vector<Item> out(tt.begin(), tt.end() - 2 * rem);
+      for (int k = npair - rem; k < npair; ++k)
+        for (unsigned h = 1; h <= 2; ++h)
+          for (int m = 0; m < 2; ++m) {
+            Item x = tt[2 * k + m];
+            x.c = (int)((unsigned)x.c | (h << 30));
+            out.push_back(x);
+          }
+      tt.swap(out);
+    }
+    Op op{OP_TC_CHOL_SCHUR, F32, 0, 0, add_items(tt), (int)tt.size()};
+    op.flops = ft;
+    op.bytes = bt;
+    op.aux = 1;             // paired launch
     ops.push_back(op);
   };
   // one Cholesky step's diagonal block + panel TRSM: fused (every CTA of the
@@ -1258,6 +1310,7 @@ void Engine::build_programs(int method) {
           if (p > 0 && la) fac_ops.push_back(ev_op(OP_EV_WAIT, 2 * p, 0));   // diagonal kernel of panel p done
           push(fac_ops, OP_TC_CHOL_TRSM, F32, 0, 0, xit, fx, bx);
           if (next && la) {
+            split_halves(tdiag);
             push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tdiag, fd, bd);
             fac_ops.push_back(ev_op(OP_EV_RECORD, 2 * p + 1, 0));
             fac_ops.push_back(ev_op(OP_EV_WAIT, 2 * p + 1, 1));
@@ -1278,20 +1331,7 @@ void Engine::build_programs(int method) {
             if (next) fac_ops.push_back(diag_op(K0 + W1));
           }
         }
-        std::vector<Item> tt;
-        double ft = 0, bt = 0;
-        for (int sl : tccf) {
-          const HostFront& f = fronts[sl];
-          if (f.ss <= 0) continue;
-          const int nch = (f.fs + 63) / 64;
-          for (int r0 = f.fs; r0 < f.n; r0 += TM)
-            for (int c0 = f.fs; c0 <= r0 + TM - 1 && c0 < f.n; c0 += TN)
-              tt.push_back(Item{sl, r0, c0, 0 | (nch << 16)});
-          ft += get_flop_syrk(0, f.fs, f.ss);
-          bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
-        }
-        split_last_round(tt, n_sm);
-        push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
+        push_schur(fac_ops, tccf);
       } else if (!tccf.empty()) {
         const int W1 = tune.tc_panel;
         const int TM = TCC_TILE_M, TN = TCC_TILE_N;
@@ -1346,20 +1386,7 @@ void Engine::build_programs(int method) {
           }
           push(fac_ops, OP_TC_CHOL_TRAIL, F32, 0, 0, tt, ft, bt);
         }
-        std::vector<Item> tt;
-        double ft = 0, bt = 0;
-        for (int sl : tccf) {
-          const HostFront& f = fronts[sl];
-          if (f.ss <= 0) continue;
-          const int nch = (f.fs + 63) / 64;
-          for (int r0 = f.fs; r0 < f.n; r0 += TM)
-            for (int c0 = f.fs; c0 <= r0 + TM - 1 && c0 < f.n; c0 += TN)
-              tt.push_back(Item{sl, r0, c0, 0 | (nch << 16)});
-          ft += get_flop_syrk(0, f.fs, f.ss);
-          bt += 8.0 * 0.5 * (double)f.ss * (f.ss + 1) + 2.0 * 2.0 * f.ss * 64.0 * nch;
-        }
-        split_last_round(tt, n_sm);
-        push(fac_ops, OP_TC_CHOL_SCHUR, F32, 0, 0, tt, ft, bt);
+        push_schur(fac_ops, tccf);
       }
     }
   }
@@ -1590,6 +1617,7 @@ void Engine::alloc_device(int method) {
     CK(cudaEventCreateWithFlags(&ev_up, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_anorm, cudaEventDisableTiming));
     CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev_mid));
     CK(cudaEventCreate(&ev1));
   }
   const int nr = mesh->n_rhs;
@@ -1908,14 +1936,15 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
       case OP_TC_CHOL_TRAIL:
       case OP_TC_CHOL_SCHUR:
         launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, st, 0, nullptr, nullptr, nullptr,
-                       profiling ? 0 : op.q0);
+                       profiling ? 0 : op.q0, op.kind == OP_TC_CHOL_SCHUR ? op.aux : 0);
         break;
       case OP_CHOL_DIAG:
         launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_ws2, d_linv_row0, st);
         break;
       case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, st); break;
       case OP_TC_CHOL_TRSM:
-        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, st, 1, d_ws2b_row0, d_linv_row0, d_ws2);
+        launch_tc_chol(ctx, ws2_map, d_ws2_row0, it, op.n_items, d_err, st, 1, d_ws2b_row0, d_linv_row0, d_ws2,
+                       profiling ? 0 : op.q0);
         break;
       case OP_FWD_GATHER: launch_fwd_gather(ctx, it, op.n_items, g_in, n_global, op.param, st); break;
       case OP_FWD_SMALL: launch_fwd_small(ctx, it, op.n_items, op.dtype, op.param, op.nb, st); break;
@@ -1950,18 +1979,38 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
   }
 }
 
-void Engine::check_status(const char* where) {
-  std::vector<int> st(fronts.size());
-  CK(cudaMemcpy(st.data(), ctx.status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost));
-  for (size_t i = 0; i < st.size(); ++i)
-    if (st[i]) {
-      const char* what = st[i] == ST_NOT_SPD ? "front is not positive definite"
-                         : st[i] == ST_ZERO_PIVOT ? "zero pivot"
-                         : st[i] == ST_WAIT ? "a bounded wait inside a kernel gave up" : "NaN in front";
-      status = 10 + st[i];
+// The fronts' status words and the wait error word, copied back behind the
+// work just enqueued (one stream sync for both instead of two round trips)
+void Engine::enqueue_status_words() {
+  const size_t need = fronts.size() + 1;
+  if (h_words_n < need) {
+    if (h_words) cudaFreeHost(h_words);
+    h_words = nullptr;
+    h_words_n = 0;
+    CK(cudaMallocHost((void**)&h_words, sizeof(int) * need));
+    h_words_n = need;
+  }
+  CK(cudaMemcpyAsync(h_words, ctx.status, sizeof(int) * fronts.size(), cudaMemcpyDeviceToHost, stream));
+  CK(cudaMemcpyAsync(h_words + fronts.size(), d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+}
+
+void Engine::read_status_words(const char* where) {
+  for (size_t i = 0; i < fronts.size(); ++i)
+    if (h_words[i]) {
+      const int st = h_words[i];
+      const char* what = st == ST_NOT_SPD ? "front is not positive definite"
+                         : st == ST_ZERO_PIVOT ? "zero pivot"
+                         : st == ST_WAIT ? "a bounded wait inside a kernel gave up" : "NaN in front";
+      status = 10 + st;
       last_error = std::string(where) + ": " + what + " (element " + std::to_string(fronts[i].e->get_id()) + ")";
-      return;
+      break;
     }
+  if (h_words[fronts.size()]) {
+    CK(cudaMemset(d_err, 0, sizeof(int)));
+    const int at = uhm_gpu::solve_wait_where();
+    fail(std::string(where) + ": a device wait gave up (bounded wait expired" +
+             (at > 0 ? ", solve hand-off " + std::to_string(at) : std::string()) + ")", 14);
+  }
 }
 
 void Engine::factor(int method) {
@@ -1980,11 +2029,8 @@ void Engine::factor(int method) {
   CK(cudaEventRecord(ev0, stream));
   upload_elements();
   CK(cudaMemsetAsync(ctx.status, 0, sizeof(int) * fronts.size(), stream));
-  CK(cudaEventRecord(ev1, stream));
-  CK(cudaEventSynchronize(ev1));
+  CK(cudaEventRecord(ev_mid, stream));
   float ms = 0;
-  CK(cudaEventElapsedTime(&ms, ev0, ev1));
-  timing.upload_ms = ms;
   // factor reuse (operation/element.cxx:202-205 skips the merge and the
   // factorisation of a reusable element): keep a front when its element is
   // flagged, its factor from the last factorisation of this plan is held,
@@ -2008,16 +2054,17 @@ void Engine::factor(int method) {
   factored = false;
   solved = false;
   front_kept.clear();
-  CK(cudaEventRecord(ev0, stream));
   if (!anorm_valid) enqueue_anorm();
   if (n_keep > 0) launch_ops(fac_ops_part, nullptr, nullptr, d_items_part);
   else run_ops(fac_ops, nullptr, nullptr);
   CK(cudaEventRecord(ev1, stream));
-  CK(cudaEventSynchronize(ev1));
-  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  enqueue_status_words();
+  CK(cudaStreamSynchronize(stream));
+  CK(cudaEventElapsedTime(&ms, ev0, ev_mid));
+  timing.upload_ms = ms;
+  CK(cudaEventElapsedTime(&ms, ev_mid, ev1));
   timing.factor_ms = ms;
-  check_status("factor");
-  check_device_error("factor");
+  read_status_words("factor");
   if (status && mode == 1) {
     // a low-precision front broke down: escalate the failed fronts to FP64
     std::vector<int> st(fronts.size());
@@ -2109,18 +2156,21 @@ void Engine::solve(int method, int phase) {
   CK(cudaEventRecord(ev0, stream));
   if (phase & 1) assemble_rhs();
   solve_into(method, d_b, d_x, phase);
+  h_x_valid = false;
+  solved = false;
+  if (mode == 1 && phase == 3) {
+    // the refinement's first read-back carries this solve's wait error word
+    // and time (ev0 .. ev_mid)
+    CK(cudaEventRecord(ev_mid, stream));
+    refine(method);
+    return;
+  }
   CK(cudaEventRecord(ev1, stream));
   CK(cudaEventSynchronize(ev1));
   CK(cudaEventElapsedTime(&ms, ev0, ev1));
   timing.solve_ms = ms;
-  h_x_valid = false;
-  solved = false;
   check_device_error("solve");
   solved = phase == 3;
-  if (mode == 1 && phase == 3) {
-    refine(method);
-    return;
-  }
   // plain path: a NaN or infinity in the right-hand sides (or factors)
   // reaches the solution; report it rather than return it silently
   if (phase & 2) {
@@ -2137,39 +2187,63 @@ void Engine::solve(int method, int phase) {
 // A miss after ir_max corrections refactors and solves in plain FP64.
 void Engine::refine(int method) {
   float ms = 0;
-  CK(cudaEventRecord(ev0, stream));
   const int64_t nv = n_global * mesh->n_rhs;
-  const double an = operator_norm_inf();
+  if (!h_red) CK(cudaMallocHost((void**)&h_red, sizeof(double) * 8));
+  const bool forest = n_trees > 1;
+  if (!anorm_valid) enqueue_anorm();
+  sync_anorm();
+  // ||b||_inf and, on the first pass, ||A||_inf and the solve's wait error
+  // word travel with the first residual norms: one stream sync per pass
   launch_absmax(d_b, nv, d_red + 1024, stream);
-  const double bn = read_scalar(d_red + 1024);
-  if (!std::isfinite(bn) || !std::isfinite(an)) {
-    // refinement cannot repair a bad input, and an FP64 redo would not either
-    timing.berr = timing.berr_first = NAN;
-    fail(std::string("refine: the ") + (std::isfinite(bn) ? "operator" : "right-hand side") +
-             " is not finite (NaN or infinity)", 13);
-  }
+  double an = anorm_inf, bn = 0.0;
   double berr = 1.0;
   int it = 0;
-  const bool forest = n_trees > 1;
   if (forest) {
     tree_max_async(d_b, nv, n_global, 2);
     tree_bnorm = read_tree_slot(2);
   }
   for (;; ++it) {
     compute_residual(d_x, d_r);
+    if (!forest) {
+      launch_absmax(d_r, nv, d_red, stream);
+      launch_absmax(d_x, nv, d_red + 512, stream);
+      CK(cudaMemcpyAsync(&h_red[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&h_red[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    }
+    if (it == 0) {
+      CK(cudaMemcpyAsync(&h_red[2], d_red + 1024, sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&h_red[3], d_red + 1536, sizeof(double), cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&h_red[4], d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    if (it == 0) {
+      int derr = 0;
+      std::memcpy(&derr, &h_red[4], sizeof(int));
+      if (derr) {
+        CK(cudaMemset(d_err, 0, sizeof(int)));
+        const int at = uhm_gpu::solve_wait_where();
+        fail(std::string("solve: a device wait gave up (bounded wait expired") +
+                 (at > 0 ? ", solve hand-off " + std::to_string(at) : std::string()) + ")", 14);
+      }
+      CK(cudaEventElapsedTime(&ms, ev0, ev_mid));
+      timing.solve_ms = ms;
+      solved = true;
+      bn = h_red[2];
+      if (!(an >= 0)) an = anorm_inf = h_red[3];
+      if (!std::isfinite(bn) || !std::isfinite(an)) {
+        // refinement cannot repair a bad input, and an FP64 redo would not either
+        timing.berr = timing.berr_first = NAN;
+        fail(std::string("refine: the ") + (std::isfinite(bn) ? "operator" : "right-hand side") +
+                 " is not finite (NaN or infinity)", 13);
+      }
+    }
     if (forest) {
       tree_max_async(d_r, nv, n_global, 0);
       tree_max_async(d_x, nv, n_global, 1);
       const std::vector<double> rn = read_tree_slot(0);
       berr = forest_berr(rn, read_tree_slot(1));
     } else {
-      launch_absmax(d_r, nv, d_red, stream);
-      launch_absmax(d_x, nv, d_red + 512, stream);
-      double h[2];
-      CK(cudaMemcpyAsync(&h[0], d_red, sizeof(double), cudaMemcpyDeviceToHost, stream));
-      CK(cudaMemcpyAsync(&h[1], d_red + 512, sizeof(double), cudaMemcpyDeviceToHost, stream));
-      CK(cudaStreamSynchronize(stream));
-      berr = h[0] / (an * h[1] + bn);
+      berr = h_red[0] / (an * h_red[1] + bn);
     }
     if (it == 0) timing.berr_first = berr;
     if (berr <= ir_tol || it >= ir_max || !(berr == berr)) break;
@@ -2178,7 +2252,7 @@ void Engine::refine(int method) {
   }
   CK(cudaEventRecord(ev1, stream));
   CK(cudaEventSynchronize(ev1));
-  CK(cudaEventElapsedTime(&ms, ev0, ev1));
+  CK(cudaEventElapsedTime(&ms, ev_mid, ev1));
   timing.refine_ms = ms;
   timing.ir_iters = it;
   timing.berr = berr;

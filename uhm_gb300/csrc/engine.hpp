@@ -237,7 +237,12 @@ class Engine {
   static bool is_kernel_op(int kind) {
     return kind != OP_CLEAR_FLAGS && kind != OP_EV_RECORD && kind != OP_EV_WAIT;
   }
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+  int* h_words = nullptr;            // pinned: the fronts' status words and the wait error word, read back together
+  size_t h_words_n = 0;
+  double* h_red = nullptr;           // pinned: scalars the refinement reads back (8)
+  void read_status_words(const char* where);   // after the stream sync that follows the copies of enqueue_status_words
+  void enqueue_status_words();
 
   // element sources
   std::vector<ElemSource> esrc;
@@ -356,7 +361,6 @@ class Engine {
   std::vector<double> read_tree_slot(int slot);
   double forest_berr(const std::vector<double>& rn, const std::vector<double>& xn);
   void refine(int method);
-  void check_status(const char* where);
   void check_device_error(const char* where);
   void* dmalloc(size_t bytes);
   int64_t add_items(const std::vector<uhm_gpu::Item>& it);

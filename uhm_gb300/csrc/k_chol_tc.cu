@@ -362,11 +362,17 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
     }
     __syncthreads();
     cp_gemm64(S.P, cj, cj, S.u.t.Lt, kbj, false);
-    for (int idx = tid; idx < 64 * kbj; idx += CP_THREADS) {
-      const int i = idx & 63, col = idx >> 6;
-      if (i < rows) G[(r0 + i) + (int64_t)(K0 + cj + col) * n] = S.P[i + (cj + col) * 64];
-    }
-    cp_publish(R + rel * 8 + j);
+    // block j of this row block, solved: for the CTAs below and the inverse's
+    // columns.  At the last step it is published after the update of this
+    // CTA's own diagonal block, which is what the chain waits for.
+    auto publish_block = [&]() {
+      for (int idx = tid; idx < 64 * kbj; idx += CP_THREADS) {
+        const int i = idx & 63, col = idx >> 6;
+        if (i < rows) G[(r0 + i) + (int64_t)(K0 + cj + col) * n] = S.P[i + (cj + col) * 64];
+      }
+      cp_publish(R + rel * 8 + j);
+    };
+    if (j < rel - 1) publish_block();
     for (int jp = j + 1; jp <= rel; ++jp) {
       const int cjp = 64 * jp, kbp = min(64, W - cjp);
       if (jp == rel) {
@@ -386,6 +392,7 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
       __syncthreads();
       cp_gemm64(S.P, cj, cjp, S.u.t.Bt, kbj, true);
     }
+    if (j == rel - 1) publish_block();
   }
   // the diagonal block itself
   const int cr = 64 * rel, kbr = rows;
@@ -538,11 +545,12 @@ __global__ void __launch_bounds__(256) k_chol_pack(DevCtx c, const Item* __restr
 // ---------------------------------------------------------------------------
 // 2./3. tensor-core update over 128 x 256 tiles
 // ---------------------------------------------------------------------------
-constexpr int TCC_BM = 128, TCC_BN = 256, TCC_STAGES = 2;
+constexpr int TCC_BM = 128, TCC_BN = 256, TCC_STAGES = 4;
+constexpr int TCC_KSUB = 2;                  // stages per 64-column chunk: 32 columns (64 bytes) each
 constexpr int TCC_THREADS = 320;             // warps 0-7 epilogue, 8 TMA producer, 9 MMA issuer
 constexpr int TCC_EPI_THREADS = 256;
-constexpr uint32_t TCC_BOX = 128 * 128;      // one TMA box: 128 rows of 64 BF16 = 16 KB
-constexpr uint32_t TCC_STAGE = 6 * TCC_BOX;  // A hi, A lo (128 rows), B hi, B lo (256 rows each): 96 KB
+constexpr uint32_t TCC_BOX = 128 * 64;       // one TMA box: 128 rows of 32 BF16 = 8 KB
+constexpr uint32_t TCC_STAGE = 6 * TCC_BOX;  // A hi, A lo (128 rows), B hi, B lo (256 rows each): 48 KB
 constexpr uint32_t TCC_SMEM = 1024 + TCC_STAGES * TCC_STAGE + 256;
 constexpr int TCC_ERR = 6;
 
@@ -550,6 +558,8 @@ constexpr int TCC_ERR = 6;
 // 128 x 256 tile, 1 / 2 its first / second 128 columns), so that the last
 // round of a launch can be spread over twice as many CTAs
 __device__ __forceinline__ int tcc_half(const Item& it) { return (int)(((unsigned)it.c >> 30) & 3u); }
+// a filler item of a pair (bit 29): computed with its partner's rows, stored nowhere
+__device__ __forceinline__ bool tcc_dummy(const Item& it) { return ((unsigned)it.c >> 29) & 1u; }
 
 // Two modes.
 // mode 0 (update): item front, a = first row r0, b = first column c0,
@@ -558,6 +568,13 @@ __device__ __forceinline__ int tcc_half(const Item& it) { return (int)(((unsigne
 // stop at fs for tiles of the factor block (c0 < fs) and at n for tiles of
 // ABR (c0 >= fs); only entries with col <= row are stored (Cholesky keeps
 // the lower triangle).
+// Paired (pair = 1, mode 0, launched in clusters of 2): items 2p and 2p + 1
+// share front, columns and chunks (two row tiles of one column of tiles, or
+// a tile and a filler), and CTA rank r of a cluster takes the items with
+// index = r mod 2.  Each CTA loads its own A and half of the shared B, sent
+// to both CTAs of the cluster (TMA multicast); a stage is reused once both
+// CTAs' MMAs have released it (the MMA completion arrives on the empty
+// barrier of both).  Operand traffic per tile falls from 1.5 to 1 KB per K.
 // mode 1 (TRSM below a panel's diagonal block): item front, a = r0, b = c0
 // (column within the panel), c = K0; X = A Linv^T with A the panel's rows
 // r0.. packed at row0b and B the packed rows c0.. of Linv (linv_row0), K =
@@ -566,7 +583,7 @@ __device__ __forceinline__ int tcc_half(const Item& it) { return (int)(((unsigne
 __global__ void __launch_bounds__(TCC_THREADS, 1)
 k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __restrict__ ws_row0,
           const Item* __restrict__ items, int n_items, int* err, int mode, const int64_t* __restrict__ row0b,
-          const int64_t* __restrict__ linv_row0, __nv_bfloat16* __restrict__ ws) {
+          const int64_t* __restrict__ linv_row0, __nv_bfloat16* __restrict__ ws, int pair) {
   extern __shared__ __align__(1024) uint8_t tcc_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tcc_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TCC_STAGES * TCC_STAGE);
@@ -581,7 +598,7 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
   if (threadIdx.x == 0) {
     for (int s = 0; s < TCC_STAGES; ++s) {
       mbar_init(smem_u32(&bars[s]), 1);
-      mbar_init(smem_u32(&bars[TCC_STAGES + s]), 1);
+      mbar_init(smem_u32(&bars[TCC_STAGES + s]), pair ? 2 : 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&acc_full[b]), 1);
@@ -598,8 +615,11 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // the peer's barriers are initialised before any multicast reaches them
+  if (pair) cluster_sync_all();
   const uint32_t tmem = *s_tmem;
   const uint32_t lim = g_wait_limit;
+  const uint32_t rank = pair ? cluster_rank() : 0;
 
   if (warp == 8) {
     if (lane == 0) {
@@ -615,7 +635,7 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         const int hsel = mode == 0 ? tcc_half(it) : 0;
         if (mode == 0) {
           kc0 = it.c & 0xFFFF;
-          kc1 = (it.c >> 16) & 0x3FFF;
+          kc1 = (it.c >> 16) & 0x1FFF;
           const int64_t row0 = ws_row0[it.front];
           const int cb = it.b + (hsel == 2 ? 128 : 0);
           ya_h = row0 + (int64_t)kc0 * n + it.a;
@@ -635,7 +655,8 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
           ya_step = n;
           yb_step = CD_W;
         }
-        for (int kc = kc0; kc < kc1; ++kc, ++g) {
+        for (int kq = TCC_KSUB * kc0; kq < TCC_KSUB * kc1; ++kq, ++g) {
+          const int kc = kq / TCC_KSUB, xq = 32 * (kq % TCC_KSUB);   // chunk and its first column
           const uint32_t s = g % TCC_STAGES;
           if (g >= TCC_STAGES &&
               !mbar_wait_lim(smem_u32(&bars[TCC_STAGES + s]), ((g / TCC_STAGES) + 1) & 1, s_abort, err, TCC_ERR,
@@ -648,12 +669,23 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
           // a half tile (128 columns) takes one box of each B part
           mbar_expect_tx(fb, hsel ? 4 * TCC_BOX : TCC_STAGE);
           const int64_t da = (int64_t)(kc - kc0) * ya_step, db = (int64_t)(kc - kc0) * yb_step;
-          tma_load_2d(st + 0 * TCC_BOX, &wsmap, 0, (int)(ya_h + da), fb);
-          tma_load_2d(st + 1 * TCC_BOX, &wsmap, 0, (int)(ya_l + da), fb);
-          tma_load_2d(st + 2 * TCC_BOX, &wsmap, 0, (int)(yb_h + db), fb);
-          if (!hsel) tma_load_2d(st + 3 * TCC_BOX, &wsmap, 0, (int)(yb_h + db + 128), fb);
-          tma_load_2d(st + 4 * TCC_BOX, &wsmap, 0, (int)(yb_l + db), fb);
-          if (!hsel) tma_load_2d(st + 5 * TCC_BOX, &wsmap, 0, (int)(yb_l + db + 128), fb);
+          tma_load_2d(st + 0 * TCC_BOX, &wsmap, xq, (int)(ya_h + da), fb);
+          tma_load_2d(st + 1 * TCC_BOX, &wsmap, xq, (int)(ya_l + da), fb);
+          if (!pair) {
+            tma_load_2d(st + 2 * TCC_BOX, &wsmap, xq, (int)(yb_h + db), fb);
+            if (!hsel) tma_load_2d(st + 3 * TCC_BOX, &wsmap, xq, (int)(yb_h + db + 128), fb);
+            tma_load_2d(st + 4 * TCC_BOX, &wsmap, xq, (int)(yb_l + db), fb);
+            if (!hsel) tma_load_2d(st + 5 * TCC_BOX, &wsmap, xq, (int)(yb_l + db + 128), fb);
+          } else if (hsel) {
+            // half tiles: rank 0 sends the hi box, rank 1 the lo box
+            if (rank == 0) tma_load_2d_mc(st + 2 * TCC_BOX, &wsmap, xq, (int)(yb_h + db), fb, 3);
+            else tma_load_2d_mc(st + 4 * TCC_BOX, &wsmap, xq, (int)(yb_l + db), fb, 3);
+          } else {
+            // rank r sends rows 128 r .. 128 r + 127 of both B parts
+            const int off = (int)rank * 128;
+            tma_load_2d_mc(st + (2 + rank) * TCC_BOX, &wsmap, xq, (int)(yb_h + db + off), fb, 3);
+            tma_load_2d_mc(st + (4 + rank) * TCC_BOX, &wsmap, xq, (int)(yb_l + db + off), fb, 3);
+          }
         }
       }
       // the last loads issued (one per stage at most) land before the CTA exits
@@ -673,7 +705,7 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         const uint32_t idesc = (mode == 0 && tcc_half(it)) ? idesc_half : idesc_full;
         if (mode == 0) {
           kc0 = it.c & 0xFFFF;
-          kc1 = (it.c >> 16) & 0x3FFF;
+          kc1 = (it.c >> 16) & 0x1FFF;
         } else {
           kc0 = 0;
           kc1 = (min(CD_W, c.fronts[it.front].fs - it.c) + 63) / 64;
@@ -682,7 +714,7 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         if (u >= 1 && !mbar_wait_lim(smem_u32(&acc_empty[b]), (u - 1) & 1, s_abort, err, TCC_ERR, lim)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t acc = tmem + b * TCC_BN;
-        for (int kc = kc0; kc < kc1; ++kc, ++g) {
+        for (int kq = TCC_KSUB * kc0; kq < TCC_KSUB * kc1; ++kq, ++g) {
           const uint32_t s = g % TCC_STAGES;
           if (!mbar_wait_lim(smem_u32(&bars[s]), (g / TCC_STAGES) & 1, s_abort, err, TCC_ERR, lim)) {
             live = false;
@@ -692,13 +724,15 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
           const uint32_t st = smem_u32(smem + s * TCC_STAGE);
           const uint32_t ah = st, al = st + TCC_BOX, bh = st + 2 * TCC_BOX, bl = st + 4 * TCC_BOX;
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            umma_bf16(acc, sdesc_sw128(ah + k * 32), sdesc_sw128(bh + k * 32), idesc, (kc > kc0 || k > 0) ? 1u : 0u);
+          for (int k = 0; k < 2; ++k)
+            umma_bf16(acc, sdesc_sw64(ah + k * 32), sdesc_sw64(bh + k * 32), idesc,
+                      (kq > TCC_KSUB * kc0 || k > 0) ? 1u : 0u);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) umma_bf16(acc, sdesc_sw128(ah + k * 32), sdesc_sw128(bl + k * 32), idesc, 1u);
+          for (int k = 0; k < 2; ++k) umma_bf16(acc, sdesc_sw64(ah + k * 32), sdesc_sw64(bl + k * 32), idesc, 1u);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) umma_bf16(acc, sdesc_sw128(al + k * 32), sdesc_sw128(bh + k * 32), idesc, 1u);
-          umma_commit(smem_u32(&bars[TCC_STAGES + s]));
+          for (int k = 0; k < 2; ++k) umma_bf16(acc, sdesc_sw64(al + k * 32), sdesc_sw64(bh + k * 32), idesc, 1u);
+          if (pair) umma_commit_mc(smem_u32(&bars[TCC_STAGES + s]), 3);
+          else umma_commit(smem_u32(&bars[TCC_STAGES + s]));
         }
         if (live) umma_commit(smem_u32(&acc_full[b]));
       }
@@ -768,7 +802,7 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
         TC_LD32(tmem + ((uint32_t)(quarter * 32) << 16) + b * TCC_BN + half * 128 + cc * 32, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         const int cb = cbase + half * 128 + cc * 32;
-        const bool rok = row < n && !*s_abort;
+        const bool rok = row < n && !*s_abort && !tcc_dummy(it);
         float cv[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -787,6 +821,8 @@ k_tc_chol(DevCtx c, const __grid_constant__ CUtensorMap wsmap, const int64_t* __
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // neither CTA of a pair leaves while the other may still send it operands
+  if (pair) cluster_sync_all();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TCC_BN));
   }
@@ -809,10 +845,10 @@ bool tcc_encode(CUtensorMap* map, void* base, int64_t rows) {
   }
   cuuint64_t dims[2] = {64, (cuuint64_t)rows};
   cuuint64_t strides[1] = {128};
-  cuuint32_t box[2] = {64, 128};
+  cuuint32_t box[2] = {32, 128};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode_cc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -849,7 +885,7 @@ void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws,
 
 void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
                     int* err, cudaStream_t s, int mode, const int64_t* row0b, const int64_t* linv_row0, void* ws,
-                    int reserve) {
+                    int reserve, int pair) {
   if (!n_items) return;
   static int n_sm = 0;
   if (!n_sm) {
@@ -860,9 +896,29 @@ void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_r
   }
   cudaFuncSetAttribute(k_tc_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TCC_SMEM);
   const int slots = n_sm - reserve > 1 ? n_sm - reserve : 1;
+  if (pair) {
+    // clusters of two CTAs (items come in pairs, n_items even)
+    const int clusters = n_items / 2 < slots / 2 ? n_items / 2 : slots / 2;
+    if (clusters < 1) return;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * clusters);
+    cfg.blockDim = dim3(TCC_THREADS);
+    cfg.dynamicSmemBytes = TCC_SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_tc_chol, c, map, ws_row0, items, n_items, err, mode, row0b, linv_row0,
+                       (__nv_bfloat16*)ws, 1);
+    return;
+  }
   const int grid = n_items < slots ? n_items : slots;
   k_tc_chol<<<grid, TCC_THREADS, TCC_SMEM, s>>>(c, map, ws_row0, items, n_items, err, mode, row0b, linv_row0,
-                                                (__nv_bfloat16*)ws);
+                                                (__nv_bfloat16*)ws, 0);
 }
 
 int chol_panel_max_w1() { return 512; }

@@ -19,7 +19,7 @@ void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, 
 // (reserve: SMs the persistent grid leaves free for a concurrent launch)
 void launch_tc_chol(const DevCtx& c, const CUtensorMap& map, const int64_t* ws_row0, const Item* items, int n_items,
                     int* err, cudaStream_t s, int mode = 0, const int64_t* row0b = nullptr,
-                    const int64_t* linv_row0 = nullptr, void* ws = nullptr, int reserve = 0);
+                    const int64_t* linv_row0 = nullptr, void* ws = nullptr, int reserve = 0, int pair = 0);
 // a 256-column panel's diagonal block and its inverse as BF16 parts (item:
 // front, a = K0, b = diagonal block, c = flag offset)
 void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,

@@ -64,6 +64,28 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// the same load delivered to the CTAs of the cluster in mask (each at the
+// same shared-memory offset, completing on the mbarrier at the same offset)
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// every thread of every CTA of the cluster
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // UMMA shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
 // groups 1024 bytes apart (SBO), descriptor version 1 (bits 46-47)
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
@@ -73,6 +95,17 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
   d |= (uint64_t)1 << 46;            // version
   d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// the same with 64-byte swizzle (rows of 32 BF16): 8-row groups 512 bytes apart
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(512 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;            // SWIZZLE_64B
   return d;
 }
 
@@ -91,6 +124,14 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint6
 
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+// the completion of this CTA's MMAs arrives on the mbarrier at the same
+// offset in each CTA of the cluster in mask
+__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+               ::"r"(bar), "h"(mask)
                : "memory");
 }
 
