@@ -91,6 +91,7 @@ void Engine::free_device() {
   d_ws2_row0 = nullptr;
   d_ws2b_row0 = d_linv_row0 = nullptr;
   d_pflags = nullptr;
+  d_hand = nullptr;
   d_err = nullptr;
   d_dof_tree = nullptr;
   d_tree_red = nullptr;
@@ -817,6 +818,8 @@ void Engine::build_programs(int method) {
   fwd_ops.clear();
   bwd_ops.clear();
   int64_t pf = 0;   // tickets and flags of the cooperative panel launches
+  int64_t hand_slots = 0;   // fronts of the largest diagonal-block launch
+  int diag_seq = 0;         // diagonal-block launches so far (their tags)
   auto push = [&](std::vector<Op>& ops, int kind, int dtype, int nb, int param, const std::vector<Item>& it,
                   double flops = 0, double bytes = 0) {
     if (it.empty()) return;
@@ -1243,26 +1246,26 @@ void Engine::build_programs(int method) {
           for (int s : tccf)
             if (fronts[s].fs > K0) act.push_back(s);
           const int64_t tick = pf++;
-          std::vector<int64_t> foff(fronts.size(), 0);
-          for (int sl : act) {
-            foff[sl] = pf;
-            pf += CP_FLAGS_PER_FRONT;
-          }
           // tickets front by front: a front's CTAs wait on one another in
           // both directions (the factorisation on smaller, the inverse's
           // column blocks on larger block rows), so the lowest unfinished
           // front's CTAs are all running once four CTAs fit beside the
-          // concurrent update (at least min(items, 16) SMs are left to them)
+          // concurrent update (at least min(items, 16) SMs are left to them).
+          // Each front hands its blocks over through its own slot of words.
           std::vector<Item> dit;
           double fp = 0;
-          for (int sl : act) {
+          for (size_t q = 0; q < act.size(); ++q) {
+            const int sl = act[q];
             const int W = std::min(W1, fronts[sl].fs - K0);
-            for (int rel = 0; rel < (W + 63) / 64; ++rel) dit.push_back(Item{sl, K0, rel, (int)foff[sl]});
+            for (int rel = 0; rel < (W + 63) / 64; ++rel) dit.push_back(Item{sl, K0, rel, (int)q});
           }
           for (int sl : act) fp += get_flop_chol(0, std::min(W1, fronts[sl].fs - K0));
+          hand_slots = std::max(hand_slots, (int64_t)act.size());
+          if (diag_seq >= CD_MAX_SEQ) fail("factor program holds more diagonal-block launches than tags allow", 6);
           Op op{OP_CHOL_DIAG, F32, W1, (int)tick, add_items(dit), (int)dit.size()};
           op.flops = fp;
           op.aux = (int)dit.size();          // CTAs: the SMs a concurrent update leaves free
+          op.q0 = diag_seq++;                // the launch's tag
           return op;
         };
         auto ev_op = [&](int kind, int id, int strm) {
@@ -1396,8 +1399,12 @@ void Engine::build_programs(int method) {
     op.q0 = (int)pf;
     fac_ops.insert(fac_ops.begin(), op);
   }
-  if (!fac_mask) pflags_n = pf;
-  else if (pf > pflags_n) fail("partial factor program needs more panel flags than allocated", 6);
+  if (!fac_mask) {
+    pflags_n = pf;
+    hand_n = hand_slots;
+  } else if (pf > pflags_n || hand_slots > hand_n) {
+    fail("partial factor program needs more panel flags than allocated", 6);
+  }
   if (fac_mask) return;   // a partial factor program (build_partial) needs no solves
   // solve programs
   const int gm = chol ? M_CHOL : (method == UHM_LU_PIV ? M_LU_PIV : M_LU_NOPIV);
@@ -1670,6 +1677,12 @@ void Engine::alloc_device(int method) {
     CK(cudaStreamSynchronize(stream));
   }
   if (pflags_n > 0) d_pflags = (int*)dmalloc(sizeof(int) * (size_t)pflags_n);
+  if (hand_n > 0) {
+    // zero: no word carries a tag (every tag has its top bit set)
+    const size_t hb = sizeof(uint64_t) * (size_t)(CD_HAND_HEAD + hand_n * CD_HAND_WORDS);
+    d_hand = (uint64_t*)dmalloc(hb);
+    CK(cudaMemsetAsync(d_hand, 0, hb, stream));
+  }
   if (ws_total > 0) {
     // one extra row block so tiles that run past the last part stay inside the tensor
     d_ws = dmalloc(sizeof(uint16_t) * (size_t)(ws_total + 256 * tune.tc_nbo));
@@ -1928,7 +1941,9 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
         launch_tc_syrk(ctx, ws_map, d_ws_off, d_ws_stride, it, op.n_items, op.nb, 3, TC_TERMS_LU_BF16X3, 0, d_err,
                        st);
         break;
-      case OP_CLEAR_FLAGS: CK(cudaMemsetAsync(d_pflags, 0, sizeof(int) * (size_t)op.q0, st)); break;
+      case OP_CLEAR_FLAGS:
+        launch_clear_flags(d_pflags, op.q0, d_hand ? reinterpret_cast<unsigned*>(d_hand) : nullptr, st);
+        break;
       case OP_CHOL_PANEL:
         launch_chol_panel(ctx, it, op.n_items, op.nb, d_pflags + op.param, d_pflags, d_err, d_ws2, d_ws2_row0,
                           st);
@@ -1939,7 +1954,8 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
                        profiling ? 0 : op.q0, op.kind == OP_TC_CHOL_SCHUR ? op.aux : 0);
         break;
       case OP_CHOL_DIAG:
-        launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_pflags, d_err, d_ws2, d_linv_row0, st);
+        launch_chol_diag(ctx, it, op.n_items, d_pflags + op.param, d_hand + CD_HAND_HEAD,
+                         reinterpret_cast<const unsigned*>(d_hand), op.q0, d_err, d_ws2, d_linv_row0, st);
         break;
       case OP_CHOL_PACK: launch_chol_pack(ctx, it, op.n_items, d_ws2, d_ws2b_row0, st); break;
       case OP_TC_CHOL_TRSM:

@@ -299,6 +299,9 @@ class Engine {
   int64_t* d_ws2b_row0 = nullptr;
   int64_t* d_linv_row0 = nullptr;
   int64_t pflags_n = 0;
+  uint64_t* d_hand = nullptr;        // the factorisation count (first word), then the diagonal-block
+                                     // launches' hand-off words, CD_HAND_WORDS per front slot
+  int64_t hand_n = 0;                // front slots of d_hand
   void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
   int64_t* d_ws_off = nullptr;
   int64_t* d_ws_stride = nullptr;

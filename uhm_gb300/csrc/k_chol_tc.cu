@@ -297,19 +297,30 @@ k_chol_panel(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, 
 //   Linv[j][j] = L_jj^{-1},
 //   Linv[r][j] = -L_rr^{-1} sum_{k=j}^{r-1} L[r][k] Linv[k][j]      (r > j),
 // keeping its column in shared memory.  The sum for row r needs only the
-// rows of L that CTA r has solved (flags R[r][k]), so it is formed while
-// CTA r still factors; only the product with L_rr^{-1} waits for CTA r's
-// diagonal block (flag D[r]).  (By rows instead, row r needed every earlier
-// row of Linv in turn and the last row finished 40 us after the last
-// diagonal block.)  The blocks are written, split into BF16 hi / lo, as the
-// B operand of the TRSM on the tensor cores (X = A Linv^T for the rows below
-// the block): row c of Linv = row c of B, chunk i = columns 64 i .. 64 i + 63.
+// rows of L that CTA r has solved, so it is formed while CTA r still
+// factors; only the product with L_rr^{-1} waits for CTA r's diagonal block.
+// (By rows instead, row r needed every earlier row of Linv in turn and the
+// last row finished 40 us after the last diagonal block.)  The blocks are
+// written, split into BF16 hi / lo, as the B operand of the TRSM on the
+// tensor cores (X = A Linv^T for the rows below the block): row c of Linv =
+// row c of B, chunk i = columns 64 i .. 64 i + 63.
+//
+// Hand-offs between the CTAs of a front are self-validating words: each
+// 64 x 64 block a CTA passes on (the inverse L_jj^{-1} of its diagonal
+// block, D_j, and each solved block L[r][k], R_rk) is written as 4096 8-byte
+// words (tag << 32 | the FP32 bits), one relaxed store per word, single-copy
+// atomic.  The tag is unique to the launch (the engine's factorisation count
+// and the launch's sequence number in its program), so a reader polls the
+// words themselves until every one carries it: no flag, no fence on the
+// writer's side and no second round trip for the data on the reader's.
+// Word e = 64 t + i holds entry (i, t) of the block (column-major).
 constexpr int CD_W = 256;
+constexpr int CD_BLOCK_WORDS = 64 * 64;
 
 struct CdSmem {
   float P[64 * CD_W];              // the CTA's rows of the diagonal block (columns 0 .. 64 j + 63 used)
   union {
-    PotrfShared<float> sh;
+    PotrfLaShared<float> sh;
     struct {
       float Lt[64 * CP_LT];
       float Bt[64 * CP_LT];
@@ -317,31 +328,144 @@ struct CdSmem {
   } u;
   float Dm[64 * 64];               // a 64 x 64 left operand, column-major (L_rk, then Dinv_r)
   float Lc[4][64 * CP_LT];         // this CTA's column block of Linv, one 64 x 64 block per row block
-  int s_t, s_ok;
+  int s_t;
+  uint32_t s_tag;
 };
 
-// item: front, a = K0, b = j (diagonal block), c = flag offset (D at +0, R at
-// +8); linv_row0: first B-operand row of the front's Linv parts.  Items come
-// front by front, and a CTA waits only on CTAs of its own front (the
-// factorisation on smaller block rows, the inverse's column on larger ones):
-// the lowest unfinished front's CTAs have all started, so every wait ends
-// once a front's CTAs fit on the GPU together.
+__device__ __forceinline__ uint32_t cd_tag(const unsigned* epoch, int seq) {
+  const uint32_t e = *reinterpret_cast<const volatile unsigned*>(epoch);
+  return 0x80000000u | ((e & 0x1FFFFFu) << 10) | ((uint32_t)seq & 0x3FFu);
+}
+
+__device__ __forceinline__ void cd_put2(uint64_t* p, uint32_t tag, float a, float b) {
+  const uint64_t w0 = ((uint64_t)tag << 32) | __float_as_uint(a);
+  const uint64_t w1 = ((uint64_t)tag << 32) | __float_as_uint(b);
+  asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p), "l"(w0), "l"(w1) : "memory");
+}
+
+__device__ __forceinline__ void cd_get2(const uint64_t* p, uint64_t& w0, uint64_t& w1) {
+  asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(p) : "memory");
+}
+
+// publish a 64 x 64 block held column-major in shared memory (leading
+// dimension 64): this thread's words e = 512 m + 2 tid, + 1
+__device__ __forceinline__ void cd_publish_smem(uint64_t* H, uint32_t tag, const float* __restrict__ B) {
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int e = 512 * m + 2 * threadIdx.x;
+    const float2 v = *reinterpret_cast<const float2*>(&B[e]);
+    cd_put2(H + e, tag, v.x, v.y);
+  }
+}
+
+// this thread's words e = 512 m + 2 tid, + 1 (m = 0 .. 7) of the block at H,
+// all eight pairs polled together until each carries tag (one round trip
+// once they are written).  False (and the error word set) when the wait
+// gives up; a wait gives up within 256 polls when another CTA has already
+// given up.
+__device__ bool cd_fetch(const uint64_t* H, uint32_t tag, float2 (&v)[8], int* err) {
+  const uint32_t lim = g_wait_limit;
+  const uint64_t* p = H + 2 * threadIdx.x;
+  for (uint32_t i = 0;; ++i) {
+    uint64_t w[8][2];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) cd_get2(p + 512 * m, w[m][0], w[m][1]);
+    bool all = true;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      all = all && (uint32_t)(w[m][0] >> 32) == tag && (uint32_t)(w[m][1] >> 32) == tag;
+      v[m] = make_float2(__uint_as_float((uint32_t)w[m][0]), __uint_as_float((uint32_t)w[m][1]));
+    }
+    if (all) return true;
+    if (i >= lim || ((i & 255) == 0 && cp_ld_acquire(err) != 0)) {
+      atomicExch(err, CP_ERR);
+      return false;
+    }
+    __nanosleep(32);
+  }
+}
+
+// the fetched words into a row-major operand with rows of CP_LT: entry
+// (i, t) of the block to row t, column i (the transpose of the block)
+__device__ __forceinline__ void cd_to_rows(const float2 (&v)[8], float* __restrict__ B) {
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int e = 512 * m + 2 * threadIdx.x, t = e >> 6, i = e & 63;
+    *reinterpret_cast<float2*>(&B[t * CP_LT + i]) = v[m];
+  }
+}
+
+// ... into a column-major operand (leading dimension 64)
+__device__ __forceinline__ void cd_to_cols(const float2 (&v)[8], float* __restrict__ B) {
+#pragma unroll
+  for (int m = 0; m < 8; ++m) *reinterpret_cast<float2*>(&B[512 * m + 2 * threadIdx.x]) = v[m];
+}
+
+// P[:, c .. c+63] = P[:, c .. c+63] T^T for the lower-triangular T given
+// transposed in Tt (Tt[t * CP_LT + jj] = T[jj][t], zero for t > jj): column
+// jj needs only t <= jj.  Warp w takes column group g = w (w < 4) or 11 - w,
+// 8 g .. 8 g + 7, and stops at t = 8 g + 8, so the two warps of each
+// scheduler (w, w + 4) run 72 steps together instead of 128.
+__device__ __forceinline__ void cd_trsm64(float* __restrict__ P, int c, const float* __restrict__ Tt) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = w < 4 ? w : 11 - w;
+  const int ti = lane & 15, tj = 2 * g + (lane >> 4);
+  float acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+  const float* X = P + c * 64;
+  const int kt = 8 * g + 8;
+#pragma unroll 4
+  for (int t = 0; t < kt; ++t) {
+    const float4 x4 = *reinterpret_cast<const float4*>(&X[4 * ti + t * 64]);
+    const float4 b4 = *reinterpret_cast<const float4*>(&Tt[t * CP_LT + 4 * tj]);
+    const float xv[4] = {x4.x, x4.y, x4.z, x4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] += xv[u] * bv[v];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+    *reinterpret_cast<float4*>(&P[4 * ti + (c + 4 * tj + v) * 64]) =
+        make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+  __syncthreads();
+}
+
+// item: front, a = K0, b = j (diagonal block), c = the front's slot in this
+// launch (its hand-off words at hand + c * CD_HAND_WORDS: D_k at block k,
+// R_rk at block 4 + r (r - 1) / 2 + k); seq: the launch's number in its
+// program; epoch: the engine's factorisation count; linv_row0: first
+// B-operand row of the front's Linv parts.  Items come front by front, and a
+// CTA waits only on CTAs of its own front (the factorisation on smaller
+// block rows, the inverse's column on larger ones): the lowest unfinished
+// front's CTAs have all started, so every wait ends once a front's CTAs fit
+// on the GPU together.
 __global__ void __launch_bounds__(CP_THREADS, 1)
-k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, int* err,
-            __nv_bfloat16* __restrict__ ws, const int64_t* __restrict__ linv_row0) {
+k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, uint64_t* __restrict__ hand,
+            const unsigned* __restrict__ epoch, int seq, int* err, __nv_bfloat16* __restrict__ ws,
+            const int64_t* __restrict__ linv_row0) {
   extern __shared__ __align__(16) unsigned char cd_raw[];
   CdSmem& S = *reinterpret_cast<CdSmem*>(cd_raw);
   const int tid = threadIdx.x;
   const int ti = tid & 15, tj = tid >> 4;
-  if (tid == 0) S.s_t = atomicAdd(ticket, 1);
+  if (tid == 0) {
+    S.s_t = atomicAdd(ticket, 1);
+    S.s_tag = cd_tag(epoch, seq);
+  }
   __syncthreads();
   const Item it = items[S.s_t];
+  const uint32_t tag = S.s_tag;
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, K0 = it.a, rel = it.b;
   const int W = min(CD_W, fs - K0);
   const int r0 = K0 + 64 * rel, rows = min(64, W - 64 * rel);
-  int* D = flags + it.c;
-  int* R = D + 8;
+  uint64_t* __restrict__ H = hand + (int64_t)it.c * CD_HAND_WORDS;
+  auto Dh = [&](int k) { return H + (int64_t)k * CD_BLOCK_WORDS; };
+  auto Rh = [&](int r, int k) { return H + (int64_t)(4 + r * (r - 1) / 2 + k) * CD_BLOCK_WORDS; };
   float* __restrict__ G = c.a32 + f.off;
   const int ncol = min(W, 64 * (rel + 1));
   for (int idx = tid; idx < 64 * ncol; idx += CP_THREADS) {
@@ -349,70 +473,74 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
     S.P[idx] = i < rows ? G[(r0 + i) + (int64_t)(K0 + col) * n] : 0.f;
   }
   __syncthreads();
-  // steps j < rel: as the diagonal owners of k_chol_panel
+  // steps j < rel: as the diagonal owners of k_chol_panel (every block j < rel
+  // is a full 64 x 64 block; rows of a ragged last block are zero)
   for (int j = 0; j < rel; ++j) {
-    const int cj = 64 * j, kbj = min(64, W - cj);
-    cp_wait(D + j, err, &S.s_ok);
+    const int cj = 64 * j;
     {
-      const float* Di = c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + j) * 4096;
-      for (int idx = tid; idx < 4096; idx += CP_THREADS) {
-        const int t = idx >> 6, jj = idx & 63;
-        S.u.t.Lt[t * CP_LT + jj] = (t < kbj && jj < kbj) ? __ldcg(Di + idx) : 0.f;
-      }
+      float2 v[8];
+      const bool ok = cd_fetch(Dh(j), tag, v, err);
+      if (__syncthreads_or(!ok)) return;
+      cd_to_rows(v, S.u.t.Lt);
     }
     __syncthreads();
-    cp_gemm64(S.P, cj, cj, S.u.t.Lt, kbj, false);
-    // block j of this row block, solved: for the CTAs below and the inverse's
-    // columns.  At the last step it is published after the update of this
-    // CTA's own diagonal block, which is what the chain waits for.
-    auto publish_block = [&]() {
-      for (int idx = tid; idx < 64 * kbj; idx += CP_THREADS) {
-        const int i = idx & 63, col = idx >> 6;
-        if (i < rows) G[(r0 + i) + (int64_t)(K0 + cj + col) * n] = S.P[i + (cj + col) * 64];
-      }
-      cp_publish(R + rel * 8 + j);
-    };
-    if (j < rel - 1) publish_block();
+    cd_trsm64(S.P, cj, S.u.t.Lt);
+    // block j of this row block, solved: for the CTAs below and the
+    // inverse's columns
+    cd_publish_smem(Rh(rel, j), tag, S.P + cj * 64);
     for (int jp = j + 1; jp <= rel; ++jp) {
       const int cjp = 64 * jp, kbp = min(64, W - cjp);
       if (jp == rel) {
         for (int idx = tid; idx < 4096; idx += CP_THREADS) {
           const int t = idx >> 6, jj = idx & 63;
-          S.u.t.Bt[t * CP_LT + jj] = (t < kbj && jj < kbp) ? S.P[jj + (cj + t) * 64] : 0.f;
+          S.u.t.Bt[t * CP_LT + jj] = jj < kbp ? S.P[jj + (cj + t) * 64] : 0.f;
         }
       } else {
-        cp_wait(R + jp * 8 + j, err, &S.s_ok);
-        const int rjp = K0 + cjp;
-        for (int idx = tid; idx < 4096; idx += CP_THREADS) {
-          const int t = idx >> 6, jj = idx & 63;
-          S.u.t.Bt[t * CP_LT + jj] =
-              (t < kbj && jj < kbp) ? __ldcg(G + (rjp + jj) + (int64_t)(K0 + cj + t) * n) : 0.f;
-        }
+        float2 v[8];
+        const bool ok = cd_fetch(Rh(jp, j), tag, v, err);
+        if (__syncthreads_or(!ok)) return;
+        cd_to_rows(v, S.u.t.Bt);
       }
       __syncthreads();
-      cp_gemm64(S.P, cj, cjp, S.u.t.Bt, kbj, true);
+      cp_gemm64(S.P, cj, cjp, S.u.t.Bt, 64, true);
     }
-    if (j == rel - 1) publish_block();
   }
   // the diagonal block itself
   const int cr = 64 * rel, kbr = rows;
   float x[4][4];
   {
     bool bad;
-    potrf_block<float>(S.P + cr * 64, 64, kbr, S.u.sh, x, bad, S.P + cr * 64);
+    potrf_block_la<float>(S.P + cr * 64, 64, kbr, S.u.sh, x, bad, S.P + cr * 64);
     if (bad && tid == 0) set_status(c, it.front, ST_NOT_SPD);
-    potrf_store_inverse<float>(kbr, x, c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + rel) * 4096);
   }
-  cp_publish(D + rel);
+  // its inverse (zero outside the block's kbr rows and columns): to the CTAs
+  // of this front first, then for the solves and into this CTA's column
+  // block of Linv, row-major with rows of CP_LT
+  float out[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int r = 4 * ti + u, cc = 4 * tj + v;
+      out[u][v] = (r < kbr && cc < kbr) ? x[u][v] : 0.f;
+    }
+  {
+    uint64_t* Dr = Dh(rel);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int e = (4 * tj + v) * 64 + 4 * ti;
+      cd_put2(Dr + e, tag, out[0][v], out[1][v]);
+      cd_put2(Dr + e + 2, tag, out[2][v], out[3][v]);
+    }
+  }
+  potrf_store_inverse<float>(kbr, x, c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + rel) * 4096);
   for (int idx = tid; idx < 64 * (cr + kbr); idx += CP_THREADS) {
     const int i = idx & 63, col = idx >> 6;
     if (i < rows) G[(r0 + i) + (int64_t)(K0 + col) * n] = S.P[idx];
   }
-  // this CTA's column block of Linv: the diagonal block first (zero outside
-  // the block's kbr rows and columns), row-major with rows of CP_LT
   const int64_t lrow0 = linv_row0[it.front];
   const int nd = (W + 63) / 64;
-  auto store_b = [&](int r, const float (&out)[4][4]) {
+  auto store_b = [&](int r, const float (&o)[4][4]) {
     // rows 64 r + 4 ti .. of Linv, chunk rel: BF16 parts as the B operand
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -420,8 +548,8 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
       __align__(8) __nv_bfloat16 hi[4], lo[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        hi[v] = __float2bfloat16_rn(out[u][v]);
-        lo[v] = __float2bfloat16_rn(out[u][v] - __bfloat162float(hi[v]));
+        hi[v] = __float2bfloat16_rn(o[u][v]);
+        lo[v] = __float2bfloat16_rn(o[u][v] - __bfloat162float(hi[v]));
       }
       const int64_t rh = lrow0 + (int64_t)(0 * 4 + rel) * CD_W + 64 * r + rr;
       const int64_t rl = lrow0 + (int64_t)(1 * 4 + rel) * CD_W + 64 * r + rr;
@@ -429,20 +557,12 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
       *reinterpret_cast<uint2*>(ws + rl * 64 + 4 * tj) = *reinterpret_cast<const uint2*>(lo);
     }
   };
-  {
-    float out[4][4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int r = 4 * ti + u, cc = 4 * tj + v;
-        out[u][v] = (r < kbr && cc < kbr) ? x[u][v] : 0.f;
-        S.Lc[rel][r * CP_LT + cc] = out[u][v];
-      }
-    store_b(rel, out);
-  }
+    for (int v = 0; v < 4; ++v) S.Lc[rel][(4 * ti + u) * CP_LT + 4 * tj + v] = out[u][v];
+  store_b(rel, out);
   for (int r = rel + 1; r < nd; ++r) {
-    const int kbrr = min(64, W - 64 * r);
     // T = sum_{k=rel}^{r-1} L[r][k] Linv[k][rel], each L[r][k] once CTA r has solved it
     float acc[4][4];
 #pragma unroll
@@ -450,41 +570,39 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
 #pragma unroll
       for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
     for (int k = rel; k < r; ++k) {
-      cp_wait(R + r * 8 + k, err, &S.s_ok);
-      for (int idx = tid; idx < 4096; idx += CP_THREADS) {
-        const int i = idx & 63, t = idx >> 6;      // Dm[t * 64 + i] = L[r][k](i, t)
-        S.Dm[idx] = i < kbrr ? __ldcg(G + (K0 + 64 * r + i) + (int64_t)(K0 + 64 * k + t) * n) : 0.f;
-      }
+      float2 v[8];
+      const bool ok = cd_fetch(Rh(r, k), tag, v, err);
+      if (__syncthreads_or(!ok)) return;   // also: the previous product has read Dm
+      cd_to_cols(v, S.Dm);
       __syncthreads();
       cp_mma_tile(S.Dm, S.Lc[k], 64, acc);
-      __syncthreads();
     }
     // T as the row-major right operand, then Linv[r][rel] = -Dinv_r T
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) S.u.t.Bt[(4 * ti + u) * CP_LT + 4 * tj + v] = acc[u][v];
-    cp_wait(D + r, err, &S.s_ok);
     {
-      const float* Di = c.dinv32 + f.dinv_off + (int64_t)(K0 / 64 + r) * 4096;
-      for (int idx = tid; idx < 4096; idx += CP_THREADS) S.Dm[idx] = __ldcg(Di + idx);
+      float2 v[8];
+      const bool ok = cd_fetch(Dh(r), tag, v, err);
+      if (__syncthreads_or(!ok)) return;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) S.u.t.Bt[(4 * ti + u) * CP_LT + 4 * tj + w] = acc[u][w];
+      cd_to_cols(v, S.Dm);
     }
     __syncthreads();
-    float out[4][4];
+    float o[4][4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) out[u][v] = 0.f;
-    cp_mma_tile(S.Dm, S.u.t.Bt, 64, out);
+      for (int v = 0; v < 4; ++v) o[u][v] = 0.f;
+    cp_mma_tile(S.Dm, S.u.t.Bt, 64, o);
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        out[u][v] = -out[u][v];
-        S.Lc[r][(4 * ti + u) * CP_LT + 4 * tj + v] = out[u][v];
+        o[u][v] = -o[u][v];
+        S.Lc[r][(4 * ti + u) * CP_LT + 4 * tj + v] = o[u][v];
       }
-    store_b(r, out);
-    __syncthreads();
+    store_b(r, o);
   }
   // chunks right of the diagonal block are zero (Linv is lower triangular)
   for (int i = rel + 1; i < 4; ++i)
@@ -495,6 +613,13 @@ k_chol_diag(DevCtx c, const Item* __restrict__ items, int* ticket, int* flags, i
       *reinterpret_cast<uint4*>(ws + rh * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
       *reinterpret_cast<uint4*>(ws + rl * 64 + 8 * q) = make_uint4(0, 0, 0, 0);
     }
+}
+
+// the panel launches' tickets and flags to zero, and the factorisation count
+// that tags the diagonal kernels' hand-off words one up (epoch may be null)
+__global__ void k_clear_flags(int* __restrict__ flags, int n, unsigned* __restrict__ epoch) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) flags[i] = 0;
+  if (epoch && blockIdx.x == 0 && threadIdx.x == 0) *epoch += 1;
 }
 
 // BF16 parts (hi, lo) of the panel's rows below its diagonal block, the A
@@ -869,12 +994,18 @@ void launch_chol_panel(const DevCtx& c, const Item* items, int n_items, int w1, 
   else throw std::invalid_argument("chol_panel: panel width must be 256 or 512, got " + std::to_string(w1));
 }
 
-void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, int* flags, int* err,
-                      void* ws, const int64_t* linv_row0, cudaStream_t s) {
+void launch_chol_diag(const DevCtx& c, const Item* items, int n_items, int* ticket, uint64_t* hand,
+                      const unsigned* epoch, int seq, int* err, void* ws, const int64_t* linv_row0, cudaStream_t s) {
   if (!n_items) return;
   const int sm = (int)sizeof(CdSmem);
   cudaFuncSetAttribute(k_chol_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  k_chol_diag<<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, flags, err, (__nv_bfloat16*)ws, linv_row0);
+  k_chol_diag<<<n_items, CP_THREADS, sm, s>>>(c, items, ticket, hand, epoch, seq, err, (__nv_bfloat16*)ws,
+                                              linv_row0);
+}
+
+void launch_clear_flags(int* flags, int n, unsigned* epoch, cudaStream_t s) {
+  const int blocks = n > 0 ? (n + 255) / 256 < 64 ? (n + 255) / 256 : 64 : 1;
+  k_clear_flags<<<blocks, 256, 0, s>>>(flags, n, epoch);
 }
 
 void launch_chol_pack(const DevCtx& c, const Item* items, int n_items, void* ws, const int64_t* row0b,

@@ -202,3 +202,240 @@ __device__ __forceinline__ void potrf_store_inverse(int kb, const T (&x)[4][4], 
 }
 
 }  // namespace uhm_gpu
+
+namespace uhm_gpu {
+
+// ---------------------------------------------------------------------------
+// The same factorisation with a lookahead: only the 16 threads that hold the
+// next pivot columns (one half warp) factor the 4 x 4 pivot block and form
+// the L rows of those columns; they write them to shared memory and arrive on
+// the step's mbarrier.  Every thread waits only for that barrier, applies the
+// rank-4 update to its tile and advances its part of the inverse, so the
+// chain from one step to the next is the half warp's update, pivot and row
+// solve, not a block-wide barrier after every thread's whole step.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct PotrfLaShared {
+  union {
+    T V[64][64];                   // the staged block (lower triangle), until every tile is loaded
+    T Lf[64][64];                  // then L, column-major: Lf[k][i] = L[i][k] (zero above the diagonal)
+  };
+  T pv[16][16];                    // step q's pivot block from its diagonal thread: pv[q][4 j + i] = a(P+i, P+j)
+  T lbr[16][20];                   // step q's pivot factor: lb[i][j] at 4 i + j, 1 / L(P+j, P+j) at 16 + j
+  T XR[8][4][8];                   // per warp: rows P..P+3 of its block of X, finished
+  unsigned long long bar[16];      // step q's columns of L written (16 arrivals)
+};
+
+constexpr uint32_t POTRF_LA_WAIT = 1u << 22;
+
+__device__ __forceinline__ bool la_wait(const unsigned long long* bar) {
+  const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+  for (uint32_t i = 0; i < POTRF_LA_WAIT; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+        " selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(b)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// the half warp of tile column q1: factor the pivot block (its tile of the
+// diagonal thread, ti == q1), solve its rows' L entries of columns 4 q1 ..,
+// publish them and arrive
+template <typename T>
+__device__ __forceinline__ void la_pivot(PotrfLaShared<T>& sh, int q1, const T (&a)[4][4], int ti, int r0,
+                                         bool& bad) {
+  const int P1 = 4 * q1;
+  const unsigned hmask = (threadIdx.x & 16) ? 0xFFFF0000u : 0x0000FFFFu;
+  if (ti == q1) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      T col[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) col[i] = a[i][j];
+      Vec4<T>::st(&sh.pv[q1][4 * j], col);
+    }
+  }
+  __syncwarp(hmask);
+  T bk[4][4];                      // bk[j][i] = a(P1+i, P1+j)
+#pragma unroll
+  for (int j = 0; j < 4; ++j) Vec4<T>::ld(&sh.pv[q1][4 * j], bk[j]);
+  T lb[4][4], rd[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    T s = bk[j][j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) s -= lb[j][m] * lb[j][m];
+    if (!(s > T(0))) { bad = true; s = T(1); }
+    T d;
+    pivot_root<T>(s, d, rd[j]);
+    lb[j][j] = d;
+#pragma unroll
+    for (int i = j + 1; i < 4; ++i) {
+      T t = bk[j][i];
+#pragma unroll
+      for (int m = 0; m < j; ++m) t -= lb[i][m] * lb[j][m];
+      lb[i][j] = t * rd[j];
+    }
+  }
+  T l[4][4];                       // l[u][j] = L(r0+u, P1+j)
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) l[u][j] = T(0);
+  if (ti > q1) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        T t = a[u][j];
+#pragma unroll
+        for (int m = 0; m < j; ++m) t -= l[u][m] * lb[j][m];
+        l[u][j] = t * rd[j];
+      }
+  } else if (ti == q1) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) l[u][j] = u >= j ? lb[u][j] : T(0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) sh.lbr[q1][4 * i + j] = lb[i][j];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sh.lbr[q1][16 + j] = rd[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    T col[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) col[u] = l[u][j];
+    Vec4<T>::st(&sh.Lf[P1 + j][r0], col);
+  }
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(&sh.bar[q1])))
+               : "memory");
+}
+
+// Factor the 64 x 64 block at G (leading dimension n, kb <= 64 valid rows and
+// columns) as potrf_block does: on return x holds this thread's tile of
+// L^{-1}, the lower triangle of L has been written to Lout (leading dimension
+// n) when it is not null, and bad (the same in every thread) is set when a
+// pivot was not positive.  Ends with a block barrier.
+template <typename T>
+__device__ __forceinline__ void potrf_block_la(const T* __restrict__ G, int n, int kb, PotrfLaShared<T>& sh,
+                                               T (&x)[4][4], bool& bad, T* __restrict__ Lout) {
+  const int tid = threadIdx.x, w = tid >> 5;
+  const int ti = tid & 15, tj = tid >> 4, h = tj & 1;
+  const int r0 = 4 * ti, c0 = 4 * tj, cb0 = 8 * w;
+  if (tid == 0) {
+#pragma unroll 1
+    for (int q = 0; q < 16; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(
+                       static_cast<uint32_t>(__cvta_generic_to_shared(&sh.bar[q]))),
+                   "r"(16));
+  }
+  {
+    T g[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      g[u] = (i >= j && i < kb && j < kb) ? G[i + (int64_t)j * n] : (i == j ? T(1) : T(0));
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = tid + 256 * u, i = idx & 63, j = idx >> 6;
+      if (i >= j) sh.V[j][i] = g[u];
+    }
+  }
+  __syncthreads();
+  T a[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = r0 + u, j = c0 + v;
+      a[u][v] = i >= j ? sh.V[j][i] : sh.V[i][j];
+      x[u][v] = i == j ? T(1) : T(0);
+    }
+  __syncthreads();   // every tile loaded before L overwrites the staged block
+  bad = false;
+  if (tj == 0) la_pivot<T>(sh, 0, a, ti, r0, bad);
+#pragma unroll 1
+  for (int q = 0; q < 16; ++q) {
+    const int P = 4 * q;
+    if (!la_wait(&sh.bar[q])) bad = true;
+    T lr[4][4], lc[4][4];          // lr[u][j] = L(r0+u, P+j), lc[v][j] = L(c0+v, P+j)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      T t4[4];
+      Vec4<T>::ld(&sh.Lf[P + j][r0], t4);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) lr[u][j] = t4[u];
+      Vec4<T>::ld(&sh.Lf[P + j][c0], t4);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) lc[v][j] = t4[v];
+    }
+    if (tj > q) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) a[u][v] -= lr[u][j] * lc[v][j];
+      if (tj == q + 1) la_pivot<T>(sh, q + 1, a, ti, r0, bad);
+    }
+    if (P + 3 >= cb0) {
+      if (ti == q) {
+        // rows P..P+3 of X: their last substitution, then published to the warp
+        T lb[4][4], rd[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Vec4<T>::ld(&sh.lbr[q][4 * i], lb[i]);
+        Vec4<T>::ld(&sh.lbr[q][16], rd);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+          for (int m = 0; m < i; ++m)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) x[i][v] -= lb[i][m] * x[m][v];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) x[i][v] *= rd[i];
+          Vec4<T>::st(&sh.XR[w][i][4 * h], x[i]);
+        }
+      }
+      __syncwarp();
+      T xr[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Vec4<T>::ld(&sh.XR[w][j][4 * h], xr[j]);
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (r0 + u > P + 3) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) x[u][v] -= lr[u][j] * xr[j][v];
+        }
+    }
+  }
+  bad = __syncthreads_or(bad);
+  if (Lout) {
+    for (int idx = tid; idx < 64 * 64; idx += 256) {
+      const int i = idx & 63, k = idx >> 6;
+      if (i >= k && i < kb && k < kb) Lout[i + (int64_t)k * n] = sh.Lf[k][i];
+    }
+  }
+  if (tid == 0) {
+#pragma unroll 1
+    for (int q = 0; q < 16; ++q)
+      asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(
+          static_cast<uint32_t>(__cvta_generic_to_shared(&sh.bar[q]))));
+  }
+  __syncthreads();
+}
+
+}  // namespace uhm_gpu
