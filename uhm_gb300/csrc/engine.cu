@@ -1432,10 +1432,9 @@ void Engine::build_programs(int method) {
       if (gm == M_LU_PIV) {
         g_items.push_back(Item{s, 0, 0, 0});
       } else {
-        // c = 1: the front takes the 64-row flag-driven solves, whose
+        // c = 1: the front takes the flag-driven (or chain) solves, whose
         // forward hand-off words the gather empties
-        const int hand = chol && nr <= NR_FLAGS_MAX && tune.solve_rows == 64 &&
-                         !solve_small(fronts[s], h_fronts[s].dtype);
+        const int hand = chol && nr <= NR_FLAGS_MAX && !solve_small(fronts[s], h_fronts[s].dtype);
         for (int r0 = 0; r0 < fronts[s].n; r0 += GATHER_ROWS) g_items.push_back(Item{s, r0, GATHER_ROWS, hand});
       }
     }
@@ -1563,7 +1562,7 @@ void Engine::build_programs(int method) {
       }
       if (chol && nr <= NR_FLAGS_MAX && !large.empty()) {
         std::vector<Item> bi;
-        const int per = tune.solve_rows / NB;    // 64-column blocks per CTA (k_bwd_flags4 at 4)
+        const int per = 1;                       // 64-column blocks per CTA
         int maxb = 0;
         for (int s : large) maxb = std::max(maxb, ((fronts[s].fs + NB - 1) / NB + per - 1) / per);
         for (int b = maxb - 1; b >= 0; --b)
@@ -1579,7 +1578,7 @@ void Engine::build_programs(int method) {
         for (int q0 = 0; q0 < nr; q0 += qstep) {
           Op op{OP_BWD_FLAGS, dt, f1 - f0, f0, io, (int)bi.size()};
           op.q0 = q0;
-          op.aux = tune.solve_rows;
+          op.aux = NB;
           bwd_ops.push_back(op);
         }
         large.clear();
@@ -1906,8 +1905,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
       case OP_SYRK: launch_syrk_update(ctx, it, op.n_items, op.dtype, op.nb, op.param, st); break;
       case OP_FWD_FLAGS:
         if (op.aux == 256)
-          launch_fwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                            st);
+          launch_fwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, d_err, op.q0, st);
         else
           launch_fwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
                            st);
@@ -1915,11 +1913,7 @@ void Engine::launch_ops(const std::vector<Op>& ops, double* g_in, double* g_out,
       case OP_FWD_CHAIN: launch_fwd_chain(ctx, it, op.n_items, d_ticket, d_err, op.q0, st); break;
       case OP_BWD_CHAIN: launch_bwd_chain(ctx, it, op.n_items, d_ticket, d_err, op.q0, st); break;
       case OP_BWD_FLAGS:
-        if (op.aux == 256)
-          launch_bwd_flags4(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
-                            st);
-        else
-          launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
+        launch_bwd_flags(ctx, it, op.n_items, op.dtype, d_ticket, ctx.flags + op.param, op.nb, d_err, op.q0,
                            st);
         break;
       case OP_TC_PACK:

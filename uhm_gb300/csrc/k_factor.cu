@@ -80,16 +80,22 @@ __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restri
 // order); then the column is written once.  Every entry therefore gets the
 // same sum in the same order as in k_assemble (bit-identical), but each
 // source entry is read once instead of every parent row looking up every
-// source.
-template <typename T>
-__global__ void __launch_bounds__(256) k_assemble_scatter(DevCtx c, const Item* __restrict__ items,
-                                                          int lower) {
+// source.  NT threads, four rows each per pass.  EARLY: a child's stored
+// part of its column (rows at or below its diagonal, every row of an
+// unsymmetric child) is read beside the row-map look-up instead of after it
+// (only rows stored transposed, and element rows, wait for their parent row
+// to be known); it paid on the root's launch (fronts above ASM_EARLY_MIN
+// rows, 512 threads) and not on the levels below.
+constexpr int ASM_EARLY_MIN = 8192;
+
+template <typename T, int NT, bool EARLY>
+__global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* __restrict__ items, int lower) {
   extern __shared__ double s_col[];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, J = it.a;
   const int istart = lower ? J : 0;
-  for (int I = istart + threadIdx.x; I < n; I += blockDim.x) s_col[I] = 0.0;
+  for (int I = istart + threadIdx.x; I < n; I += NT) s_col[I] = 0.0;
   const int64_t* __restrict__ cp = c.colptr + f.colptr_off;
   const int64_t k0 = cp[J], k1 = cp[J + 1];
   __syncthreads();
@@ -102,46 +108,64 @@ __global__ void __launch_bounds__(256) k_assemble_scatter(DevCtx c, const Item* 
     // look-ups, then all its loads, then the shared-memory adds
     const double* __restrict__ b64 = !sd.is_child ? c.emat + sd.off : (sd.dtype == F64 ? c.a64 + sd.off : nullptr);
     const float* __restrict__ b32 = (sd.is_child && sd.dtype != F64) ? c.a32 + sd.off : nullptr;
-    for (int r0 = 0; r0 < sd.m; r0 += 4 * 256) {
+    const int cc = cs.y;
+    // rows r >= rs are stored in column cc and read at once (EARLY)
+    const int rs = !EARLY ? sd.m : (sd.is_child ? (sym ? cc : 0) : sd.m);
+    for (int r0 = 0; r0 < sd.m; r0 += 4 * NT) {
       int I[4];
       double v[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int r = r0 + threadIdx.x + 256 * u;
+        const int r = r0 + threadIdx.x + NT * u;
         I[u] = r < sd.m ? __ldg(fw + r) : -1;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int r = r0 + threadIdx.x + 256 * u;
+        const int r = r0 + threadIdx.x + NT * u;
         v[u] = 0.0;
-        if (I[u] >= istart) {
-          int rr = r, cc = cs.y;
-          if (sym && rr < cc) { const int t = rr; rr = cc; cc = t; }
-          const int64_t idx = rr + (int64_t)cc * sd.ld;
+        if (r < sd.m && r >= rs) {
+          const int64_t idx = r + (int64_t)cc * sd.ld;
           v[u] = b32 ? (double)b32[idx] : b64[idx];
         }
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (I[u] >= istart) s_col[I[u]] += v[u];
+      for (int u = 0; u < 4; ++u) {
+        const int r = r0 + threadIdx.x + NT * u;
+        if (I[u] >= istart) {
+          if (r < rs) {
+            int rr = r, cl = cc;
+            if (sym && rr < cl) { const int t = rr; rr = cl; cl = t; }
+            const int64_t idx = rr + (int64_t)cl * sd.ld;
+            v[u] = b32 ? (double)b32[idx] : b64[idx];
+          }
+          s_col[I[u]] += v[u];
+        }
+      }
     }
     __syncthreads();
   }
   T* __restrict__ P = arena<T>(c) + f.off + (int64_t)J * n;
-  for (int I = istart + threadIdx.x; I < n; I += blockDim.x) P[I] = (T)s_col[I];
+  for (int I = istart + threadIdx.x; I < n; I += NT) P[I] = (T)s_col[I];
+}
+
+template <typename T>
+static void assemble_scatter_t(const DevCtx& c, const Item* items, int n_items, int lower, int n_max,
+                               cudaStream_t s) {
+  const size_t sm = sizeof(double) * (size_t)n_max;
+  if (n_max >= ASM_EARLY_MIN) {
+    cudaFuncSetAttribute(k_assemble_scatter<T, 512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_assemble_scatter<T, 512, true><<<n_items, 512, sm, s>>>(c, items, lower);
+  } else {
+    cudaFuncSetAttribute(k_assemble_scatter<T, 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_assemble_scatter<T, 256, false><<<n_items, 256, sm, s>>>(c, items, lower);
+  }
 }
 
 void launch_assemble_scatter(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
                              int n_max, cudaStream_t s) {
   if (!n_items) return;
-  const size_t sm = sizeof(double) * (size_t)n_max;
-  if (dtype == F64) {
-    cudaFuncSetAttribute(k_assemble_scatter<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_assemble_scatter<double><<<n_items, 256, sm, s>>>(c, items, lower);
-  } else {
-    cudaFuncSetAttribute(k_assemble_scatter<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_assemble_scatter<float><<<n_items, 256, sm, s>>>(c, items, lower);
-  }
+  if (dtype == F64) assemble_scatter_t<double>(c, items, n_items, lower, n_max, s);
+  else assemble_scatter_t<float>(c, items, n_items, lower, n_max, s);
 }
 
 void launch_assemble(const DevCtx& c, const Item* items, int n_items, int dtype, int lower,
@@ -198,14 +222,13 @@ __global__ void __launch_bounds__(NT) k_small_factor(DevCtx c, const Item* __res
   T* __restrict__ G = arena<T>(c) + f.off;
   const bool chol = method == M_CHOL;
   const bool pivot = method == M_LU_PIV;
-  const int64_t nn = (int64_t)n * n;
-  for (int64_t idx = threadIdx.x; idx < nn; idx += NT) {
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    if (!chol || i >= j) A[idx] = G[idx];
-  }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int NW = NT / 32;
+  // the front in (its lower triangle for Cholesky): a warp per column, no
+  // index division
+  for (int j = warp; j < n; j += NW)
+    for (int i = (chol ? j : 0) + lane; i < n; i += 32) A[i + (int64_t)j * n] = G[i + (int64_t)j * n];
+  __syncthreads();
   for (int k = 0; k < fs; ++k) {
     if (chol) {
       if (threadIdx.x == 0) {
@@ -258,10 +281,8 @@ __global__ void __launch_bounds__(NT) k_small_factor(DevCtx c, const Item* __res
       __syncthreads();
     }
   }
-  for (int64_t idx = threadIdx.x; idx < nn; idx += NT) {
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    if (!chol || i >= j) G[idx] = A[idx];
-  }
+  for (int j = warp; j < n; j += NW)
+    for (int i = (chol ? j : 0) + lane; i < n; i += 32) G[i + (int64_t)j * n] = A[i + (int64_t)j * n];
 }
 
 void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dtype, int method,

@@ -117,15 +117,19 @@ __global__ void __launch_bounds__(NT) k_fwd_small(DevCtx c, const Item* __restri
 
 // Cholesky small fronts with the factor panel (n x fs) staged in shared
 // memory by one batch of loads: every column step then works on shared data
-// (one barrier per column instead of a global round trip per column).
+// (one barrier per column instead of a global round trip per column).  The
+// right-hand sides are solved in the factor's precision (as in the
+// flag-driven solves of large fronts): FP32 fronts take no FP64 arithmetic,
+// which runs at a small fraction of the FP32 rate on this GPU.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_fwd_small_staged(DevCtx c, const Item* __restrict__ items) {
+  using CT = T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs;
-  double* z = reinterpret_cast<double*>(smem_raw);
-  T* Ls = reinterpret_cast<T*>(z + (size_t)n * nr);
+  CT* z = reinterpret_cast<CT*>(smem_raw);
+  T* Ls = z + (size_t)n * nr;
   const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ zg = c.vec + f.voff;
   const int tot = n * fs;
@@ -142,24 +146,25 @@ __global__ void __launch_bounds__(NT) k_fwd_small_staged(DevCtx c, const Item* _
       if (idx < tot) Ls[idx] = v[u];
     }
   }
-  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = zg[idx];
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = (CT)zg[idx];
   __syncthreads();
   for (int j = 0; j < fs; ++j) {
-    if (threadIdx.x < nr) z[j + threadIdx.x * n] /= (double)Ls[j + j * n];
+    if (threadIdx.x < nr) z[j + threadIdx.x * n] /= (CT)Ls[j + j * n];
     __syncthreads();
     const int h = n - j - 1;
-    for (int idx = threadIdx.x; idx < h * nr; idx += NT) {
-      const int i = j + 1 + idx % h, q = idx / h;
-      z[i + q * n] -= (double)Ls[i + j * n] * z[j + q * n];
+    for (int q = 0; q < nr; ++q) {
+      const CT zj = z[j + q * n];
+      for (int i = j + 1 + threadIdx.x; i < n; i += NT) z[i + q * n] -= (CT)Ls[i + j * n] * zj;
     }
+    (void)h;
     __syncthreads();
   }
   double* __restrict__ yg = zg + (int64_t)n * nr;
-  for (int idx = threadIdx.x; idx < n * nr; idx += NT) {
-    const int i = idx % n;
-    if (i < fs) yg[idx] = z[idx];
-    else zg[idx] = z[idx];
-  }
+  for (int q = 0; q < nr; ++q)
+    for (int i = threadIdx.x; i < n; i += NT) {
+      if (i < fs) yg[i + (int64_t)q * n] = (double)z[i + q * n];
+      else zg[i + (int64_t)q * n] = (double)z[i + q * n];
+    }
 }
 
 // x_F = L_FF^{-T} (y_F - L_SF^T x_S): the Schur-row products for all factor
@@ -167,13 +172,14 @@ __global__ void __launch_bounds__(NT) k_fwd_small_staged(DevCtx c, const Item* _
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) k_bwd_small_staged(DevCtx c, const Item* __restrict__ items,
                                                          double* __restrict__ g, int64_t ldg) {
+  using CT = T;                       // the factor's precision, as in the forward sweep
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs;
-  double* z = reinterpret_cast<double*>(smem_raw);
-  double* w = z + (size_t)n * nr;
-  T* Ls = reinterpret_cast<T*>(w + fs);
+  CT* z = reinterpret_cast<CT*>(smem_raw);
+  CT* w = z + (size_t)n * nr;
+  T* Ls = w + fs;
   const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ zg = c.vec + f.voff + (int64_t)n * nr;   // y slab
   const int tot = n * fs;
@@ -190,26 +196,26 @@ __global__ void __launch_bounds__(NT) k_bwd_small_staged(DevCtx c, const Item* _
       if (idx < tot) Ls[idx] = v[u];
     }
   }
-  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = zg[idx];
+  for (int idx = threadIdx.x; idx < n * nr; idx += NT) z[idx] = (CT)zg[idx];
   __syncthreads();
   for (int q = 0; q < nr; ++q) {
-    double* zq = z + q * n;
+    CT* zq = z + q * n;
     for (int j = threadIdx.x; j < fs; j += NT) {
-      double sacc = 0.0;
+      CT sacc = CT(0);
       const T* col = Ls + (size_t)j * n;
-      for (int i = fs; i < n; ++i) sacc += (double)col[i] * zq[i];
+      for (int i = fs; i < n; ++i) sacc += (CT)col[i] * zq[i];
       w[j] = zq[j] - sacc;
     }
     __syncthreads();
     for (int j = fs - 1; j >= 0; --j) {
-      const double xj = w[j] / (double)Ls[j + j * n];
-      for (int i = threadIdx.x; i < j; i += NT) w[i] -= (double)Ls[j + i * n] * xj;
+      const CT xj = w[j] / (CT)Ls[j + j * n];
+      for (int i = threadIdx.x; i < j; i += NT) w[i] -= (CT)Ls[j + i * n] * xj;
       if (threadIdx.x == 0) zq[j] = xj;
       __syncthreads();
     }
   }
   for (int q = 0; q < nr; ++q)
-    for (int i = threadIdx.x; i < fs; i += NT) g[(f.g0 + i) + q * ldg] = z[i + q * n];
+    for (int i = threadIdx.x; i < fs; i += NT) g[(f.g0 + i) + q * ldg] = (double)z[i + q * n];
 }
 
 void launch_fwd_small(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
@@ -780,57 +786,7 @@ namespace uhm_gpu {
 constexpr int FB = 64;
 constexpr int SF_NR = FLAG_NR;    // right-hand sides handled by one launch
 
-__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_gpu(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
-  int v;
-  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-// Thread 0 waits (bounded) until flag[first] is set, extends the ready range
-// while further flags are set (step +1 or -1), issues one acquire fence for
-// all of them and returns the end of the range (exclusive) in *s_ready.
 UHM_DEFINE_WAIT_LIMIT(set_wait_limit_solve, 1u << 22)
-
-__device__ __forceinline__ void ready_range(const int* flg, int first, int last, int step, int* s_ready,
-                                            int* err) {
-  if (threadIdx.x == 0) {
-    bool ok = false;
-    const uint32_t lim = g_wait_limit;
-    for (uint32_t i = 0; i < lim; ++i) {
-      if (ld_relaxed_gpu(flg + first) == 1) { ok = true; break; }
-      __nanosleep(32);
-    }
-    int k = first;
-    if (ok) {
-      k = first + step;
-      while (k != last && ld_relaxed_gpu(flg + k) == 1) k += step;
-    } else {
-      atomicExch(err, 2);
-      k = last;
-    }
-    __threadfence();
-    *s_ready = k;
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ bool wait_flag(const int* p, int* err) {
-  const uint32_t lim = g_wait_limit;
-  for (uint32_t i = 0; i < lim; ++i) {
-    if (ld_acquire_gpu(p) == 1) return true;
-    __nanosleep(32);
-  }
-  atomicExch(err, 2);
-  return false;
-}
 
 template <typename T> __device__ __forceinline__ const T* dinv_arena(const DevCtx& c);
 template <> __device__ __forceinline__ const double* dinv_arena<double>(const DevCtx& c) { return c.dinv64; }
@@ -1064,30 +1020,33 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
 // 4 B .. 4 B + 3, solved here in turn), otherwise the ABL rows
 // fs + 256 (B - nfb4) ...  One thread per row; the row's 64 factor entries of
 // the next column block are loaded into registers before that block's
-// values are waited for.  Column blocks left of the CTA come from other CTAs
-// (their completion flags, one per 64-row block); the CTA's own blocks are
-// solved in order: the block's rows form v = z - (sum so far), y = Dinv v,
-// y is published (its warps fence and raise the flag while the rest of the
-// CTA goes on with the rows below), and every later row of the CTA adds
-// its product with y.  Tickets in item order: every CTA waits only on
-// smaller tickets.
+// solution is waited for.  Column blocks left of the CTA come from other
+// CTAs as hand-off words (warp 0 polls and stages them, the next block's
+// words already in flight); the CTA's own blocks are solved in turn on all
+// its threads (v = z - sum on the block's rows, y = Dinv v by four column
+// groups, summed in group order), each published at once as hand-off words,
+// and every later row of the CTA adds its product with y.  One hand-off
+// between CTAs per 256 rows instead of per 64.  Tickets in item order: every
+// CTA waits only on smaller tickets.
 constexpr int F4_ROWS = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_flags4(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
-                                                    int q0) {
+__global__ void __launch_bounds__(256, 1) k_fwd_hand4(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
+                                                      int q0) {
   using CT = T;
   extern __shared__ __align__(16) unsigned char f4_dyn[];
-  T* dsh = reinterpret_cast<T*>(f4_dyn);          // 4 inverse diagonal blocks, dsh[s][t * 65 + i] = Dinv_s[i][t]
-  __shared__ int s_t, s_ready;
-  __shared__ CT ysh[SF_NR][FB];
+  T* dsh = reinterpret_cast<T*>(f4_dyn);          // own inverse diagonal blocks, dsh[s][t * 65 + i] = Dinv_s[i][t]
+  __shared__ int s_t;
+  __shared__ CT ysh[2][SF_NR][FB];
   __shared__ CT vsh[SF_NR][FB];
+  __shared__ CT red[4][FB][SF_NR];
   const int tid = threadIdx.x;
   if (tid == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs;
+  const int nq = min(SF_NR, nr - q0);
   const int nfb = (fs + FB - 1) / FB, nfb4 = (nfb + 3) / 4;
   const bool factor_cta = it.a < nfb4;
   const int b0 = factor_cta ? 4 * it.a : nfb;                 // first own 64-row block (factor CTAs)
@@ -1100,7 +1059,6 @@ __global__ void __launch_bounds__(256) k_fwd_flags4(DevCtx c, const Item* __rest
   const T* __restrict__ G = arena<T>(c) + f.off;
   double* __restrict__ z = c.vec + f.voff;
   double* __restrict__ y = z + (int64_t)n * nr;
-  int* flg = c.flags + f.flag_off;
   if (factor_cta) {
     const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b0 * FB * FB;
     for (int idx = tid; idx < ns * FB * FB; idx += 256) {
@@ -1112,10 +1070,16 @@ __global__ void __launch_bounds__(256) k_fwd_flags4(DevCtx c, const Item* __rest
 #pragma unroll
   for (int q = 0; q < SF_NR; ++q) {
     acc[q] = CT(0);
-    zr[q] = (rv && q0 + q < nr) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);
+    zr[q] = (rv && q < nq) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);
+  }
+  // the factor rows of z are not read again: they become the backward
+  // solve's hand-off words
+  if (factor_cta && rv) {
+#pragma unroll
+    for (int q = 0; q < SF_NR; ++q)
+      if (q < nq) z[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
   }
   const int jext = b0;                    // column blocks solved by other CTAs
-  const int jend = factor_cta ? b0 + ns : nfb;
   // the row's entries of column block j, where this row needs them
   CT tile[FB];
   auto load_tile = [&](int j) {
@@ -1124,102 +1088,137 @@ __global__ void __launch_bounds__(256) k_fwd_flags4(DevCtx c, const Item* __rest
 #pragma unroll
     for (int u = 0; u < FB; ++u) tile[u] = (need && u < kbj) ? (CT)G[row + (int64_t)(j * FB + u) * n] : CT(0);
   };
-  if (jend > 0) load_tile(0);
-  int ready = 0;                          // external blocks known to be complete: [0, ready)
-  for (int j = 0; j < jend; ++j) {
-    const int kbj = min(FB, fs - j * FB);
-    if (j < jext) {
-      if (j >= ready) {
-        // every thread reaches this together (ready is the same in all of
-        // them); s_ready is read only after ready_range's closing barrier
-        ready_range(flg, j, jext, 1, &s_ready, err);
-        ready = s_ready;
+  const int jlast = factor_cta ? b0 + ns - 1 : nfb;          // tiles needed: blocks 0 .. jlast - 1
+  if (jlast > 0) load_tile(0);
+  const bool w0 = tid < 32;
+  HandWords hw;
+  bool live = true;      // warp 0: false once a wait has run out (no more waiting)
+  if (jext > 0 && w0) hw.load(y + (int64_t)q0 * n, min(FB, fs));
+  for (int j = 0; j < jext; ++j) {
+    const int buf = j & 1;
+    if (w0) {
+      const int kbj = min(FB, fs - j * FB);
+      const double* yj = y + j * FB;
+      if (live) live = hw.wait(yj + (int64_t)q0 * n, kbj, err, wait_code(1, j, b0));
+      hw.stage(ysh[buf][0]);
+      for (int q = 1; q < nq; ++q) {
+        HandWords hq;
+        hq.load(yj + (int64_t)(q0 + q) * n, kbj);
+        if (live) live = hq.wait(yj + (int64_t)(q0 + q) * n, kbj, err, wait_code(1, j, b0));
+        hq.stage(ysh[buf][q]);
       }
-      if (tid < 32) {
-        for (int q = 0; q < SF_NR && q0 + q < nr; ++q) {
-          const double* yj = y + j * FB + (int64_t)(q0 + q) * n;
-          for (int cc = tid; cc < FB; cc += 32) ysh[q][cc] = cc < kbj ? (CT)__ldcg(yj + cc) : CT(0);
-        }
-      }
-      __syncthreads();
-    } else {
-      // own block s: v = z - acc on its rows, y = Dinv_s v
-      const int s2 = j - b0;
-      if (sub == s2) {
-#pragma unroll
-        for (int q = 0; q < SF_NR; ++q) vsh[q][tid & 63] = (rv && q0 + q < nr) ? zr[q] - acc[q] : CT(0);
-      }
-      __syncthreads();
-      if (sub == s2) {
-        const int i = tid & 63;
-        const T* Ds = dsh + s2 * FB * (FB + 1);
-        CT yv[SF_NR];
-#pragma unroll
-        for (int q = 0; q < SF_NR; ++q) yv[q] = CT(0);
-        for (int t = 0; t <= i && t < kbj; ++t) {
-          const CT d = (CT)Ds[t * (FB + 1) + i];
-#pragma unroll
-          for (int q = 0; q < SF_NR; ++q) yv[q] += d * vsh[q][t];
-        }
-#pragma unroll
-        for (int q = 0; q < SF_NR; ++q) {
-          ysh[q][i] = (i < kbj) ? yv[q] : CT(0);
-          if (rv && q0 + q < nr) y[row + (int64_t)(q0 + q) * n] = (double)yv[q];
-        }
-      }
-      __syncthreads();
-      if (sub == s2) {
-        // this block's warps publish it; the rest of the CTA goes on
-        __threadfence();
-        asm volatile("bar.sync %0, %1;" ::"r"(1 + s2), "r"(64) : "memory");
-        if ((tid & 63) == 0) st_release_gpu(flg + j, 1);
-      }
+      if (j + 1 < jext) hw.load(y + (j + 1) * FB + (int64_t)q0 * n, min(FB, fs - (j + 1) * FB));
     }
-    const bool use = j < jext || sub > j - b0;
+    __syncthreads();
     if constexpr (sizeof(T) == 4) {
       // FP32: the next block's loads are issued before this block's products
       CT cur[FB];
 #pragma unroll
       for (int u = 0; u < FB; ++u) cur[u] = tile[u];
-      if (j + 1 < jend) load_tile(j + 1);
-      if (use) {
+      if (j + 1 < jlast) load_tile(j + 1);
+      if (rv) {
 #pragma unroll
         for (int u = 0; u < FB; ++u)
 #pragma unroll
-          for (int q = 0; q < SF_NR; ++q) acc[q] += cur[u] * ysh[q][u];
+          for (int q = 0; q < SF_NR; ++q) acc[q] += cur[u] * ysh[buf][q][u];
       }
     } else {
       // FP64 (register budget): products first, then the next block's loads
-      if (use) {
+      if (rv) {
 #pragma unroll
         for (int u = 0; u < FB; ++u)
 #pragma unroll
-          for (int q = 0; q < SF_NR; ++q) acc[q] += tile[u] * ysh[q][u];
+          for (int q = 0; q < SF_NR; ++q) acc[q] += tile[u] * ysh[buf][q][u];
       }
-      if (j + 1 < jend) load_tile(j + 1);
+      if (j + 1 < jlast) load_tile(j + 1);
+    }
+  }
+  // own blocks s: v = z - acc on its rows, y = Dinv_s v, published; the rows
+  // below add their products with y
+  for (int s = 0; s < ns; ++s) {
+    const int j = b0 + s, kbj = min(FB, fs - j * FB);
+    if (sub == s) {
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q) vsh[q][tid & 63] = rv ? zr[q] - acc[q] : CT(0);
+    }
+    // FP32: the next block's tile is loaded before this block's solve (the
+    // rows below need it right after); FP64 (register budget) loads it after
+    // the products
+    CT cur[sizeof(T) == 4 ? FB : 1];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+      for (int u = 0; u < FB; ++u) cur[u] = tile[u];
+      if (j + 1 < jlast) load_tile(j + 1);
     }
     __syncthreads();
+    {
+      // y = Dinv v: column group g sums t in [16 g, 16 g + 16) (Dinv is
+      // lower triangular: t <= i)
+      const int i = tid & 63, g = tid >> 6;
+      const T* Ds = dsh + s * FB * (FB + 1);
+      CT xp[SF_NR];
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q) xp[q] = CT(0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int t = g * 16 + u;
+        if (t <= i && t < kbj) {
+          const CT d = (CT)Ds[t * (FB + 1) + i];
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) xp[q] += d * vsh[q][t];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q) red[g][i][q] = xp[q];
+    }
+    __syncthreads();
+    if (tid < FB) {
+      const int i = tid, r = r0 + FB * s + i;
+#pragma unroll
+      for (int q = 0; q < SF_NR; ++q) {
+        const CT yv = red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q];
+        ysh[0][q][i] = i < kbj ? yv : CT(0);
+        if (i < kbj && q < nq) st_hand(y + r + (int64_t)(q0 + q) * n, (double)yv);
+      }
+    }
+    __syncthreads();
+    if constexpr (sizeof(T) == 4) {
+      if (rv && sub > s) {
+#pragma unroll
+        for (int u = 0; u < FB; ++u)
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) acc[q] += cur[u] * ysh[0][q][u];
+      }
+    } else {
+      (void)cur;
+      if (rv && sub > s) {
+#pragma unroll
+        for (int u = 0; u < FB; ++u)
+#pragma unroll
+          for (int q = 0; q < SF_NR; ++q) acc[q] += tile[u] * ysh[0][q][u];
+      }
+      if (j + 1 < jlast) load_tile(j + 1);
+    }
   }
   if (!factor_cta && rv) {
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q)
-      if (q0 + q < nr) z[row + (int64_t)(q0 + q) * n] = (double)(zr[q] - acc[q]);
+      if (q < nq) z[row + (int64_t)(q0 + q) * n] = (double)(zr[q] - acc[q]);
   }
 }
 
-void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
-                       int n_flags, int* err, int q0, cudaStream_t s) {
+void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* err, int q0,
+                       cudaStream_t s) {
   if (!n_items) return;
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
-  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
   if (dtype == F64) {
     const int sm = (int)(sizeof(double) * 4 * FB * (FB + 1));
-    cudaFuncSetAttribute(k_fwd_flags4<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    k_fwd_flags4<double><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
+    cudaFuncSetAttribute(k_fwd_hand4<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    k_fwd_hand4<double><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
   } else {
     const int sm = (int)(sizeof(float) * 4 * FB * (FB + 1));
-    cudaFuncSetAttribute(k_fwd_flags4<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    k_fwd_flags4<float><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
+    cudaFuncSetAttribute(k_fwd_hand4<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    k_fwd_hand4<float><<<n_items, 256, sm, s>>>(c, items, ticket, err, q0);
   }
 }
 
@@ -1386,184 +1385,6 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
       y[c0 + ii + (int64_t)(q0 + q) * n] = x;
       st_hand(hx + c0 + ii + (int64_t)(q0 + q) * n, x);
     }
-  }
-}
-
-// Backward solve of large Cholesky fronts with 256-column CTAs.  Item:
-// front, a = B, the factor columns 256 B .. (64-column blocks 4 B .. 4 B + 3);
-// tickets in descending B.  One thread per column accumulates
-// sum_r L[r][col] x_r over the rows below the CTA's blocks: 32-row chunks of
-// L are loaded coalesced (a warp reads 32 consecutive rows of a column)
-// into registers one chunk ahead, staged in shared memory and read along
-// the row.  Order: the ABL rows (x known from the parent), the factor rows
-// of later CTAs as their flags arrive (last block first), then the CTA's own
-// blocks from the last one down: x_s = Dinv_s^T (y_s - sum), published (its
-// warps fence and raise the flag while the rest go on), and its rows are
-// added into the columns left of it.
-constexpr int B4_CH = 32;          // rows per chunk
-
-template <typename T, int NQ>
-__global__ void __launch_bounds__(256) k_bwd_flags4(DevCtx c, const Item* __restrict__ items, int* ticket, int* err,
-                                                    int q0) {
-  using CT = T;
-  extern __shared__ __align__(16) unsigned char b4_dyn[];
-  T* dsh = reinterpret_cast<T*>(b4_dyn);                          // 4 x 64 x 65: dsh[s][t * 65 + i] = Dinv_s[i][t]
-  T* tile = dsh + 4 * FB * (FB + 1);                              // B4_CH x 257
-  __shared__ CT xs[NQ][B4_CH];
-  __shared__ CT vsh[NQ][FB];
-  __shared__ int s_t, s_ready;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_t = atomicAdd(ticket, 1);
-  __syncthreads();
-  const Item it = items[s_t];
-  const FrontDev f = c.fronts[it.front];
-  const int n = f.n, fs = f.fs, nr = c.n_rhs;
-  const int nfb = (fs + FB - 1) / FB;
-  const int b0 = 4 * it.a, ns = min(4, nfb - b0);
-  const int c0 = FB * b0, c1 = min(c0 + 4 * FB, fs);
-  const int col = c0 + tid;
-  const bool cv = col < c1;
-  const int sub = tid >> 6;
-  const T* __restrict__ G = arena<T>(c) + f.off;
-  double* __restrict__ y = c.vec + f.voff + (int64_t)n * nr;
-  int* flg = c.flags + f.flag_off;
-  {
-    const T* __restrict__ Dg = dinv_arena<T>(c) + f.dinv_off + (int64_t)b0 * FB * FB;
-    for (int idx = tid; idx < ns * FB * FB; idx += 256) {
-      const int s2 = idx / (FB * FB), e = idx % (FB * FB);
-      dsh[s2 * FB * (FB + 1) + (e / FB) * (FB + 1) + e % FB] = Dg[idx];
-    }
-  }
-  CT acc[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) acc[q] = CT(0);
-  // chunk list: ABL rows, then later factor blocks (last first), then own blocks (last first)
-  const int n_abl = (n - fs + B4_CH - 1) / B4_CH;
-  const int n_ext_blk = nfb - (b0 + ns);
-  const int n_chunks = n_abl + 2 * n_ext_blk + 2 * ns;
-  auto chunk_row = [&](int k) -> int {       // first row of chunk k
-    if (k < n_abl) return fs + B4_CH * k;
-    k -= n_abl;
-    if (k < 2 * n_ext_blk) return FB * (nfb - 1 - k / 2) + B4_CH * (k & 1);
-    k -= 2 * n_ext_blk;
-    return FB * (b0 + ns - 1 - k / 2) + B4_CH * (k & 1);
-  };
-  auto chunk_end = [&](int k) -> int {       // end of the rows that chunk k may hold
-    if (k < n_abl) return n;
-    k -= n_abl;
-    const int blk = k < 2 * n_ext_blk ? nfb - 1 - k / 2 : b0 + ns - 1 - (k - 2 * n_ext_blk) / 2;
-    return min(FB * (blk + 1), fs);
-  };
-  // this thread's 32 values of a chunk: warp w takes columns 32 w .. 32 w + 31, lane = row
-  CT reg[B4_CH];
-  auto load_chunk = [&](int k) {
-    const int r = chunk_row(k) + lane, re = chunk_end(k);
-#pragma unroll
-    for (int u = 0; u < B4_CH; ++u) {
-      const int cc = c0 + 32 * warp + u;
-      reg[u] = (r < re && cc < c1) ? (CT)G[r + (int64_t)cc * n] : CT(0);
-    }
-  };
-  if (n_chunks > 0) load_chunk(0);
-  int ready = nfb;                              // factor blocks >= ready are known complete
-  for (int k = 0; k < n_chunks; ++k) {
-    const int rk = chunk_row(k), re = chunk_end(k);
-    __syncthreads();                            // the previous chunk's tile has been read
-#pragma unroll
-    for (int u = 0; u < B4_CH; ++u) tile[lane * (4 * FB + 1) + 32 * warp + u] = reg[u];
-    if (k + 1 < n_chunks) load_chunk(k + 1);
-    const bool ext = k >= n_abl && k < n_abl + 2 * n_ext_blk;
-    const bool own = k >= n_abl + 2 * n_ext_blk;
-    const int blk = rk / FB;
-    if (ext && blk < ready) {
-      // every thread reaches this together; s_ready is read after ready_range's barrier
-      ready_range(flg, blk, b0 + ns - 1, -1, &s_ready, err);
-      ready = s_ready + 1;
-    }
-    if (own && (rk % FB) == 0) {
-      // own block s: its columns are complete once the rows below have been added
-      const int s2 = blk - b0, kbs = min(FB, fs - FB * blk);
-      if (sub == s2) {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q)
-          vsh[q][tid & 63] = (cv && q0 + q < nr) ? (CT)y[col + (int64_t)(q0 + q) * n] - acc[q] : CT(0);
-      }
-      __syncthreads();
-      CT xv[NQ];
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) xv[q] = CT(0);
-      if (sub == s2) {
-        const int i = tid & 63;
-        const T* Ds = dsh + s2 * FB * (FB + 1);
-        for (int t = i; t < kbs; ++t) {
-          const CT d = (CT)Ds[i * (FB + 1) + t];     // Dinv_s[t][i]
-#pragma unroll
-          for (int q = 0; q < NQ; ++q) xv[q] += d * vsh[q][t];
-        }
-      }
-      __syncthreads();                            // every v read before x replaces it
-      if (sub == s2) {
-        const int i = tid & 63;
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          vsh[q][i] = i < kbs ? xv[q] : CT(0);
-          if (cv && q0 + q < nr) y[col + (int64_t)(q0 + q) * n] = (double)xv[q];
-        }
-      }
-      __syncthreads();
-      if (sub == s2) {
-        __threadfence();
-        asm volatile("bar.sync %0, %1;" ::"r"(1 + s2), "r"(64) : "memory");
-        if ((tid & 63) == 0) st_release_gpu(flg + blk, 1);
-      }
-    }
-    // x of the chunk's rows
-    if (own) {
-      if (tid < B4_CH) {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) xs[q][tid] = rk + tid < re ? vsh[q][(rk % FB) + tid] : CT(0);
-      }
-    } else if (tid < B4_CH) {
-#pragma unroll
-      for (int q = 0; q < NQ; ++q)
-        xs[q][tid] = (rk + tid < re && q0 + q < nr) ? (CT)__ldcg(y + rk + tid + (int64_t)(q0 + q) * n) : CT(0);
-    }
-    __syncthreads();
-    // own rows add only into the columns left of their block
-    if (!own || tid < (blk - b0) * FB) {
-#pragma unroll 8
-      for (int r = 0; r < B4_CH; ++r) {
-        const CT lv = tile[r * (4 * FB + 1) + tid];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) acc[q] += lv * xs[q][r];
-      }
-    }
-  }
-}
-
-template <typename T, int NQ>
-static void bwd_flags4_nq(const DevCtx& c, const Item* items, int n_items, int* ticket, int* err, int q0,
-                          cudaStream_t s) {
-  const size_t dyn = sizeof(T) * (4 * FB * (FB + 1) + B4_CH * (4 * FB + 1));
-  cudaFuncSetAttribute(k_bwd_flags4<T, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-  k_bwd_flags4<T, NQ><<<n_items, 256, dyn, s>>>(c, items, ticket, err, q0);
-}
-
-void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
-                       int n_flags, int* err, int q0, cudaStream_t s) {
-  if (!n_items) return;
-  cudaMemsetAsync(ticket, 0, sizeof(int), s);
-  cudaMemsetAsync(flag_base, 0, sizeof(int) * n_flags, s);
-  const int nq = c.n_rhs - q0 < FLAG_NR ? c.n_rhs - q0 : FLAG_NR;
-  // NQ covers every right-hand side of the group (3 of them take the 4-wide kernel)
-  if (dtype == F64) {
-    if (nq >= 3) bwd_flags4_nq<double, 4>(c, items, n_items, ticket, err, q0, s);
-    else if (nq == 2) bwd_flags4_nq<double, 2>(c, items, n_items, ticket, err, q0, s);
-    else bwd_flags4_nq<double, 1>(c, items, n_items, ticket, err, q0, s);
-  } else {
-    if (nq >= 3) bwd_flags4_nq<float, 4>(c, items, n_items, ticket, err, q0, s);
-    else if (nq == 2) bwd_flags4_nq<float, 2>(c, items, n_items, ticket, err, q0, s);
-    else bwd_flags4_nq<float, 1>(c, items, n_items, ticket, err, q0, s);
   }
 }
 

@@ -124,12 +124,10 @@ constexpr int FLAG_NR_BWD_F64 = 2;   // backward FP64 launches take two
 void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
                       int* flag_base, int n_flags, int* err, int q0, cudaStream_t s);
 // the same with 256-row CTAs (item a: 256-row block of the factor rows, then
-// of ABL), each solving its own four 64-row blocks in turn
-void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
-                       int n_flags, int* err, int q0, cudaStream_t s);
-// the backward solve with 256-column CTAs (item a: 256-column block, tickets descending)
-void launch_bwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* flag_base,
-                       int n_flags, int* err, int q0, cudaStream_t s);
+// of ABL), each solving its own four 64-row blocks in turn; the same
+// hand-off words in and out
+void launch_fwd_flags4(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket, int* err, int q0,
+                       cudaStream_t s);
 void launch_bwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype, int* ticket,
                       int* flag_base, int n_flags, int* err, int q0, cudaStream_t s);
 // chain solves of large FP32 Cholesky fronts (one launch per level and group
