@@ -15,6 +15,9 @@
 // exactly once as  0 + sum over sources in source order  (element
 // contributions, then children in child order), which is the reference's
 // summation order onto a zeroed parent; no atomics, bitwise reproducible.
+// The sum is formed in the front's precision: FP64 fronts in FP64, FP32
+// fronts in FP32 (FP64 arithmetic runs at a small fraction of the FP32 rate
+// on this GPU, and the FP32 front stores the sum in FP32 either way).
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -56,7 +59,7 @@ __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restri
     const int64_t k0 = cp[J], k1 = cp[J + 1];
     const int istart = lower ? J : 0;
     for (int I = istart + threadIdx.x; I < n; I += blockDim.x) {
-      double acc = 0.0;
+      T acc = T(0);
       for (int64_t k = k0; k < k1; ++k) {
         const int2 cs = c.colsrc[k];
         const int is = inv[(int64_t)cs.x * n + I];
@@ -64,16 +67,16 @@ __global__ void __launch_bounds__(256) k_assemble(DevCtx c, const Item* __restri
           const SrcDev sd = cs.x < ASM_MAXSRC ? s_src[cs.x] : c.srcs[f.src0 + cs.x];
           int r = is, cc = cs.y;
           if (sd.is_child && c.symmetric && r < cc) { int t = r; r = cc; cc = t; }
-          acc += load_src(c, sd, r + (int64_t)cc * sd.ld);
+          acc += (T)load_src(c, sd, r + (int64_t)cc * sd.ld);
         }
       }
-      P[I + (int64_t)J * n] = (T)acc;
+      P[I + (int64_t)J * n] = acc;
     }
   }
 }
 
 // Extend-add of a large front, one parent column J per CTA.  The column is
-// accumulated in shared memory in FP64: zero, then each source holding
+// accumulated in shared memory (in the front's precision): zero, then each source holding
 // column J in source order (the element, then the children in child order)
 // scatters its column through its row map (an injective map, so a source
 // never hits the same entry twice and one barrier between sources keeps the
@@ -90,12 +93,13 @@ constexpr int ASM_EARLY_MIN = 8192;
 
 template <typename T, int NT, bool EARLY>
 __global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* __restrict__ items, int lower) {
-  extern __shared__ double s_col[];
+  extern __shared__ __align__(16) unsigned char sc_raw[];
+  T* s_col = reinterpret_cast<T*>(sc_raw);
   const Item it = items[blockIdx.x];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, J = it.a;
   const int istart = lower ? J : 0;
-  for (int I = istart + threadIdx.x; I < n; I += NT) s_col[I] = 0.0;
+  for (int I = istart + threadIdx.x; I < n; I += NT) s_col[I] = T(0);
   const int64_t* __restrict__ cp = c.colptr + f.colptr_off;
   const int64_t k0 = cp[J], k1 = cp[J + 1];
   __syncthreads();
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* _
     const int rs = !EARLY ? sd.m : (sd.is_child ? (sym ? cc : 0) : sd.m);
     for (int r0 = 0; r0 < sd.m; r0 += 4 * NT) {
       int I[4];
-      double v[4];
+      T v[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int r = r0 + threadIdx.x + NT * u;
@@ -122,10 +126,10 @@ __global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* _
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int r = r0 + threadIdx.x + NT * u;
-        v[u] = 0.0;
+        v[u] = T(0);
         if (r < sd.m && r >= rs) {
           const int64_t idx = r + (int64_t)cc * sd.ld;
-          v[u] = b32 ? (double)b32[idx] : b64[idx];
+          v[u] = b32 ? (T)b32[idx] : (T)b64[idx];
         }
       }
 #pragma unroll
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* _
             int rr = r, cl = cc;
             if (sym && rr < cl) { const int t = rr; rr = cl; cl = t; }
             const int64_t idx = rr + (int64_t)cl * sd.ld;
-            v[u] = b32 ? (double)b32[idx] : b64[idx];
+            v[u] = b32 ? (T)b32[idx] : (T)b64[idx];
           }
           s_col[I[u]] += v[u];
         }
@@ -145,13 +149,13 @@ __global__ void __launch_bounds__(NT) k_assemble_scatter(DevCtx c, const Item* _
     __syncthreads();
   }
   T* __restrict__ P = arena<T>(c) + f.off + (int64_t)J * n;
-  for (int I = istart + threadIdx.x; I < n; I += NT) P[I] = (T)s_col[I];
+  for (int I = istart + threadIdx.x; I < n; I += NT) P[I] = s_col[I];
 }
 
 template <typename T>
 static void assemble_scatter_t(const DevCtx& c, const Item* items, int n_items, int lower, int n_max,
                                cudaStream_t s) {
-  const size_t sm = sizeof(double) * (size_t)n_max;
+  const size_t sm = sizeof(T) * (size_t)n_max;
   if (n_max >= ASM_EARLY_MIN) {
     cudaFuncSetAttribute(k_assemble_scatter<T, 512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_assemble_scatter<T, 512, true><<<n_items, 512, sm, s>>>(c, items, lower);
