@@ -289,9 +289,139 @@ __global__ void __launch_bounds__(NT) k_small_factor(DevCtx c, const Item* __res
     for (int i = (chol ? j : 0) + lane; i < n; i += 32) G[i + (int64_t)j * n] = A[i + (int64_t)j * n];
 }
 
+// Cholesky fronts in shared memory, one CTA per front: the lower triangle is
+// staged with eight loads in flight per thread; the fs factor columns are
+// factored column by column as in k_small_factor, but each step updates only
+// the panel's later columns; the Schur block is then updated once from the
+// factor panel in 4 x 4 register tiles, subtracting the fs products in
+// column order -- the same operations in the same order as k_small_factor's
+// rank-1 steps (bit-identical), with one shared-memory read and write per
+// Schur entry instead of one per entry and step.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_small_chol(DevCtx c, const Item* __restrict__ items) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* A = reinterpret_cast<T*>(smem_raw);
+  const Item it = items[blockIdx.x];
+  const FrontDev f = c.fronts[it.front];
+  const int n = f.n, fs = f.fs;
+  T* __restrict__ G = arena<T>(c) + f.off;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NW = NT / 32;
+  const int nn = n * n;
+  // flat index e = i + j n walked in steps of NT with (i, j) kept by carry
+  const int qs = NT / n, rs = NT % n;
+  {
+    int i0 = threadIdx.x % n, j0 = threadIdx.x / n;
+    for (int e0 = 0; e0 < nn; e0 += 8 * NT) {
+      T v[8];
+      int i = i0, j = j0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + threadIdx.x + u * NT;
+        v[u] = (e < nn && i >= j) ? G[e] : T(0);
+        i += rs; j += qs;
+        if (i >= n) { i -= n; ++j; }
+      }
+      i = i0; j = j0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + threadIdx.x + u * NT;
+        if (e < nn && i >= j) A[e] = v[u];
+        i += rs; j += qs;
+        if (i >= n) { i -= n; ++j; }
+      }
+      i0 = i; j0 = j;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < fs; ++k) {
+    if (threadIdx.x == 0) {
+      T d = A[k + k * n];
+      if (!(d > (T)0)) { set_status(c, it.front, d != d ? ST_NAN : ST_NOT_SPD); d = (T)1; }
+      A[k + k * n] = my_sqrt<T>(d);
+    }
+    __syncthreads();
+    const T dkk = A[k + k * n];
+    for (int i = k + 1 + threadIdx.x; i < n; i += NT) A[i + k * n] /= dkk;
+    __syncthreads();
+    for (int j = k + 1 + warp; j < fs; j += NW) {
+      const T ajk = A[j + k * n];
+      T* __restrict__ col = A + j * n;
+      const T* __restrict__ colk = A + k * n;
+      for (int i = j + lane; i < n; i += 32) col[i] -= colk[i] * ajk;
+    }
+    __syncthreads();
+  }
+  // Schur block S (rows / columns fs .. n-1): S -= L21 L21^T by 4 x 4 tiles
+  // of its lower triangle, tile t -> (ti, tj), ti >= tj
+  const int m = n - fs, tm = (m + 3) / 4, ntile = tm * (tm + 1) / 2;
+  for (int t = threadIdx.x; t < ntile; t += NT) {
+    int ti = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while (ti * (ti + 1) / 2 > t) --ti;
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    const int tj = t - ti * (ti + 1) / 2;
+    const int r0 = fs + 4 * ti, c0 = fs + 4 * tj;
+    T acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int i = r0 + u, j = c0 + v;
+        acc[u][v] = (i < n && j < n && i >= j) ? A[i + j * n] : T(0);
+      }
+    for (int k = 0; k < fs; ++k) {
+      const T* __restrict__ colk = A + k * n;
+      T x[4], y[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[u] = r0 + u < n ? colk[r0 + u] : T(0);
+        y[u] = c0 + u < n ? colk[c0 + u] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] -= x[u] * y[v];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int i = r0 + u, j = c0 + v;
+        if (i < n && j < n && i >= j) A[i + j * n] = acc[u][v];
+      }
+  }
+  __syncthreads();
+  {
+    int i0 = threadIdx.x % n, j0 = threadIdx.x / n;
+    for (int e0 = 0; e0 < nn; e0 += 8 * NT) {
+      int i = i0, j = j0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + threadIdx.x + u * NT;
+        if (e < nn && i >= j) G[e] = A[e];
+        i += rs; j += qs;
+        if (i >= n) { i -= n; ++j; }
+      }
+      i0 = i; j0 = j;
+    }
+  }
+}
+
 void launch_small_factor(const DevCtx& c, const Item* items, int n_items, int dtype, int method,
                          int max_n, cudaStream_t s) {
   if (!n_items) return;
+  if (method == M_CHOL) {
+    if (dtype == F64) {
+      const size_t sm = (size_t)max_n * max_n * sizeof(double);
+      cudaFuncSetAttribute(k_small_chol<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_small_chol<double, 256><<<n_items, 256, sm, s>>>(c, items);
+    } else {
+      const size_t sm = (size_t)max_n * max_n * sizeof(float);
+      cudaFuncSetAttribute(k_small_chol<float, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_small_chol<float, 256><<<n_items, 256, sm, s>>>(c, items);
+    }
+    return;
+  }
   if (dtype == F64) {
     size_t sm = (size_t)max_n * max_n * sizeof(double);
     cudaFuncSetAttribute(k_small_factor<double, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
