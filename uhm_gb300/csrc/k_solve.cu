@@ -981,22 +981,22 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   }
   __syncthreads();
   if (factor_block) {
-    // y = Dinv v on all 256 threads: column group g sums t in [16 g, 16 g + 16)
-    // (Dinv is lower triangular: t <= i), then the four partial sums are
-    // added in group order; this takes the 64-step dependent chain of one
-    // thread per row off the hand-off to the next block
-    const int kb = r1 - r0;
+    // y = Dinv v on all 256 threads: column group g sums t in [16 g, 16 g + 16),
+    // then the four partial sums are added in group order; this takes the
+    // 64-step dependent chain of one thread per row off the hand-off to the
+    // next block.  The stored inverse is zero above its diagonal and past the
+    // block's kb rows and columns, so every thread runs the same unbranched
+    // loop (its loads issued together) and the sums equal the skipped-term
+    // ones exactly.
     CT xp[SF_NR];
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q) xp[q] = CT(0);
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int t = g * 16 + u;
-      if (t <= i && t < kb) {
-        const CT d = (CT)dsh[t * (FB + 1) + i];     // Dinv[i][t], column t staged as row t
+      const CT d = (CT)dsh[t * (FB + 1) + i];     // Dinv[i][t], column t staged as row t
 #pragma unroll
-        for (int q = 0; q < SF_NR; ++q) xp[q] += d * v[t][q];
-      }
+      for (int q = 0; q < SF_NR; ++q) xp[q] += d * v[t][q];
     }
 #pragma unroll
     for (int q = 0; q < SF_NR; ++q) red[g][i][q] = xp[q];
@@ -1344,18 +1344,32 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
   for (int q = 0; q < NQ; ++q)
 #pragma unroll
     for (int u = 0; u < 16; ++u) acc[q][u] = CT(0);
+  // this block's right-hand sides, loaded before any wait
+  CT yb[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+    yb[q] = (threadIdx.x < kb && q < nq) ? (CT)y[c0 + threadIdx.x + (int64_t)(q0 + q) * n] : CT(0);
   bwd_gather_rows<T, NQ>(c, f, b, b, q0, nq, err, acc, xsh);
+  // the column sums over the 64 row lanes: four parts of 16 rows on all
+  // 256 threads (the loads issued together), then the parts in order
+  __shared__ CT part[4][FB];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 16; ++u) red[rl][g * 16 + u] = acc[q][u];
     __syncthreads();
+    {
+      const int col = threadIdx.x % FB, pr = threadIdx.x / FB;
+      CT sp = CT(0);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) sp += red[16 * pr + r][col];
+      part[pr][col] = sp;
+    }
+    __syncthreads();
     if (threadIdx.x < FB) {
-      CT s = CT(0);
-      for (int r = 0; r < FB; ++r) s += red[r][threadIdx.x];
-      v[threadIdx.x][q] = (threadIdx.x < kb && q < nq)
-                              ? (CT)y[c0 + threadIdx.x + (int64_t)(q0 + q) * n] - s : CT(0);
+      const CT sum = part[0][threadIdx.x] + part[1][threadIdx.x] + part[2][threadIdx.x] + part[3][threadIdx.x];
+      v[threadIdx.x][q] = (threadIdx.x < kb && q < nq) ? yb[q] - sum : CT(0);
     }
   }
   __syncthreads();
@@ -1367,10 +1381,11 @@ __global__ void __launch_bounds__(256) k_bwd_flags(DevCtx c, const Item* __restr
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       CT xp = CT(0);
+      // Dinv[t][ii] is zero for t < ii and past kb: the unbranched sum is exact
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
         const int t = gg * 16 + u;
-        if (t >= ii && t < kb) xp += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
+        xp += (CT)dsh[ii * (FB + 1) + t] * v[t][q];
       }
       red[gg * NQ + q][ii] = xp;
     }
