@@ -10,8 +10,9 @@ order of the additions within a row differs between the two forms.
 
 Checked: mixed precision (FP32 fronts) and plain FP64 fronts, a root front
 with a ragged last block, ABL rows (fronts below the root), several
-right-hand sides in two launch groups, and that both forms give the same
-first-solve backward error (same factors)."""
+right-hand sides in two launch groups (4 + 3 and 4 + 2, which take the 4-
+and 2-wide 64-row kernels), and that both forms give the same first-solve
+backward error (same factors)."""
 import numpy as np
 import pytest
 
@@ -43,6 +44,8 @@ CASES = [
     ("3d_8_p4_fp32", lambda: hpfem.poisson3d(8, 4, seed=72), 1, api.PREC_FP32, REL_TOL_MIXED),
     ("3d_8_p3_fp64", lambda: hpfem.poisson3d(8, 3, seed=73), 0, api.PREC_FP64, REL_TOL_FP64),
     ("3d_6_p4_rhs7", lambda: hpfem.poisson3d(6, 4, seed=74, n_rhs=7), 1, api.PREC_FP32, REL_TOL_MIXED),
+    # launch groups of 4 and 2 right-hand sides (the 4- and 2-wide kernels)
+    ("3d_6_p4_rhs6", lambda: hpfem.poisson3d(6, 4, seed=76, n_rhs=6), 1, api.PREC_FP32, REL_TOL_MIXED),
     ("diff_8_p3", lambda: hpfem.diffusion3d(8, 3, seed=75, contrast=1e3), 1, api.PREC_FP32, REL_TOL_MIXED),
 ]
 

@@ -869,10 +869,9 @@ struct HandWords {
 // the CTA's rows (thread: row lane tid % 64, column group tid / 64), y_j read
 // from its hand-off words: warp 0 polls and stages them (the next block's
 // words already in flight), the other warps wait at the block barrier.
-template <typename T>
+template <typename T, int NQ>
 __device__ __forceinline__ void fwd_gather_blocks(const DevCtx& c, const FrontDev& f, int row, bool rv, int jend,
-                                                  int q0, int nq, int* err, T (&acc)[SF_NR],
-                                                  T (*ysh)[SF_NR][FB]) {
+                                                  int q0, int nq, int* err, T (&acc)[NQ], T (*ysh)[NQ][FB]) {
   using CT = T;
   const int n = f.n, fs = f.fs, g = threadIdx.x / FB;
   const T* __restrict__ G = arena<T>(c) + f.off;
@@ -920,30 +919,33 @@ __device__ __forceinline__ void fwd_gather_blocks(const DevCtx& c, const FrontDe
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
 #pragma unroll
-      for (int q = 0; q < SF_NR; ++q)
+      for (int q = 0; q < NQ; ++q)
         if (q < nq) acc[q] += cur[u] * ysh[buf][q][g * 16 + u];
     }
   }
 }
 
 // item: front, a = block index (factor blocks 0..nfb-1, ABL blocks nfb..);
-// right-hand sides q0 .. q0+SF_NR-1 (more are solved by further launches)
-template <typename T>
+// right-hand sides q0 .. q0+nq-1, nq <= NQ <= SF_NR (more are solved by
+// further launches); NQ is the launch's right-hand sides rounded up to 1, 2
+// or 4, so that a launch for one right-hand side issues no products for
+// absent ones
+template <typename T, int NQ>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCtx c, const Item* __restrict__ items,
                                                    int* ticket, int* err, int q0) {
   using CT = T;
   __shared__ int s_t;
-  __shared__ CT red[4][FB][SF_NR];
-  __shared__ CT v[FB][SF_NR];
+  __shared__ CT red[4][FB][NQ];
+  __shared__ CT v[FB][NQ];
   __shared__ T dsh[FB * (FB + 1)];     // inverse diagonal block, staged before any wait
   // y_j staged by warp 0, two buffers alternating by block: one barrier per block
-  __shared__ CT ysh[2][SF_NR][FB];
+  __shared__ CT ysh[2][NQ][FB];
   if (threadIdx.x == 0) s_t = atomicAdd(ticket, 1);
   __syncthreads();
   const Item it = items[s_t];
   const FrontDev f = c.fronts[it.front];
   const int n = f.n, fs = f.fs, nr = c.n_rhs, b = it.a;
-  const int nq = min(SF_NR, nr - q0);
+  const int nq = min(NQ, nr - q0);
   const int nfb = (fs + FB - 1) / FB;
   const bool factor_block = b < nfb;
   if (factor_block) {
@@ -957,9 +959,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   const int i = threadIdx.x % FB, g = threadIdx.x / FB;
   const int row = r0 + i;
   const bool rv = row < r1;
-  CT acc[SF_NR], zr[SF_NR];
+  CT acc[NQ], zr[NQ];
 #pragma unroll
-  for (int q = 0; q < SF_NR; ++q) {
+  for (int q = 0; q < NQ; ++q) {
     acc[q] = CT(0);
     zr[q] = (rv && q < nq && g == 0) ? (CT)z[row + (int64_t)(q0 + q) * n] : CT(0);   // before any wait
   }
@@ -967,16 +969,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
   // solve's hand-off words for this block
   if (factor_block && rv && g == 0) {
 #pragma unroll
-    for (int q = 0; q < SF_NR; ++q)
+    for (int q = 0; q < NQ; ++q)
       if (q < nq) z[row + (int64_t)(q0 + q) * n] = __longlong_as_double((long long)HAND_EMPTY);
   }
-  fwd_gather_blocks<T>(c, f, row, rv, factor_block ? b : nfb, q0, nq, err, acc, ysh);
+  fwd_gather_blocks<T, NQ>(c, f, row, rv, factor_block ? b : nfb, q0, nq, err, acc, ysh);
 #pragma unroll
-  for (int q = 0; q < SF_NR; ++q) red[g][i][q] = acc[q];
+  for (int q = 0; q < NQ; ++q) red[g][i][q] = acc[q];
   __syncthreads();
   if (threadIdx.x < FB) {
 #pragma unroll
-    for (int q = 0; q < SF_NR; ++q)
+    for (int q = 0; q < NQ; ++q)
       v[i][q] = (rv && q < nq) ? zr[q] - (red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]) : CT(0);
   }
   __syncthreads();
@@ -988,29 +990,29 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_fwd_flags(DevCt
     // block's kb rows and columns, so every thread runs the same unbranched
     // loop (its loads issued together) and the sums equal the skipped-term
     // ones exactly.
-    CT xp[SF_NR];
+    CT xp[NQ];
 #pragma unroll
-    for (int q = 0; q < SF_NR; ++q) xp[q] = CT(0);
+    for (int q = 0; q < NQ; ++q) xp[q] = CT(0);
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int t = g * 16 + u;
       const CT d = (CT)dsh[t * (FB + 1) + i];     // Dinv[i][t], column t staged as row t
 #pragma unroll
-      for (int q = 0; q < SF_NR; ++q) xp[q] += d * v[t][q];
+      for (int q = 0; q < NQ; ++q) xp[q] += d * v[t][q];
     }
 #pragma unroll
-    for (int q = 0; q < SF_NR; ++q) red[g][i][q] = xp[q];
+    for (int q = 0; q < NQ; ++q) red[g][i][q] = xp[q];
     __syncthreads();
     if (threadIdx.x < FB && rv) {
 #pragma unroll
-      for (int q = 0; q < SF_NR; ++q)
+      for (int q = 0; q < NQ; ++q)
         if (q < nq)
           st_hand(y + row + (int64_t)(q0 + q) * n,
                   (double)(red[0][i][q] + red[1][i][q] + red[2][i][q] + red[3][i][q]));
     }
   } else if (threadIdx.x < FB && rv) {
 #pragma unroll
-    for (int q = 0; q < SF_NR; ++q)
+    for (int q = 0; q < NQ; ++q)
       if (q < nq) z[row + (int64_t)(q0 + q) * n] = (double)v[i][q];
   }
 }
@@ -1408,8 +1410,17 @@ void launch_fwd_flags(const DevCtx& c, const Item* items, int n_items, int dtype
   if (!n_items) return;
   (void)flag_base; (void)n_flags;     // hand-off words, no flags
   cudaMemsetAsync(ticket, 0, sizeof(int), s);
-  if (dtype == F64) k_fwd_flags<double><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
-  else k_fwd_flags<float><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+  const int nq = c.n_rhs - q0 < FLAG_NR ? c.n_rhs - q0 : FLAG_NR;
+  // NQ covers every right-hand side of the group (3 of them take the 4-wide kernel)
+  if (dtype == F64) {
+    if (nq >= 3) k_fwd_flags<double, 4><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+    else if (nq == 2) k_fwd_flags<double, 2><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+    else k_fwd_flags<double, 1><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+  } else {
+    if (nq >= 3) k_fwd_flags<float, 4><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+    else if (nq == 2) k_fwd_flags<float, 2><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+    else k_fwd_flags<float, 1><<<n_items, 256, 0, s>>>(c, items, ticket, err, q0);
+  }
 }
 
 template <typename T, int NQ>
