@@ -38,10 +38,34 @@ __global__ void __launch_bounds__(256) k_fwd_gather(DevCtx c, const Item* __rest
   // rows [it.a, it.a + it.b) of the front (it.b == 0: all rows; only then
   // are pivots applied, which needs the whole gathered vector)
   const int I0 = it.a, I1 = it.b > 0 ? min(n, it.a + it.b) : n;
+  // the sources decoded once per CTA (in source order): a child's updated
+  // bottom block and its leading dimension, null for an element source
+  constexpr int GMAXSRC = 64;
+  __shared__ const double* s_xb[GMAXSRC];
+  __shared__ int s_ld[GMAXSRC];
+  const int ns = min(f.nsrc, GMAXSRC);
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+    const SrcDev sd = c.srcs[f.src0 + s];
+    if (sd.is_child) {
+      const FrontDev ch = c.fronts[sd.slot];
+      s_xb[s] = c.vec + ch.voff + ch.fs;
+      s_ld[s] = ch.n;
+    } else {
+      s_xb[s] = nullptr;
+      s_ld[s] = 0;
+    }
+  }
+  __syncthreads();
   for (int q = 0; q < c.n_rhs; ++q) {
     for (int I = I0 + threadIdx.x; I < I1; I += blockDim.x) {
       double acc = I < f.fs ? g[(f.g0 + I) + q * ldg] : 0.0;
-      for (int s = 0; s < f.nsrc; ++s) {
+      for (int s = 0; s < ns; ++s) {
+        const double* xb = s_xb[s];
+        if (!xb) continue;
+        const int is = inv[(int64_t)s * n + I];
+        if (is >= 0) acc += xb[is + (int64_t)q * s_ld[s]];
+      }
+      for (int s = ns; s < f.nsrc; ++s) {
         const SrcDev sd = c.srcs[f.src0 + s];
         if (!sd.is_child) continue;
         const int is = inv[(int64_t)s * n + I];
