@@ -2065,6 +2065,11 @@ void Engine::factor(int method) {
   solved = false;
   front_kept.clear();
   if (!anorm_valid) enqueue_anorm();
+  // the diagonal kernels' hand-off words carry 21 bits of the factorisation
+  // count in their tag: cleared every 2^20 factorisations (and before the
+  // first), no word is left to meet its tag again after the count wraps
+  if (d_hand && (hand_factorisations++ & ((int64_t(1) << 20) - 1)) == 0)
+    CK(cudaMemsetAsync(d_hand + CD_HAND_HEAD, 0, sizeof(uint64_t) * (size_t)(hand_n * CD_HAND_WORDS), stream));
   if (n_keep > 0) launch_ops(fac_ops_part, nullptr, nullptr, d_items_part);
   else run_ops(fac_ops, nullptr, nullptr);
   CK(cudaEventRecord(ev1, stream));

@@ -302,6 +302,7 @@ class Engine {
   uint64_t* d_hand = nullptr;        // the factorisation count (first word), then the diagonal-block
                                      // launches' hand-off words, CD_HAND_WORDS per front slot
   int64_t hand_n = 0;                // front slots of d_hand
+  int64_t hand_factorisations = 0;   // factorisations run (the clearing of d_hand's words)
   void* d_ws = nullptr;              // BF16 operand parts of tensor-core fronts
   int64_t* d_ws_off = nullptr;
   int64_t* d_ws_stride = nullptr;
